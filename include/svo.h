@@ -1,0 +1,176 @@
+/*
+ * svo.h — C ABI of the GB300 sparse-voxel-octree library (libsvo_gb300.so).
+ *
+ * Drop-in boundary for the reference's VoxelOctree hot path
+ * (tunabrain/sparse-voxel-octrees, src/VoxelOctree.hpp:37-58):
+ *   build (voxels -> 32-bit child-descriptor octree), .oct load/save, and the
+ *   FP32 ESVO raymarch returning hit t, leaf payload word, leaf index and the
+ *   viewer's shaded colour.
+ *
+ * Conventions
+ *   - Every function returns an int status: SVO_OK (0) or a negative SVO_ERR_*.
+ *     svo_last_error() returns a message for the calling thread's last failure.
+ *   - No exceptions cross this boundary; no allocation is hidden from the
+ *     caller except inside the opaque svo_octree handle and its staging pool.
+ *   - `stream` is a cudaStream_t passed as void*; NULL selects the legacy
+ *     default stream.  Functions taking device pointers are asynchronous with
+ *     respect to the host on that stream; *_host functions return after their
+ *     results are in host memory.
+ *   - Octree words live in HBM for the lifetime of the handle; a host copy is
+ *     made on demand (svo_octree_copy_words, svo_octree_save).
+ *   - The word layout is the reference's: bits [31:18] child offset (or its
+ *     high part when far), [17] far flag, [16] children carry far words,
+ *     [15:8] valid mask, [7:0] non-leaf mask, child octant i on bit 128>>i,
+ *     child slots in descending octant order, root at index 0.
+ *
+ * Limits: the GPU paths address at most 2^32-1 octree words and 2^32-1 rays
+ * per call; the build accepts virtual sides 2..65536.
+ */
+#ifndef SVO_GB300_H
+#define SVO_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SVO_OK 0
+#define SVO_ERR_INVALID (-1) /* bad argument (null pointer, bad size, bad option) */
+#define SVO_ERR_IO (-2)      /* a file could not be opened, read or written */
+#define SVO_ERR_FORMAT (-3)  /* truncated or corrupt .oct / .voxel / .ply stream */
+#define SVO_ERR_MEMORY (-4)  /* host or device allocation failed, or `mem` budget below the minimum */
+#define SVO_ERR_CUDA (-5)    /* a CUDA runtime call failed */
+#define SVO_ERR_LIMIT (-6)   /* input beyond a documented limit */
+#define SVO_ERR_DEVICE (-7)  /* a kernel raised its error flag (step cap or bounds check) */
+
+typedef struct svo_octree svo_octree;
+typedef void *svo_stream;
+
+/* Message for the calling thread's last failing call ("" if none). */
+const char *svo_last_error(void);
+/* Library version, major*10000 + minor*100 + patch. */
+int svo_version(void);
+
+/* ------------------------------------------------------------------ handle */
+
+/* Replaces VoxelOctree::VoxelOctree(const char *path), VoxelOctree.cpp:57-90.
+ * Reads the .oct header (float center[3], uint64 nWords) and the 64 MiB
+ * LZ4 blocks, then uploads the words to the current device.  Unlike the
+ * reference (which leaves a broken object when fopen fails) a missing or
+ * corrupt file returns SVO_ERR_IO / SVO_ERR_FORMAT. */
+int svo_octree_load(const char *path, svo_octree **out);
+
+/* Replaces VoxelOctree::save(const char *path), VoxelOctree.cpp:92-123.
+ * Same header and block framing; each 64 MiB block is LZ4-compressed
+ * independently, which the reference's streaming decoder reads unchanged. */
+int svo_octree_save(const svo_octree *oct, const char *path);
+
+/* Host-only .oct codec (no device involved): svo_oct_read decodes a file
+ * into a malloc'd word array (free it with svo_free); svo_oct_write encodes
+ * host words.  svo_octree_load / svo_octree_save are these plus the upload /
+ * download of the words. */
+int svo_oct_read(const char *path, uint32_t **words, uint64_t *n_words, float center[3]);
+int svo_oct_write(const char *path, const uint32_t *words, uint64_t n_words, const float center[3]);
+void svo_free(void *p);
+
+/* Wraps an existing word array (host memory) with its center; the words are
+ * copied to the device.  Used to trace octrees produced elsewhere. */
+int svo_octree_from_words(const uint32_t *words, uint64_t n_words, const float center[3], svo_octree **out);
+
+/* Frees the handle and its device memory. */
+int svo_octree_destroy(svo_octree *oct);
+
+/* Number of 32-bit words (VoxelOctree::_octreeSize, VoxelOctree.hpp:40). */
+int svo_octree_num_words(const svo_octree *oct, uint64_t *n_words);
+
+/* Copies the words to host memory `dst` (n_words entries). */
+int svo_octree_copy_words(const svo_octree *oct, uint32_t *dst, uint64_t n_words);
+
+/* Device pointer to the resident words (valid until svo_octree_destroy). */
+int svo_octree_device_words(const svo_octree *oct, const uint32_t **d_words);
+
+/* Replaces VoxelOctree::center(), VoxelOctree.hpp:55-57. */
+int svo_octree_center(const svo_octree *oct, float center[3]);
+
+/* Reads and clears the handle's device error word.  Bit 0 is set when an
+ * asynchronous svo_trace call had a ray stop at the traversal step cap or at
+ * an out-of-range word index (only possible on a corrupt octree). */
+int svo_octree_device_status(svo_octree *oct, uint32_t *flags);
+
+/* Walks the octree from the root and checks the descriptor invariants
+ * (offsets in range, far words present, leaf masks, no cycles).  Returns
+ * SVO_OK and the number of descriptors and leaves, or SVO_ERR_FORMAT. */
+int svo_octree_validate(const svo_octree *oct, uint64_t *n_descriptors, uint64_t *n_leaves);
+
+/* ------------------------------------------------------------------- build */
+
+/* Replaces VoxelOctree::VoxelOctree(VoxelData *) (VoxelOctree.cpp:125-205)
+ * over VoxelData(const char *path, size_t mem) (VoxelData.cpp:37-48) on the
+ * GPU: occupied-voxel extraction in Morton order, then a bottom-up level
+ * pass (valid masks, subtree word counts, far-pointer decisions) and a
+ * top-down placement pass that writes the reference's exact word stream.
+ *   grid: w*h*d uint32 voxels, x fastest, 0 = empty (the .voxel payload,
+ *         PlyLoader.cpp:521-528); host memory, or device memory when
+ *         grid_on_device != 0.
+ *   mem:  the reference's memory budget; it selects VoxelData's cache-block
+ *         edge (VoxelData.cpp:211-244), which decides two corner cases of the
+ *         reference's output that this build reproduces: a buffer of odd
+ *         depth never marks its last z slice (VoxelData.cpp:163-170), and a
+ *         cache block whose only voxels lie in that slice still appears as
+ *         an empty descriptor.  Pass 1 << 30 for the reference's default.
+ * Returns SVO_ERR_MEMORY when `mem` admits no cache block (the reference
+ * exits the process) and SVO_ERR_INVALID when the virtual side is below 2. */
+int svo_octree_build_dense(const uint32_t *grid, int w, int h, int d, uint64_t mem, int grid_on_device,
+                           svo_stream stream, svo_octree **out);
+
+/* Same as svo_octree_build_dense, reading a .voxel file (int32 w, h, d then
+ * w*h*d uint32, x fastest), i.e. VoxelData(const char *path, size_t mem). */
+int svo_octree_build_voxel_file(const char *path, uint64_t mem, svo_stream stream, svo_octree **out);
+
+/* ------------------------------------------------------------------- trace */
+
+/* Per-ray outputs; any pointer may be NULL to skip that output.
+ *   hit:  0 miss, 1 leaf hit, 2 level-of-detail exit (ray_scale > 0,
+ *         VoxelOctree.cpp:265-268)
+ *   t:    raymarch's t on a hit, +inf on a miss
+ *   leaf: index into the word array of the hit leaf's payload word
+ *         (VoxelOctree.cpp:282), 0xFFFFFFFF when no leaf was hit
+ *   word: the leaf payload (raymarch's `normal` out-parameter), 0 when none
+ *   rgb:  3 floats per ray, the viewer's shade() (Main.cpp:81-90) of the leaf
+ *         word for the ray direction and `light`; 0 when no leaf was hit */
+typedef struct svo_trace_out {
+    uint8_t *hit;
+    float *t;
+    uint32_t *leaf;
+    uint32_t *word;
+    float *rgb;
+} svo_trace_out;
+
+/* Replaces a loop of VoxelOctree::raymarch(o, d, rayScale, normal, t)
+ * (VoxelOctree.cpp:207-346) over n rays, one GPU launch.  rays: 6 floats per
+ * ray (ox, oy, oz, dx, dy, dz) in the octree's [1,2]^3 frame, d normalised
+ * by the caller as in the reference; light: 3 floats (host memory).  All
+ * array pointers are device pointers; asynchronous on `stream`. */
+int svo_trace(const svo_octree *oct, const float *rays, uint64_t n, float ray_scale, const float light[3],
+              const svo_trace_out *out, svo_stream stream);
+
+/* Same as svo_trace with host arrays: rays are copied in and results out
+ * through the handle's staging buffers in chunks, copies overlapped with
+ * tracing on two internal streams.  Returns when results are on the host. */
+int svo_trace_host(svo_octree *oct, const float *rays, uint64_t n, float ray_scale, const float light[3],
+                   const svo_trace_out *out);
+
+/* Device-side load counter for the roofline: for each ray, the number of
+ * octree words the reference's raymarch reads (descriptor fetches at
+ * VoxelOctree.cpp:254, far words at :279, the leaf word at :282).  Slower
+ * than svo_trace; not for timing. */
+int svo_trace_count_loads(const svo_octree *oct, const float *rays, uint64_t n, float ray_scale,
+                          uint32_t *loads, svo_stream stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SVO_GB300_H */

@@ -1,0 +1,264 @@
+"""ctypes bindings for the test oracles.
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by ``__graft_entry__.smoke()``
+(as the checker) and by bench.py's CPU-baseline and reference legs.
+
+* ``Oracle``   — liboracle.so, the C restatement of the reference's hot path
+                 (svo_oracle.c).  Built by ``make -C oracle``; builds anywhere.
+* ``Reference`` — oracle/_ref/libsvo_ref.so, the reference's own sources
+                 compiled in place (``make -C oracle ref``).  Exists only where
+                 the reference sources are present.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "liboracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libsvo_ref.so")
+REF_SRC = os.environ.get("SVO_REFERENCE_DIR", "/root/reference")
+
+_u8p = ctypes.POINTER(ctypes.c_uint8)
+_u32p = ctypes.POINTER(ctypes.c_uint32)
+_u64p = ctypes.POINTER(ctypes.c_uint64)
+_f32p = ctypes.POINTER(ctypes.c_float)
+_vp = ctypes.c_void_p
+
+
+def _ptr(a, t):
+    if a is None:
+        return None
+    return a.ctypes.data_as(t)
+
+
+def build_oracle(with_reference=None):
+    """Compile liboracle.so (and, when the reference sources exist, _ref)."""
+    subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
+    if with_reference is None:
+        with_reference = os.path.isdir(os.path.join(REF_SRC, "src"))
+    if with_reference:
+        subprocess.run(["make", "-s", "-C", HERE, "-j8", "ref", "REF=" + REF_SRC], check=True)
+
+
+class Oracle:
+    """The C restatement (svo_oracle.c)."""
+
+    def __init__(self, path=ORACLE_SO):
+        if not os.path.exists(path):
+            build_oracle(with_reference=False)
+        L = ctypes.CDLL(path)
+        self.L = L
+        L.svo_oracle_inv_sqrt.restype = ctypes.c_float
+        L.svo_oracle_inv_sqrt.argtypes = [ctypes.c_float]
+        L.svo_oracle_compress_material.restype = ctypes.c_uint32
+        L.svo_oracle_compress_material.argtypes = [_f32p, ctypes.c_float]
+        L.svo_oracle_decompress_material.argtypes = [ctypes.c_uint32, _f32p, _f32p]
+        L.svo_oracle_shade.restype = ctypes.c_float
+        L.svo_oracle_shade.argtypes = [ctypes.c_uint32, _f32p, _f32p]
+        L.svo_oracle_raymarch_batch.argtypes = [_u32p, ctypes.c_uint64, _f32p, ctypes.c_uint64,
+                                                ctypes.c_float, _f32p, _u8p, _f32p, _u32p, _u32p,
+                                                _f32p, _u32p, ctypes.c_int]
+        L.svo_oracle_build_dense.restype = ctypes.c_int
+        L.svo_oracle_build_dense.argtypes = [_u32p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                             ctypes.c_uint64, ctypes.POINTER(_u32p), _u64p, _f32p]
+        L.svo_oracle_cache_block.restype = ctypes.c_uint64
+        L.svo_oracle_cache_block.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                             ctypes.c_uint64, ctypes.c_uint64]
+        L.svo_oracle_oct_decode.restype = ctypes.c_int
+        L.svo_oracle_oct_decode.argtypes = [_u8p, ctypes.c_uint64, ctypes.POINTER(_u32p), _u64p, _f32p]
+        L.svo_oracle_free.argtypes = [_vp]
+
+    # -- codec / shading
+    def inv_sqrt(self, x):
+        return self.L.svo_oracle_inv_sqrt(float(x))
+
+    def compress_material(self, n, shade):
+        a = np.ascontiguousarray(n, dtype=np.float32)
+        return int(self.L.svo_oracle_compress_material(_ptr(a, _f32p), float(shade)))
+
+    def decompress_material(self, word):
+        n = np.zeros(3, np.float32)
+        s = ctypes.c_float()
+        self.L.svo_oracle_decompress_material(int(word), _ptr(n, _f32p), ctypes.byref(s))
+        return n, s.value
+
+    def shade(self, word, d, light):
+        d = np.ascontiguousarray(d, dtype=np.float32)
+        light = np.ascontiguousarray(light, dtype=np.float32)
+        return self.L.svo_oracle_shade(int(word), _ptr(d, _f32p), _ptr(light, _f32p))
+
+    # -- raymarch
+    def raymarch(self, words, rays, ray_scale=0.0, light=(0.0, 0.0, 1.0), threads=1, loads=False):
+        """rays: (R, 6) float32.  Returns dict of hit (u8), t, leaf, word, grey[, loads]."""
+        words = np.ascontiguousarray(words, dtype=np.uint32)
+        rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 6)
+        light = np.ascontiguousarray(light, dtype=np.float32)
+        R = rays.shape[0]
+        out = {
+            "hit": np.zeros(R, np.uint8),
+            "t": np.zeros(R, np.float32),
+            "leaf": np.zeros(R, np.uint32),
+            "word": np.zeros(R, np.uint32),
+            "grey": np.zeros(R, np.float32),
+        }
+        ld = np.zeros(R, np.uint32) if loads else None
+        self.L.svo_oracle_raymarch_batch(_ptr(words, _u32p), words.size, _ptr(rays, _f32p), R,
+                                         float(ray_scale), _ptr(light, _f32p),
+                                         _ptr(out["hit"], _u8p), _ptr(out["t"], _f32p),
+                                         _ptr(out["leaf"], _u32p), _ptr(out["word"], _u32p),
+                                         _ptr(out["grey"], _f32p), _ptr(ld, _u32p), int(threads))
+        if loads:
+            out["loads"] = ld
+        return out
+
+    # -- build
+    def build_dense(self, grid, mem=1 << 30):
+        """grid: (d, h, w) uint32 array (x fastest).  Returns (words, center)."""
+        grid = np.ascontiguousarray(grid, dtype=np.uint32)
+        d, h, w = grid.shape
+        p = _u32p()
+        n = ctypes.c_uint64()
+        c = np.zeros(3, np.float32)
+        rc = self.L.svo_oracle_build_dense(_ptr(grid, _u32p), w, h, d, int(mem), ctypes.byref(p),
+                                           ctypes.byref(n), _ptr(c, _f32p))
+        if rc != 0:
+            raise RuntimeError("svo_oracle_build_dense failed: %d" % rc)
+        words = np.ctypeslib.as_array(p, shape=(n.value,)).copy() if n.value else np.zeros(0, np.uint32)
+        self.L.svo_oracle_free(ctypes.cast(p, _vp))
+        return words, c
+
+    def cache_block(self, w, h, d, mem, cell_cost=4):
+        return int(self.L.svo_oracle_cache_block(w, h, d, int(mem), int(cell_cost)))
+
+    def oct_decode(self, data):
+        buf = np.frombuffer(data, dtype=np.uint8)
+        p = _u32p()
+        n = ctypes.c_uint64()
+        c = np.zeros(3, np.float32)
+        rc = self.L.svo_oracle_oct_decode(_ptr(buf, _u8p), buf.size, ctypes.byref(p), ctypes.byref(n),
+                                          _ptr(c, _f32p))
+        if rc != 0:
+            raise ValueError("corrupt .oct stream (%d)" % rc)
+        words = np.ctypeslib.as_array(p, shape=(n.value,)).copy() if n.value else np.zeros(0, np.uint32)
+        self.L.svo_oracle_free(ctypes.cast(p, _vp))
+        return words, c
+
+
+class Reference:
+    """The reference's own code, compiled in place from its sources."""
+
+    _threads_started = None
+
+    def __init__(self, path=REF_SO):
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        L = ctypes.CDLL(path)
+        self.L = L
+        L.ref_start_threads.argtypes = [ctypes.c_int]
+        L.ref_build_voxel_file.restype = _vp
+        L.ref_build_voxel_file.argtypes = [ctypes.c_char_p, ctypes.c_uint64]
+        L.ref_build_ply.restype = _vp
+        L.ref_build_ply.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_uint64]
+        L.ref_ply_to_voxel_file.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_uint64]
+        L.ref_load.restype = _vp
+        L.ref_load.argtypes = [ctypes.c_char_p]
+        L.ref_save.argtypes = [_vp, ctypes.c_char_p]
+        L.ref_free.argtypes = [_vp]
+        L.ref_num_words.restype = ctypes.c_uint64
+        L.ref_num_words.argtypes = [_vp]
+        L.ref_words.restype = _vp
+        L.ref_words.argtypes = [_vp]
+        L.ref_center.argtypes = [_vp, _f32p]
+        L.ref_raymarch.argtypes = [_vp, _f32p, ctypes.c_uint64, ctypes.c_float, _u8p, _f32p, _u32p,
+                                   ctypes.c_int]
+        L.ref_compress_material.restype = ctypes.c_uint32
+        L.ref_compress_material.argtypes = [_f32p, ctypes.c_float]
+        L.ref_decompress_material.argtypes = [ctypes.c_uint32, _f32p, _f32p]
+        L.ref_inv_sqrt.restype = ctypes.c_float
+        L.ref_inv_sqrt.argtypes = [ctypes.c_float]
+        L.ref_tri_box_overlap.restype = ctypes.c_int
+        L.ref_tri_box_overlap.argtypes = [_f32p, _f32p, _f32p]
+
+    def start_threads(self, n):
+        if Reference._threads_started != n:
+            self.L.ref_start_threads(int(n))
+            Reference._threads_started = n
+
+    def _take(self, tree):
+        n = self.L.ref_num_words(tree)
+        p = self.L.ref_words(tree)
+        words = np.ctypeslib.as_array((ctypes.c_uint32 * n).from_address(p)).copy() if n else \
+            np.zeros(0, np.uint32)
+        c = np.zeros(3, np.float32)
+        self.L.ref_center(tree, _ptr(c, _f32p))
+        return words, c
+
+    def load(self, path):
+        """Returns an opaque tree handle (free with ``free``)."""
+        return self.L.ref_load(path.encode())
+
+    def free(self, tree):
+        self.L.ref_free(tree)
+
+    def words(self, tree):
+        return self._take(tree)
+
+    def save(self, tree, path):
+        self.L.ref_save(tree, path.encode())
+
+    def build_voxel_file(self, path, mem=1 << 30, threads=1, keep=False):
+        self.start_threads(threads)
+        tree = self.L.ref_build_voxel_file(path.encode(), int(mem))
+        out = self._take(tree)
+        if keep:
+            return out, tree
+        self.L.ref_free(tree)
+        return out
+
+    def build_ply(self, path, side, mem=1 << 30, threads=1):
+        self.start_threads(threads)
+        tree = self.L.ref_build_ply(path.encode(), int(side), int(mem))
+        out = self._take(tree)
+        self.L.ref_free(tree)
+        return out
+
+    def raymarch(self, tree, rays, ray_scale=0.0, threads=1):
+        rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 6)
+        R = rays.shape[0]
+        hit = np.zeros(R, np.uint8)
+        t = np.zeros(R, np.float32)
+        w = np.zeros(R, np.uint32)
+        self.L.ref_raymarch(tree, _ptr(rays, _f32p), R, float(ray_scale), _ptr(hit, _u8p), _ptr(t, _f32p),
+                            _ptr(w, _u32p), int(threads))
+        return hit, t, w
+
+    def compress_material(self, n, shade):
+        a = np.ascontiguousarray(n, dtype=np.float32)
+        return int(self.L.ref_compress_material(_ptr(a, _f32p), float(shade)))
+
+    def decompress_material(self, word):
+        n = np.zeros(3, np.float32)
+        s = np.zeros(1, np.float32)
+        self.L.ref_decompress_material(int(word), _ptr(n, _f32p), _ptr(s, _f32p))
+        return n, float(s[0])
+
+    def inv_sqrt(self, x):
+        return self.L.ref_inv_sqrt(float(x))
+
+    def tri_box_overlap(self, center, half, verts):
+        c = np.ascontiguousarray(center, dtype=np.float32)
+        h = np.ascontiguousarray(half, dtype=np.float32)
+        v = np.ascontiguousarray(verts, dtype=np.float32).reshape(9)
+        return int(self.L.ref_tri_box_overlap(_ptr(c, _f32p), _ptr(h, _f32p), _ptr(v, _f32p)))
+
+
+def write_voxel_file(path, grid):
+    """Write a reference .voxel file (PlyLoader.cpp:521-528 layout): int32 w, h, d
+    then uint32 voxels with x fastest.  grid has shape (d, h, w)."""
+    grid = np.ascontiguousarray(grid, dtype=np.uint32)
+    d, h, w = grid.shape
+    with open(path, "wb") as f:
+        f.write(np.array([w, h, d], dtype=np.int32).tobytes())
+        f.write(grid.tobytes())

@@ -1,0 +1,289 @@
+"""Python host interface of the GB300 sparse-voxel-octree library.
+
+A thin ctypes layer over the C ABI in include/svo.h (libsvo_gb300.so).  It
+mirrors the reference's C++ interface (src/VoxelOctree.hpp:37-58,
+src/VoxelData.hpp:101-144) so tests read like uses of the reference:
+
+    VoxelData(path_or_grid, mem)       -> VoxelData(const char*, size_t) / in-memory grid
+    VoxelOctree(path)                  -> VoxelOctree(const char *path)
+    VoxelOctree(voxel_data)            -> VoxelOctree(VoxelData *)  (built on the GPU)
+    octree.save(path)                  -> VoxelOctree::save
+    octree.raymarch(o, d, ray_scale)   -> VoxelOctree::raymarch (one ray; returns (hit, normal, t))
+    octree.center()                    -> VoxelOctree::center
+
+plus batched forms (trace over device or host ray arrays).  Every compute call
+goes through the CUDA library; importing this module fails loudly when the
+library has not been built, and there is no CPU fallback.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libsvo_gb300.so")
+
+SVO_OK = 0
+SVO_ERR_INVALID = -1
+SVO_ERR_IO = -2
+SVO_ERR_FORMAT = -3
+SVO_ERR_MEMORY = -4
+SVO_ERR_CUDA = -5
+SVO_ERR_LIMIT = -6
+SVO_ERR_DEVICE = -7
+
+DEFAULT_MEM = 1 << 30  # Main.cpp:269
+
+_vp = ctypes.c_void_p
+_u32p = ctypes.POINTER(ctypes.c_uint32)
+_u64p = ctypes.POINTER(ctypes.c_uint64)
+_f32p = ctypes.POINTER(ctypes.c_float)
+
+
+class SvoError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("svo error %d: %s" % (code, msg))
+        self.code = code
+
+
+class TraceOut(ctypes.Structure):
+    _fields_ = [("hit", _vp), ("t", _vp), ("leaf", _vp), ("word", _vp), ("rgb", _vp)]
+
+
+def _load():
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("libsvo_gb300.so is not built (run __graft_entry__.build() or "
+                          "python sparse-voxel-octrees_gb300/build_lib.py)")
+    L = ctypes.CDLL(LIB_PATH)
+    sig = {
+        "svo_last_error": (ctypes.c_char_p, []),
+        "svo_version": (ctypes.c_int, []),
+        "svo_octree_load": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_vp)]),
+        "svo_octree_save": (ctypes.c_int, [_vp, ctypes.c_char_p]),
+        "svo_oct_read": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_u32p), _u64p, _f32p]),
+        "svo_oct_write": (ctypes.c_int, [ctypes.c_char_p, _vp, ctypes.c_uint64, _f32p]),
+        "svo_free": (None, [_vp]),
+        "svo_octree_from_words": (ctypes.c_int, [_vp, ctypes.c_uint64, _f32p, ctypes.POINTER(_vp)]),
+        "svo_octree_destroy": (ctypes.c_int, [_vp]),
+        "svo_octree_num_words": (ctypes.c_int, [_vp, _u64p]),
+        "svo_octree_copy_words": (ctypes.c_int, [_vp, _vp, ctypes.c_uint64]),
+        "svo_octree_device_words": (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
+        "svo_octree_center": (ctypes.c_int, [_vp, _f32p]),
+        "svo_octree_device_status": (ctypes.c_int, [_vp, _u32p]),
+        "svo_octree_validate": (ctypes.c_int, [_vp, _u64p, _u64p]),
+        "svo_octree_build_dense": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_uint64,
+                                                  ctypes.c_int, _vp, ctypes.POINTER(_vp)]),
+        "svo_octree_build_voxel_file": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_uint64, _vp, ctypes.POINTER(_vp)]),
+        "svo_trace": (ctypes.c_int, [_vp, _vp, ctypes.c_uint64, ctypes.c_float, _f32p, ctypes.POINTER(TraceOut), _vp]),
+        "svo_trace_host": (ctypes.c_int, [_vp, _vp, ctypes.c_uint64, ctypes.c_float, _f32p,
+                                          ctypes.POINTER(TraceOut)]),
+        "svo_trace_count_loads": (ctypes.c_int, [_vp, _vp, ctypes.c_uint64, ctypes.c_float, _vp, _vp]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    return L
+
+
+lib = _load()
+
+
+def check(rc):
+    if rc != SVO_OK:
+        raise SvoError(rc, lib.svo_last_error().decode(errors="replace"))
+    return rc
+
+
+def _np_ptr(a):
+    return a.ctypes.data_as(_vp) if a is not None else None
+
+
+def _dev_ptr(x):
+    """Device pointer of a torch CUDA tensor (or an int address)."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return _vp(x)
+    return _vp(x.data_ptr())
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return _vp(stream)
+    return _vp(stream.cuda_stream)
+
+
+def oct_read(path):
+    """Decode a .oct file on the host: returns (words, center)."""
+    p = _u32p()
+    n = ctypes.c_uint64()
+    c = np.zeros(3, np.float32)
+    check(lib.svo_oct_read(os.fsencode(path), ctypes.byref(p), ctypes.byref(n), c.ctypes.data_as(_f32p)))
+    words = np.ctypeslib.as_array(p, shape=(n.value,)).copy()
+    lib.svo_free(ctypes.cast(p, _vp))
+    return words, c
+
+
+def oct_write(path, words, center):
+    """Encode host words as a .oct file."""
+    words = np.ascontiguousarray(words, dtype=np.uint32)
+    c = np.ascontiguousarray(center, dtype=np.float32)
+    check(lib.svo_oct_write(os.fsencode(path), _np_ptr(words), words.size, c.ctypes.data_as(_f32p)))
+
+
+class VoxelData:
+    """Input of the octree build: VoxelData(const char *path, size_t mem)
+    (VoxelData.cpp:37-48) or an in-memory dense grid of shape (d, h, w),
+    x fastest, 0 = empty.  `grid` may be a numpy array or a CUDA tensor."""
+
+    def __init__(self, source, mem=DEFAULT_MEM):
+        self.mem = int(mem)
+        self.path = None
+        self.grid = None
+        if isinstance(source, (str, bytes, os.PathLike)):
+            self.path = os.fsdecode(source)
+        else:
+            self.grid = source
+
+    @property
+    def on_device(self):
+        return self.grid is not None and hasattr(self.grid, "is_cuda") and self.grid.is_cuda
+
+
+class VoxelOctree:
+    """Resident GPU octree; see the module docstring for the reference mapping."""
+
+    def __init__(self, source=None, stream=None, _handle=None):
+        self._h = _vp()
+        if _handle is not None:
+            self._h = _handle
+        elif isinstance(source, (str, bytes, os.PathLike)):
+            check(lib.svo_octree_load(os.fsencode(source), ctypes.byref(self._h)))
+        elif isinstance(source, VoxelData):
+            if source.path is not None:
+                check(lib.svo_octree_build_voxel_file(os.fsencode(source.path), source.mem, _stream_ptr(stream),
+                                                      ctypes.byref(self._h)))
+            else:
+                g = source.grid
+                d, h, w = g.shape
+                if source.on_device:
+                    assert str(g.dtype) in ("torch.int32", "torch.uint32") and g.is_contiguous()
+                    check(lib.svo_octree_build_dense(_dev_ptr(g), w, h, d, source.mem, 1, _stream_ptr(stream),
+                                                     ctypes.byref(self._h)))
+                else:
+                    a = np.ascontiguousarray(g, dtype=np.uint32)
+                    check(lib.svo_octree_build_dense(_np_ptr(a), w, h, d, source.mem, 0, _stream_ptr(stream),
+                                                     ctypes.byref(self._h)))
+        else:
+            raise TypeError("VoxelOctree(path | VoxelData)")
+
+    @classmethod
+    def from_words(cls, words, center):
+        words = np.ascontiguousarray(words, dtype=np.uint32)
+        c = np.ascontiguousarray(center, dtype=np.float32)
+        h = _vp()
+        check(lib.svo_octree_from_words(_np_ptr(words), words.size, c.ctypes.data_as(_f32p), ctypes.byref(h)))
+        return cls(_handle=h)
+
+    def close(self):
+        if self._h:
+            lib.svo_octree_destroy(self._h)
+            self._h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    # -- VoxelOctree.hpp surface
+    def save(self, path):
+        check(lib.svo_octree_save(self._h, os.fsencode(path)))
+
+    def center(self):
+        c = np.zeros(3, np.float32)
+        check(lib.svo_octree_center(self._h, c.ctypes.data_as(_f32p)))
+        return c
+
+    def raymarch(self, o, d, ray_scale=0.0):
+        """One ray, as VoxelOctree::raymarch: returns (hit, normal, t).
+        `normal` and `t` are None where the reference leaves them unset."""
+        rays = np.array([list(o) + list(d)], dtype=np.float32)
+        r = self.trace_host(rays, ray_scale=ray_scale, outputs=("hit", "t", "word"))
+        hit = int(r["hit"][0])
+        if hit == 0:
+            return False, None, None
+        return True, (int(r["word"][0]) if hit == 1 else None), float(r["t"][0])
+
+    # -- words
+    def num_words(self):
+        n = ctypes.c_uint64()
+        check(lib.svo_octree_num_words(self._h, ctypes.byref(n)))
+        return n.value
+
+    def words(self):
+        n = self.num_words()
+        out = np.empty(n, np.uint32)
+        check(lib.svo_octree_copy_words(self._h, _np_ptr(out), n))
+        return out
+
+    def device_words_ptr(self):
+        p = _vp()
+        check(lib.svo_octree_device_words(self._h, ctypes.byref(p)))
+        return p.value
+
+    def validate(self):
+        nd = ctypes.c_uint64()
+        nl = ctypes.c_uint64()
+        check(lib.svo_octree_validate(self._h, ctypes.byref(nd), ctypes.byref(nl)))
+        return nd.value, nl.value
+
+    def device_status(self):
+        f = ctypes.c_uint32()
+        check(lib.svo_octree_device_status(self._h, ctypes.byref(f)))
+        return f.value
+
+    # -- batched tracing
+    def trace(self, rays, n=None, ray_scale=0.0, light=(0.0, 0.0, 1.0), out=None, stream=None):
+        """Device form: rays is a CUDA tensor (R, 6) float32; out maps any of
+        hit/t/leaf/word/rgb to preallocated CUDA tensors."""
+        if n is None:
+            n = rays.shape[0]
+        o = TraceOut()
+        for k in ("hit", "t", "leaf", "word", "rgb"):
+            v = (out or {}).get(k)
+            setattr(o, k, _dev_ptr(v).value if v is not None else None)
+        lt = np.ascontiguousarray(light, dtype=np.float32)
+        check(lib.svo_trace(self._h, _dev_ptr(rays), int(n), float(ray_scale), lt.ctypes.data_as(_f32p),
+                            ctypes.byref(o), _stream_ptr(stream)))
+
+    def trace_host(self, rays, ray_scale=0.0, light=(0.0, 0.0, 1.0), outputs=("hit", "t", "leaf", "word", "rgb"),
+                   out=None):
+        """Host form: rays is a numpy (R, 6) float32 array (pinned or not);
+        returns a dict of numpy outputs (or fills `out`)."""
+        rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 6)
+        R = rays.shape[0]
+        shapes = {"hit": ((R,), np.uint8), "t": ((R,), np.float32), "leaf": ((R,), np.uint32),
+                  "word": ((R,), np.uint32), "rgb": ((R, 3), np.float32)}
+        res = out if out is not None else {k: np.empty(*shapes[k]) for k in outputs}
+        o = TraceOut()
+        for k in ("hit", "t", "leaf", "word", "rgb"):
+            v = res.get(k)
+            setattr(o, k, v.ctypes.data if v is not None else None)
+        lt = np.ascontiguousarray(light, dtype=np.float32)
+        check(lib.svo_trace_host(self._h, _np_ptr(rays), R, float(ray_scale), lt.ctypes.data_as(_f32p),
+                                 ctypes.byref(o)))
+        return res
+
+    def count_loads(self, rays, n=None, ray_scale=0.0, loads=None, stream=None):
+        if n is None:
+            n = rays.shape[0]
+        check(lib.svo_trace_count_loads(self._h, _dev_ptr(rays), int(n), float(ray_scale), _dev_ptr(loads),
+                                        _stream_ptr(stream)))

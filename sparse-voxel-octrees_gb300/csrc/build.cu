@@ -1,0 +1,519 @@
+// build.cu — GPU octree construction from a dense voxel grid.
+//
+// Replaces VoxelOctree(VoxelData*) (VoxelOctree.cpp:125-205) with its
+// ChunkedAllocator far-pointer splice (ChunkedAllocator.hpp:76-114).  The
+// reference builds depth first and patches far pointers afterwards; this
+// pipeline computes the same word stream in three data-parallel phases:
+//
+//  1. Extraction.  The grid is read brick by brick (16^3 voxels per CTA,
+//     bricks visited in Morton order) and occupied voxels are emitted as
+//     (Morton key, payload) pairs in global Morton order.  Child slots in the
+//     reference are in descending octant index i, and octant i = 7 - m where
+//     m = xbit | ybit<<1 | zbit<<2 (VoxelOctree.cpp:144-146), so ascending
+//     Morton order is exactly the reference's depth-first child order.
+//  2. Bottom-up levels.  Children are grouped by key>>3 (head flags + scan);
+//     each parent gets its valid mask (bit m for child m, i.e. 128>>i) and,
+//     from its children's subtree word counts S, the far-pointer decision of
+//     VoxelOctree.cpp:172-183: offset_i = (k-i) + sum_{j<i} S_j and the
+//     parent's children carry far words when any offset_i > 0x3FFF.
+//     S = k*(far ? 2 : 1) + sum_j S_j (k payload words at the bottom level).
+//  3. Top-down placement.  Root at 0 with its child block at 1; a parent with
+//     block start B puts child i at B + i*stride and child i's block at
+//     B + k*stride + sum_{j<i} S_j, then writes the child's descriptor with
+//     offset = block - position (plus k-i far words, VoxelOctree.cpp:190-191)
+//     and, when far, the low 32 bits in the next word.
+//
+// VoxelData corner cases (VoxelData.cpp:160-175, 120-158, 211-262) that the
+// reference's output depends on, for cache-block edge M chosen from `mem`:
+//   - with M >= 4 and odd data depth the last z slice never reaches the
+//     low-level lookup table, so its voxels are dropped;
+//   - nodes of edge >= M come from the top lookup table, which is built from
+//     the full data, so an M-block whose only voxels lie in that slice still
+//     appears as a descriptor with no children.
+#include <cstdio>
+
+#include "scan.cuh"
+#include "svo_internal.h"
+
+namespace svo {
+namespace {
+
+constexpr int kBrickThreads = 256;
+
+__device__ __forceinline__ uint64_t spread3(uint32_t v) {
+    uint64_t x = v & 0x1fffffu;
+    x = (x | x << 32) & 0x1f00000000ffffull;
+    x = (x | x << 16) & 0x1f0000ff0000ffull;
+    x = (x | x << 8) & 0x100f00f00f00f00full;
+    x = (x | x << 4) & 0x10c30c30c30c30c3ull;
+    x = (x | x << 2) & 0x1249249249249249ull;
+    return x;
+}
+
+__device__ __forceinline__ uint32_t compact3(uint64_t x) {
+    x &= 0x1249249249249249ull;
+    x = (x ^ (x >> 2)) & 0x10c30c30c30c30c3ull;
+    x = (x ^ (x >> 4)) & 0x100f00f00f00f00full;
+    x = (x ^ (x >> 8)) & 0x1f0000ff0000ffull;
+    x = (x ^ (x >> 16)) & 0x1f00000000ffffull;
+    x = (x ^ (x >> 32)) & 0x1fffffull;
+    return (uint32_t)x;
+}
+
+__device__ __forceinline__ uint64_t morton3(uint32_t x, uint32_t y, uint32_t z) {
+    return spread3(x) | (spread3(y) << 1) | (spread3(z) << 2);
+}
+
+struct GridGeom {
+    const uint32_t *grid;
+    int w, h, d;
+    int log_brick;      // brick edge E = 1 << log_brick
+    int drop_last_z;    // 1: voxels at z == d-1 are excluded from the output
+    int log_block;      // cache-block edge M = 1 << log_block
+    uint8_t *topflag;   // per M-block "has any voxel" (Morton-indexed), or null
+};
+
+// Phase 1a: per brick, count voxels that survive (V') and flag M-blocks that
+// hold any voxel (V).  One CTA per brick; consecutive threads read
+// consecutive x so each warp load covers whole 32-byte sectors of a row.
+__global__ void __launch_bounds__(kBrickThreads) k_brick_count(GridGeom g, uint64_t n_bricks, uint32_t *__restrict__ counts) {
+    const int lb = g.log_brick;
+    const int E = 1 << lb;
+    const int cells = E * E * E;
+    for (uint64_t b = blockIdx.x; b < n_bricks; b += gridDim.x) {
+        uint32_t bx = compact3(b), by = compact3(b >> 1), bz = compact3(b >> 2);
+        int gx0 = (int)(bx << lb), gy0 = (int)(by << lb), gz0 = (int)(bz << lb);
+        uint32_t cnt = 0, any = 0;
+        if (gx0 < g.w && gy0 < g.h && gz0 < g.d) {
+            for (int c = threadIdx.x; c < cells; c += kBrickThreads) {
+                int gx = gx0 + (c & (E - 1)), gy = gy0 + ((c >> lb) & (E - 1)), gz = gz0 + (c >> (2 * lb));
+                if (gx < g.w && gy < g.h && gz < g.d) {
+                    uint32_t v = __ldg(g.grid + (uint64_t)gx + (uint64_t)g.w * ((uint64_t)gy + (uint64_t)g.h * gz));
+                    if (v) {
+                        any = 1;
+                        if (!(g.drop_last_z && gz == g.d - 1)) ++cnt;
+                        if (g.topflag && g.log_block < lb)
+                            g.topflag[morton3((uint32_t)gx >> g.log_block, (uint32_t)gy >> g.log_block,
+                                              (uint32_t)gz >> g.log_block)] = 1;
+                    }
+                }
+            }
+        }
+        uint32_t total;
+        block_excl_scan<uint32_t>(cnt, &total);
+        int block_any = __syncthreads_or(any);
+        if (threadIdx.x == 0) {
+            counts[b] = total;
+            if (block_any && g.topflag && g.log_block >= lb)
+                g.topflag[b >> (3 * (g.log_block - lb))] = 1;
+        }
+    }
+}
+
+// Phase 1b: emit (key, payload) for V' in Morton order.  The brick is staged
+// in shared memory with coalesced row reads, then each thread walks a run of
+// consecutive local Morton codes.
+__global__ void __launch_bounds__(kBrickThreads) k_brick_emit(GridGeom g, uint64_t n_bricks, const uint32_t *__restrict__ counts,
+                                                            const uint64_t *__restrict__ offsets,
+                                                            uint64_t *__restrict__ keys, uint32_t *__restrict__ payload) {
+    __shared__ uint32_t tile[16 * 16 * 16];
+    const int E = 1 << g.log_brick;
+    const int cells = E * E * E;
+    const int per = (cells + kBrickThreads - 1) / kBrickThreads;
+    for (uint64_t b = blockIdx.x; b < n_bricks; b += gridDim.x) {
+        if (counts[b] == 0) continue;  // uniform across the CTA
+        uint32_t bx = compact3(b), by = compact3(b >> 1), bz = compact3(b >> 2);
+        int gx0 = (int)(bx << g.log_brick), gy0 = (int)(by << g.log_brick), gz0 = (int)(bz << g.log_brick);
+        for (int c = threadIdx.x; c < cells; c += kBrickThreads) {
+            int gx = gx0 + (c & (E - 1)), gy = gy0 + ((c >> g.log_brick) & (E - 1)), gz = gz0 + (c >> (2 * g.log_brick));
+            uint32_t v = 0;
+            if (gx < g.w && gy < g.h && gz < g.d && !(g.drop_last_z && gz == g.d - 1))
+                v = __ldg(g.grid + (uint64_t)gx + (uint64_t)g.w * ((uint64_t)gy + (uint64_t)g.h * gz));
+            tile[c] = v;
+        }
+        __syncthreads();
+        uint32_t cnt = 0;
+        int m0 = threadIdx.x * per;
+        for (int k = 0; k < per; ++k) {
+            int m = m0 + k;
+            if (m < cells) {
+                uint32_t lx = compact3((uint64_t)m), ly = compact3((uint64_t)m >> 1), lz = compact3((uint64_t)m >> 2);
+                cnt += tile[lx + E * (ly + E * lz)] != 0;
+            }
+        }
+        uint32_t total;
+        uint32_t pre = block_excl_scan<uint32_t>(cnt, &total);
+        uint64_t out = offsets[b] + pre;
+        uint64_t kbase = b << (3 * g.log_brick);
+        for (int k = 0; k < per; ++k) {
+            int m = m0 + k;
+            if (m < cells) {
+                uint32_t lx = compact3((uint64_t)m), ly = compact3((uint64_t)m >> 1), lz = compact3((uint64_t)m >> 2);
+                uint32_t v = tile[lx + E * (ly + E * lz)];
+                if (v) {
+                    keys[out] = kbase | (uint64_t)m;
+                    payload[out] = v;
+                    ++out;
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---- level grouping --------------------------------------------------------
+
+__global__ void k_heads(const uint64_t *__restrict__ key, uint64_t n, uint32_t *__restrict__ head) {
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    head[i] = (i == 0 || (key[i] >> 3) != (key[i - 1] >> 3)) ? 1u : 0u;
+}
+
+__global__ void k_parents_from_heads(const uint64_t *__restrict__ ckey, uint64_t n, const uint32_t *__restrict__ head,
+                                     const uint32_t *__restrict__ pidx, uint64_t *__restrict__ pkey,
+                                     uint32_t *__restrict__ pstart) {
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !head[i]) return;
+    uint32_t p = pidx[i];
+    pkey[p] = ckey[i] >> 3;
+    pstart[p] = (uint32_t)i;
+}
+
+// Dense grouping at the cache-block level: blk_first[b] = first child of
+// block b (or 0xFFFFFFFF); present = has children or top flag.
+__global__ void k_block_first(const uint64_t *__restrict__ ckey, uint64_t n, const uint32_t *__restrict__ head,
+                              uint32_t *__restrict__ blk_first) {
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !head[i]) return;
+    blk_first[ckey[i] >> 3] = (uint32_t)i;
+}
+
+__global__ void k_block_present(const uint32_t *__restrict__ blk_first, const uint8_t *__restrict__ topflag,
+                                uint64_t nb, uint32_t *__restrict__ present) {
+    uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    present[b] = (blk_first[b] != 0xFFFFFFFFu || topflag[b]) ? 1u : 0u;
+}
+
+__global__ void k_block_parents(const uint32_t *__restrict__ blk_first, const uint32_t *__restrict__ present,
+                                const uint32_t *__restrict__ bidx, uint64_t nb, uint64_t n_child,
+                                uint64_t *__restrict__ pkey, uint32_t *__restrict__ pstart) {
+    uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb || !present[b]) return;
+    uint32_t p = bidx[b];
+    pkey[p] = b;
+    pstart[p] = blk_first[b] != 0xFFFFFFFFu ? blk_first[b] : (uint32_t)n_child;
+}
+
+__global__ void k_child_pidx_from_blocks(const uint64_t *__restrict__ ckey, uint64_t n, const uint32_t *__restrict__ bidx,
+                                         uint32_t *__restrict__ pidx) {
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    pidx[i] = bidx[ckey[i] >> 3];
+}
+
+// Per parent: valid mask and child count from its run of children.
+__global__ void k_parent_masks(const uint64_t *__restrict__ pkey, const uint32_t *__restrict__ pstart, uint64_t np,
+                               const uint64_t *__restrict__ ckey, uint64_t nc, uint8_t *__restrict__ mask,
+                               uint8_t *__restrict__ count) {
+    uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    uint64_t k = pkey[p];
+    uint32_t m = 0, c = 0;
+    for (uint64_t i = pstart[p]; i < nc && c < 8 && (ckey[i] >> 3) == k; ++i, ++c) m |= 1u << (ckey[i] & 7);
+    mask[p] = (uint8_t)m;
+    count[p] = (uint8_t)c;
+}
+
+// ---- subtree sizes and far-pointer decisions (bottom-up) -------------------
+
+__global__ void k_subtree(uint64_t np, const uint8_t *__restrict__ count, const uint32_t *__restrict__ pstart,
+                          const uint64_t *__restrict__ childS, int bottom, uint64_t *__restrict__ S,
+                          uint8_t *__restrict__ large) {
+    uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    uint32_t k = count[p];
+    if (bottom) {
+        S[p] = k;
+        large[p] = 0;
+        return;
+    }
+    uint64_t run = 0;
+    bool far = false;
+    uint32_t s0 = pstart[p];
+    for (uint32_t i = 0; i < k; ++i) {
+        if ((uint64_t)(k - i) + run > 0x3FFFull) far = true;
+        run += childS[s0 + i];
+    }
+    S[p] = (uint64_t)k * (far ? 2u : 1u) + run;
+    large[p] = far ? 1 : 0;
+}
+
+// ---- placement (top-down) ---------------------------------------------------
+
+__global__ void k_root_word(const uint8_t *__restrict__ mask, const uint8_t *__restrict__ large, int root_is_bottom,
+                            uint32_t *__restrict__ words) {
+    uint32_t m = mask[0];
+    words[0] = (m << 8) | (root_is_bottom ? 0u : m) | (large[0] ? 0x10000u : 0u) | (1u << 18);
+}
+
+// Parents at one level place their (internal) children and write the
+// children's descriptors; child_is_bottom selects leafMask = 0.
+__global__ void k_place(uint64_t np, const uint8_t *__restrict__ count, const uint32_t *__restrict__ pstart,
+                        const uint8_t *__restrict__ plarge, const uint64_t *__restrict__ pB,
+                        const uint64_t *__restrict__ cS, const uint8_t *__restrict__ cmask,
+                        const uint8_t *__restrict__ clarge, int child_is_bottom, uint64_t *__restrict__ cB,
+                        uint32_t *__restrict__ words) {
+    uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    uint32_t k = count[p];
+    bool far = plarge[p] != 0;
+    uint64_t stride = far ? 2 : 1;
+    uint64_t B = pB[p];
+    uint64_t run = 0;
+    uint32_t s0 = pstart[p];
+    for (uint32_t i = 0; i < k; ++i) {
+        uint32_t c = s0 + i;
+        uint64_t pos = B + (uint64_t)i * stride;
+        uint64_t blk = B + (uint64_t)k * stride + run;
+        run += cS[c];
+        cB[c] = blk;
+        uint64_t off = blk - pos;
+        uint32_t m = cmask[c];
+        uint32_t w = (m << 8) | (child_is_bottom ? 0u : m) | (clarge[c] ? 0x10000u : 0u);
+        if (far) {
+            w |= 0x20000u | (uint32_t)((off >> 32) << 18);
+            words[pos + 1] = (uint32_t)off;
+        } else {
+            w |= (uint32_t)(off << 18);
+        }
+        words[pos] = w;
+    }
+}
+
+__global__ void k_place_leaves(uint64_t n, const uint32_t *__restrict__ pidx, const uint32_t *__restrict__ pstart,
+                               const uint64_t *__restrict__ pB, const uint32_t *__restrict__ payload,
+                               uint32_t *__restrict__ words) {
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t p = pidx[i];
+    words[pB[p] + (i - pstart[p])] = payload[i];
+}
+
+__global__ void k_set_u64(uint64_t *p, uint64_t v) { *p = v; }
+
+inline unsigned blocks_for(uint64_t n, int t = 256) { return (unsigned)((n + t - 1) / t); }
+
+// Stream-ordered temporary buffer.
+template <typename T>
+struct DevBuf {
+    T *p = nullptr;
+    cudaStream_t st = nullptr;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    cudaError_t alloc(uint64_t n, cudaStream_t s) {
+        st = s;
+        return cudaMallocAsync((void **)&p, (size_t)(n ? n : 1) * sizeof(T), s);
+    }
+    void release() {
+        if (p) cudaFreeAsync(p, st);
+        p = nullptr;
+    }
+    ~DevBuf() { release(); }
+};
+
+struct LevelArrays {
+    uint64_t n = 0;
+    DevBuf<uint64_t> key;
+    DevBuf<uint32_t> start;
+    DevBuf<uint8_t> mask, count, large;
+    DevBuf<uint64_t> S, B;
+};
+
+#define SVO_TRY_ALLOC(expr)                                                   \
+    do {                                                                      \
+        cudaError_t _e = (expr);                                              \
+        if (_e != cudaSuccess) return ::svo::cuda_fail(_e, "device allocation in build"); \
+    } while (0)
+
+template <typename TO>
+int scan_to(const uint32_t *in, TO *out, uint64_t n, TO *total_host, cudaStream_t st) {
+    DevBuf<TO> scratch, tot;
+    SVO_TRY_ALLOC(scratch.alloc(scan_scratch_elems(n), st));
+    SVO_TRY_ALLOC(tot.alloc(1, st));
+    SVO_CUDA_TRY((exclusive_scan<uint32_t, TO>(in, out, n, tot.p, scratch.p, st)));
+    SVO_CUDA_TRY(cudaMemcpyAsync(total_host, tot.p, sizeof(TO), cudaMemcpyDeviceToHost, st));
+    SVO_CUDA_TRY(cudaStreamSynchronize(st));
+    return SVO_OK;
+}
+
+}  // namespace
+
+int build_dense_device(const uint32_t *d_grid, int w, int h, int d, int log_side, int log_block, cudaStream_t st,
+                       uint32_t **d_words_out, uint64_t *n_words_out) {
+    const int D = log_side;
+    const int log_brick = D < 4 ? D : 4;
+    const uint64_t n_bricks = 1ull << (3 * (D - log_brick));
+    const bool multi_block = log_block < D;
+
+    GridGeom g;
+    g.grid = d_grid;
+    g.w = w;
+    g.h = h;
+    g.d = d;
+    g.log_brick = log_brick;
+    g.drop_last_z = ((d & 1) && log_block >= 2) ? 1 : 0;
+    g.log_block = log_block;
+    g.topflag = nullptr;
+
+    const uint64_t n_blocks = multi_block ? (1ull << (3 * (D - log_block))) : 0;
+    if (n_blocks > (1ull << 27))
+        return set_error(SVO_ERR_LIMIT, "memory budget gives %llu cache blocks; the GPU build supports at most 2^27",
+                         (unsigned long long)n_blocks);
+    DevBuf<uint8_t> topflag;
+    if (multi_block) {
+        SVO_TRY_ALLOC(topflag.alloc(n_blocks, st));
+        SVO_CUDA_TRY(cudaMemsetAsync(topflag.p, 0, n_blocks, st));
+        g.topflag = topflag.p;
+    }
+
+    // Phase 1: extraction in Morton order.
+    DevBuf<uint32_t> bcount;
+    DevBuf<uint64_t> boff;
+    SVO_TRY_ALLOC(bcount.alloc(n_bricks, st));
+    SVO_TRY_ALLOC(boff.alloc(n_bricks, st));
+    unsigned grid1 = (unsigned)(n_bricks < (1ull << 20) ? n_bricks : (1ull << 20));
+    k_brick_count<<<grid1, kBrickThreads, 0, st>>>(g, n_bricks, bcount.p);
+    SVO_CUDA_TRY(cudaGetLastError());
+    uint64_t N = 0;
+    int rc = scan_to<uint64_t>(bcount.p, boff.p, n_bricks, &N, st);
+    if (rc) return rc;
+    if (N >= 0xFFFFFFFFull) return set_error(SVO_ERR_LIMIT, "%llu occupied voxels exceed 2^32-1", (unsigned long long)N);
+
+    DevBuf<uint64_t> lkey;
+    DevBuf<uint32_t> lpay;
+    SVO_TRY_ALLOC(lkey.alloc(N, st));
+    SVO_TRY_ALLOC(lpay.alloc(N, st));
+    if (N) {
+        k_brick_emit<<<grid1, kBrickThreads, 0, st>>>(g, n_bricks, bcount.p, boff.p, lkey.p, lpay.p);
+        SVO_CUDA_TRY(cudaGetLastError());
+    }
+    bcount.release();
+    boff.release();
+
+    // Phase 2: levels e = 1..D (node edge 2^e); level 0 is the leaves.
+    std::vector<LevelArrays> lv(D + 1);
+    DevBuf<uint32_t> leaf_pidx;
+    const uint64_t *ckey = lkey.p;
+    uint64_t nc = N;
+    for (int e = 1; e <= D; ++e) {
+        LevelArrays &L = lv[e];
+        DevBuf<uint32_t> head, pidx;
+        SVO_TRY_ALLOC(head.alloc(nc, st));
+        SVO_TRY_ALLOC(pidx.alloc(nc, st));
+        if (nc) {
+            k_heads<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, head.p);
+            SVO_CUDA_TRY(cudaGetLastError());
+        }
+        if (multi_block && e == log_block) {
+            // Dense grouping over cache blocks, adding blocks that only the top
+            // lookup table marks (descriptors without children).
+            DevBuf<uint32_t> first, present, bidx;
+            SVO_TRY_ALLOC(first.alloc(n_blocks, st));
+            SVO_TRY_ALLOC(present.alloc(n_blocks, st));
+            SVO_TRY_ALLOC(bidx.alloc(n_blocks, st));
+            SVO_CUDA_TRY(cudaMemsetAsync(first.p, 0xFF, n_blocks * sizeof(uint32_t), st));
+            if (nc) k_block_first<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, head.p, first.p);
+            k_block_present<<<blocks_for(n_blocks), 256, 0, st>>>(first.p, topflag.p, n_blocks, present.p);
+            SVO_CUDA_TRY(cudaGetLastError());
+            uint32_t np = 0;
+            rc = scan_to<uint32_t>(present.p, bidx.p, n_blocks, &np, st);
+            if (rc) return rc;
+            L.n = np;
+            SVO_TRY_ALLOC(L.key.alloc(np, st));
+            SVO_TRY_ALLOC(L.start.alloc(np, st));
+            k_block_parents<<<blocks_for(n_blocks), 256, 0, st>>>(first.p, present.p, bidx.p, n_blocks, nc, L.key.p,
+                                                                  L.start.p);
+            if (nc) k_child_pidx_from_blocks<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, bidx.p, pidx.p);
+            SVO_CUDA_TRY(cudaGetLastError());
+        } else {
+            uint32_t np = 0;
+            rc = scan_to<uint32_t>(head.p, pidx.p, nc, &np, st);
+            if (rc) return rc;
+            L.n = np;
+            SVO_TRY_ALLOC(L.key.alloc(np, st));
+            SVO_TRY_ALLOC(L.start.alloc(np, st));
+            if (nc) {
+                k_parents_from_heads<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, head.p, pidx.p, L.key.p, L.start.p);
+                SVO_CUDA_TRY(cudaGetLastError());
+            }
+        }
+        // The root always exists, even over an empty grid.
+        if (e == D && L.n == 0) {
+            L.n = 1;
+            SVO_TRY_ALLOC(L.key.alloc(1, st));
+            SVO_TRY_ALLOC(L.start.alloc(1, st));
+            SVO_CUDA_TRY(cudaMemsetAsync(L.key.p, 0, sizeof(uint64_t), st));
+            SVO_CUDA_TRY(cudaMemsetAsync(L.start.p, 0, sizeof(uint32_t), st));
+        }
+        SVO_TRY_ALLOC(L.mask.alloc(L.n, st));
+        SVO_TRY_ALLOC(L.count.alloc(L.n, st));
+        k_parent_masks<<<blocks_for(L.n), 256, 0, st>>>(L.key.p, L.start.p, L.n, ckey, nc, L.mask.p, L.count.p);
+        SVO_CUDA_TRY(cudaGetLastError());
+        if (e == 1) {
+            leaf_pidx.p = pidx.p;
+            leaf_pidx.st = st;
+            pidx.p = nullptr;
+        }
+        ckey = L.key.p;
+        nc = L.n;
+    }
+    lkey.release();
+
+    // Subtree sizes, bottom-up.
+    for (int e = 1; e <= D; ++e) {
+        LevelArrays &L = lv[e];
+        SVO_TRY_ALLOC(L.S.alloc(L.n, st));
+        SVO_TRY_ALLOC(L.large.alloc(L.n, st));
+        k_subtree<<<blocks_for(L.n), 256, 0, st>>>(L.n, L.count.p, L.start.p, e > 1 ? lv[e - 1].S.p : nullptr,
+                                                  e == 1, L.S.p, L.large.p);
+        SVO_CUDA_TRY(cudaGetLastError());
+    }
+    uint64_t S_root = 0;
+    SVO_CUDA_TRY(cudaMemcpyAsync(&S_root, lv[D].S.p, sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+    SVO_CUDA_TRY(cudaStreamSynchronize(st));
+    const uint64_t W = 1 + S_root;
+    if (W > 0xFFFFFFFFull)
+        return set_error(SVO_ERR_LIMIT, "octree of %llu words exceeds 2^32-1", (unsigned long long)W);
+
+    uint32_t *words = nullptr;
+    SVO_CUDA_TRY(cudaMallocAsync((void **)&words, (size_t)W * sizeof(uint32_t), st));
+
+    // Placement, top-down.
+    SVO_TRY_ALLOC(lv[D].B.alloc(1, st));
+    k_set_u64<<<1, 1, 0, st>>>(lv[D].B.p, 1);
+    k_root_word<<<1, 1, 0, st>>>(lv[D].mask.p, lv[D].large.p, D == 1, words);
+    for (int e = D; e >= 2; --e) {
+        LevelArrays &P = lv[e];
+        LevelArrays &C = lv[e - 1];
+        SVO_TRY_ALLOC(C.B.alloc(C.n, st));
+        k_place<<<blocks_for(P.n), 256, 0, st>>>(P.n, P.count.p, P.start.p, P.large.p, P.B.p, C.S.p, C.mask.p,
+                                                C.large.p, e - 1 == 1, C.B.p, words);
+        SVO_CUDA_TRY(cudaGetLastError());
+    }
+    if (N) {
+        k_place_leaves<<<blocks_for(N), 256, 0, st>>>(N, leaf_pidx.p, lv[1].start.p, lv[1].B.p, lpay.p, words);
+        SVO_CUDA_TRY(cudaGetLastError());
+    }
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        cudaFree(words);
+        return cuda_fail(e, "octree build");
+    }
+    *d_words_out = words;
+    *n_words_out = W;
+    return SVO_OK;
+}
+
+}  // namespace svo

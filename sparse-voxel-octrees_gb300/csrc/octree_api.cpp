@@ -1,0 +1,432 @@
+// octree_api.cpp — the C ABI (include/svo.h): handle lifetime, .oct and
+// .voxel I/O, build and trace entry points, validation, errors.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <thread>
+
+#include "svo_internal.h"
+
+namespace svo {
+
+namespace {
+thread_local std::string g_last_error;
+constexpr uint64_t kOctBlock = 64ull * 1024 * 1024;  // VoxelOctree.cpp:55
+constexpr uint64_t kStageRays = 1ull << 21;          // rays per staging chunk
+}  // namespace
+
+int set_error(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what) {
+    return set_error(SVO_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+void clear_error() { g_last_error.clear(); }
+
+// Util.hpp:102-106
+static int round_to_pow2(int x) {
+    int y;
+    for (y = 1; y < x; y *= 2) {
+    }
+    return y;
+}
+
+static int log2_exact(uint64_t v) {
+    int r = 0;
+    while ((1ull << r) < v) ++r;
+    return r;
+}
+
+static uint64_t pyramid_cells(int levels) {  // VoxelData.cpp:65-74
+    uint64_t r = 0, s = 1;
+    for (int i = 0; i < levels; ++i) {
+        r += s;
+        s *= 8;
+    }
+    return r;
+}
+
+int cache_block_log2(int w, int h, int d, uint64_t mem, uint64_t cell_cost) {
+    int side = std::max(round_to_pow2(w), std::max(round_to_pow2(h), round_to_pow2(d)));
+    int hb = log2_exact((uint64_t)side);
+    int largest = -1;
+    for (int i = hb; i >= 0; --i) {  // VoxelData.cpp:221-235
+        int low = hb - i;
+        uint64_t cost = pyramid_cells(i + 1) + pyramid_cells(low) + ((uint64_t)1 << (uint64_t)(low * 3)) * cell_cost;
+        if (cost < mem) largest = hb - i;
+    }
+    return largest;
+}
+
+int make_handle(uint32_t *d_words, uint64_t n_words, const float center[3], svo_octree **out) {
+    std::unique_ptr<svo_octree> h(new svo_octree());
+    h->d_words = d_words;
+    h->n_words = n_words;
+    std::memcpy(h->center, center, sizeof(h->center));
+    cudaGetDevice(&h->device);
+    cudaError_t e = cudaMalloc((void **)&h->d_status, sizeof(uint32_t));
+    if (e != cudaSuccess) {
+        cudaFree(d_words);
+        h->d_words = nullptr;
+        return cuda_fail(e, "cudaMalloc(status)");
+    }
+    e = cudaMemset(h->d_status, 0, sizeof(uint32_t));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemset(status)");
+    *out = h.release();
+    return SVO_OK;
+}
+
+static int upload_words(const uint32_t *words, uint64_t n, const float center[3], svo_octree **out) {
+    if (n == 0) return set_error(SVO_ERR_FORMAT, "octree has no words");
+    if (n > 0xFFFFFFFFull) return set_error(SVO_ERR_LIMIT, "octree of %llu words exceeds 2^32-1", (unsigned long long)n);
+    uint32_t *d = nullptr;
+    SVO_CUDA_TRY(cudaMalloc((void **)&d, n * sizeof(uint32_t)));
+    cudaError_t e = cudaMemcpy(d, words, n * sizeof(uint32_t), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(d);
+        return cuda_fail(e, "upload octree words");
+    }
+    return make_handle(d, n, center, out);
+}
+
+static int ensure_staging(svo_octree *oct, size_t dev_bytes) {
+    if (oct->stage_dev_bytes >= dev_bytes) return SVO_OK;
+    if (oct->stage_dev) cudaFree(oct->stage_dev);
+    oct->stage_dev = nullptr;
+    oct->stage_dev_bytes = 0;
+    SVO_CUDA_TRY(cudaMalloc(&oct->stage_dev, dev_bytes));
+    oct->stage_dev_bytes = dev_bytes;
+    for (auto &s : oct->stage_streams)
+        if (!s) SVO_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    return SVO_OK;
+}
+
+static int check_device_status(const svo_octree *oct) {
+    uint32_t flags = 0;
+    SVO_CUDA_TRY(cudaMemcpy(&flags, oct->d_status, sizeof(flags), cudaMemcpyDeviceToHost));
+    if (flags) {
+        cudaMemset(oct->d_status, 0, sizeof(uint32_t));
+        return set_error(SVO_ERR_DEVICE, "a ray hit the traversal step cap or an out-of-range word index "
+                                         "(corrupt octree?)");
+    }
+    return SVO_OK;
+}
+
+}  // namespace svo
+
+using namespace svo;
+
+extern "C" {
+
+const char *svo_last_error(void) { return g_last_error.c_str(); }
+
+int svo_version(void) { return 100; }
+
+void svo_free(void *p) { free(p); }
+
+int svo_oct_read(const char *path, uint32_t **words_out, uint64_t *n_out, float center[3]) {
+    if (!path || !words_out || !n_out || !center) return set_error(SVO_ERR_INVALID, "null argument");
+    FILE *fp = fopen(path, "rb");
+    if (!fp) return set_error(SVO_ERR_IO, "cannot open %s", path);
+    std::unique_ptr<FILE, int (*)(FILE *)> guard(fp, fclose);
+    uint64_t n = 0;
+    if (fread(center, sizeof(float), 3, fp) != 3 || fread(&n, sizeof(uint64_t), 1, fp) != 1)
+        return set_error(SVO_ERR_FORMAT, "%s: truncated header", path);
+    if (n == 0 || n > (1ull << 36))
+        return set_error(n ? SVO_ERR_LIMIT : SVO_ERR_FORMAT, "%s: unsupported word count %llu", path,
+                         (unsigned long long)n);
+    uint32_t *words = (uint32_t *)malloc(n * sizeof(uint32_t));
+    if (!words) return set_error(SVO_ERR_MEMORY, "cannot allocate %llu words", (unsigned long long)n);
+    std::unique_ptr<uint32_t, void (*)(void *)> wguard(words, free);
+    std::vector<uint8_t> comp;
+    uint8_t *dst = reinterpret_cast<uint8_t *>(words);
+    for (uint64_t off = 0; off < n * 4; off += kOctBlock) {
+        uint64_t csize = 0;
+        if (fread(&csize, sizeof(uint64_t), 1, fp) != 1)
+            return set_error(SVO_ERR_FORMAT, "%s: truncated block header", path);
+        if (csize > lz4_compress_bound(kOctBlock)) return set_error(SVO_ERR_FORMAT, "%s: bad block size", path);
+        comp.resize(csize);
+        if (fread(comp.data(), 1, csize, fp) != csize) return set_error(SVO_ERR_FORMAT, "%s: truncated block", path);
+        uint64_t out_len = std::min<uint64_t>(n * 4 - off, kOctBlock);
+        if (lz4_decompress_block(comp.data(), csize, dst, off, out_len) != 0)
+            return set_error(SVO_ERR_FORMAT, "%s: corrupt LZ4 block at payload offset %llu", path,
+                             (unsigned long long)off);
+    }
+    *words_out = wguard.release();
+    *n_out = n;
+    return SVO_OK;
+}
+
+int svo_oct_write(const char *path, const uint32_t *words, uint64_t n_words, const float center[3]) {
+    if (!path || !words || !center || n_words == 0) return set_error(SVO_ERR_INVALID, "bad argument");
+    const uint64_t bytes = n_words * 4;
+    const uint64_t nblocks = (bytes + kOctBlock - 1) / kOctBlock;
+    // Blocks are independent, so they compress in parallel.
+    std::vector<std::vector<uint8_t>> comp(nblocks);
+    std::vector<size_t> csize(nblocks, 0);
+    auto work = [&](uint64_t b) {
+        uint64_t off = b * kOctBlock;
+        size_t len = (size_t)std::min<uint64_t>(bytes - off, kOctBlock);
+        comp[b].resize(lz4_compress_bound(len));
+        csize[b] = lz4_compress_block(reinterpret_cast<const uint8_t *>(words) + off, len, comp[b].data(),
+                                      comp[b].size());
+    };
+    unsigned nt = std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), (unsigned)nblocks));
+    std::vector<std::thread> pool;
+    for (unsigned t = 0; t < nt; ++t)
+        pool.emplace_back([&, t] {
+            for (uint64_t b = t; b < nblocks; b += nt) work(b);
+        });
+    for (auto &th : pool) th.join();
+    FILE *fp = fopen(path, "wb");
+    if (!fp) return set_error(SVO_ERR_IO, "cannot create %s", path);
+    std::unique_ptr<FILE, int (*)(FILE *)> guard(fp, fclose);
+    bool ok = fwrite(center, sizeof(float), 3, fp) == 3 && fwrite(&n_words, sizeof(uint64_t), 1, fp) == 1;
+    for (uint64_t b = 0; ok && b < nblocks; ++b) {
+        uint64_t cs = csize[b];
+        ok = fwrite(&cs, sizeof(uint64_t), 1, fp) == 1 && fwrite(comp[b].data(), 1, cs, fp) == cs;
+    }
+    if (!ok) return set_error(SVO_ERR_IO, "write to %s failed", path);
+    return SVO_OK;
+}
+
+int svo_octree_load(const char *path, svo_octree **out) {
+    if (!path || !out) return set_error(SVO_ERR_INVALID, "null argument");
+    uint32_t *words = nullptr;
+    uint64_t n = 0;
+    float center[3];
+    int rc = svo_oct_read(path, &words, &n, center);
+    if (rc) return rc;
+    std::unique_ptr<uint32_t, void (*)(void *)> wguard(words, free);
+    return upload_words(words, n, center, out);
+}
+
+int svo_octree_save(const svo_octree *oct, const char *path) {
+    if (!oct || !path) return set_error(SVO_ERR_INVALID, "null argument");
+    std::vector<uint32_t> words(oct->n_words);
+    SVO_CUDA_TRY(cudaMemcpy(words.data(), oct->d_words, oct->n_words * 4, cudaMemcpyDeviceToHost));
+    return svo_oct_write(path, words.data(), oct->n_words, oct->center);
+}
+
+int svo_octree_from_words(const uint32_t *words, uint64_t n_words, const float center[3], svo_octree **out) {
+    if (!words || !center || !out) return set_error(SVO_ERR_INVALID, "null argument");
+    return upload_words(words, n_words, center, out);
+}
+
+int svo_octree_destroy(svo_octree *oct) {
+    if (!oct) return SVO_OK;
+    if (oct->d_words) cudaFree(oct->d_words);
+    if (oct->d_status) cudaFree(oct->d_status);
+    if (oct->stage_dev) cudaFree(oct->stage_dev);
+    for (auto &s : oct->stage_streams)
+        if (s) cudaStreamDestroy(s);
+    delete oct;
+    return SVO_OK;
+}
+
+int svo_octree_num_words(const svo_octree *oct, uint64_t *n) {
+    if (!oct || !n) return set_error(SVO_ERR_INVALID, "null argument");
+    *n = oct->n_words;
+    return SVO_OK;
+}
+
+int svo_octree_copy_words(const svo_octree *oct, uint32_t *dst, uint64_t n) {
+    if (!oct || !dst) return set_error(SVO_ERR_INVALID, "null argument");
+    if (n != oct->n_words) return set_error(SVO_ERR_INVALID, "destination holds %llu words, octree has %llu",
+                                            (unsigned long long)n, (unsigned long long)oct->n_words);
+    SVO_CUDA_TRY(cudaMemcpy(dst, oct->d_words, n * 4, cudaMemcpyDeviceToHost));
+    return SVO_OK;
+}
+
+int svo_octree_device_words(const svo_octree *oct, const uint32_t **d_words) {
+    if (!oct || !d_words) return set_error(SVO_ERR_INVALID, "null argument");
+    *d_words = oct->d_words;
+    return SVO_OK;
+}
+
+int svo_octree_center(const svo_octree *oct, float center[3]) {
+    if (!oct || !center) return set_error(SVO_ERR_INVALID, "null argument");
+    std::memcpy(center, oct->center, sizeof(oct->center));
+    return SVO_OK;
+}
+
+int svo_octree_device_status(svo_octree *oct, uint32_t *flags) {
+    if (!oct || !flags) return set_error(SVO_ERR_INVALID, "null argument");
+    SVO_CUDA_TRY(cudaMemcpy(flags, oct->d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    SVO_CUDA_TRY(cudaMemset(oct->d_status, 0, sizeof(uint32_t)));
+    return SVO_OK;
+}
+
+int svo_octree_validate(const svo_octree *oct, uint64_t *n_desc, uint64_t *n_leaves) {
+    if (!oct) return set_error(SVO_ERR_INVALID, "null argument");
+    const uint64_t n = oct->n_words;
+    std::vector<uint32_t> w(n);
+    SVO_CUDA_TRY(cudaMemcpy(w.data(), oct->d_words, n * 4, cudaMemcpyDeviceToHost));
+    // Iterative walk: (descriptor index, depth).  Child blocks always follow
+    // their parent (offset >= 1), so the walk terminates.
+    std::vector<std::pair<uint64_t, int>> stack;
+    stack.push_back({0, 0});
+    uint64_t nd = 0, nl = 0;
+    while (!stack.empty()) {
+        uint64_t p = stack.back().first;
+        int depth = stack.back().second;
+        stack.pop_back();
+        if (p >= n) return set_error(SVO_ERR_FORMAT, "descriptor index %llu out of range", (unsigned long long)p);
+        if (depth > 22) return set_error(SVO_ERR_FORMAT, "octree deeper than 23 levels at %llu", (unsigned long long)p);
+        ++nd;
+        uint32_t d = w[p];
+        uint32_t valid = (d >> 8) & 0xFF, nonleaf = d & 0xFF;
+        if (nonleaf & ~valid) return set_error(SVO_ERR_FORMAT, "descriptor %llu: non-leaf bit outside valid mask",
+                                               (unsigned long long)p);
+        uint64_t off = d >> 18;
+        if (d & 0x20000u) {
+            if (p + 1 >= n) return set_error(SVO_ERR_FORMAT, "far word of %llu out of range", (unsigned long long)p);
+            off = (off << 32) | w[p + 1];
+        }
+        if (valid == 0) continue;
+        if (off == 0) return set_error(SVO_ERR_FORMAT, "descriptor %llu: zero child offset", (unsigned long long)p);
+        uint64_t base = p + off;
+        uint64_t stride = (d & 0x10000u) ? 2 : 1;
+        // Slots in descending octant order; leaves index by valid bits,
+        // internal children by non-leaf bits (VoxelOctree.cpp:282, :290-293).
+        for (int i = 0; i < 8; ++i) {
+            uint32_t bit = 128u >> i;
+            if (!(valid & bit)) continue;
+            uint32_t higher = (uint32_t)__builtin_popcount(valid & (bit - 1));
+            if (nonleaf & bit) {
+                uint32_t sib = (uint32_t)__builtin_popcount(nonleaf & (bit - 1));
+                stack.push_back({base + sib * stride, depth + 1});
+            } else {
+                if (base + higher >= n) return set_error(SVO_ERR_FORMAT, "leaf of %llu out of range",
+                                                         (unsigned long long)p);
+                ++nl;
+            }
+        }
+    }
+    if (n_desc) *n_desc = nd;
+    if (n_leaves) *n_leaves = nl;
+    return SVO_OK;
+}
+
+int svo_octree_build_dense(const uint32_t *grid, int w, int h, int d, uint64_t mem, int grid_on_device,
+                           svo_stream stream, svo_octree **out) {
+    if (!grid || !out || w <= 0 || h <= 0 || d <= 0) return set_error(SVO_ERR_INVALID, "bad grid arguments");
+    int side = std::max(round_to_pow2(w), std::max(round_to_pow2(h), round_to_pow2(d)));
+    if (side < 2) return set_error(SVO_ERR_INVALID, "virtual side %d below 2 (the reference recurses forever)", side);
+    if (side > 65536) return set_error(SVO_ERR_LIMIT, "virtual side %d above 65536", side);
+    int lb = cache_block_log2(w, h, d, mem, 4);
+    if (lb < 1) return set_error(SVO_ERR_MEMORY, "memory budget %llu admits no cache block", (unsigned long long)mem);
+    cudaStream_t st = (cudaStream_t)stream;
+    const uint32_t *dg = grid;
+    uint32_t *owned = nullptr;
+    const uint64_t cells = (uint64_t)w * h * d;
+    if (!grid_on_device) {
+        SVO_CUDA_TRY(cudaMalloc((void **)&owned, cells * 4));
+        cudaError_t e = cudaMemcpyAsync(owned, grid, cells * 4, cudaMemcpyHostToDevice, st);
+        if (e != cudaSuccess) {
+            cudaFree(owned);
+            return cuda_fail(e, "upload grid");
+        }
+        dg = owned;
+    }
+    uint32_t *dw = nullptr;
+    uint64_t nw = 0;
+    int rc = build_dense_device(dg, w, h, d, log2_exact((uint64_t)side), lb, st, &dw, &nw);
+    if (owned) cudaFree(owned);
+    if (rc) return rc;
+    float center[3] = {(float)w * 0.5f / (float)side, (float)h * 0.5f / (float)side, (float)d * 0.5f / (float)side};
+    return make_handle(dw, nw, center, out);
+}
+
+int svo_octree_build_voxel_file(const char *path, uint64_t mem, svo_stream stream, svo_octree **out) {
+    if (!path || !out) return set_error(SVO_ERR_INVALID, "null argument");
+    FILE *fp = fopen(path, "rb");
+    if (!fp) return set_error(SVO_ERR_IO, "cannot open %s", path);
+    std::unique_ptr<FILE, int (*)(FILE *)> guard(fp, fclose);
+    int32_t dims[3];
+    if (fread(dims, 4, 3, fp) != 3) return set_error(SVO_ERR_FORMAT, "%s: truncated header", path);
+    int w = dims[0], h = dims[1], d = dims[2];
+    if (w <= 0 || h <= 0 || d <= 0) return set_error(SVO_ERR_FORMAT, "%s: bad dimensions", path);
+    const uint64_t slab = (uint64_t)w * h;
+    uint32_t *dg = nullptr;
+    SVO_CUDA_TRY(cudaMalloc((void **)&dg, slab * d * 4));
+    std::unique_ptr<uint32_t, cudaError_t (*)(void *)> dguard(dg, cudaFree);
+    // Stream z slabs through a pinned buffer of about 64 MiB.
+    uint64_t zs = std::max<uint64_t>(1, (64ull << 20) / (slab * 4));
+    uint32_t *pin = nullptr;
+    SVO_CUDA_TRY(cudaMallocHost((void **)&pin, zs * slab * 4));
+    std::unique_ptr<uint32_t, cudaError_t (*)(void *)> pguard(pin, cudaFreeHost);
+    for (uint64_t z = 0; z < (uint64_t)d; z += zs) {
+        uint64_t nz = std::min<uint64_t>(zs, (uint64_t)d - z);
+        size_t want = (size_t)(nz * slab);
+        size_t got = fread(pin, 4, want, fp);
+        if (got != want) return set_error(SVO_ERR_FORMAT, "%s: truncated voxel data", path);
+        SVO_CUDA_TRY(cudaMemcpy(dg + z * slab, pin, want * 4, cudaMemcpyHostToDevice));
+    }
+    return svo_octree_build_dense(dg, w, h, d, mem, 1, stream, out);
+}
+
+int svo_trace(const svo_octree *oct, const float *rays, uint64_t n, float ray_scale, const float light[3],
+              const svo_trace_out *out, svo_stream stream) {
+    if (!oct || (!rays && n) || !out) return set_error(SVO_ERR_INVALID, "null argument");
+    if (n > 0xFFFFFFFFull) return set_error(SVO_ERR_LIMIT, "more than 2^32-1 rays");
+    return launch_trace(oct, rays, n, ray_scale, light, *out, (cudaStream_t)stream);
+}
+
+int svo_trace_count_loads(const svo_octree *oct, const float *rays, uint64_t n, float ray_scale, uint32_t *loads,
+                          svo_stream stream) {
+    if (!oct || (!rays && n) || (!loads && n)) return set_error(SVO_ERR_INVALID, "null argument");
+    return launch_count_loads(oct, rays, n, ray_scale, loads, (cudaStream_t)stream);
+}
+
+int svo_trace_host(svo_octree *oct, const float *rays, uint64_t n, float ray_scale, const float light[3],
+                   const svo_trace_out *out) {
+    if (!oct || (!rays && n) || !out) return set_error(SVO_ERR_INVALID, "null argument");
+    if (n > 0xFFFFFFFFull) return set_error(SVO_ERR_LIMIT, "more than 2^32-1 rays");
+    std::lock_guard<std::mutex> lock(oct->staging_mtx);
+    const uint64_t C = kStageRays;
+    // Per half: rays 24 B, hit 1, t 4, leaf 4, word 4, rgb 12 (padded to 64 B alignment per array).
+    auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+    const size_t half = al(C * 24) + al(C) + al(C * 4) * 3 + al(C * 12);
+    int rc = ensure_staging(oct, 2 * half);
+    if (rc) return rc;
+    for (uint64_t c0 = 0, j = 0; c0 < n; c0 += C, ++j) {
+        uint64_t m = std::min(C, n - c0);
+        cudaStream_t st = oct->stage_streams[j & 1];
+        uint8_t *base = (uint8_t *)oct->stage_dev + (j & 1) * half;
+        float *d_rays = (float *)base;
+        uint8_t *d_hit = base + al(C * 24);
+        float *d_t = (float *)(d_hit + al(C));
+        uint32_t *d_leaf = (uint32_t *)((uint8_t *)d_t + al(C * 4));
+        uint32_t *d_word = (uint32_t *)((uint8_t *)d_leaf + al(C * 4));
+        float *d_rgb = (float *)((uint8_t *)d_word + al(C * 4));
+        SVO_CUDA_TRY(cudaMemcpyAsync(d_rays, rays + 6 * c0, m * 24, cudaMemcpyHostToDevice, st));
+        svo_trace_out o;
+        o.hit = out->hit ? d_hit : nullptr;
+        o.t = out->t ? d_t : nullptr;
+        o.leaf = out->leaf ? d_leaf : nullptr;
+        o.word = out->word ? d_word : nullptr;
+        o.rgb = out->rgb ? d_rgb : nullptr;
+        rc = launch_trace(oct, d_rays, m, ray_scale, light, o, st);
+        if (rc) return rc;
+        if (out->hit) SVO_CUDA_TRY(cudaMemcpyAsync(out->hit + c0, d_hit, m, cudaMemcpyDeviceToHost, st));
+        if (out->t) SVO_CUDA_TRY(cudaMemcpyAsync(out->t + c0, d_t, m * 4, cudaMemcpyDeviceToHost, st));
+        if (out->leaf) SVO_CUDA_TRY(cudaMemcpyAsync(out->leaf + c0, d_leaf, m * 4, cudaMemcpyDeviceToHost, st));
+        if (out->word) SVO_CUDA_TRY(cudaMemcpyAsync(out->word + c0, d_word, m * 4, cudaMemcpyDeviceToHost, st));
+        if (out->rgb) SVO_CUDA_TRY(cudaMemcpyAsync(out->rgb + 3 * c0, d_rgb, m * 12, cudaMemcpyDeviceToHost, st));
+    }
+    SVO_CUDA_TRY(cudaStreamSynchronize(oct->stage_streams[0]));
+    SVO_CUDA_TRY(cudaStreamSynchronize(oct->stage_streams[1]));
+    return check_device_status(oct);
+}
+
+}  // extern "C"

@@ -1,0 +1,68 @@
+// svo_internal.h — host-side internals shared by the library's translation units.
+#pragma once
+
+#include <cstdarg>
+#include <cstdint>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "svo.h"
+
+// The opaque handle behind svo_octree*.
+struct svo_octree {
+    uint32_t *d_words = nullptr;  // resident octree words (HBM)
+    uint64_t n_words = 0;
+    float center[3] = {0.0f, 0.0f, 0.0f};
+    int device = 0;
+    uint32_t *d_status = nullptr;  // device error word: bit 0 = a ray ended with kFault
+
+    // Staging for svo_trace_host: one device arena and one pinned host arena,
+    // split into two halves that alternate between two streams.
+    std::mutex staging_mtx;
+    void *stage_dev = nullptr;
+    size_t stage_dev_bytes = 0;
+    void *stage_host = nullptr;
+    size_t stage_host_bytes = 0;
+    cudaStream_t stage_streams[2] = {nullptr, nullptr};
+};
+
+namespace svo {
+
+// Records a formatted message for svo_last_error() and returns `code`.
+int set_error(int code, const char *fmt, ...);
+int cuda_fail(cudaError_t e, const char *what);
+void clear_error();
+
+#define SVO_CUDA_TRY(call)                                   \
+    do {                                                     \
+        cudaError_t _e = (call);                             \
+        if (_e != cudaSuccess) return ::svo::cuda_fail(_e, #call); \
+    } while (0)
+
+// LZ4 block format (independent blocks; decoder accepts history before pos0).
+size_t lz4_compress_bound(size_t n);
+size_t lz4_compress_block(const uint8_t *src, size_t n, uint8_t *dst, size_t cap);
+int lz4_decompress_block(const uint8_t *src, size_t src_len, uint8_t *out, size_t pos0, size_t out_len);
+
+// VoxelData::init cache-block search (VoxelData.cpp:211-244): log2 of the
+// cache-block edge, or -1 when no partition fits `mem`.
+int cache_block_log2(int w, int h, int d, uint64_t mem, uint64_t cell_cost);
+
+// GPU build from a device-resident dense grid (build.cu).  On success the
+// caller owns *d_words (cudaFree).
+int build_dense_device(const uint32_t *d_grid, int w, int h, int d, int log_side, int log_block, cudaStream_t st,
+                       uint32_t **d_words, uint64_t *n_words);
+
+// Trace launchers (trace.cu).
+int launch_trace(const svo_octree *oct, const float *d_rays, uint64_t n, float ray_scale, const float light[3],
+                 const svo_trace_out &out, cudaStream_t st);
+int launch_count_loads(const svo_octree *oct, const float *d_rays, uint64_t n, float ray_scale, uint32_t *loads,
+                       cudaStream_t st);
+
+// Creates a handle around device words (takes ownership).
+int make_handle(uint32_t *d_words, uint64_t n_words, const float center[3], svo_octree **out);
+
+}  // namespace svo

@@ -1,0 +1,109 @@
+// trace.cu — ray traversal kernels over the resident octree.
+//
+// k_trace_plain: one thread per ray, the drop-in for a loop of
+// VoxelOctree::raymarch (VoxelOctree.cpp:207-346) plus the viewer's shade()
+// (Main.cpp:81-90).  Rays are 24-byte records (o, d) read as three float2;
+// outputs are structure-of-arrays so every store is coalesced.
+#include "svo_device.cuh"
+#include "svo_internal.h"
+
+namespace svo {
+namespace {
+
+struct TraceArgs {
+    const uint32_t *oct;
+    uint32_t n_words;
+    const float *rays;
+    uint64_t n;
+    float ray_scale;
+    float lx, ly, lz;
+    uint8_t *hit;
+    float *t;
+    uint32_t *leaf;
+    uint32_t *word;
+    float *rgb;
+    uint32_t *status;
+};
+
+__device__ __forceinline__ void load_ray(const float *rays, uint64_t i, float &ox, float &oy, float &oz, float &dx,
+                                         float &dy, float &dz) {
+    const float2 *r = reinterpret_cast<const float2 *>(rays) + 3 * i;
+    float2 a = __ldg(r), b = __ldg(r + 1), c = __ldg(r + 2);
+    ox = a.x; oy = a.y; oz = b.x;
+    dx = b.y; dy = c.x; dz = c.y;
+}
+
+__device__ __forceinline__ void store_result(const TraceArgs &a, uint64_t i, const RayResult &r, float dx, float dy,
+                                             float dz) {
+    if (r.status == kFault) atomicOr(a.status, 1u);
+    uint8_t hs = r.status == kFault ? 0 : (uint8_t)r.status;
+    if (a.hit) a.hit[i] = hs;
+    if (a.t) a.t[i] = (hs == 0) ? __int_as_float(0x7f800000) : r.t;
+    bool leaf = r.status == kLeafHit;
+    if (a.leaf) a.leaf[i] = leaf ? r.leaf : 0xFFFFFFFFu;
+    if (a.word) a.word[i] = leaf ? r.word : 0u;
+    if (a.rgb) {
+        float g = leaf ? shade_grey(r.word, dx, dy, dz, a.lx, a.ly, a.lz) : 0.0f;
+        a.rgb[3 * i + 0] = g;
+        a.rgb[3 * i + 1] = g;
+        a.rgb[3 * i + 2] = g;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_trace_plain(TraceArgs a) {
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    float ox, oy, oz, dx, dy, dz;
+    load_ray(a.rays, i, ox, oy, oz, dx, dy, dz);
+    RayResult r = raymarch<false>(a.oct, a.n_words, ox, oy, oz, dx, dy, dz, a.ray_scale, nullptr);
+    store_result(a, i, r, dx, dy, dz);
+}
+
+__global__ void __launch_bounds__(256) k_count_loads(const uint32_t *oct, uint32_t n_words, const float *rays,
+                                                    uint64_t n, float ray_scale, uint32_t *loads,
+                                                    uint32_t *status) {
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float ox, oy, oz, dx, dy, dz;
+    load_ray(rays, i, ox, oy, oz, dx, dy, dz);
+    uint32_t nl = 0;
+    RayResult r = raymarch<true>(oct, n_words, ox, oy, oz, dx, dy, dz, ray_scale, &nl);
+    if (r.status == kFault) atomicOr(status, 1u);
+    loads[i] = nl;
+}
+
+}  // namespace
+
+int launch_trace(const svo_octree *oct, const float *d_rays, uint64_t n, float ray_scale, const float light[3],
+                 const svo_trace_out &out, cudaStream_t st) {
+    if (n == 0) return SVO_OK;
+    TraceArgs a;
+    a.oct = oct->d_words;
+    a.n_words = (uint32_t)oct->n_words;
+    a.rays = d_rays;
+    a.n = n;
+    a.ray_scale = ray_scale;
+    a.lx = light ? light[0] : 0.0f;
+    a.ly = light ? light[1] : 0.0f;
+    a.lz = light ? light[2] : 0.0f;
+    a.hit = out.hit;
+    a.t = out.t;
+    a.leaf = out.leaf;
+    a.word = out.word;
+    a.rgb = out.rgb;
+    a.status = oct->d_status;
+    k_trace_plain<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(a);
+    SVO_CUDA_TRY(cudaGetLastError());
+    return SVO_OK;
+}
+
+int launch_count_loads(const svo_octree *oct, const float *d_rays, uint64_t n, float ray_scale, uint32_t *loads,
+                       cudaStream_t st) {
+    if (n == 0) return SVO_OK;
+    k_count_loads<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(oct->d_words, (uint32_t)oct->n_words, d_rays, n,
+                                                               ray_scale, loads, oct->d_status);
+    SVO_CUDA_TRY(cudaGetLastError());
+    return SVO_OK;
+}
+
+}  // namespace svo

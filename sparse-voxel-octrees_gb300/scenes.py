@@ -1,0 +1,304 @@
+"""Seeded synthetic scenes and camera rays for tests and benchmarks.
+
+The reference ships no benchmark inputs, so the workloads are generated:
+
+* sphere unions (union of solid spheres; voxel (x, y, z) is occupied when its
+  centre (x+.5, y+.5, z+.5) lies within radius r of a sphere centre, tested
+  in float32 as dx*dx + dy*dy + dz*dz <= r*r),
+* a value-noise heightfield terrain (y up) with a shell of fixed thickness,
+* voxel payload words as the reference's voxelizer would store them: a
+  normal from the central difference of occupancy (outward, each component
+  occ(-1) - occ(+1); (0, 1, 0) where it vanishes) and a shade equal to the
+  Rec.709 luminance / 256 of an RGB8 colour taken from a 32-bit hash of the
+  voxel coordinates (PlyLoader.cpp:315), packed by compressMaterial
+  (Util.hpp:64-84); a word that packs to 0 (= empty) is stored as 1,
+* camera rays by the reference viewer's formula (Main.cpp:149-176):
+  pos = INV_MODELVIEW * 0 + center + 1, direction (dx*a11 + dy*a12 + zx, ...)
+  with dx = -1 + x*2/W, dy = H/W - y*2/W, zx = a13/tan(pi/6), normalised with
+  the Quake inverse square root.  INV_MODELVIEW is MODEL^-1 * VIEW with
+  MODEL = rotXYZ(pitch, 0, 0) * rotXYZ(0, yaw, 0) and VIEW = translate(0, 0, -r).
+
+All float arithmetic is float32 in the reference's operation order, so the
+CUDA generators (when used) produce the same bits.
+"""
+import math
+
+import numpy as np
+
+F = np.float32
+
+
+# ---------------------------------------------------------------- codec (numpy)
+
+def inv_sqrt(x):
+    """Util.hpp:47-58, vectorised."""
+    x = np.asarray(x, dtype=np.float32)
+    x2 = x * F(0.5)
+    i = x.view(np.uint32)
+    i = np.uint32(0x5F3759DF) - (i >> np.uint32(1))
+    y = i.view(np.float32)
+    return y * (F(1.5) - x2 * y * y)
+
+
+def compress_material(nx, ny, nz, shade):
+    """Util.hpp:64-84, vectorised over float32 arrays."""
+    nx = np.asarray(nx, np.float32)
+    ny = np.asarray(ny, np.float32)
+    nz = np.asarray(nz, np.float32)
+    shade = np.asarray(shade, np.float32)
+    ax, ay, az = np.abs(nx), np.abs(ny), np.abs(nz)
+    face = np.zeros(nx.shape, np.uint32)
+    dom = ax.copy()
+    m = ay > dom
+    face[m] = 1
+    dom[m] = ay[m]
+    m = az > dom
+    face[m] = 2
+    dom[m] = az[m]
+    n = np.stack([nx, ny, nz])
+    idx = np.arange(nx.size).reshape(nx.shape)
+    f1 = np.where(face == 2, 0, face + 1)
+    f2 = np.where(face == 0, 2, face - 1)
+    sel = n.reshape(3, -1)
+    nf = sel[face.ravel(), idx.ravel()].reshape(nx.shape)
+    n1 = sel[f1.ravel(), idx.ravel()].reshape(nx.shape) / dom
+    n2 = sel[f2.ravel(), idx.ravel()].reshape(nx.shape) / dom
+    sign = (nf < F(0)).astype(np.uint32)
+    u = np.minimum(((n1 * F(0.5) + F(0.5)) * F(2047)).astype(np.int32), 0x7FF).astype(np.uint32)
+    v = np.minimum(((n2 * F(0.5) + F(0.5)) * F(2047)).astype(np.int32), 0x7FF).astype(np.uint32)
+    c = np.minimum((shade * F(127)).astype(np.int32), 0x7F).astype(np.uint32)
+    return (sign << 31) | (face << 29) | (u << 18) | (v << 7) | c
+
+
+def hash32(x, y, z):
+    """32-bit coordinate hash (multiply-xor mix followed by a murmur3 finaliser)."""
+    x = np.asarray(x, np.uint32)
+    y = np.asarray(y, np.uint32)
+    z = np.asarray(z, np.uint32)
+    with np.errstate(over="ignore"):
+        h = (x * np.uint32(0x8DA6B343)) ^ (y * np.uint32(0xD8163841)) ^ (z * np.uint32(0xCB1AB31F))
+        h ^= h >> np.uint32(16)
+        h *= np.uint32(0x85EBCA6B)
+        h ^= h >> np.uint32(13)
+        h *= np.uint32(0xC2B2AE35)
+        h ^= h >> np.uint32(16)
+    return h
+
+
+def hash_shade(x, y, z):
+    h = hash32(x, y, z)
+    r = (h & np.uint32(255)).astype(np.float32)
+    g = ((h >> np.uint32(8)) & np.uint32(255)).astype(np.float32)
+    b = ((h >> np.uint32(16)) & np.uint32(255)).astype(np.float32)
+    return (r * F(0.2126) + g * F(0.7152) + b * F(0.0722)) * F(1.0 / 256.0)
+
+
+# ---------------------------------------------------------------- occupancy
+
+def sphere_params(n, seed, lo, hi, rmin, rmax):
+    rng = np.random.default_rng(seed)
+    centers = rng.uniform(lo, hi, (n, 3)).astype(np.float32)
+    radii = rng.uniform(rmin, rmax, n).astype(np.float32)
+    return centers, radii
+
+
+def occupancy_spheres(shape, centers, radii, occ=None):
+    """shape = (d, h, w); returns bool occupancy (d, h, w)."""
+    d, h, w = shape
+    if occ is None:
+        occ = np.zeros(shape, bool)
+    for (cx, cy, cz), r in zip(centers, radii):
+        x0, x1 = max(0, int(math.floor(cx - r)) - 1), min(w, int(math.ceil(cx + r)) + 2)
+        y0, y1 = max(0, int(math.floor(cy - r)) - 1), min(h, int(math.ceil(cy + r)) + 2)
+        z0, z1 = max(0, int(math.floor(cz - r)) - 1), min(d, int(math.ceil(cz + r)) + 2)
+        if x0 >= x1 or y0 >= y1 or z0 >= z1:
+            continue
+        dx = (np.arange(x0, x1, dtype=np.float32) + F(0.5)) - F(cx)
+        dy = (np.arange(y0, y1, dtype=np.float32) + F(0.5)) - F(cy)
+        dz = (np.arange(z0, z1, dtype=np.float32) + F(0.5)) - F(cz)
+        s = (dx[None, None, :] * dx[None, None, :] + dy[None, :, None] * dy[None, :, None]) + \
+            dz[:, None, None] * dz[:, None, None]
+        occ[z0:z1, y0:y1, x0:x1] |= s <= F(r) * F(r)
+    return occ
+
+
+def value_noise_fbm(n, seed, octaves, base_cells=4):
+    """Seeded fractal value noise on an n x n lattice in [0, 1) (float64 math,
+    returned as float32).  Octave k uses a (base_cells * 2^k + 1)^2 lattice of
+    uniform values, smoothstep-interpolated, with amplitude 2^-k."""
+    rng = np.random.default_rng(seed)
+    out = np.zeros((n, n), np.float64)
+    total = 0.0
+    coords = (np.arange(n) + 0.5) / n
+    for k in range(octaves):
+        cells = base_cells << k
+        lat = rng.random((cells + 1, cells + 1))
+        p = coords * cells
+        i = np.minimum(p.astype(np.int64), cells - 1)
+        f = p - i
+        s = f * f * (3 - 2 * f)
+        a = lat[i[:, None], i[None, :]]
+        b = lat[i[:, None], i[None, :] + 1]
+        c = lat[i[:, None] + 1, i[None, :]]
+        d = lat[i[:, None] + 1, i[None, :] + 1]
+        top = a + (b - a) * s[None, :]
+        bot = c + (d - c) * s[None, :]
+        out += (top + (bot - top) * s[:, None]) * 0.5 ** k
+        total += 0.5 ** k
+    return (out / total).astype(np.float32)
+
+
+def terrain_heights(n, seed, octaves=5, amplitude=0.3, base=0.1):
+    """Heights (in voxels) per (z, x) column: n * (base + amplitude * fbm)."""
+    f = value_noise_fbm(n, seed, octaves)
+    return (F(n) * (F(base) + F(amplitude) * f)).astype(np.float32)
+
+
+def occupancy_terrain(shape, heights, thickness=2.0, occ=None):
+    """Voxel (x, y, z) is in the shell when h - thickness < y + 0.5 <= h,
+    h = heights[z, x]."""
+    d, h, w = shape
+    if occ is None:
+        occ = np.zeros(shape, bool)
+    yc = np.arange(h, dtype=np.float32) + F(0.5)
+    for z in range(d):
+        hz = heights[z, :w]
+        occ[z] |= (yc[:, None] <= hz[None, :]) & (yc[:, None] > hz[None, :] - F(thickness))
+    return occ
+
+
+def payload_from_occupancy(occ):
+    """uint32 words (0 = empty) from a bool occupancy grid (d, h, w)."""
+    d, h, w = occ.shape
+    o = np.pad(occ.astype(np.int8), 1)
+    nx = (o[1:-1, 1:-1, :-2] - o[1:-1, 1:-1, 2:]).astype(np.float32)
+    ny = (o[1:-1, :-2, 1:-1] - o[1:-1, 2:, 1:-1]).astype(np.float32)
+    nz = (o[:-2, 1:-1, 1:-1] - o[2:, 1:-1, 1:-1]).astype(np.float32)
+    zi, yi, xi = np.nonzero(occ)
+    gx, gy, gz = nx[zi, yi, xi], ny[zi, yi, xi], nz[zi, yi, xi]
+    flat = (gx == 0) & (gy == 0) & (gz == 0)
+    gy = np.where(flat, F(1), gy)
+    words = compress_material(gx, gy, gz, hash_shade(xi, yi, zi))
+    words[words == 0] = 1
+    grid = np.zeros(occ.shape, np.uint32)
+    grid[zi, yi, xi] = words
+    return grid
+
+
+# ---------------------------------------------------------------- scenes
+
+def sphere_scene(side, n_spheres, seed, shape=None):
+    """Config-0 family: centres U[side/8, 7 side/8]^3, radii U[6, 32] * side/256."""
+    s = side / 256.0
+    centers, radii = sphere_params(n_spheres, seed, 32 * s, 224 * s, 6 * s, 32 * s)
+    occ = occupancy_spheres(shape or (side, side, side), centers, radii)
+    return payload_from_occupancy(occ)
+
+
+def terrain_scene(side, n_spheres, seed, shape=None):
+    """Config-1 family: 5-octave terrain (amplitude 0.3*side, 2-voxel shell)
+    plus spheres with radii U[10, 120] * side/2048 and centres U[0.1, 0.9]*side."""
+    shape = shape or (side, side, side)
+    heights = terrain_heights(side, seed)
+    occ = occupancy_terrain(shape, heights)
+    s = side / 2048.0
+    centers, radii = sphere_params(n_spheres, seed + 1000003, 0.1 * side, 0.9 * side, 10 * s, 120 * s)
+    occupancy_spheres(shape, centers, radii, occ)
+    return payload_from_occupancy(occ)
+
+
+def random_grid(shape, density, seed):
+    rng = np.random.default_rng(seed)
+    occ = rng.random(shape) < density
+    vals = rng.integers(1, 2 ** 32 - 1, shape, dtype=np.uint64).astype(np.uint32)
+    return np.where(occ, vals, 0).astype(np.uint32)
+
+
+# ---------------------------------------------------------------- cameras
+
+def rot_xyz(rx, ry, rz):
+    """Mat4::rotXYZ (math/Mat4.cpp:114-125) rotation block, degrees, float64."""
+    r = np.radians([rx, ry, rz])
+    c, s = np.cos(r), np.sin(r)
+    return np.array([
+        [c[1] * c[2], -c[0] * s[2] + s[0] * s[1] * c[2], s[0] * s[2] + c[0] * s[1] * c[2]],
+        [c[1] * s[2], c[0] * c[2] + s[0] * s[1] * s[2], -s[0] * c[2] + c[0] * s[1] * s[2]],
+        [-s[1], s[0] * c[1], c[0] * c[1]],
+    ])
+
+
+def camera(yaw, pitch, radius, center):
+    """Returns the 12 float32 camera values (a11..a33 row-major, then pos)."""
+    R = rot_xyz(pitch, 0, 0) @ rot_xyz(0, yaw, 0)
+    Rt = R.T  # pseudoInvert of a pure rotation (Mat4.cpp:76-82)
+    pos = Rt @ np.array([0.0, 0.0, -radius]) + np.asarray(center, np.float64) + 1.0
+    return np.concatenate([Rt.reshape(9), pos]).astype(np.float32)
+
+
+def headlight(cam):
+    """Main.cpp:163: normalize(R^T * (-1, 1, -1)), float32."""
+    a = cam[:9].reshape(3, 3).astype(np.float32)
+    v = np.array([-1, 1, -1], np.float32)
+    l = (a[:, 0] * v[0] + a[:, 1] * v[1]) + a[:, 2] * v[2]
+    n = F(1) / np.sqrt(l[0] * l[0] + l[1] * l[1] + l[2] * l[2], dtype=np.float32)
+    return (l * n).astype(np.float32)
+
+
+PLANE_DIST = F(1.0) / F(math.tan(F(math.pi) / F(6.0)))
+
+
+def camera_rays(cam, W, H, x0=0, y0=0, x1=None, y1=None):
+    """(n, 6) float32 rays for pixels [x0, x1) x [y0, y1) in row-major order."""
+    x1 = W if x1 is None else x1
+    y1 = H if y1 is None else y1
+    a = cam[:9].astype(np.float32)
+    pos = cam[9:12].astype(np.float32)
+    scale = F(2.0) / F(W)
+    aspect = F(H) / F(W)
+    zx, zy, zz = PLANE_DIST * a[2], PLANE_DIST * a[5], PLANE_DIST * a[8]
+    xs = np.arange(x0, x1, dtype=np.float32)
+    ys = np.arange(y0, y1, dtype=np.float32)
+    dx = (F(-1.0) + xs * scale)[None, :]
+    dy = (aspect - ys * scale)[:, None]
+    vx = (dx * a[0] + dy * a[1]) + zx
+    vy = (dx * a[3] + dy * a[4]) + zy
+    vz = (dx * a[6] + dy * a[7]) + zz
+    n = inv_sqrt((vx * vx + vy * vy) + vz * vz)
+    rays = np.empty((y1 - y0, x1 - x0, 6), np.float32)
+    rays[..., 0] = pos[0]
+    rays[..., 1] = pos[1]
+    rays[..., 2] = pos[2]
+    rays[..., 3] = vx * n
+    rays[..., 4] = vy * n
+    rays[..., 5] = vz * n
+    return rays.reshape(-1, 6)
+
+
+def orbit_cameras(n, seed, center, radius=2.0, radius_hi=None, pitch=60.0):
+    """n cameras with yaw U[0, 360), pitch U[-pitch, pitch] and radius r
+    (or U[radius, radius_hi]) around `center`."""
+    rng = np.random.default_rng(seed)
+    cams = []
+    for _ in range(n):
+        yaw = rng.uniform(0, 360)
+        pit = rng.uniform(-pitch, pitch)
+        r = radius if radius_hi is None else rng.uniform(radius, radius_hi)
+        cams.append(camera(yaw, pit, r, center))
+    return cams
+
+
+def random_rays(n, seed, lo=-1.0, hi=4.0):
+    """Rays from U[lo, hi]^3 towards U[1, 2]^3 (unit directions), plus
+    axis-aligned and grazing directions in the first rows."""
+    rng = np.random.default_rng(seed)
+    o = rng.uniform(lo, hi, (n, 3)).astype(np.float32)
+    t = rng.uniform(1.0, 2.0, (n, 3)).astype(np.float32)
+    d = t - o
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    d = d.astype(np.float32)
+    k = n // 16
+    d[:k, 0] = 0.0
+    d[k:2 * k, 1] = 1e-5
+    d[2 * k:3 * k, 2] = -3e-5
+    o[3 * k:4 * k] = rng.uniform(1.0, 2.0, (k, 3)).astype(np.float32)  # origins inside the cube
+    return np.concatenate([o, d], axis=1).astype(np.float32)

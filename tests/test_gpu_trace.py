@@ -1,0 +1,136 @@
+"""GPU traversal parity: svo_trace / svo_trace_host against the oracle's
+restatement of VoxelOctree::raymarch and the viewer's shade() — bit-exact
+hit flags, t bits, leaf indices, leaf words and shaded colours."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _device_trace(cuda, svo, tree, rays, ray_scale=0.0, light=(0.0, 0.0, 1.0)):
+    torch = cuda
+    R = rays.shape[0]
+    d_rays = torch.from_numpy(np.ascontiguousarray(rays)).cuda()
+    out = {
+        "hit": torch.empty(R, dtype=torch.uint8, device="cuda"),
+        "t": torch.empty(R, dtype=torch.float32, device="cuda"),
+        "leaf": torch.empty(R, dtype=torch.int32, device="cuda"),
+        "word": torch.empty(R, dtype=torch.int32, device="cuda"),
+        "rgb": torch.empty((R, 3), dtype=torch.float32, device="cuda"),
+    }
+    tree.trace(d_rays, ray_scale=ray_scale, light=light, out=out)
+    torch.cuda.synchronize()
+    res = {k: v.cpu().numpy() for k, v in out.items()}
+    res["leaf"] = res["leaf"].view(np.uint32)
+    res["word"] = res["word"].view(np.uint32)
+    assert tree.device_status() == 0
+    return res
+
+
+def _assert_same(res, ref, grey=True):
+    assert np.array_equal(res["hit"], ref["hit"])
+    assert np.array_equal(res["t"].view(np.uint32), ref["t"].view(np.uint32))
+    assert np.array_equal(res["leaf"], ref["leaf"])
+    assert np.array_equal(res["word"], ref["word"])
+    if grey:
+        g = ref["grey"]
+        assert np.array_equal(res["rgb"][:, 0].view(np.uint32), g.view(np.uint32))
+        assert np.array_equal(res["rgb"][:, 1], res["rgb"][:, 0])
+        assert np.array_equal(res["rgb"][:, 2], res["rgb"][:, 0])
+
+
+def test_dragon_golden_rays(cuda, svo, golden, oracle):
+    g = golden["dragon"]
+    tree = svo.VoxelOctree.from_words(g["words"], g["center"])
+    light = np.array([0.3, -0.8, 0.52], np.float32)
+    res = _device_trace(cuda, svo, tree, g["rays"], light=light)
+    # against the reference's own outputs
+    hit = res["hit"] == 1
+    assert np.array_equal(hit.astype(np.uint8), g["hit"])
+    assert np.array_equal(res["t"][hit].view(np.uint32), g["t"][hit].view(np.uint32))
+    assert np.array_equal(res["word"][hit], g["word"][hit])
+    # and every output against the oracle
+    _assert_same(res, oracle.raymarch(g["words"], g["rays"], light=light, threads=4))
+
+
+def test_dragon_lod(cuda, svo, golden, oracle):
+    g = golden["dragon"]
+    tree = svo.VoxelOctree.from_words(g["words"], g["center"])
+    res = _device_trace(cuda, svo, tree, g["rays"], ray_scale=0.02)
+    hit = res["hit"] > 0
+    assert np.array_equal(hit.astype(np.uint8), g["lod_hit"])
+    assert np.array_equal(res["t"][hit].view(np.uint32), g["lod_t"][hit].view(np.uint32))
+    _assert_same(res, oracle.raymarch(g["words"], g["rays"], ray_scale=0.02, threads=4), grey=False)
+
+
+def test_dragon_camera_views(cuda, svo, golden, oracle, scenes):
+    g = golden["dragon"]
+    tree = svo.VoxelOctree.from_words(g["words"], g["center"])
+    for cam in scenes.orbit_cameras(3, 7, g["center"], radius=1.5):
+        rays = scenes.camera_rays(cam, 320, 240)
+        light = scenes.headlight(cam)
+        res = _device_trace(cuda, svo, tree, rays, light=light)
+        ref = oracle.raymarch(g["words"], rays, light=light, threads=4)
+        _assert_same(res, ref)
+        assert (ref["hit"] == 1).mean() > 0.05
+
+
+def test_sphere_scene_random_and_edge_rays(cuda, svo, oracle, scenes):
+    grid = scenes.sphere_scene(128, 24, 0)
+    words, center = oracle.build_dense(grid)
+    tree = svo.VoxelOctree.from_words(words, center)
+    rays = scenes.random_rays(200_000, 5)
+    res = _device_trace(cuda, svo, tree, rays, light=(0.0, 1.0, 0.0))
+    _assert_same(res, oracle.raymarch(words, rays, light=(0.0, 1.0, 0.0), threads=4))
+
+
+def test_far_pointer_tree(cuda, svo, oracle, scenes):
+    grid = scenes.random_grid((64, 64, 64), 0.5, 3)
+    words, center = oracle.build_dense(grid)
+    assert ((words >> 17) & 1).sum() > 0
+    tree = svo.VoxelOctree.from_words(words, center)
+    rays = scenes.random_rays(100_000, 6)
+    _assert_same(_device_trace(cuda, svo, tree, rays), oracle.raymarch(words, rays, threads=4))
+
+
+def test_trace_host_matches_device(cuda, svo, golden, oracle, scenes):
+    g = golden["dragon"]
+    tree = svo.VoxelOctree.from_words(g["words"], g["center"])
+    rays = np.concatenate([scenes.random_rays(3_000_000, 8, lo=0.0, hi=3.0), g["rays"]])
+    host = tree.trace_host(rays, light=(0.0, 0.0, 1.0))
+    ref = oracle.raymarch(g["words"], rays, light=(0.0, 0.0, 1.0), threads=8)
+    _assert_same(host, ref)
+
+
+def test_single_ray_api(svo, golden, oracle):
+    g = golden["dragon"]
+    tree = svo.VoxelOctree.from_words(g["words"], g["center"])
+    for i in range(0, 64):
+        r = g["rays"][i]
+        hit, normal, t = tree.raymarch(r[:3], r[3:])
+        assert hit == bool(g["hit"][i])
+        if hit:
+            assert normal == int(g["word"][i]) and np.float32(t) == g["t"][i]
+
+
+def test_count_loads_matches_oracle(cuda, svo, golden, oracle):
+    torch = cuda
+    g = golden["dragon"]
+    tree = svo.VoxelOctree.from_words(g["words"], g["center"])
+    rays = torch.from_numpy(g["rays"]).cuda()
+    loads = torch.zeros(rays.shape[0], dtype=torch.int32, device="cuda")
+    tree.count_loads(rays, loads=loads)
+    torch.cuda.synchronize()
+    ref = oracle.raymarch(g["words"], g["rays"], loads=True, threads=4)
+    assert np.array_equal(loads.cpu().numpy().view(np.uint32), ref["loads"])
+
+
+def test_corrupt_tree_raises_device_flag(cuda, svo):
+    # A descriptor whose child offset points past the end: the kernel's bounds
+    # check ends the ray and sets the handle's error flag (no fault).
+    words = np.array([(0x3FFF << 18) | (0xFF << 8) | 0xFF], np.uint32)
+    tree = svo.VoxelOctree.from_words(words, (0.5, 0.5, 0.5))
+    rays = np.array([[1.5, 1.5, -1.0, 0.0, 0.0, 1.0]], np.float32)
+    with pytest.raises(svo.SvoError) as e:
+        tree.trace_host(rays)
+    assert e.value.code == svo.SVO_ERR_DEVICE
