@@ -1,0 +1,379 @@
+"""Benchmark: Mrays/s of the octree raymarch hot path on GB300.
+
+Workload (default, the plain-traversal configuration): a 2048^3 octree
+(depth 11) of a 5-octave value-noise terrain (amplitude 0.3*N, 2-voxel shell)
+plus 200 solid spheres with radii U[10, 120], built on the GPU from the dense
+grid; 32 seeded cameras at 1920x1080 FP32 primary rays plus one shadow ray per
+primary hit towards a fixed directional light.  One step traces all primary
+rays (t, leaf index, shaded rgb out) and all shadow rays (hit flag out).
+Inputs are synthetic (seeded generators in scenes.py) and resident in HBM
+before timing; the octree (~1.8 GB) and ray arrays (~1.6 GB + shadow) are far
+larger than L2, so no explicit flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference's raymarch restated in C (the oracle,
+the reference's own code cannot run on the GPU host) over all host threads on
+the same octree and rays; rank 0 only.
+Multi-GPU (torchrun): every rank traces its own 32 cameras over a replica of
+the octree (weak scaling, no collective on the data path).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SIDE = 2048
+N_SPHERES = 200
+SCENE_SEED = 1
+N_CAMS = 32
+W_PIX, H_PIX = 1920, 1080
+MEM_BUDGET = 8 << 30
+LIGHT = np.array([0.3, 0.8, 0.52], np.float32)
+LIGHT = (LIGHT / np.linalg.norm(LIGHT)).astype(np.float32)
+SHADOW_EPS = np.float32(1.5 / SIDE)
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--side", type=int, default=SIDE)
+    p.add_argument("--cams", type=int, default=N_CAMS)
+    p.add_argument("--width", type=int, default=W_PIX)
+    p.add_argument("--height", type=int, default=H_PIX)
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(args):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def cpu_trace_sample(oracle, words, prim_rays, shadow_rays, cam_slices, shadow_slices, budget_s=12.0):
+    """Time the oracle's raymarch over whole cameras (primary + their shadow
+    rays) on all host threads until about `budget_s` seconds have elapsed."""
+    threads = cpu_threads()
+    rays_done, elapsed, cams = 0, 0.0, 0
+    for (a, b), (sa, sb) in zip(cam_slices, shadow_slices):
+        t0 = time.perf_counter()
+        oracle.raymarch(words, prim_rays[a:b], light=LIGHT, threads=threads)
+        oracle.raymarch(words, shadow_rays[sa:sb], threads=threads)
+        elapsed += time.perf_counter() - t0
+        rays_done += (b - a) + (sb - sa)
+        cams += 1
+        if elapsed >= budget_s:
+            break
+    return rays_done, elapsed, cams, threads
+
+
+def setup_scene(args, rank, torch, svo, scenes):
+    """Builds the octree on the GPU and the primary/shadow ray arrays."""
+    side = args.side
+    heights, centers, radii = scenes.terrain_scene_params(side, N_SPHERES, SCENE_SEED)
+    t0 = time.perf_counter()
+    bm = scenes.gpu_occupancy(side, heights, centers, radii)
+    grid = scenes.gpu_payload_grid(bm, side)
+    del bm
+    torch.cuda.synchronize()
+    t_gen = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    tree = svo.VoxelOctree(svo.VoxelData(grid, MEM_BUDGET))
+    torch.cuda.synchronize()
+    t_build = time.perf_counter() - t0
+    n_vox = int((grid != 0).sum().item())
+    del grid
+    torch.cuda.empty_cache()
+    center = tree.center()
+    cams = scenes.orbit_cameras(args.cams, 1000 + rank, center, radius=1.25, radius_hi=2.0, pitch=45.0)
+    npix = args.width * args.height
+    prim = torch.empty((len(cams) * npix, 6), dtype=torch.float32, device="cuda")
+    for i, cam in enumerate(cams):
+        scenes.gpu_camera_rays(cam, args.width, args.height, out=prim[i * npix:(i + 1) * npix])
+    # primary pass once to derive the shadow rays (setup, not timed)
+    R = prim.shape[0]
+    t = torch.empty(R, dtype=torch.float32, device="cuda")
+    hit = torch.empty(R, dtype=torch.uint8, device="cuda")
+    tree.trace(prim, out={"t": t, "hit": hit})
+    torch.cuda.synchronize()
+    idx = torch.nonzero(hit == 1).squeeze(1)
+    o = prim[idx, :3]
+    d = prim[idx, 3:]
+    p = o + t[idx, None] * d
+    L = torch.from_numpy(LIGHT).cuda()
+    so = p + SHADOW_EPS * L
+    shadow = torch.cat([so, L.expand_as(so)], dim=1).contiguous()
+    # per-camera slices of the shadow array (hits are in camera order)
+    cam_of_hit = (idx // npix).cpu().numpy()
+    counts = np.bincount(cam_of_hit, minlength=len(cams))
+    starts = np.concatenate([[0], np.cumsum(counts)])
+    shadow_slices = [(int(starts[i]), int(starts[i + 1])) for i in range(len(cams))]
+    cam_slices = [(i * npix, (i + 1) * npix) for i in range(len(cams))]
+    del t, hit, idx, o, d, p, so
+    info = {"gen_s": t_gen, "build_s": t_build, "voxels": n_vox, "words": tree.num_words()}
+    return tree, prim, shadow, cam_slices, shadow_slices, info
+
+
+def run_ours(args):
+    rank, world, local = dist_setup(args)
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import __graft_entry__ as ge
+    ge.build()
+    svo = ge._package()
+    import svo_gb300.scenes as scenes
+
+    tree, prim, shadow, cam_slices, shadow_slices, info = setup_scene(args, rank, torch, svo, scenes)
+    Rp, Rs = prim.shape[0], shadow.shape[0]
+    rays_per_step = Rp + Rs
+    out_p = {"t": torch.empty(Rp, dtype=torch.float32, device="cuda"),
+             "leaf": torch.empty(Rp, dtype=torch.int32, device="cuda"),
+             "rgb": torch.empty((Rp, 3), dtype=torch.float32, device="cuda")}
+    out_s = {"hit": torch.empty(Rs, dtype=torch.uint8, device="cuda")}
+    stream = torch.cuda.current_stream()
+
+    # loads per ray (the reference's word reads), for the algorithmic bytes
+    loads = torch.empty(max(Rp, Rs), dtype=torch.int32, device="cuda")
+    tree.count_loads(prim, loads=loads[:Rp])
+    lp = int(loads[:Rp].sum().item())
+    tree.count_loads(shadow, loads=loads[:Rs])
+    ls = int(loads[:Rs].sum().item())
+    del loads
+    bytes_prim = 4 * lp + Rp * (24 + 20)
+    bytes_shadow = 4 * ls + Rs * (24 + 1)
+
+    def step(ev=None):
+        if ev is not None:
+            ev[0].record(stream)
+        tree.trace(prim, out=out_p, light=LIGHT, stream=stream)
+        if ev is not None:
+            ev[1].record(stream)
+        tree.trace(shadow, out=out_s, stream=stream)
+        if ev is not None:
+            ev[2].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        start.record(stream)
+        for k in range(args.steps):
+            step(evs[k])
+        end.record(stream)
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ms = start.elapsed_time(end)
+    t_prim = [e[0].elapsed_time(e[1]) for e in evs]
+    t_shadow = [e[1].elapsed_time(e[2]) for e in evs]
+    if tree.device_status() != 0:
+        raise RuntimeError("traversal error flag raised")
+    ms_max = ms
+    if world > 1:
+        tt = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        ms_max = float(tt.item())
+    total_rays = rays_per_step * args.steps * world
+    value = total_rays / (ms_max / 1e3) / 1e6
+
+    # end to end through the C ABI with host buffers (copies inside the timed region)
+    e2e = None
+    if not args.no_e2e:
+        hp = prim.cpu().numpy()
+        hs = shadow.cpu().numpy()
+        hp_pin = torch.from_numpy(hp).pin_memory().numpy()
+        hs_pin = torch.from_numpy(hs).pin_memory().numpy()
+        op = {"t": torch.empty(Rp, dtype=torch.float32).pin_memory().numpy(),
+              "leaf": torch.empty(Rp, dtype=torch.int32).pin_memory().numpy(),
+              "rgb": torch.empty((Rp, 3), dtype=torch.float32).pin_memory().numpy()}
+        os_ = {"hit": torch.empty(Rs, dtype=torch.uint8).pin_memory().numpy()}
+        for _ in range(max(1, args.warmup)):
+            tree.trace_host(hp_pin, light=LIGHT, out=op)
+            tree.trace_host(hs_pin, out=os_)
+        if world > 1:
+            torch.distributed.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            tree.trace_host(hp_pin, light=LIGHT, out=op)
+            tree.trace_host(hs_pin, out=os_)
+        e2e_s = time.perf_counter() - t0
+        if world > 1:
+            tt = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            e2e_s = float(tt.item())
+        e2e = {"value": round(total_rays / e2e_s / 1e6, 2), "unit": "Mrays/s",
+               "h2d_bytes_per_step": (Rp + Rs) * 24, "d2h_bytes_per_step": Rp * 20 + Rs * 1,
+               "api": "svo_trace_host (pinned host rays in, t/leaf/rgb and shadow hit out)"}
+
+    peaks, peak_kind = load_peaks()
+    t_prim_avg = sum(t_prim) / len(t_prim)
+    achieved = bytes_prim / (t_prim_avg / 1e3) / 1e9
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": profiled_traffic(Rp),
+                "kernel": "k_trace_plain (primary rays)", "peak_kind": peak_kind,
+                "algorithmic_bytes_per_launch": bytes_prim,
+                "bytes_per_ray": round(bytes_prim / Rp, 2), "launch_ms": round(t_prim_avg, 3)}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import pyoracle
+        pyoracle.build_oracle(with_reference=False)
+        oracle = pyoracle.Oracle()
+        words = tree.words()
+        n, secs, ncam, thr = cpu_trace_sample(oracle, words, prim.cpu().numpy(), shadow.cpu().numpy(),
+                                              cam_slices, shadow_slices)
+        cpu = {"value": round(n / secs / 1e6, 3), "unit": "Mrays/s", "cores": thr, "kind": "port",
+               "sample": "%d of %d cameras: %d primary+shadow rays in %.1f s (oracle C restatement of "
+                         "VoxelOctree::raymarch, %d threads)" % (ncam, len(cam_slices), n, secs, thr)}
+
+    if rank == 0:
+        line = {
+            "metric": "Mrays/s", "value": round(value, 2), "unit": "Mrays/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded terrain + spheres, seeded orbit cameras)",
+            "config": {"workload": "plain traversal: %d^3 octree (terrain + %d spheres), %d cams %dx%d primary rays "
+                                   "+ 1 shadow ray per hit" % (args.side, N_SPHERES, args.cams, args.width,
+                                                               args.height),
+                       "octree_words": info["words"], "voxels": info["voxels"], "primary_rays": Rp,
+                       "shadow_rays": Rs, "rays_per_step": rays_per_step,
+                       "l2": "no flush: octree %.2f GB and rays %.2f GB exceed L2" % (info["words"] * 4 / 1e9,
+                                                                                      rays_per_step * 24 / 1e9),
+                       "parallelism": "replicas x%d" % world},
+            "e2e": e2e, "gpu_launches": 2 * args.steps, "roofline": roofline, "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "build": {"build_s": round(info["build_s"], 3), "scene_gen_s": round(info["gen_s"], 3),
+                      "voxels_per_s": round(info["voxels"] / info["build_s"], 1)},
+            "kernel_ms": {"primary": round(t_prim_avg, 3), "shadow": round(sum(t_shadow) / len(t_shadow), 3)},
+        }
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def profiled_traffic(rays):
+    """DRAM bytes per launch from the committed ncu summary (scaled per ray), or None."""
+    path = os.path.join(ROOT, "profiles", "trace_plain_config1.txt")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_ray:"):
+                return int(float(line.split(":")[1]) * rays)
+    except OSError:
+        pass
+    return None
+
+
+def run_reference(args):
+    rank, world, local = dist_setup(args)
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    pyoracle.build_oracle(with_reference=False)
+    print(json.dumps({"impl": "reference", "unavailable": "CPU-side scene build for the reference arm not wired "
+                                                          "yet"}))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

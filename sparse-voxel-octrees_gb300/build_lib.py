@@ -18,6 +18,8 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libsvo_gb300.so")
+SCENES_SRC = os.path.join(HERE, "scenes_gpu.cu")
+SCENES_LIB = os.path.join(HERE, "libsvo_scenes.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC]
@@ -35,11 +37,11 @@ def sources():
 
 
 def _needs_rebuild():
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or not os.path.exists(SCENES_LIB):
         return True
-    t = os.path.getmtime(LIB)
+    t = min(os.path.getmtime(LIB), os.path.getmtime(SCENES_LIB))
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE)]
-    deps.append(os.path.abspath(__file__))
+    deps += [os.path.abspath(__file__), SCENES_SRC]
     return any(os.path.getmtime(p) > t for p in deps)
 
 
@@ -62,15 +64,21 @@ def build(force=False, verbose=False):
             sys.stderr.write(r.stdout + r.stderr)
         return obj
 
-    srcs = sources()
+    srcs = sources() + [SCENES_SRC]
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(compile_one, srcs))
-    tmp = LIB + ".tmp"
-    cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread"]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))
-    os.replace(tmp, LIB)
+    scene_obj = objs.pop()
+
+    def link(out, objects):
+        tmp = out + ".tmp"
+        cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objects + ["-lpthread"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))
+        os.replace(tmp, out)
+
+    link(LIB, objs)
+    link(SCENES_LIB, [scene_obj])
     return LIB
 
 

@@ -179,6 +179,14 @@ __global__ void k_parents_from_heads(const uint64_t *__restrict__ ckey, uint64_t
     pstart[p] = (uint32_t)i;
 }
 
+// pidx holds the exclusive scan of head flags: right for a head, one too high
+// for the siblings after it.  Turn it into the parent index of every child.
+__global__ void k_child_pidx_from_heads(const uint32_t *__restrict__ head, uint64_t n, uint32_t *__restrict__ pidx) {
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    pidx[i] = pidx[i] + head[i] - 1u;
+}
+
 // Dense grouping at the cache-block level: blk_first[b] = first child of
 // block b (or 0xFFFFFFFF); present = has children or top flag.
 __global__ void k_block_first(const uint64_t *__restrict__ ckey, uint64_t n, const uint32_t *__restrict__ head,
@@ -259,11 +267,13 @@ __global__ void k_root_word(const uint8_t *__restrict__ mask, const uint8_t *__r
 
 // Parents at one level place their (internal) children and write the
 // children's descriptors; child_is_bottom selects leafMask = 0.
+// Every word write is checked against W; a violation (an internal
+// inconsistency) is skipped and reported through *err.
 __global__ void k_place(uint64_t np, const uint8_t *__restrict__ count, const uint32_t *__restrict__ pstart,
                         const uint8_t *__restrict__ plarge, const uint64_t *__restrict__ pB,
                         const uint64_t *__restrict__ cS, const uint8_t *__restrict__ cmask,
                         const uint8_t *__restrict__ clarge, int child_is_bottom, uint64_t *__restrict__ cB,
-                        uint32_t *__restrict__ words) {
+                        uint32_t *__restrict__ words, uint64_t W, uint32_t *__restrict__ err) {
     uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= np) return;
     uint32_t k = count[p];
@@ -281,6 +291,10 @@ __global__ void k_place(uint64_t np, const uint8_t *__restrict__ count, const ui
         uint64_t off = blk - pos;
         uint32_t m = cmask[c];
         uint32_t w = (m << 8) | (child_is_bottom ? 0u : m) | (clarge[c] ? 0x10000u : 0u);
+        if (pos + (far ? 1 : 0) >= W) {
+            atomicOr(err, 1u);
+            continue;
+        }
         if (far) {
             w |= 0x20000u | (uint32_t)((off >> 32) << 18);
             words[pos + 1] = (uint32_t)off;
@@ -291,18 +305,37 @@ __global__ void k_place(uint64_t np, const uint8_t *__restrict__ count, const ui
     }
 }
 
-__global__ void k_place_leaves(uint64_t n, const uint32_t *__restrict__ pidx, const uint32_t *__restrict__ pstart,
-                               const uint64_t *__restrict__ pB, const uint32_t *__restrict__ payload,
-                               uint32_t *__restrict__ words) {
+__global__ void k_place_leaves(uint64_t n, const uint32_t *__restrict__ pidx, uint64_t np,
+                               const uint32_t *__restrict__ pstart, const uint64_t *__restrict__ pB,
+                               const uint32_t *__restrict__ payload, uint32_t *__restrict__ words, uint64_t W,
+                               uint32_t *__restrict__ err) {
     uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     uint32_t p = pidx[i];
-    words[pB[p] + (i - pstart[p])] = payload[i];
+    if (p >= np || i < pstart[p] || i - pstart[p] >= 8) {
+        atomicOr(err, 2u);
+        return;
+    }
+    uint64_t dst = pB[p] + (i - pstart[p]);
+    if (dst >= W) {
+        atomicOr(err, 4u);
+        return;
+    }
+    words[dst] = payload[i];
 }
 
 __global__ void k_set_u64(uint64_t *p, uint64_t v) { *p = v; }
 
-inline unsigned blocks_for(uint64_t n, int t = 256) { return (unsigned)((n + t - 1) / t); }
+inline unsigned blocks_for(uint64_t n, int t = 256) {
+    uint64_t b = (n + t - 1) / t;
+    return (unsigned)(b ? b : 1);  // kernels check their own bounds; never launch an empty grid
+}
+
+#define SVO_LAUNCH_CHECK(name)                                        \
+    do {                                                              \
+        cudaError_t _e = cudaGetLastError();                          \
+        if (_e != cudaSuccess) return ::svo::cuda_fail(_e, "launch of " name); \
+    } while (0)
 
 // Stream-ordered temporary buffer.
 template <typename T>
@@ -385,7 +418,7 @@ int build_dense_device(const uint32_t *d_grid, int w, int h, int d, int log_side
     SVO_TRY_ALLOC(boff.alloc(n_bricks, st));
     unsigned grid1 = (unsigned)(n_bricks < (1ull << 20) ? n_bricks : (1ull << 20));
     k_brick_count<<<grid1, kBrickThreads, 0, st>>>(g, n_bricks, bcount.p);
-    SVO_CUDA_TRY(cudaGetLastError());
+    SVO_LAUNCH_CHECK("k_brick_count");
     uint64_t N = 0;
     int rc = scan_to<uint64_t>(bcount.p, boff.p, n_bricks, &N, st);
     if (rc) return rc;
@@ -397,7 +430,7 @@ int build_dense_device(const uint32_t *d_grid, int w, int h, int d, int log_side
     SVO_TRY_ALLOC(lpay.alloc(N, st));
     if (N) {
         k_brick_emit<<<grid1, kBrickThreads, 0, st>>>(g, n_bricks, bcount.p, boff.p, lkey.p, lpay.p);
-        SVO_CUDA_TRY(cudaGetLastError());
+        SVO_LAUNCH_CHECK("k_brick_emit");
     }
     bcount.release();
     boff.release();
@@ -414,7 +447,7 @@ int build_dense_device(const uint32_t *d_grid, int w, int h, int d, int log_side
         SVO_TRY_ALLOC(pidx.alloc(nc, st));
         if (nc) {
             k_heads<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, head.p);
-            SVO_CUDA_TRY(cudaGetLastError());
+            SVO_LAUNCH_CHECK("k_heads");
         }
         if (multi_block && e == log_block) {
             // Dense grouping over cache blocks, adding blocks that only the top
@@ -426,7 +459,7 @@ int build_dense_device(const uint32_t *d_grid, int w, int h, int d, int log_side
             SVO_CUDA_TRY(cudaMemsetAsync(first.p, 0xFF, n_blocks * sizeof(uint32_t), st));
             if (nc) k_block_first<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, head.p, first.p);
             k_block_present<<<blocks_for(n_blocks), 256, 0, st>>>(first.p, topflag.p, n_blocks, present.p);
-            SVO_CUDA_TRY(cudaGetLastError());
+            SVO_LAUNCH_CHECK("k_block_present");
             uint32_t np = 0;
             rc = scan_to<uint32_t>(present.p, bidx.p, n_blocks, &np, st);
             if (rc) return rc;
@@ -436,7 +469,7 @@ int build_dense_device(const uint32_t *d_grid, int w, int h, int d, int log_side
             k_block_parents<<<blocks_for(n_blocks), 256, 0, st>>>(first.p, present.p, bidx.p, n_blocks, nc, L.key.p,
                                                                   L.start.p);
             if (nc) k_child_pidx_from_blocks<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, bidx.p, pidx.p);
-            SVO_CUDA_TRY(cudaGetLastError());
+            SVO_LAUNCH_CHECK("k_child_pidx_from_blocks");
         } else {
             uint32_t np = 0;
             rc = scan_to<uint32_t>(head.p, pidx.p, nc, &np, st);
@@ -446,7 +479,8 @@ int build_dense_device(const uint32_t *d_grid, int w, int h, int d, int log_side
             SVO_TRY_ALLOC(L.start.alloc(np, st));
             if (nc) {
                 k_parents_from_heads<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, head.p, pidx.p, L.key.p, L.start.p);
-                SVO_CUDA_TRY(cudaGetLastError());
+                k_child_pidx_from_heads<<<blocks_for(nc), 256, 0, st>>>(head.p, nc, pidx.p);
+                SVO_LAUNCH_CHECK("k_child_pidx_from_heads");
             }
         }
         // The root always exists, even over an empty grid.
@@ -460,7 +494,7 @@ int build_dense_device(const uint32_t *d_grid, int w, int h, int d, int log_side
         SVO_TRY_ALLOC(L.mask.alloc(L.n, st));
         SVO_TRY_ALLOC(L.count.alloc(L.n, st));
         k_parent_masks<<<blocks_for(L.n), 256, 0, st>>>(L.key.p, L.start.p, L.n, ckey, nc, L.mask.p, L.count.p);
-        SVO_CUDA_TRY(cudaGetLastError());
+        SVO_LAUNCH_CHECK("k_parent_masks");
         if (e == 1) {
             leaf_pidx.p = pidx.p;
             leaf_pidx.st = st;
@@ -478,7 +512,7 @@ int build_dense_device(const uint32_t *d_grid, int w, int h, int d, int log_side
         SVO_TRY_ALLOC(L.large.alloc(L.n, st));
         k_subtree<<<blocks_for(L.n), 256, 0, st>>>(L.n, L.count.p, L.start.p, e > 1 ? lv[e - 1].S.p : nullptr,
                                                   e == 1, L.S.p, L.large.p);
-        SVO_CUDA_TRY(cudaGetLastError());
+        SVO_LAUNCH_CHECK("k_subtree");
     }
     uint64_t S_root = 0;
     SVO_CUDA_TRY(cudaMemcpyAsync(&S_root, lv[D].S.p, sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
@@ -489,6 +523,9 @@ int build_dense_device(const uint32_t *d_grid, int w, int h, int d, int log_side
 
     uint32_t *words = nullptr;
     SVO_CUDA_TRY(cudaMallocAsync((void **)&words, (size_t)W * sizeof(uint32_t), st));
+    DevBuf<uint32_t> err;
+    SVO_TRY_ALLOC(err.alloc(1, st));
+    SVO_CUDA_TRY(cudaMemsetAsync(err.p, 0, sizeof(uint32_t), st));
 
     // Placement, top-down.
     SVO_TRY_ALLOC(lv[D].B.alloc(1, st));
@@ -499,17 +536,24 @@ int build_dense_device(const uint32_t *d_grid, int w, int h, int d, int log_side
         LevelArrays &C = lv[e - 1];
         SVO_TRY_ALLOC(C.B.alloc(C.n, st));
         k_place<<<blocks_for(P.n), 256, 0, st>>>(P.n, P.count.p, P.start.p, P.large.p, P.B.p, C.S.p, C.mask.p,
-                                                C.large.p, e - 1 == 1, C.B.p, words);
-        SVO_CUDA_TRY(cudaGetLastError());
+                                                C.large.p, e - 1 == 1, C.B.p, words, W, err.p);
+        SVO_LAUNCH_CHECK("k_place");
     }
     if (N) {
-        k_place_leaves<<<blocks_for(N), 256, 0, st>>>(N, leaf_pidx.p, lv[1].start.p, lv[1].B.p, lpay.p, words);
-        SVO_CUDA_TRY(cudaGetLastError());
+        k_place_leaves<<<blocks_for(N), 256, 0, st>>>(N, leaf_pidx.p, lv[1].n, lv[1].start.p, lv[1].B.p, lpay.p,
+                                                      words, W, err.p);
+        SVO_LAUNCH_CHECK("k_place_leaves");
     }
-    cudaError_t e = cudaStreamSynchronize(st);
+    uint32_t err_h = 0;
+    cudaError_t e = cudaMemcpyAsync(&err_h, err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) {
         cudaFree(words);
         return cuda_fail(e, "octree build");
+    }
+    if (err_h) {
+        cudaFree(words);
+        return set_error(SVO_ERR_DEVICE, "octree build placement check failed (flags %u)", err_h);
     }
     *d_words_out = words;
     *n_words_out = W;

@@ -102,15 +102,22 @@ def sphere_params(n, seed, lo, hi, rmin, rmax):
     return centers, radii
 
 
+def sphere_boxes(shape, centers, radii):
+    """Half-open, clipped voxel boxes (x0, x1, y0, y1, z0, z1) enclosing each sphere."""
+    d, h, w = shape
+    boxes = []
+    for (cx, cy, cz), r in zip(centers, radii):
+        boxes.append((max(0, int(math.floor(cx - r)) - 1), min(w, int(math.ceil(cx + r)) + 2),
+                      max(0, int(math.floor(cy - r)) - 1), min(h, int(math.ceil(cy + r)) + 2),
+                      max(0, int(math.floor(cz - r)) - 1), min(d, int(math.ceil(cz + r)) + 2)))
+    return boxes
+
+
 def occupancy_spheres(shape, centers, radii, occ=None):
     """shape = (d, h, w); returns bool occupancy (d, h, w)."""
-    d, h, w = shape
     if occ is None:
         occ = np.zeros(shape, bool)
-    for (cx, cy, cz), r in zip(centers, radii):
-        x0, x1 = max(0, int(math.floor(cx - r)) - 1), min(w, int(math.ceil(cx + r)) + 2)
-        y0, y1 = max(0, int(math.floor(cy - r)) - 1), min(h, int(math.ceil(cy + r)) + 2)
-        z0, z1 = max(0, int(math.floor(cz - r)) - 1), min(d, int(math.ceil(cz + r)) + 2)
+    for (cx, cy, cz), r, (x0, x1, y0, y1, z0, z1) in zip(centers, radii, sphere_boxes(shape, centers, radii)):
         if x0 >= x1 or y0 >= y1 or z0 >= z1:
             continue
         dx = (np.arange(x0, x1, dtype=np.float32) + F(0.5)) - F(cx)
@@ -187,22 +194,31 @@ def payload_from_occupancy(occ):
 
 # ---------------------------------------------------------------- scenes
 
-def sphere_scene(side, n_spheres, seed, shape=None):
+def sphere_scene_params(side, n_spheres, seed):
     """Config-0 family: centres U[side/8, 7 side/8]^3, radii U[6, 32] * side/256."""
     s = side / 256.0
-    centers, radii = sphere_params(n_spheres, seed, 32 * s, 224 * s, 6 * s, 32 * s)
+    return sphere_params(n_spheres, seed, 32 * s, 224 * s, 6 * s, 32 * s)
+
+
+def terrain_scene_params(side, n_spheres, seed):
+    """Config-1 family: 5-octave terrain (amplitude 0.3*side, 2-voxel shell)
+    plus spheres with radii U[10, 120] * side/2048 and centres U[0.1, 0.9]*side."""
+    heights = terrain_heights(side, seed)
+    s = side / 2048.0
+    centers, radii = sphere_params(n_spheres, seed + 1000003, 0.1 * side, 0.9 * side, 10 * s, 120 * s)
+    return heights, centers, radii
+
+
+def sphere_scene(side, n_spheres, seed, shape=None):
+    centers, radii = sphere_scene_params(side, n_spheres, seed)
     occ = occupancy_spheres(shape or (side, side, side), centers, radii)
     return payload_from_occupancy(occ)
 
 
 def terrain_scene(side, n_spheres, seed, shape=None):
-    """Config-1 family: 5-octave terrain (amplitude 0.3*side, 2-voxel shell)
-    plus spheres with radii U[10, 120] * side/2048 and centres U[0.1, 0.9]*side."""
     shape = shape or (side, side, side)
-    heights = terrain_heights(side, seed)
+    heights, centers, radii = terrain_scene_params(side, n_spheres, seed)
     occ = occupancy_terrain(shape, heights)
-    s = side / 2048.0
-    centers, radii = sphere_params(n_spheres, seed + 1000003, 0.1 * side, 0.9 * side, 10 * s, 120 * s)
     occupancy_spheres(shape, centers, radii, occ)
     return payload_from_occupancy(occ)
 
@@ -302,3 +318,89 @@ def random_rays(n, seed, lo=-1.0, hi=4.0):
     d[2 * k:3 * k, 2] = -3e-5
     o[3 * k:4 * k] = rng.uniform(1.0, 2.0, (k, 3)).astype(np.float32)  # origins inside the cube
     return np.concatenate([o, d], axis=1).astype(np.float32)
+
+
+# ---------------------------------------------------------------- GPU generators
+
+_SCENE_LIB = None
+
+
+def _scene_lib():
+    global _SCENE_LIB
+    if _SCENE_LIB is None:
+        import ctypes
+        import os
+        path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libsvo_scenes.so")
+        if not os.path.exists(path):
+            raise ImportError("libsvo_scenes.so is not built")
+        L = ctypes.CDLL(path)
+        vp = ctypes.c_void_p
+        L.svo_scene_terrain.argtypes = [vp, ctypes.c_int, vp, ctypes.c_float, vp]
+        L.svo_scene_spheres.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, vp, vp]
+        L.svo_scene_payload.argtypes = [vp, ctypes.c_int, vp, vp]
+        L.svo_scene_camera_rays.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp]
+        _SCENE_LIB = L
+    return _SCENE_LIB
+
+
+def _chk(rc):
+    if rc != 0:
+        raise RuntimeError("scene kernel launch failed (cudaError %d)" % rc)
+
+
+def gpu_occupancy(side, heights=None, centers=None, radii=None, thickness=2.0):
+    """Occupancy bitmap (int32 CUDA tensor, 32 voxels per word along x)."""
+    import torch
+    w32 = max(1, side // 32)
+    bm = torch.zeros(w32 * side * side, dtype=torch.int32, device="cuda")
+    L = _scene_lib()
+    if heights is not None:
+        ht = torch.from_numpy(np.ascontiguousarray(heights, np.float32)).cuda()
+        _chk(L.svo_scene_terrain(bm.data_ptr(), side, ht.data_ptr(), float(thickness), None))
+    if centers is not None and len(centers):
+        boxes = np.array(sphere_boxes((side, side, side), centers, radii), np.int32)
+        params = np.concatenate([np.asarray(centers, np.float32), np.asarray(radii, np.float32)[:, None]], 1)
+        bt = torch.from_numpy(boxes).cuda()
+        pt = torch.from_numpy(np.ascontiguousarray(params)).cuda()
+        _chk(L.svo_scene_spheres(bm.data_ptr(), side, len(radii), bt.data_ptr(), pt.data_ptr(), None))
+        torch.cuda.synchronize()
+    return bm
+
+
+def gpu_payload_grid(bm, side):
+    """Dense (side, side, side) int32 CUDA tensor of payload words."""
+    import torch
+    grid = torch.empty((side, side, side), dtype=torch.int32, device="cuda")
+    _chk(_scene_lib().svo_scene_payload(bm.data_ptr(), side, grid.data_ptr(), None))
+    return grid
+
+
+def gpu_sphere_scene(side, n_spheres, seed):
+    centers, radii = sphere_scene_params(side, n_spheres, seed)
+    return gpu_payload_grid(gpu_occupancy(side, centers=centers, radii=radii), side)
+
+
+def gpu_terrain_scene(side, n_spheres, seed):
+    heights, centers, radii = terrain_scene_params(side, n_spheres, seed)
+    return gpu_payload_grid(gpu_occupancy(side, heights, centers, radii), side)
+
+
+def camera_constants(cam, W, H):
+    a = cam[:9].astype(np.float32)
+    c = np.zeros(17, np.float32)
+    c[:12] = cam[:12]
+    c[12] = F(2.0) / F(W)
+    c[13] = F(H) / F(W)
+    c[14], c[15], c[16] = PLANE_DIST * a[2], PLANE_DIST * a[5], PLANE_DIST * a[8]
+    return c
+
+
+def gpu_camera_rays(cam, W, H, out=None):
+    """(H*W, 6) float32 CUDA tensor of camera rays (same bits as camera_rays)."""
+    import torch
+    c = torch.from_numpy(camera_constants(cam, W, H)).cuda()
+    if out is None:
+        out = torch.empty((H * W, 6), dtype=torch.float32, device="cuda")
+    _chk(_scene_lib().svo_scene_camera_rays(c.data_ptr(), 0, 0, W, H, out.data_ptr(), None))
+    torch.cuda.synchronize()
+    return out
