@@ -40,7 +40,11 @@ W_PIX, H_PIX = 1920, 1080
 MEM_BUDGET = 8 << 30
 LIGHT = np.array([0.3, 0.8, 0.52], np.float32)
 LIGHT = (LIGHT / np.linalg.norm(LIGHT)).astype(np.float32)
-SHADOW_EPS = np.float32(1.5 / SIDE)
+
+
+def shadow_offset(side):
+    """Shadow-ray origin offset: 1.5 voxels along the light, float32."""
+    return (np.float32(1.5 / side) * LIGHT).astype(np.float32)
 
 
 def parse():
@@ -185,7 +189,7 @@ def setup_scene(args, rank, torch, svo, scenes):
     d = prim[idx, 3:]
     p = o + t[idx, None] * d
     L = torch.from_numpy(LIGHT).cuda()
-    so = p + SHADOW_EPS * L
+    so = p + torch.from_numpy(shadow_offset(side)).cuda()
     shadow = torch.cat([so, L.expand_as(so)], dim=1).contiguous()
     # per-camera slices of the shadow array (hits are in camera order)
     cam_of_hit = (idx // npix).cpu().numpy()
@@ -247,7 +251,9 @@ def run_ours(args):
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+    smi_index = vis.split(",")[local] if vis else local
+    with ClockSampler(smi_index) as clk:
         start.record(stream)
         for k in range(args.steps):
             step(evs[k])
@@ -357,14 +363,81 @@ def profiled_traffic(rays):
 
 
 def run_reference(args):
+    """The reference's raymarch (VoxelOctree::raymarch restated in C, the
+    oracle) over all host threads, on the same octree and rays as our arm.
+    Setup uses no GPU code: the scene and octree come from oracle/scene_build.c
+    and the rays from scenes.py (both bit-identical to the GPU generators)."""
     rank, world, local = dist_setup(args)
     if rank != 0:
         return
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import importlib.util
     import pyoracle
     pyoracle.build_oracle(with_reference=False)
-    print(json.dumps({"impl": "reference", "unavailable": "CPU-side scene build for the reference arm not wired "
-                                                          "yet"}))
+    oracle = pyoracle.Oracle()
+    spec = importlib.util.spec_from_file_location("svo_scenes_cpu",
+                                                  os.path.join(ROOT, "sparse-voxel-octrees_gb300", "scenes.py"))
+    scenes = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(scenes)
+    threads = cpu_threads()
+    side = args.side
+    log_side = side.bit_length() - 1
+    t0 = time.perf_counter()
+    heights, centers, radii = scenes.terrain_scene_params(side, N_SPHERES, SCENE_SEED)
+    boxes = scenes.sphere_boxes((side,) * 3, centers, radii)
+    params = np.concatenate([centers, radii[:, None]], 1)
+    keys, pay = oracle.scene_voxels(side, heights, boxes, params, threads=threads)
+    words = oracle.build_sorted(keys, pay, log_side)
+    n_vox = keys.size
+    del keys, pay
+    center = np.array([0.5, 0.5, 0.5], np.float32)
+    cams = scenes.orbit_cameras(args.cams, 1000 + rank, center, radius=1.25, radius_hi=2.0, pitch=45.0)
+    prims = [scenes.camera_rays(c, args.width, args.height) for c in cams]
+    shadows = []
+    for r in prims:  # primary pass once to derive the shadow rays, as in our arm
+        out = oracle.raymarch(words, r, threads=threads)
+        hit = out["hit"] == 1
+        p = r[hit, :3] + out["t"][hit, None] * r[hit, 3:]
+        so = p + shadow_offset(side)
+        shadows.append(np.concatenate([so, np.broadcast_to(LIGHT, so.shape)], 1).astype(np.float32))
+    setup_s = time.perf_counter() - t0
+    per_step = 4  # cameras per timed step (a bounded sample of the 32-camera step)
+
+    def step(k):
+        n = 0
+        for j in range(per_step):
+            i = (k * per_step + j) % len(prims)
+            oracle.raymarch(words, prims[i], light=LIGHT, threads=threads)
+            oracle.raymarch(words, shadows[i], threads=threads)
+            n += prims[i].shape[0] + shadows[i].shape[0]
+        return n
+
+    for k in range(args.warmup):
+        step(k)
+    t0 = time.perf_counter()
+    rays = 0
+    for k in range(args.steps):
+        rays += step(args.warmup + k)
+    secs = time.perf_counter() - t0
+    value = rays / secs / 1e6
+    rays_full = sum(p.shape[0] for p in prims) + sum(s.shape[0] for s in shadows)
+    sample = ("%d cameras (primary + shadow rays) per step of the %d-camera workload; %d rays in %.1f s on %d host "
+              "threads; oracle C restatement of VoxelOctree::raymarch (the reference's own build needs its sources, "
+              "absent on the GPU host)" % (per_step, len(prims), rays, secs, threads))
+    line = {
+        "impl": "reference", "metric": "Mrays/s", "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(secs / args.steps * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded terrain + spheres, seeded orbit cameras)",
+        "config": {"workload": "plain traversal: %d^3 octree (terrain + %d spheres), %d cams %dx%d primary rays "
+                               "+ 1 shadow ray per hit" % (side, N_SPHERES, args.cams, args.width, args.height),
+                   "octree_words": int(words.size), "voxels": int(n_vox), "rays_per_full_step": int(rays_full),
+                   "setup_s": round(setup_s, 1)},
+        "cpu_baseline": {"value": round(value, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
 
 
 def main():

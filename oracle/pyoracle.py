@@ -69,6 +69,13 @@ class Oracle:
         L.svo_oracle_oct_decode.restype = ctypes.c_int
         L.svo_oracle_oct_decode.argtypes = [_u8p, ctypes.c_uint64, ctypes.POINTER(_u32p), _u64p, _f32p]
         L.svo_oracle_free.argtypes = [_vp]
+        L.svo_oracle_scene_voxels.restype = ctypes.c_int
+        L.svo_oracle_scene_voxels.argtypes = [ctypes.c_int, _f32p, ctypes.c_float, ctypes.POINTER(ctypes.c_int),
+                                              _f32p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_u64p),
+                                              ctypes.POINTER(_u32p), _u64p]
+        L.svo_oracle_build_sorted.restype = ctypes.c_int
+        L.svo_oracle_build_sorted.argtypes = [_u64p, _u32p, ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(_u32p),
+                                              _u64p]
 
     # -- codec / shading
     def inv_sqrt(self, x):
@@ -128,6 +135,41 @@ class Oracle:
         words = np.ctypeslib.as_array(p, shape=(n.value,)).copy() if n.value else np.zeros(0, np.uint32)
         self.L.svo_oracle_free(ctypes.cast(p, _vp))
         return words, c
+
+    def scene_voxels(self, side, heights=None, boxes=None, params=None, thickness=2.0, threads=None):
+        """CPU scene generation (scene_build.c): Morton-ordered (keys, payload)."""
+        threads = threads or os.cpu_count() or 1
+        hp = None
+        if heights is not None:
+            heights = np.ascontiguousarray(heights, dtype=np.float32)
+            hp = _ptr(heights, _f32p)
+        n = 0 if boxes is None else len(boxes)
+        bx = np.ascontiguousarray(np.asarray(boxes if n else np.zeros((1, 6)), dtype=np.int32))
+        pr = np.ascontiguousarray(np.asarray(params if n else np.zeros((1, 4)), dtype=np.float32))
+        kp, pp, nv = _u64p(), _u32p(), ctypes.c_uint64()
+        rc = self.L.svo_oracle_scene_voxels(int(side), hp, float(thickness), bx.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                            _ptr(pr, _f32p), n, int(threads), ctypes.byref(kp), ctypes.byref(pp),
+                                            ctypes.byref(nv))
+        if rc != 0:
+            raise RuntimeError("svo_oracle_scene_voxels failed: %d" % rc)
+        N = nv.value
+        keys = np.ctypeslib.as_array(kp, shape=(N,)).copy() if N else np.zeros(0, np.uint64)
+        pay = np.ctypeslib.as_array(pp, shape=(N,)).copy() if N else np.zeros(0, np.uint32)
+        self.L.svo_oracle_free(ctypes.cast(kp, _vp))
+        self.L.svo_oracle_free(ctypes.cast(pp, _vp))
+        return keys, pay
+
+    def build_sorted(self, keys, payload, log_side):
+        keys = np.ascontiguousarray(keys, dtype=np.uint64)
+        payload = np.ascontiguousarray(payload, dtype=np.uint32)
+        p, n = _u32p(), ctypes.c_uint64()
+        rc = self.L.svo_oracle_build_sorted(_ptr(keys, _u64p), _ptr(payload, _u32p), keys.size, int(log_side),
+                                            ctypes.byref(p), ctypes.byref(n))
+        if rc != 0:
+            raise RuntimeError("svo_oracle_build_sorted failed: %d" % rc)
+        words = np.ctypeslib.as_array(p, shape=(n.value,)).copy()
+        self.L.svo_oracle_free(ctypes.cast(p, _vp))
+        return words
 
     def cache_block(self, w, h, d, mem, cell_cost=4):
         return int(self.L.svo_oracle_cache_block(w, h, d, int(mem), int(cell_cost)))

@@ -69,6 +69,19 @@ int svo_oracle_oct_decode(const uint8_t *bytes, uint64_t len, uint32_t **words, 
 
 void svo_oracle_free(void *p);
 
+/* scene_build.c: the synthetic scene of scenes.py on host threads.  box: 6
+ * ints per sphere (x0, x1, y0, y1, z0, z1), params: 4 floats (cx, cy, cz, r);
+ * heights may be NULL.  Returns Morton-ordered keys and payload words
+ * (free both with svo_oracle_free). */
+int svo_oracle_scene_voxels(int side, const float *heights, float thickness, const int *box, const float *params,
+                            int n_spheres, int threads, uint64_t **keys, uint32_t **payload, uint64_t *n_voxels);
+
+/* Octree words of VoxelOctree(VoxelData*) for a cube of edge 2^log_side
+ * given its voxels in ascending Morton order (equal power-of-two dims only,
+ * where the reference's VoxelData corner cases do not arise). */
+int svo_oracle_build_sorted(const uint64_t *keys, const uint32_t *payload, uint64_t n, int log_side,
+                            uint32_t **words, uint64_t *n_words);
+
 #ifdef __cplusplus
 }
 #endif
