@@ -129,6 +129,27 @@ int svo_octree_build_dense(const uint32_t *grid, int w, int h, int d, uint64_t m
  * w*h*d uint32, x fastest), i.e. VoxelData(const char *path, size_t mem). */
 int svo_octree_build_voxel_file(const char *path, uint64_t mem, svo_stream stream, svo_octree **out);
 
+/* No counterpart in the reference.  The GPU build of svo_octree_build_dense
+ * for callers that cannot allocate device memory while they run: a host
+ * application whose device memory is already handed to its own pool, or a
+ * frame loop that must not take the device-wide synchronisation that
+ * cudaMalloc / cudaFree imply.  This call allocates nothing: its working
+ * memory is one fixed 32 MiB device arena inside the library (reserved on
+ * every device that loads the library, until the process exits), and the
+ * caller passes the device grid and a device buffer of `capacity` words for
+ * the result.  On success *n_words holds the octree's word count and
+ * center[3] its center; the words are byte-identical to svo_octree_build_dense.
+ *   Limits: virtual side <= 256 and at most 262,144 occupied voxels;
+ *   larger inputs, or an output buffer smaller than the octree (*n_words is
+ *   still set), return SVO_ERR_LIMIT.
+ *   The first call on a device looks up the arena's device address; make
+ *   that first call before any stream capture on that device.
+ *   All calls share the one arena, so calls that overlap on the GPU (from
+ *   several host threads or streams at once) race and must be serialised by
+ *   the caller.  The call returns after its work on `stream` is complete. */
+int svo_octree_build_dense_noalloc(const uint32_t *d_grid, int w, int h, int d, uint64_t mem, uint32_t *d_words,
+                                   uint64_t capacity, uint64_t *n_words, float center[3], svo_stream stream);
+
 /* ------------------------------------------------------------------- trace */
 
 /* Per-ray outputs; any pointer may be NULL to skip that output.

@@ -31,6 +31,7 @@
 //     the full data, so an M-block whose only voxels lie in that slice still
 //     appears as a descriptor with no children.
 #include <cstdio>
+#include <mutex>
 
 #include "scan.cuh"
 #include "svo_internal.h"
@@ -561,3 +562,255 @@ int build_dense_device(const uint32_t *d_grid, int w, int h, int d, int log_side
 }
 
 }  // namespace svo
+
+// ---- allocation-free build ---------------------------------------------------
+//
+// svo_octree_build_dense_noalloc: the build above for callers that must not
+// allocate device memory at call time.  Its scratch is the file-scope arena
+// below (32 MiB, reserved on every device that loads the library until the
+// process exits); inputs and the output word buffer come from the caller.
+namespace svo {
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = 32ull << 20;
+constexpr uint64_t kNoAllocMaxVoxels = 1ull << 18;
+constexpr int kNoAllocMaxSide = 256;
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_build_scratch[kNoAllocScratchBytes];
+
+std::mutex g_scratch_mtx;
+void *g_scratch_addr[kNoAllocMaxDevices] = {};
+
+// Device address of the arena for the current device.  The first call on a
+// device resolves it (cudaGetSymbolAddress) with that device current.
+int scratch_for_current_device(unsigned char **out) {
+    int dev = 0;
+    SVO_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return set_error(SVO_ERR_LIMIT, "device ordinal %d unsupported", dev);
+    std::lock_guard<std::mutex> lock(g_scratch_mtx);
+    if (!g_scratch_addr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_build_scratch);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(build scratch)");
+        g_scratch_addr[dev] = p;
+    }
+    *out = (unsigned char *)g_scratch_addr[dev];
+    return SVO_OK;
+}
+
+// Bump allocator over the arena; every call starts from offset 0.
+struct Arena {
+    unsigned char *base;
+    size_t used = 0;
+    template <typename T>
+    T *take(uint64_t n) {
+        size_t bytes = ((size_t)(n ? n : 1) * sizeof(T) + 255) & ~size_t(255);
+        if (used + bytes > kNoAllocScratchBytes) return nullptr;
+        T *p = (T *)(base + used);
+        used += bytes;
+        return p;
+    }
+};
+
+#define SVO_ARENA_TAKE(ptr, T, n)                                                                  \
+    T *ptr = arena.take<T>(n);                                                                     \
+    if (!ptr) return set_error(SVO_ERR_LIMIT, "build scratch (%zu bytes) exhausted", kNoAllocScratchBytes)
+
+template <typename TO>
+int arena_scan(Arena &arena, const uint32_t *in, TO *out, uint64_t n, TO *total_host, cudaStream_t st) {
+    size_t mark = arena.used;
+    SVO_ARENA_TAKE(scratch, TO, scan_scratch_elems(n));
+    SVO_ARENA_TAKE(tot, TO, 1);
+    SVO_CUDA_TRY((exclusive_scan<uint32_t, TO>(in, out, n, tot, scratch, st)));
+    SVO_CUDA_TRY(cudaMemcpyAsync(total_host, tot, sizeof(TO), cudaMemcpyDeviceToHost, st));
+    SVO_CUDA_TRY(cudaStreamSynchronize(st));
+    arena.used = mark;
+    return SVO_OK;
+}
+
+struct ArenaLevel {
+    uint64_t n = 0;
+    uint64_t *key = nullptr, *S = nullptr, *B = nullptr;
+    uint32_t *start = nullptr;
+    uint8_t *mask = nullptr, *count = nullptr, *large = nullptr;
+};
+
+int build_dense_noalloc(const uint32_t *d_grid, int w, int h, int d, int log_side, int log_block, cudaStream_t st,
+                        uint32_t *d_words, uint64_t capacity, uint64_t *n_words_out) {
+    Arena arena;
+    int rc = scratch_for_current_device(&arena.base);
+    if (rc) return rc;
+    const int D = log_side;
+    const int log_brick = D < 4 ? D : 4;
+    const uint64_t n_bricks = 1ull << (3 * (D - log_brick));
+    const bool multi_block = log_block < D;
+    const uint64_t n_blocks = multi_block ? (1ull << (3 * (D - log_block))) : 0;
+
+    GridGeom g;
+    g.grid = d_grid;
+    g.w = w;
+    g.h = h;
+    g.d = d;
+    g.log_brick = log_brick;
+    g.drop_last_z = ((d & 1) && log_block >= 2) ? 1 : 0;
+    g.log_block = log_block;
+    g.topflag = nullptr;
+    if (multi_block) {
+        SVO_ARENA_TAKE(tf, uint8_t, n_blocks);
+        SVO_CUDA_TRY(cudaMemsetAsync(tf, 0, n_blocks, st));  // the arena keeps the previous call's bytes
+        g.topflag = tf;
+    }
+    SVO_ARENA_TAKE(bcount, uint32_t, n_bricks);
+    SVO_ARENA_TAKE(boff, uint64_t, n_bricks);
+    unsigned grid1 = (unsigned)(n_bricks < (1ull << 20) ? n_bricks : (1ull << 20));
+    k_brick_count<<<grid1, kBrickThreads, 0, st>>>(g, n_bricks, bcount);
+    SVO_LAUNCH_CHECK("k_brick_count");
+    uint64_t N = 0;
+    rc = arena_scan<uint64_t>(arena, bcount, boff, n_bricks, &N, st);
+    if (rc) return rc;
+    if (N > kNoAllocMaxVoxels)
+        return set_error(SVO_ERR_LIMIT, "%llu occupied voxels exceed the allocation-free build's limit of %llu",
+                         (unsigned long long)N, (unsigned long long)kNoAllocMaxVoxels);
+    SVO_ARENA_TAKE(lkey, uint64_t, N);
+    SVO_ARENA_TAKE(lpay, uint32_t, N);
+    if (N) {
+        k_brick_emit<<<grid1, kBrickThreads, 0, st>>>(g, n_bricks, bcount, boff, lkey, lpay);
+        SVO_LAUNCH_CHECK("k_brick_emit");
+    }
+
+    ArenaLevel lv[17];
+    uint32_t *leaf_pidx = nullptr;
+    const uint64_t *ckey = lkey;
+    uint64_t nc = N;
+    for (int e = 1; e <= D; ++e) {
+        ArenaLevel &L = lv[e];
+        SVO_ARENA_TAKE(head, uint32_t, nc);
+        SVO_ARENA_TAKE(pidx, uint32_t, nc);
+        if (nc) {
+            k_heads<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, head);
+            SVO_LAUNCH_CHECK("k_heads");
+        }
+        uint32_t np = 0;
+        if (multi_block && e == log_block) {
+            SVO_ARENA_TAKE(first, uint32_t, n_blocks);
+            SVO_ARENA_TAKE(present, uint32_t, n_blocks);
+            SVO_ARENA_TAKE(bidx, uint32_t, n_blocks);
+            SVO_CUDA_TRY(cudaMemsetAsync(first, 0xFF, n_blocks * sizeof(uint32_t), st));
+            if (nc) k_block_first<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, head, first);
+            k_block_present<<<blocks_for(n_blocks), 256, 0, st>>>(first, g.topflag, n_blocks, present);
+            SVO_LAUNCH_CHECK("k_block_present");
+            rc = arena_scan<uint32_t>(arena, present, bidx, n_blocks, &np, st);
+            if (rc) return rc;
+            L.n = np;
+            SVO_ARENA_TAKE(key, uint64_t, np);
+            SVO_ARENA_TAKE(start, uint32_t, np);
+            L.key = key;
+            L.start = start;
+            k_block_parents<<<blocks_for(n_blocks), 256, 0, st>>>(first, present, bidx, n_blocks, nc, L.key, L.start);
+            if (nc) k_child_pidx_from_blocks<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, bidx, pidx);
+            SVO_LAUNCH_CHECK("k_child_pidx_from_blocks");
+        } else {
+            rc = arena_scan<uint32_t>(arena, head, pidx, nc, &np, st);
+            if (rc) return rc;
+            L.n = np;
+            SVO_ARENA_TAKE(key, uint64_t, np);
+            SVO_ARENA_TAKE(start, uint32_t, np);
+            L.key = key;
+            L.start = start;
+            if (nc) {
+                k_parents_from_heads<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, head, pidx, L.key, L.start);
+                k_child_pidx_from_heads<<<blocks_for(nc), 256, 0, st>>>(head, nc, pidx);
+                SVO_LAUNCH_CHECK("k_child_pidx_from_heads");
+            }
+        }
+        if (e == D && L.n == 0) {
+            L.n = 1;
+            SVO_ARENA_TAKE(key, uint64_t, 1);
+            SVO_ARENA_TAKE(start, uint32_t, 1);
+            L.key = key;
+            L.start = start;
+            SVO_CUDA_TRY(cudaMemsetAsync(L.key, 0, sizeof(uint64_t), st));
+            SVO_CUDA_TRY(cudaMemsetAsync(L.start, 0, sizeof(uint32_t), st));
+        }
+        SVO_ARENA_TAKE(mask, uint8_t, L.n);
+        SVO_ARENA_TAKE(count, uint8_t, L.n);
+        L.mask = mask;
+        L.count = count;
+        k_parent_masks<<<blocks_for(L.n), 256, 0, st>>>(L.key, L.start, L.n, ckey, nc, L.mask, L.count);
+        SVO_LAUNCH_CHECK("k_parent_masks");
+        if (e == 1) leaf_pidx = pidx;
+        ckey = L.key;
+        nc = L.n;
+    }
+    for (int e = 1; e <= D; ++e) {
+        ArenaLevel &L = lv[e];
+        SVO_ARENA_TAKE(S, uint64_t, L.n);
+        SVO_ARENA_TAKE(large, uint8_t, L.n);
+        L.S = S;
+        L.large = large;
+        k_subtree<<<blocks_for(L.n), 256, 0, st>>>(L.n, L.count, L.start, e > 1 ? lv[e - 1].S : nullptr, e == 1,
+                                                  L.S, L.large);
+        SVO_LAUNCH_CHECK("k_subtree");
+    }
+    uint64_t S_root = 0;
+    SVO_CUDA_TRY(cudaMemcpyAsync(&S_root, lv[D].S, sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+    SVO_CUDA_TRY(cudaStreamSynchronize(st));
+    const uint64_t W = 1 + S_root;
+    *n_words_out = W;
+    if (W > capacity)
+        return set_error(SVO_ERR_LIMIT, "octree needs %llu words; the output buffer holds %llu",
+                         (unsigned long long)W, (unsigned long long)capacity);
+    SVO_ARENA_TAKE(err, uint32_t, 1);
+    SVO_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(uint32_t), st));
+    SVO_ARENA_TAKE(rootB, uint64_t, 1);
+    lv[D].B = rootB;
+    k_set_u64<<<1, 1, 0, st>>>(lv[D].B, 1);
+    k_root_word<<<1, 1, 0, st>>>(lv[D].mask, lv[D].large, D == 1, d_words);
+    for (int e = D; e >= 2; --e) {
+        ArenaLevel &P = lv[e];
+        ArenaLevel &C = lv[e - 1];
+        SVO_ARENA_TAKE(cB, uint64_t, C.n);
+        C.B = cB;
+        k_place<<<blocks_for(P.n), 256, 0, st>>>(P.n, P.count, P.start, P.large, P.B, C.S, C.mask, C.large,
+                                                e - 1 == 1, C.B, d_words, W, err);
+        SVO_LAUNCH_CHECK("k_place");
+    }
+    if (N) {
+        k_place_leaves<<<blocks_for(N), 256, 0, st>>>(N, leaf_pidx, lv[1].n, lv[1].start, lv[1].B, lpay, d_words, W,
+                                                      err);
+        SVO_LAUNCH_CHECK("k_place_leaves");
+    }
+    uint32_t err_h = 0;
+    SVO_CUDA_TRY(cudaMemcpyAsync(&err_h, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    SVO_CUDA_TRY(cudaStreamSynchronize(st));
+    if (err_h) return set_error(SVO_ERR_DEVICE, "octree build placement check failed (flags %u)", err_h);
+    return SVO_OK;
+}
+
+}  // namespace
+}  // namespace svo
+
+extern "C" int svo_octree_build_dense_noalloc(const uint32_t *d_grid, int w, int h, int d, uint64_t mem,
+                                              uint32_t *d_words, uint64_t capacity, uint64_t *n_words,
+                                              float center[3], svo_stream stream) {
+    using namespace svo;
+    if (!d_grid || !d_words || !n_words || !center || w <= 0 || h <= 0 || d <= 0)
+        return set_error(SVO_ERR_INVALID, "bad arguments");
+    int side = 1;
+    while (side < w || side < h || side < d) side *= 2;
+    if (side < 2) return set_error(SVO_ERR_INVALID, "virtual side %d below 2 (the reference recurses forever)", side);
+    if (side > kNoAllocMaxSide)
+        return set_error(SVO_ERR_LIMIT, "virtual side %d exceeds the allocation-free build's limit of %d", side,
+                         kNoAllocMaxSide);
+    int lb = cache_block_log2(w, h, d, mem, 4);
+    if (lb < 1) return set_error(SVO_ERR_MEMORY, "memory budget %llu admits no cache block", (unsigned long long)mem);
+    int log_side = 0;
+    while ((1 << log_side) < side) ++log_side;
+    int rc = build_dense_noalloc(d_grid, w, h, d, log_side, lb, (cudaStream_t)stream, d_words, capacity, n_words);
+    if (rc) return rc;
+    center[0] = (float)w * 0.5f / (float)side;
+    center[1] = (float)h * 0.5f / (float)side;
+    center[2] = (float)d * 0.5f / (float)side;
+    return SVO_OK;
+}
