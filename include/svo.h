@@ -190,6 +190,63 @@ int svo_trace_host(svo_octree *oct, const float *rays, uint64_t n, float ray_sca
 int svo_trace_count_loads(const svo_octree *oct, const float *rays, uint64_t n, float ray_scale,
                           uint32_t *loads, svo_stream stream);
 
+/* ----------------------------------------------------------------- batched */
+
+/* One (octree, view) pair of a batched trace.  A view is either
+ *   - an image: width x height pixels, rays from `rays` (device, row-major
+ *     width*height records) or, when rays == NULL, generated in the kernel
+ *     from `camera` with the viewer's formula (Main.cpp:149-176):
+ *     camera = {a11..a33 (row-major rotation), px, py, pz (position),
+ *     2/width, height/width, zx, zy, zz} with (zx, zy, zz) = (a13, a23, a33)
+ *     / tan(pi/6); outputs are indexed y*width + x;
+ *   - or linear: width == 0, n_rays rays from `rays`, outputs by ray index.
+ * Each view has its own ray_scale, light and device outputs. */
+typedef struct svo_view {
+    const svo_octree *octree;
+    const float *rays;
+    uint64_t n_rays;
+    uint32_t width, height;
+    float camera[17];
+    float ray_scale;
+    float light[3];
+    svo_trace_out out;
+} svo_view;
+
+/* Launch shape of the persistent traversal kernel (see svo_batch_autotune). */
+typedef struct svo_trace_config {
+    int block_threads;   /* threads per CTA, multiple of 32, <= 1024 */
+    int blocks_per_sm;   /* persistent grid = SM count x blocks_per_sm */
+    int refill_idle;     /* a warp refills its idle lanes once this many (1..32) are idle */
+    int steps_per_round; /* traversal steps between refill checks */
+    int tile_w;          /* image tile width in pixels: 4, 8, 16 or 32 (tile = tile_w x 32/tile_w) */
+    int chunk;           /* ray slots a warp takes from the work queue at once (multiple of 32) */
+} svo_trace_config;
+
+typedef struct svo_batch svo_batch;
+
+/* No counterpart in the reference (its viewer renders one octree per frame
+ * on host threads, Main.cpp:139-262).  Records the views and uploads the job
+ * table; the octrees and output buffers must outlive the batch. */
+int svo_batch_create(const svo_view *views, int n_views, svo_batch **out);
+int svo_batch_default_config(svo_trace_config *cfg);
+/* Number of work-queue slots (rays plus padding of partial pixel tiles). */
+int svo_batch_num_slots(svo_batch *b, uint64_t *slots);
+/* One persistent launch over every view (asynchronous on `stream`). */
+int svo_batch_trace(svo_batch *b, const svo_trace_config *cfg, svo_stream stream);
+/* Captures the queue reset and the launch into a CUDA graph owned by the
+ * batch; svo_batch_launch_graph replays it on any stream. */
+int svo_batch_capture_graph(svo_batch *b, const svo_trace_config *cfg);
+int svo_batch_launch_graph(svo_batch *b, svo_stream stream);
+/* Times candidate launch shapes (block size, refill threshold, steps per
+ * round, tile width) on this batch and returns the fastest; results are
+ * cached per device and workload in a JSON-lines file ($SVO_AUTOTUNE_CACHE,
+ * default ~/.cache/svo_gb300_autotune.jsonl; SVO_AUTOTUNE_FORCE=1 re-times).
+ * *best_ms is -1 when the cache answered.  Synchronises `stream`. */
+int svo_batch_autotune(svo_batch *b, svo_trace_config *best, float *best_ms, svo_stream stream);
+/* Reads and clears the batch's device error word (as svo_octree_device_status). */
+int svo_batch_status(svo_batch *b, uint32_t *flags);
+int svo_batch_destroy(svo_batch *b);
+
 #ifdef __cplusplus
 }
 #endif

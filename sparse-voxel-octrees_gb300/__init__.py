@@ -50,6 +50,20 @@ class TraceOut(ctypes.Structure):
     _fields_ = [("hit", _vp), ("t", _vp), ("leaf", _vp), ("word", _vp), ("rgb", _vp)]
 
 
+class View(ctypes.Structure):
+    _fields_ = [("octree", _vp), ("rays", _vp), ("n_rays", ctypes.c_uint64), ("width", ctypes.c_uint32),
+                ("height", ctypes.c_uint32), ("camera", ctypes.c_float * 17), ("ray_scale", ctypes.c_float),
+                ("light", ctypes.c_float * 3), ("out", TraceOut)]
+
+
+class TraceConfig(ctypes.Structure):
+    _fields_ = [("block_threads", ctypes.c_int), ("blocks_per_sm", ctypes.c_int), ("refill_idle", ctypes.c_int),
+                ("steps_per_round", ctypes.c_int), ("tile_w", ctypes.c_int), ("chunk", ctypes.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 def _load():
     if not os.path.exists(LIB_PATH):
         raise ImportError("libsvo_gb300.so is not built (run __graft_entry__.build() or "
@@ -78,6 +92,15 @@ def _load():
         "svo_trace_host": (ctypes.c_int, [_vp, _vp, ctypes.c_uint64, ctypes.c_float, _f32p,
                                           ctypes.POINTER(TraceOut)]),
         "svo_trace_count_loads": (ctypes.c_int, [_vp, _vp, ctypes.c_uint64, ctypes.c_float, _vp, _vp]),
+        "svo_batch_create": (ctypes.c_int, [ctypes.POINTER(View), ctypes.c_int, ctypes.POINTER(_vp)]),
+        "svo_batch_default_config": (ctypes.c_int, [ctypes.POINTER(TraceConfig)]),
+        "svo_batch_num_slots": (ctypes.c_int, [_vp, _u64p]),
+        "svo_batch_trace": (ctypes.c_int, [_vp, ctypes.POINTER(TraceConfig), _vp]),
+        "svo_batch_capture_graph": (ctypes.c_int, [_vp, ctypes.POINTER(TraceConfig)]),
+        "svo_batch_launch_graph": (ctypes.c_int, [_vp, _vp]),
+        "svo_batch_autotune": (ctypes.c_int, [_vp, ctypes.POINTER(TraceConfig), ctypes.POINTER(ctypes.c_float), _vp]),
+        "svo_batch_status": (ctypes.c_int, [_vp, _u32p]),
+        "svo_batch_destroy": (ctypes.c_int, [_vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -287,3 +310,84 @@ class VoxelOctree:
             n = rays.shape[0]
         check(lib.svo_trace_count_loads(self._h, _dev_ptr(rays), int(n), float(ray_scale), _dev_ptr(loads),
                                         _stream_ptr(stream)))
+
+
+def default_config(**overrides):
+    c = TraceConfig()
+    check(lib.svo_batch_default_config(ctypes.byref(c)))
+    for k, v in overrides.items():
+        setattr(c, k, int(v))
+    return c
+
+
+class Batch:
+    """Many (octree, view) pairs traced by one persistent launch (svo_batch_*).
+
+    views: list of dicts with keys octree (VoxelOctree), and either
+      rays (CUDA tensor (R, 6)) [+ width, height for image order], or
+      camera (17 floats, scenes.camera_constants) + width + height;
+    optional ray_scale, light, and out: dict of CUDA tensors (hit/t/leaf/word/rgb).
+    """
+
+    def __init__(self, views):
+        self._keep = views
+        arr = (View * len(views))()
+        for i, v in enumerate(views):
+            cv = arr[i]
+            cv.octree = v["octree"].handle.value
+            rays = v.get("rays")
+            cv.rays = _dev_ptr(rays).value if rays is not None else None
+            cv.width = int(v.get("width", 0))
+            cv.height = int(v.get("height", 0))
+            cv.n_rays = int(v.get("n_rays", rays.shape[0] if (rays is not None and not cv.width) else 0))
+            cam = v.get("camera")
+            if cam is not None:
+                for k in range(17):
+                    cv.camera[k] = float(cam[k])
+            cv.ray_scale = float(v.get("ray_scale", 0.0))
+            lt = v.get("light", (0.0, 0.0, 1.0))
+            for k in range(3):
+                cv.light[k] = float(lt[k])
+            out = v.get("out", {})
+            for k in ("hit", "t", "leaf", "word", "rgb"):
+                t = out.get(k)
+                setattr(cv.out, k, _dev_ptr(t).value if t is not None else None)
+        self._h = _vp()
+        check(lib.svo_batch_create(arr, len(views), ctypes.byref(self._h)))
+
+    def close(self):
+        if self._h:
+            lib.svo_batch_destroy(self._h)
+            self._h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def num_slots(self):
+        n = ctypes.c_uint64()
+        check(lib.svo_batch_num_slots(self._h, ctypes.byref(n)))
+        return n.value
+
+    def trace(self, config=None, stream=None):
+        check(lib.svo_batch_trace(self._h, ctypes.byref(config) if config is not None else None,
+                                  _stream_ptr(stream)))
+
+    def capture_graph(self, config=None):
+        check(lib.svo_batch_capture_graph(self._h, ctypes.byref(config) if config is not None else None))
+
+    def launch_graph(self, stream=None):
+        check(lib.svo_batch_launch_graph(self._h, _stream_ptr(stream)))
+
+    def autotune(self, stream=None):
+        c = TraceConfig()
+        ms = ctypes.c_float()
+        check(lib.svo_batch_autotune(self._h, ctypes.byref(c), ctypes.byref(ms), _stream_ptr(stream)))
+        return c, ms.value
+
+    def status(self):
+        f = ctypes.c_uint32()
+        check(lib.svo_batch_status(self._h, ctypes.byref(f)))
+        return f.value

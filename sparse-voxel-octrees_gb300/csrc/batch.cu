@@ -1,0 +1,553 @@
+// batch.cu — persistent, queue-driven traversal over many (octree, view)
+// pairs in one launch, its CUDA-graph capture and its autotuner.
+//
+// Work is a global space of ray slots: each view contributes either one slot
+// per ray (linear views) or 32 slots per tile_w x tile_h pixel tile (image
+// views, so a warp's lanes start on neighbouring pixels).  A persistent grid
+// of SMs x blocks_per_sm CTAs drains the space: each warp takes `chunk`
+// consecutive slots from one device counter with a single atomicAdd and hands
+// them to its idle lanes in ballot-rank order.  Lanes whose ray finishes go
+// idle; once at least `refill_idle` lanes of a warp are idle the warp refills
+// them, so lanes keep doing traversal steps instead of waiting for the
+// slowest ray of a fixed 32-ray batch.  Nothing waits on another warp or CTA.
+//
+// Each ray runs the same ray_init / ray_step as svo_trace (VoxelOctree.cpp:
+// 207-346), so results are bit-identical to the plain kernel's.
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "svo_device.cuh"
+#include "svo_internal.h"
+
+namespace svo {
+namespace {
+
+constexpr int kMaxSmemJobs = 2048;  // views whose slot offsets are staged in shared memory
+
+struct JobDev {
+    const uint32_t *oct;
+    uint32_t n_words;
+    uint32_t width, height, tiles_x;
+    const float *rays;
+    float cam[17];
+    float ray_scale, lx, ly, lz;
+    uint8_t *hit;
+    float *t;
+    uint32_t *leaf;
+    uint32_t *word;
+    float *rgb;
+};
+
+struct BatchArgs {
+    const JobDev *jobs;
+    const uint64_t *begin;  // n_jobs + 1 slot offsets
+    int n_jobs;
+    uint64_t total;
+    unsigned long long *queue;
+    uint32_t *status;
+    int refill_idle;
+    int steps_per_round;
+    int log_tile_w;
+    int chunk;
+};
+
+__device__ __forceinline__ int find_job(const uint64_t *beg, int n_jobs, uint64_t slot) {
+    int lo = 0, hi = n_jobs;  // beg[lo] <= slot < beg[hi]
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (beg[mid] <= slot) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+template <bool kLod>
+__global__ void k_trace_persistent(BatchArgs a) {
+    extern __shared__ uint64_t s_begin[];
+    const bool staged = a.n_jobs + 1 <= kMaxSmemJobs;
+    if (staged)
+        for (int i = threadIdx.x; i <= a.n_jobs; i += blockDim.x) s_begin[i] = a.begin[i];
+    __syncthreads();
+    const uint64_t *beg = staged ? s_begin : a.begin;
+
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    const int tile_w = 1 << a.log_tile_w;
+
+    RayState st;
+    RayStack stk;
+    bool active = false;
+    int job = 0;
+    uint32_t out_idx = 0, nw = 0;
+    const uint32_t *oct = nullptr;
+    float rdx = 0.f, rdy = 0.f, rdz = 0.f, rs = 0.f;
+    uint64_t pool_next = 0, pool_end = 0;
+    bool exhausted = false;
+
+    while (true) {
+        unsigned idle = ~__ballot_sync(FULL, active);
+        if (__popc(idle) >= a.refill_idle) {
+            while (idle) {
+                if (pool_next >= pool_end) {
+                    if (exhausted) break;
+                    unsigned long long base = 0;
+                    if (lane == 0) base = atomicAdd(a.queue, (unsigned long long)a.chunk);
+                    base = __shfl_sync(FULL, base, 0);
+                    if (base >= a.total) {
+                        exhausted = true;
+                        break;
+                    }
+                    pool_next = base;
+                    pool_end = min(base + (unsigned long long)a.chunk, (unsigned long long)a.total);
+                }
+                uint32_t avail = (uint32_t)(pool_end - pool_next);
+                uint32_t rank = __popc(idle & lt_mask);
+                bool mine = ((idle >> lane) & 1u) && rank < avail;
+                if (mine) {
+                    uint64_t slot = pool_next + rank;
+                    int j = find_job(beg, a.n_jobs, slot);
+                    const JobDev &J = a.jobs[j];
+                    uint64_t local = slot - beg[j];
+                    uint32_t px = 0, py = 0;
+                    bool live = true;
+                    if (J.width) {
+                        uint64_t tile = local >> 5;
+                        uint32_t r = (uint32_t)(local & 31);
+                        px = (uint32_t)(tile % J.tiles_x) * tile_w + (r & (tile_w - 1));
+                        py = (uint32_t)(tile / J.tiles_x) * (32 >> a.log_tile_w) + (r >> a.log_tile_w);
+                        live = px < J.width && py < J.height;
+                        out_idx = py * J.width + px;
+                    } else {
+                        out_idx = (uint32_t)local;
+                    }
+                    if (live) {
+                        float ox, oy, oz, dx, dy, dz;
+                        if (J.rays) {
+                            const float2 *r2 = reinterpret_cast<const float2 *>(J.rays) + 3 * (uint64_t)out_idx;
+                            float2 p0 = __ldg(r2), p1 = __ldg(r2 + 1), p2 = __ldg(r2 + 2);
+                            ox = p0.x; oy = p0.y; oz = p1.x;
+                            dx = p1.y; dy = p2.x; dz = p2.y;
+                        } else {
+                            // The viewer's camera ray (Main.cpp:167-176), as scenes.camera_rays.
+                            const float *c = J.cam;
+                            float sx = -1.0f + (float)px * c[12];
+                            float sy = c[13] - (float)py * c[12];
+                            float vx = (sx * c[0] + sy * c[1]) + c[14];
+                            float vy = (sx * c[3] + sy * c[4]) + c[15];
+                            float vz = (sx * c[6] + sy * c[7]) + c[16];
+                            float n = inv_sqrt((vx * vx + vy * vy) + vz * vz);
+                            ox = c[9]; oy = c[10]; oz = c[11];
+                            dx = vx * n; dy = vy * n; dz = vz * n;
+                        }
+                        ray_init(st, J.oct, ox, oy, oz, dx, dy, dz);
+                        rdx = dx; rdy = dy; rdz = dz;
+                        job = j;
+                        oct = J.oct;
+                        nw = J.n_words;
+                        rs = J.ray_scale;
+                        active = true;
+                    }
+                }
+                unsigned taken = __ballot_sync(FULL, mine);
+                pool_next += __popc(taken);
+                idle &= ~taken;
+            }
+        }
+        if (!__any_sync(FULL, active)) {
+            if (exhausted && pool_next >= pool_end) break;
+            continue;
+        }
+        if (active) {
+            for (int k = 0; k < a.steps_per_round; ++k) {
+                RayResult res;
+                if (ray_step<false, kLod>(st, stk, oct, nw, rs, res)) {
+                    const JobDev &J = a.jobs[job];
+                    if (res.status == kFault) atomicOr(a.status, 1u);
+                    uint8_t hs = res.status == kFault ? 0 : (uint8_t)res.status;
+                    bool leaf = res.status == kLeafHit;
+                    if (J.hit) J.hit[out_idx] = hs;
+                    if (J.t) J.t[out_idx] = hs == 0 ? __int_as_float(0x7f800000) : res.t;
+                    if (J.leaf) J.leaf[out_idx] = leaf ? res.leaf : 0xFFFFFFFFu;
+                    if (J.word) J.word[out_idx] = leaf ? res.word : 0u;
+                    if (J.rgb) {
+                        float g = leaf ? shade_grey(res.word, rdx, rdy, rdz, J.lx, J.ly, J.lz) : 0.0f;
+                        J.rgb[3 * (uint64_t)out_idx + 0] = g;
+                        J.rgb[3 * (uint64_t)out_idx + 1] = g;
+                        J.rgb[3 * (uint64_t)out_idx + 2] = g;
+                    }
+                    active = false;
+                    break;
+                }
+            }
+        }
+    }
+}
+
+int log2_of(int v) {
+    int r = 0;
+    while ((1 << r) < v) ++r;
+    return r;
+}
+
+bool config_ok(const svo_trace_config &c) {
+    return c.block_threads >= 32 && c.block_threads <= 1024 && c.block_threads % 32 == 0 && c.blocks_per_sm >= 1 &&
+           c.blocks_per_sm <= 32 && c.refill_idle >= 1 && c.refill_idle <= 32 && c.steps_per_round >= 1 &&
+           c.steps_per_round <= 4096 && (c.tile_w == 4 || c.tile_w == 8 || c.tile_w == 16 || c.tile_w == 32) &&
+           c.chunk >= 32 && c.chunk <= 8192 && c.chunk % 32 == 0;
+}
+
+}  // namespace
+}  // namespace svo
+
+struct svo_batch {
+    std::vector<svo_view> views;
+    std::vector<uint64_t> begin_h;  // slot offsets for the tile width of begin_tile_w
+    int begin_tile_w = 0;
+    svo::JobDev *jobs_d = nullptr;
+    uint64_t *begin_d = nullptr;
+    unsigned long long *queue_d = nullptr;
+    uint32_t *status_d = nullptr;
+    uint64_t total = 0;
+    bool any_lod = false;
+    int device = 0, num_sms = 0;
+    cudaStream_t cap_stream = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+namespace svo {
+namespace {
+
+// Uploads the job table and slot offsets for tile width `tile_w`.
+int prepare_jobs(svo_batch *b, int tile_w) {
+    if (b->begin_tile_w == tile_w) return SVO_OK;
+    const int n = (int)b->views.size();
+    const int th = 32 / tile_w;
+    std::vector<JobDev> jobs(n);
+    std::vector<uint64_t> beg(n + 1, 0);
+    for (int i = 0; i < n; ++i) {
+        const svo_view &v = b->views[i];
+        JobDev &J = jobs[i];
+        std::memset(&J, 0, sizeof(J));
+        J.oct = v.octree->d_words;
+        J.n_words = (uint32_t)v.octree->n_words;
+        J.width = v.width;
+        J.height = v.height;
+        J.tiles_x = v.width ? (v.width + tile_w - 1) / tile_w : 0;
+        J.rays = v.rays;
+        std::memcpy(J.cam, v.camera, sizeof(J.cam));
+        J.ray_scale = v.ray_scale;
+        J.lx = v.light[0];
+        J.ly = v.light[1];
+        J.lz = v.light[2];
+        J.hit = v.out.hit;
+        J.t = v.out.t;
+        J.leaf = v.out.leaf;
+        J.word = v.out.word;
+        J.rgb = v.out.rgb;
+        uint64_t slots = v.width ? (uint64_t)J.tiles_x * ((v.height + th - 1) / th) * 32 : v.n_rays;
+        beg[i + 1] = beg[i] + slots;
+    }
+    SVO_CUDA_TRY(cudaMemcpy(b->jobs_d, jobs.data(), n * sizeof(JobDev), cudaMemcpyHostToDevice));
+    SVO_CUDA_TRY(cudaMemcpy(b->begin_d, beg.data(), (n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice));
+    b->begin_h = beg;
+    b->total = beg[n];
+    b->begin_tile_w = tile_w;
+    return SVO_OK;
+}
+
+int enqueue_trace(svo_batch *b, const svo_trace_config &c, cudaStream_t st) {
+    BatchArgs a;
+    a.jobs = b->jobs_d;
+    a.begin = b->begin_d;
+    a.n_jobs = (int)b->views.size();
+    a.total = b->total;
+    a.queue = b->queue_d;
+    a.status = b->status_d;
+    a.refill_idle = c.refill_idle;
+    a.steps_per_round = c.steps_per_round;
+    a.log_tile_w = log2_of(c.tile_w);
+    a.chunk = c.chunk;
+    size_t smem = (a.n_jobs + 1 <= kMaxSmemJobs) ? (size_t)(a.n_jobs + 1) * sizeof(uint64_t) : 0;
+    // A persistent grid larger than what is resident only adds CTAs that
+    // start after the queue is drained: clamp to the occupancy limit.
+    int resident = 0;
+    if (b->any_lod)
+        SVO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k_trace_persistent<true>,
+                                                                   c.block_threads, smem));
+    else
+        SVO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k_trace_persistent<false>,
+                                                                   c.block_threads, smem));
+    int per_sm = std::max(1, std::min(c.blocks_per_sm, resident));
+    SVO_CUDA_TRY(cudaMemsetAsync(b->queue_d, 0, sizeof(unsigned long long), st));
+    dim3 grid((unsigned)(b->num_sms * per_sm));
+    if (b->any_lod)
+        k_trace_persistent<true><<<grid, c.block_threads, smem, st>>>(a);
+    else
+        k_trace_persistent<false><<<grid, c.block_threads, smem, st>>>(a);
+    SVO_CUDA_TRY(cudaGetLastError());
+    return SVO_OK;
+}
+
+// ---- autotuner cache: one JSON object per line, keyed by device and workload.
+std::string cache_path() {
+    const char *p = getenv("SVO_AUTOTUNE_CACHE");
+    if (p && *p) return p;
+    const char *home = getenv("HOME");
+    return std::string(home ? home : "/tmp") + "/.cache/svo_gb300_autotune.jsonl";
+}
+
+std::string workload_key(const svo_batch *b) {
+    cudaDeviceProp prop;
+    cudaGetDeviceProperties(&prop, b->device);
+    uint64_t words = 0, rays = 0;
+    int images = 0;
+    for (const auto &v : b->views) {
+        words += v.octree->n_words;
+        rays += v.width ? (uint64_t)v.width * v.height : v.n_rays;
+        images += v.width != 0;
+    }
+    char key[512];
+    snprintf(key, sizeof(key), "%s|views=%zu|images=%d|rays_log2=%d|words_log2=%d", prop.name, b->views.size(),
+             images, log2_of((int)std::min<uint64_t>(rays, 1u << 30)),
+             log2_of((int)std::min<uint64_t>(words, 1u << 30)));
+    for (char *c = key; *c; ++c)
+        if (*c == '"') *c = '\'';
+    return key;
+}
+
+bool cache_lookup(const std::string &key, svo_trace_config *c) {
+    FILE *fp = fopen(cache_path().c_str(), "r");
+    if (!fp) return false;
+    char line[1024];
+    bool found = false;
+    while (fgets(line, sizeof(line), fp)) {
+        std::string s(line);
+        std::string tag = "\"key\": \"" + key + "\"";
+        if (s.find(tag) == std::string::npos) continue;
+        svo_trace_config t;
+        const char *q = strstr(line, "\"block_threads\":");
+        if (q && sscanf(q, "\"block_threads\": %d, \"blocks_per_sm\": %d, \"refill_idle\": %d, \"steps_per_round\": %d, "
+                           "\"tile_w\": %d, \"chunk\": %d",
+                        &t.block_threads, &t.blocks_per_sm, &t.refill_idle, &t.steps_per_round, &t.tile_w,
+                        &t.chunk) == 6 &&
+            config_ok(t)) {
+            *c = t;
+            found = true;  // the last matching line wins
+        }
+    }
+    fclose(fp);
+    return found;
+}
+
+void cache_store(const std::string &key, const svo_trace_config &c, float ms) {
+    std::string path = cache_path();
+    size_t slash = path.rfind('/');
+    if (slash != std::string::npos) {
+        std::string dir = path.substr(0, slash);
+        std::string cmd = "mkdir -p '" + dir + "' 2>/dev/null";
+        if (system(cmd.c_str()) != 0) return;
+    }
+    FILE *fp = fopen(path.c_str(), "a");
+    if (!fp) return;
+    fprintf(fp,
+            "{\"key\": \"%s\", \"block_threads\": %d, \"blocks_per_sm\": %d, \"refill_idle\": %d, \"steps_per_round\": "
+            "%d, \"tile_w\": %d, \"chunk\": %d, \"ms\": %.4f}\n",
+            key.c_str(), c.block_threads, c.blocks_per_sm, c.refill_idle, c.steps_per_round, c.tile_w, c.chunk, ms);
+    fclose(fp);
+}
+
+}  // namespace
+}  // namespace svo
+
+using namespace svo;
+
+extern "C" {
+
+int svo_batch_destroy(svo_batch *b);
+
+int svo_batch_default_config(svo_trace_config *cfg) {
+    if (!cfg) return set_error(SVO_ERR_INVALID, "null argument");
+    cfg->block_threads = 256;
+    cfg->blocks_per_sm = 6;
+    cfg->refill_idle = 16;
+    cfg->steps_per_round = 8;
+    cfg->tile_w = 8;
+    cfg->chunk = 64;
+    return SVO_OK;
+}
+
+int svo_batch_create(const svo_view *views, int n_views, svo_batch **out) {
+    if (!views || n_views <= 0 || !out) return set_error(SVO_ERR_INVALID, "bad arguments");
+    std::unique_ptr<svo_batch> b(new svo_batch());
+    for (int i = 0; i < n_views; ++i) {
+        const svo_view &v = views[i];
+        if (!v.octree) return set_error(SVO_ERR_INVALID, "view %d has no octree", i);
+        if (!v.rays && (v.width == 0 || v.height == 0))
+            return set_error(SVO_ERR_INVALID, "view %d: camera rays need width and height", i);
+        if (v.width && (uint64_t)v.width * v.height > 0xFFFFFFFFull)
+            return set_error(SVO_ERR_LIMIT, "view %d: more than 2^32-1 pixels", i);
+        if (!v.width && v.n_rays > 0xFFFFFFFFull) return set_error(SVO_ERR_LIMIT, "view %d: more than 2^32-1 rays", i);
+        if (v.ray_scale != 0.0f) b->any_lod = true;
+    }
+    b->views.assign(views, views + n_views);
+    auto setup = [&]() -> int {
+        SVO_CUDA_TRY(cudaGetDevice(&b->device));
+        SVO_CUDA_TRY(cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, b->device));
+        SVO_CUDA_TRY(cudaMalloc((void **)&b->jobs_d, n_views * sizeof(JobDev)));
+        SVO_CUDA_TRY(cudaMalloc((void **)&b->begin_d, (n_views + 1) * sizeof(uint64_t)));
+        SVO_CUDA_TRY(cudaMalloc((void **)&b->queue_d, sizeof(unsigned long long)));
+        SVO_CUDA_TRY(cudaMalloc((void **)&b->status_d, sizeof(uint32_t)));
+        SVO_CUDA_TRY(cudaMemset(b->status_d, 0, sizeof(uint32_t)));
+        return prepare_jobs(b.get(), 8);
+    };
+    int rc = setup();
+    if (rc) {
+        svo_batch_destroy(b.release());
+        return rc;
+    }
+    *out = b.release();
+    return SVO_OK;
+}
+
+int svo_batch_num_slots(svo_batch *b, uint64_t *slots) {
+    if (!b || !slots) return set_error(SVO_ERR_INVALID, "null argument");
+    *slots = b->total;
+    return SVO_OK;
+}
+
+int svo_batch_trace(svo_batch *b, const svo_trace_config *cfg, svo_stream stream) {
+    if (!b) return set_error(SVO_ERR_INVALID, "null batch");
+    svo_trace_config c;
+    if (cfg) c = *cfg;
+    else svo_batch_default_config(&c);
+    if (!config_ok(c)) return set_error(SVO_ERR_INVALID, "bad trace config");
+    int rc = prepare_jobs(b, c.tile_w);
+    if (rc) return rc;
+    return enqueue_trace(b, c, (cudaStream_t)stream);
+}
+
+int svo_batch_capture_graph(svo_batch *b, const svo_trace_config *cfg) {
+    if (!b) return set_error(SVO_ERR_INVALID, "null batch");
+    svo_trace_config c;
+    if (cfg) c = *cfg;
+    else svo_batch_default_config(&c);
+    if (!config_ok(c)) return set_error(SVO_ERR_INVALID, "bad trace config");
+    int rc = prepare_jobs(b, c.tile_w);
+    if (rc) return rc;
+    if (b->exec) {
+        cudaGraphExecDestroy(b->exec);
+        b->exec = nullptr;
+    }
+    if (b->graph) {
+        cudaGraphDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    if (!b->cap_stream) SVO_CUDA_TRY(cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking));
+    SVO_CUDA_TRY(cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal));
+    rc = enqueue_trace(b, c, b->cap_stream);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(b->cap_stream, &g);
+    if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+    b->graph = g;
+    SVO_CUDA_TRY(cudaGraphInstantiate(&b->exec, b->graph, 0));
+    return SVO_OK;
+}
+
+int svo_batch_launch_graph(svo_batch *b, svo_stream stream) {
+    if (!b || !b->exec) return set_error(SVO_ERR_INVALID, "no captured graph");
+    SVO_CUDA_TRY(cudaGraphLaunch(b->exec, (cudaStream_t)stream));
+    return SVO_OK;
+}
+
+int svo_batch_autotune(svo_batch *b, svo_trace_config *best, float *best_ms, svo_stream stream) {
+    if (!b || !best) return set_error(SVO_ERR_INVALID, "null argument");
+    cudaStream_t st = (cudaStream_t)stream;
+    std::string key = workload_key(b);
+    const char *force = getenv("SVO_AUTOTUNE_FORCE");
+    if (!(force && *force == '1') && cache_lookup(key, best)) {
+        if (best_ms) *best_ms = -1.0f;
+        return prepare_jobs(b, best->tile_w);
+    }
+    std::vector<svo_trace_config> cands;
+    for (int bt : {128, 256})
+        for (int refill : {8, 16, 24})
+            for (int steps : {4, 8, 16})
+                for (int tw : {8, 4, 16}) {
+                    svo_trace_config c;
+                    c.block_threads = bt;
+                    c.blocks_per_sm = bt == 128 ? 12 : 6;
+                    c.refill_idle = refill;
+                    c.steps_per_round = steps;
+                    c.tile_w = tw;
+                    c.chunk = 64;
+                    cands.push_back(c);
+                }
+    cudaEvent_t e0, e1;
+    SVO_CUDA_TRY(cudaEventCreate(&e0));
+    SVO_CUDA_TRY(cudaEventCreate(&e1));
+    float best_t = 1e30f;
+    svo_trace_config best_c = cands[0];
+    int rc = SVO_OK;
+    for (const auto &c : cands) {
+        rc = prepare_jobs(b, c.tile_w);
+        if (rc) break;
+        rc = enqueue_trace(b, c, st);  // warm-up
+        if (rc) break;
+        float total = 0.0f;
+        const int reps = 3;
+        for (int r = 0; r < reps && !rc; ++r) {
+            cudaEventRecord(e0, st);
+            rc = enqueue_trace(b, c, st);
+            cudaEventRecord(e1, st);
+            cudaEventSynchronize(e1);
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            total += ms;
+        }
+        if (rc) break;
+        float avg = total / reps;
+        if (avg < best_t) {
+            best_t = avg;
+            best_c = c;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    cache_store(key, best_c, best_t);
+    *best = best_c;
+    if (best_ms) *best_ms = best_t;
+    return prepare_jobs(b, best_c.tile_w);
+}
+
+int svo_batch_status(svo_batch *b, uint32_t *flags) {
+    if (!b || !flags) return set_error(SVO_ERR_INVALID, "null argument");
+    SVO_CUDA_TRY(cudaMemcpy(flags, b->status_d, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    SVO_CUDA_TRY(cudaMemset(b->status_d, 0, sizeof(uint32_t)));
+    return SVO_OK;
+}
+
+int svo_batch_destroy(svo_batch *b) {
+    if (!b) return SVO_OK;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
+    cudaFree(b->jobs_d);
+    cudaFree(b->begin_d);
+    cudaFree(b->queue_d);
+    cudaFree(b->status_d);
+    delete b;
+    return SVO_OK;
+}
+
+}  // extern "C"

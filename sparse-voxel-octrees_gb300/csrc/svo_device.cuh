@@ -82,11 +82,31 @@ __device__ __forceinline__ float shade_grey(uint32_t word, float dx, float dy, f
 
 enum : int { kMiss = 0, kLeafHit = 1, kLodHit = 2, kFault = 3 };
 
-// Per-ray traversal state for VoxelOctree::raymarch (VoxelOctree.cpp:207-346).
-// The reference's stack holds {uint64 offset, float maxT} per scale; this one
-// also keeps the descriptor word so a POP needs no reload (the octree is
-// immutable, so the reloaded word would be identical).  Words are addressed
-// with 32-bit indices (octrees up to 2^32-1 words).
+// Per-ray traversal state of VoxelOctree::raymarch (VoxelOctree.cpp:207-346),
+// split into ray_init (setup, :213-250) and ray_step (one pass of the loop
+// body, :252-339) so a persistent kernel can suspend a ray between steps and
+// refill idle lanes.
+//
+// Differences in mechanism (not in results) from the reference:
+//   - the reference's stack holds {uint64 offset, float maxT} per scale; here
+//     one 16-byte record {parent, maxT, descriptor} per scale, so a PUSH is one
+//     store, a POP one load, and a POP needs no descriptor reload (the octree
+//     is immutable, so the reloaded word would be identical);
+//   - the reference fetches a node's descriptor at the top of the next pass
+//     (`if (current == 0)`, :253-254); here it is fetched at the PUSH that
+//     enters the node (and at init for the root), the same word;
+//   - word indices are 32-bit (octrees of up to 2^32-1 words) and checked
+//     against n_words; more than kPushCap PUSHes, or a PUSH below scale 0
+//     (both only possible on a corrupt octree), end the ray with kFault.
+//     Every pass that does not PUSH either advances to a sibling or pops
+//     towards the root, so the PUSH cap bounds the whole loop;
+//   - the per-pass corner minimum uses fminf: for finite rays no operand is
+//     NaN or -0 (corner t = pos*dT - bT with pos*dT nonzero), where fminf and
+//     the reference's std::min agree bit for bit (a NaN ray never terminates
+//     in the reference);
+//   - the POP's highest differing bit is 31 - clz(differing) instead of the
+//     exponent of (float)differing: equal below 2^24, and at or above it both
+//     give a scale >= 23, which leaves the octree.
 struct RayResult {
     int status;
     float t;
@@ -94,163 +114,179 @@ struct RayResult {
     uint32_t word;
 };
 
-// kCountLoads: count the words the reference reads (descriptor at :254 on
-// every PUSH/POP/start, far word :279, leaf word :282) instead of caching.
-// Every index is checked against n_words; a violation or more than
-// kStepCap iterations ends the ray with kFault.
-constexpr uint32_t kStepCap = 1u << 20;
+struct RayStack {
+    uint4 e[kMaxScale];  // {parent, maxT bits, descriptor, unused} per scale
+};
+
+struct RayState {
+    float dTx, dTy, dTz, bTx, bTy, bTz;
+    float minT, maxT, posX, posY, posZ, scaleExp2;
+    uint32_t current, parent, pushes, nload;
+    int idx, scale, octantMask;
+};
+
+constexpr uint32_t kPushCap = 1u << 20;
+
+// Initialises the state for ray (o, d) and fetches the root descriptor
+// (n_words >= 1 for every octree handle).
+__device__ __forceinline__ void ray_init(RayState &s, const uint32_t *__restrict__ oct, float ox, float oy, float oz,
+                                         float dx, float dy, float dz) {
+    if (fabsf(dx) < 1e-4f) dx = 1e-4f;
+    if (fabsf(dy) < 1e-4f) dy = 1e-4f;
+    if (fabsf(dz) < 1e-4f) dz = 1e-4f;
+    s.dTx = 1.0f / -fabsf(dx);
+    s.dTy = 1.0f / -fabsf(dy);
+    s.dTz = 1.0f / -fabsf(dz);
+    s.bTx = s.dTx * ox;
+    s.bTy = s.dTy * oy;
+    s.bTz = s.dTz * oz;
+    s.octantMask = 7;
+    if (dx > 0.0f) { s.octantMask ^= 1; s.bTx = 3.0f * s.dTx - s.bTx; }
+    if (dy > 0.0f) { s.octantMask ^= 2; s.bTy = 3.0f * s.dTy - s.bTy; }
+    if (dz > 0.0f) { s.octantMask ^= 4; s.bTz = 3.0f * s.dTz - s.bTz; }
+    s.minT = smax(2.0f * s.dTx - s.bTx, smax(2.0f * s.dTy - s.bTy, 2.0f * s.dTz - s.bTz));
+    s.maxT = smin(s.dTx - s.bTx, smin(s.dTy - s.bTy, s.dTz - s.bTz));
+    s.minT = smax(s.minT, 0.0f);
+    s.parent = 0;
+    s.current = __ldg(oct);
+    s.idx = 0;
+    s.posX = 1.0f;
+    s.posY = 1.0f;
+    s.posZ = 1.0f;
+    s.scale = kMaxScale - 1;
+    s.scaleExp2 = 0.5f;
+    if (1.5f * s.dTx - s.bTx > s.minT) { s.idx ^= 1; s.posX = 1.5f; }
+    if (1.5f * s.dTy - s.bTy > s.minT) { s.idx ^= 2; s.posY = 1.5f; }
+    if (1.5f * s.dTz - s.bTz > s.minT) { s.idx ^= 4; s.posZ = 1.5f; }
+    s.pushes = 0;
+    s.nload = 1;
+}
+
+// One pass of the loop body.  Returns false while the ray continues; true
+// when it has finished, with `res` filled (status kMiss/kLeafHit/kLodHit/kFault).
+// kCountLoads: also count the words the reference reads (descriptor at :254
+// at the start and after every PUSH and POP, far word :279, leaf word :282)
+// in s.nload.  kLod: evaluate the level-of-detail exit (:265-268); with
+// rayScale == 0 that test is always false, so kLod=false skips it.
+template <bool kCountLoads, bool kLod>
+__device__ __forceinline__ bool ray_step(RayState &s, RayStack &stk, const uint32_t *__restrict__ oct,
+                                         uint32_t n_words, float rayScale, RayResult &res) {
+    // The loop condition of :252 (scale < MaxScale) holds on entry: scale
+    // starts at 22, a PUSH lowers it and a POP past the root returns below.
+    float cornerTX = s.posX * s.dTx - s.bTx;
+    float cornerTY = s.posY * s.dTy - s.bTy;
+    float cornerTZ = s.posZ * s.dTz - s.bTz;
+    float maxTC = fminf(cornerTX, fminf(cornerTY, cornerTZ));
+
+    int childShift = s.idx ^ s.octantMask;
+    uint32_t childMasks = s.current << childShift;
+
+    if ((childMasks & 0x8000u) && s.minT <= s.maxT) {
+        if (kLod && maxTC * rayScale >= s.scaleExp2) {
+            res.status = kLodHit;
+            res.t = maxTC;
+            return true;
+        }
+        float maxTV = fminf(s.maxT, maxTC);
+        float half = s.scaleExp2 * 0.5f;
+        float centerTX = half * s.dTx + cornerTX;
+        float centerTY = half * s.dTy + cornerTY;
+        float centerTZ = half * s.dTz + cornerTZ;
+
+        if (s.minT <= maxTV) {
+            uint64_t childOffset = s.current >> 18;
+            if (s.current & 0x20000u) {
+                if (s.parent + 1u >= n_words) { res.status = kFault; return true; }
+                childOffset = (childOffset << 32) | (uint64_t)__ldg(oct + s.parent + 1);
+                if (kCountLoads) ++s.nload;
+            }
+            if (!(childMasks & 0x80u)) {
+                uint64_t li = childOffset + s.parent +
+                              (uint64_t)__popc(((childMasks >> (8 + childShift)) << childShift) & 127u);
+                if (li >= n_words) { res.status = kFault; return true; }
+                res.word = __ldg(oct + li);
+                res.leaf = (uint32_t)li;
+                res.status = kLeafHit;
+                res.t = s.minT;
+                if (kCountLoads) ++s.nload;
+                return true;
+            }
+            uint32_t siblingCount = __popc(childMasks & 127u);
+            uint64_t np = (uint64_t)s.parent + childOffset + siblingCount;
+            if (s.current & 0x10000u) np += siblingCount;
+            if (np >= n_words || s.scale <= 0 || ++s.pushes > kPushCap) { res.status = kFault; return true; }
+            stk.e[s.scale] = make_uint4(s.parent, __float_as_uint(s.maxT), s.current, 0u);
+            s.parent = (uint32_t)np;
+            s.current = __ldg(oct + np);
+            if (kCountLoads) ++s.nload;
+
+            s.idx = 0;
+            s.scale--;
+            s.scaleExp2 = half;
+            if (centerTX > s.minT) { s.idx ^= 1; s.posX += s.scaleExp2; }
+            if (centerTY > s.minT) { s.idx ^= 2; s.posY += s.scaleExp2; }
+            if (centerTZ > s.minT) { s.idx ^= 4; s.posZ += s.scaleExp2; }
+            s.maxT = maxTV;
+            return false;
+        }
+    }
+
+    int stepMask = 0;
+    if (cornerTX <= maxTC) { stepMask ^= 1; s.posX -= s.scaleExp2; }
+    if (cornerTY <= maxTC) { stepMask ^= 2; s.posY -= s.scaleExp2; }
+    if (cornerTZ <= maxTC) { stepMask ^= 4; s.posZ -= s.scaleExp2; }
+
+    s.minT = maxTC;
+    s.idx ^= stepMask;
+
+    if ((s.idx & stepMask) != 0) {
+        uint32_t differing = 0;
+        if (stepMask & 1) differing |= __float_as_uint(s.posX) ^ __float_as_uint(s.posX + s.scaleExp2);
+        if (stepMask & 2) differing |= __float_as_uint(s.posY) ^ __float_as_uint(s.posY + s.scaleExp2);
+        if (stepMask & 4) differing |= __float_as_uint(s.posZ) ^ __float_as_uint(s.posZ + s.scaleExp2);
+        s.scale = 31 - __clz((int)differing);
+        if (s.scale >= kMaxScale || s.scale < 0) {  // left the root: a miss (:341)
+            res.status = kMiss;
+            return true;
+        }
+        s.scaleExp2 = __uint_as_float((uint32_t)(s.scale - kMaxScale + 127) << 23);
+        uint4 e = stk.e[s.scale];
+        s.parent = e.x;
+        s.maxT = __uint_as_float(e.y);
+        s.current = e.z;
+        if (kCountLoads) ++s.nload;
+        uint32_t shX = __float_as_uint(s.posX) >> s.scale;
+        uint32_t shY = __float_as_uint(s.posY) >> s.scale;
+        uint32_t shZ = __float_as_uint(s.posZ) >> s.scale;
+        s.posX = __uint_as_float(shX << s.scale);
+        s.posY = __uint_as_float(shY << s.scale);
+        s.posZ = __uint_as_float(shZ << s.scale);
+        s.idx = (int)((shX & 1u) | ((shY & 1u) << 1) | ((shZ & 1u) << 2));
+    }
+    return false;
+}
 
 template <bool kCountLoads>
 __device__ __forceinline__ RayResult raymarch(const uint32_t *__restrict__ oct, uint32_t n_words, float ox, float oy,
                                               float oz, float dx, float dy, float dz, float rayScale,
                                               uint32_t *loads) {
-    uint32_t stkParent[kMaxScale + 1];
-    float stkMaxT[kMaxScale + 1];
-    uint32_t stkDesc[kMaxScale + 1];
-    uint32_t nload = 0;
+    RayStack stk;
+    RayState s;
     RayResult res;
     res.status = kMiss;
     res.t = __int_as_float(0x7f800000);
     res.leaf = 0xFFFFFFFFu;
     res.word = 0;
-
-    if (fabsf(dx) < 1e-4f) dx = 1e-4f;
-    if (fabsf(dy) < 1e-4f) dy = 1e-4f;
-    if (fabsf(dz) < 1e-4f) dz = 1e-4f;
-
-    float dTx = 1.0f / -fabsf(dx);
-    float dTy = 1.0f / -fabsf(dy);
-    float dTz = 1.0f / -fabsf(dz);
-    float bTx = dTx * ox;
-    float bTy = dTy * oy;
-    float bTz = dTz * oz;
-
-    int octantMask = 7;
-    if (dx > 0.0f) { octantMask ^= 1; bTx = 3.0f * dTx - bTx; }
-    if (dy > 0.0f) { octantMask ^= 2; bTy = 3.0f * dTy - bTy; }
-    if (dz > 0.0f) { octantMask ^= 4; bTz = 3.0f * dTz - bTz; }
-
-    float minT = smax(2.0f * dTx - bTx, smax(2.0f * dTy - bTy, 2.0f * dTz - bTz));
-    float maxT = smin(dTx - bTx, smin(dTy - bTy, dTz - bTz));
-    minT = smax(minT, 0.0f);
-
-    uint32_t current = 0;
-    uint32_t parent = 0;
-    int idx = 0;
-    float posX = 1.0f, posY = 1.0f, posZ = 1.0f;
-    int scale = kMaxScale - 1;
-    float scaleExp2 = 0.5f;
-
-    if (1.5f * dTx - bTx > minT) { idx ^= 1; posX = 1.5f; }
-    if (1.5f * dTy - bTy > minT) { idx ^= 2; posY = 1.5f; }
-    if (1.5f * dTz - bTz > minT) { idx ^= 4; posZ = 1.5f; }
-
-    bool need_load = true;
-    uint32_t steps = 0;
-    while (scale < kMaxScale) {
-        if (++steps > kStepCap) { res.status = kFault; return res; }
-        if (need_load) {
-            if (parent >= n_words) { res.status = kFault; return res; }
-            current = __ldg(oct + parent);
-            if (kCountLoads) ++nload;
-            need_load = false;
+    ray_init(s, oct, ox, oy, oz, dx, dy, dz);
+    if (rayScale != 0.0f) {
+        while (!ray_step<kCountLoads, true>(s, stk, oct, n_words, rayScale, res)) {
         }
-        float cornerTX = posX * dTx - bTx;
-        float cornerTY = posY * dTy - bTy;
-        float cornerTZ = posZ * dTz - bTz;
-        float maxTC = smin(cornerTX, smin(cornerTY, cornerTZ));
-
-        int childShift = idx ^ octantMask;
-        uint32_t childMasks = current << childShift;
-
-        if ((childMasks & 0x8000u) && minT <= maxT) {
-            if (maxTC * rayScale >= scaleExp2) {
-                res.status = kLodHit;
-                res.t = maxTC;
-                if (kCountLoads) *loads = nload;
-                return res;
-            }
-            float maxTV = smin(maxT, maxTC);
-            float half = scaleExp2 * 0.5f;
-            float centerTX = half * dTx + cornerTX;
-            float centerTY = half * dTy + cornerTY;
-            float centerTZ = half * dTz + cornerTZ;
-
-            if (minT <= maxTV) {
-                uint64_t childOffset = current >> 18;
-                if (current & 0x20000u) {
-                    if (parent + 1u >= n_words) { res.status = kFault; return res; }
-                    childOffset = (childOffset << 32) | (uint64_t)__ldg(oct + parent + 1);
-                    if (kCountLoads) ++nload;
-                }
-                if (!(childMasks & 0x80u)) {
-                    uint64_t li = childOffset + parent +
-                                  (uint64_t)__popc(((childMasks >> (8 + childShift)) << childShift) & 127u);
-                    if (li >= n_words) { res.status = kFault; return res; }
-                    res.word = __ldg(oct + li);
-                    res.leaf = (uint32_t)li;
-                    res.status = kLeafHit;
-                    res.t = minT;
-                    if (kCountLoads) *loads = nload + 1;
-                    return res;
-                }
-                stkParent[scale] = parent;
-                stkMaxT[scale] = maxT;
-                stkDesc[scale] = current;
-
-                uint32_t siblingCount = __popc(childMasks & 127u);
-                uint64_t np = (uint64_t)parent + childOffset + siblingCount;
-                if (current & 0x10000u) np += siblingCount;
-                if (np >= n_words) { res.status = kFault; return res; }
-                parent = (uint32_t)np;
-
-                idx = 0;
-                scale--;
-                scaleExp2 = half;
-                if (centerTX > minT) { idx ^= 1; posX += scaleExp2; }
-                if (centerTY > minT) { idx ^= 2; posY += scaleExp2; }
-                if (centerTZ > minT) { idx ^= 4; posZ += scaleExp2; }
-                maxT = maxTV;
-                need_load = true;
-                continue;
-            }
-        }
-
-        int stepMask = 0;
-        if (cornerTX <= maxTC) { stepMask ^= 1; posX -= scaleExp2; }
-        if (cornerTY <= maxTC) { stepMask ^= 2; posY -= scaleExp2; }
-        if (cornerTZ <= maxTC) { stepMask ^= 4; posZ -= scaleExp2; }
-
-        minT = maxTC;
-        idx ^= stepMask;
-
-        if ((idx & stepMask) != 0) {
-            uint32_t differing = 0;
-            if (stepMask & 1) differing |= __float_as_uint(posX) ^ __float_as_uint(posX + scaleExp2);
-            if (stepMask & 2) differing |= __float_as_uint(posY) ^ __float_as_uint(posY + scaleExp2);
-            if (stepMask & 4) differing |= __float_as_uint(posZ) ^ __float_as_uint(posZ + scaleExp2);
-            scale = (int)(__float_as_uint((float)(int32_t)differing) >> 23) - 127;
-            scaleExp2 = __uint_as_float((uint32_t)(scale - kMaxScale + 127) << 23);
-            if (scale >= kMaxScale || scale < 0) break;  // exits the tree (miss)
-
-            parent = stkParent[scale];
-            maxT = stkMaxT[scale];
-            uint32_t shX = __float_as_uint(posX) >> scale;
-            uint32_t shY = __float_as_uint(posY) >> scale;
-            uint32_t shZ = __float_as_uint(posZ) >> scale;
-            posX = __uint_as_float(shX << scale);
-            posY = __uint_as_float(shY << scale);
-            posZ = __uint_as_float(shZ << scale);
-            idx = (int)((shX & 1u) | ((shY & 1u) << 1) | ((shZ & 1u) << 2));
-            if (kCountLoads) {
-                need_load = true;
-            } else {
-                current = stkDesc[scale];
-            }
+    } else {
+        while (!ray_step<kCountLoads, false>(s, stk, oct, n_words, rayScale, res)) {
         }
     }
-    if (kCountLoads) *loads = nload;
-    return res;  // miss
+    if (kCountLoads) *loads = s.nload;
+    return res;
 }
 
 }  // namespace svo
