@@ -59,6 +59,10 @@ def parse():
     p.add_argument("--height", type=int, default=H_PIX)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--config", type=int, default=1, choices=[1, 3],
+                   help="1: plain traversal (headline); 3: batched vs plain over 96 octrees and views")
+    p.add_argument("--no-extra", action="store_true", help="skip the config-3 batched comparison in the default run")
+    p.add_argument("--views", type=int, default=96)
     return p.parse_args()
 
 
@@ -202,6 +206,19 @@ def setup_scene(args, rank, torch, svo, scenes):
     return tree, prim, shadow, cam_slices, shadow_slices, info
 
 
+def _timed(torch, fn, steps, warmup, stream, events=None):
+    for _ in range(warmup):
+        fn(None)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for k in range(steps):
+        fn(events[k] if events else None)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1)
+
+
 def run_ours(args):
     rank, world, local = dist_setup(args)
     import torch
@@ -213,14 +230,28 @@ def run_ours(args):
     ge.build()
     svo = ge._package()
     import svo_gb300.scenes as scenes
+    os.environ.setdefault("SVO_AUTOTUNE_CACHE", os.path.join(ROOT, "gpurun_out", "autotune.jsonl"))
+
+    if args.config == 3:
+        r3 = run_config3(args, torch, svo, scenes)
+        if rank == 0:
+            print(json.dumps({"metric": "Mrays/s", "value": r3["batched_mrays_s"], "unit": "Mrays/s",
+                              "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                              "ms_per_step": r3["batched_ms"], "higher_is_better": True, "scaling": "weak",
+                              "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                              "config": {"workload": "batched: " + r3["workload"]}, "batched_vs_plain": r3,
+                              "gpu_launches": args.steps}))
+        return
 
     tree, prim, shadow, cam_slices, shadow_slices, info = setup_scene(args, rank, torch, svo, scenes)
     Rp, Rs = prim.shape[0], shadow.shape[0]
+    W, H = args.width, args.height * args.cams  # the cameras' images stacked row-major
     rays_per_step = Rp + Rs
-    out_p = {"t": torch.empty(Rp, dtype=torch.float32, device="cuda"),
-             "leaf": torch.empty(Rp, dtype=torch.int32, device="cuda"),
-             "rgb": torch.empty((Rp, 3), dtype=torch.float32, device="cuda")}
-    out_s = {"hit": torch.empty(Rs, dtype=torch.uint8, device="cuda")}
+    mk = lambda: ({"t": torch.empty(Rp, dtype=torch.float32, device="cuda"),
+                   "leaf": torch.empty(Rp, dtype=torch.int32, device="cuda"),
+                   "rgb": torch.empty((Rp, 3), dtype=torch.float32, device="cuda")},
+                  {"hit": torch.empty(Rs, dtype=torch.uint8, device="cuda")})
+    out_p, out_s = mk()
     stream = torch.cuda.current_stream()
 
     # loads per ray (the reference's word reads), for the algorithmic bytes
@@ -233,39 +264,32 @@ def run_ours(args):
     bytes_prim = 4 * lp + Rp * (24 + 20)
     bytes_shadow = 4 * ls + Rs * (24 + 1)
 
-    def step(ev=None):
+    # 1. the drop-in path: svo_trace_image (primary rays) + svo_trace (shadow rays)
+    def image_step(ev):
         if ev is not None:
             ev[0].record(stream)
-        tree.trace(prim, out=out_p, light=LIGHT, stream=stream)
+        tree.trace_image(prim, W, H, out=out_p, light=LIGHT, stream=stream)
         if ev is not None:
             ev[1].record(stream)
         tree.trace(shadow, out=out_s, stream=stream)
         if ev is not None:
             ev[2].record(stream)
 
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
     evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
-    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     if world > 1:
         torch.distributed.barrier()
-    torch.cuda.synchronize()
     vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
     smi_index = vis.split(",")[local] if vis else local
     with ClockSampler(smi_index) as clk:
-        start.record(stream)
-        for k in range(args.steps):
-            step(evs[k])
-        end.record(stream)
-        torch.cuda.synchronize()
+        ms = _timed(torch, image_step, args.steps, args.warmup, stream, evs)
     if world > 1:
         torch.distributed.barrier()
-    ms = start.elapsed_time(end)
     t_prim = [e[0].elapsed_time(e[1]) for e in evs]
     t_shadow = [e[1].elapsed_time(e[2]) for e in evs]
     if tree.device_status() != 0:
         raise RuntimeError("traversal error flag raised")
+    ref_p = {k: v.clone() for k, v in out_p.items()}
+    ref_s = out_s["hit"].clone()
     ms_max = ms
     if world > 1:
         tt = torch.tensor([ms], dtype=torch.float64, device="cuda")
@@ -274,41 +298,68 @@ def run_ours(args):
     total_rays = rays_per_step * args.steps * world
     value = total_rays / (ms_max / 1e3) / 1e6
 
+    # 2. the plain per-ray kernel on the same rays (svo_trace for both sets)
+    out_p2, out_s2 = mk()
+
+    def plain_step(ev):
+        tree.trace(prim, out=out_p2, light=LIGHT, stream=stream)
+        tree.trace(shadow, out=out_s2, stream=stream)
+
+    ms_plain = _timed(torch, plain_step, args.steps, args.warmup, stream) / args.steps
+    exact_plain = all(torch.equal(out_p2[k], ref_p[k]) for k in ref_p) and torch.equal(out_s2["hit"], ref_s)
+    del out_p2, out_s2
+
+    # 3. one autotuned, graph-captured persistent launch over the 32 images + the shadow rays
+    npix = args.width * args.height
+    out_p3, out_s3 = mk()
+    views = [{"octree": tree, "rays": prim[i * npix:(i + 1) * npix], "width": args.width, "height": args.height,
+              "light": LIGHT, "out": {k: v[i * npix:(i + 1) * npix] for k, v in out_p3.items()}}
+             for i in range(args.cams)]
+    views.append({"octree": tree, "rays": shadow, "out": out_s3})
+    batch = svo.Batch(views)
+    cfg, _ = batch.autotune()
+    batch.capture_graph(cfg)
+    ms_batched = _timed(torch, lambda ev: batch.launch_graph(stream), args.steps, args.warmup, stream) / args.steps
+    exact_batched = all(torch.equal(out_p3[k], ref_p[k]) for k in ref_p) and torch.equal(out_s3["hit"], ref_s)
+    del batch, views, out_p3, out_s3
+
     # end to end through the C ABI with host buffers (copies inside the timed region)
     e2e = None
     if not args.no_e2e:
-        hp = prim.cpu().numpy()
-        hs = shadow.cpu().numpy()
-        hp_pin = torch.from_numpy(hp).pin_memory().numpy()
-        hs_pin = torch.from_numpy(hs).pin_memory().numpy()
+        hp_pin = prim.cpu().pin_memory().numpy()
+        hs_pin = shadow.cpu().pin_memory().numpy()
         op = {"t": torch.empty(Rp, dtype=torch.float32).pin_memory().numpy(),
               "leaf": torch.empty(Rp, dtype=torch.int32).pin_memory().numpy(),
               "rgb": torch.empty((Rp, 3), dtype=torch.float32).pin_memory().numpy()}
         os_ = {"hit": torch.empty(Rs, dtype=torch.uint8).pin_memory().numpy()}
         for _ in range(max(1, args.warmup)):
-            tree.trace_host(hp_pin, light=LIGHT, out=op)
+            tree.trace_image_host(hp_pin, W, H, light=LIGHT, out=op)
             tree.trace_host(hs_pin, out=os_)
         if world > 1:
             torch.distributed.barrier()
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            tree.trace_host(hp_pin, light=LIGHT, out=op)
+            tree.trace_image_host(hp_pin, W, H, light=LIGHT, out=op)
             tree.trace_host(hs_pin, out=os_)
         e2e_s = time.perf_counter() - t0
         if world > 1:
             tt = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
             torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
             e2e_s = float(tt.item())
+        exact_e2e = np.array_equal(op["leaf"], ref_p["leaf"].cpu().numpy()) and \
+            np.array_equal(os_["hit"], ref_s.cpu().numpy())
         e2e = {"value": round(total_rays / e2e_s / 1e6, 2), "unit": "Mrays/s",
                "h2d_bytes_per_step": (Rp + Rs) * 24, "d2h_bytes_per_step": Rp * 20 + Rs * 1,
-               "api": "svo_trace_host (pinned host rays in, t/leaf/rgb and shadow hit out)"}
+               "api": "svo_trace_image_host (primary) + svo_trace_host (shadow): pinned host rays in, "
+                      "t/leaf/rgb and shadow hit out", "exact": bool(exact_e2e)}
+        del hp_pin, hs_pin, op, os_
 
     peaks, peak_kind = load_peaks()
     t_prim_avg = sum(t_prim) / len(t_prim)
     achieved = bytes_prim / (t_prim_avg / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": profiled_traffic(Rp),
-                "kernel": "k_trace_plain (primary rays)", "peak_kind": peak_kind,
+                "kernel": "k_trace_single (svo_trace_image, primary rays)", "peak_kind": peak_kind,
                 "algorithmic_bytes_per_launch": bytes_prim,
                 "bytes_per_ray": round(bytes_prim / Rp, 2), "launch_ms": round(t_prim_avg, 3)}
 
@@ -324,6 +375,13 @@ def run_ours(args):
         cpu = {"value": round(n / secs / 1e6, 3), "unit": "Mrays/s", "cores": thr, "kind": "port",
                "sample": "%d of %d cameras: %d primary+shadow rays in %.1f s (oracle C restatement of "
                          "VoxelOctree::raymarch, %d threads)" % (ncam, len(cam_slices), n, secs, thr)}
+        del words
+
+    extra = None
+    if not args.no_extra and world == 1:
+        del prim, shadow, out_p, out_s, ref_p, ref_s, tree
+        torch.cuda.empty_cache()
+        extra = run_config3(args, torch, svo, scenes)
 
     if rank == 0:
         line = {
@@ -334,6 +392,7 @@ def run_ours(args):
             "config": {"workload": "plain traversal: %d^3 octree (terrain + %d spheres), %d cams %dx%d primary rays "
                                    "+ 1 shadow ray per hit" % (args.side, N_SPHERES, args.cams, args.width,
                                                                args.height),
+                       "api": "svo_trace_image (primary, 8x4-pixel tiles, persistent) + svo_trace (shadow)",
                        "octree_words": info["words"], "voxels": info["voxels"], "primary_rays": Rp,
                        "shadow_rays": Rs, "rays_per_step": rays_per_step,
                        "l2": "no flush: octree %.2f GB and rays %.2f GB exceed L2" % (info["words"] * 4 / 1e9,
@@ -341,6 +400,13 @@ def run_ours(args):
                        "parallelism": "replicas x%d" % world},
             "e2e": e2e, "gpu_launches": 2 * args.steps, "roofline": roofline, "cpu_baseline": cpu,
             "clocks": clk.summary(),
+            "plain": {"api": "svo_trace for primary and shadow rays (one thread per ray)",
+                      "ms_per_step": round(ms_plain, 3), "mrays_s": round(rays_per_step / ms_plain / 1e3, 1),
+                      "exact_vs_value_path": bool(exact_plain)},
+            "batched": {"api": "svo_batch: 32 image views + shadow view, autotuned, CUDA graph",
+                        "ms_per_step": round(ms_batched, 3), "mrays_s": round(rays_per_step / ms_batched / 1e3, 1),
+                        "config": cfg.as_dict(), "exact_vs_value_path": bool(exact_batched)},
+            "batched_vs_plain": extra,
             "build": {"build_s": round(info["build_s"], 3), "scene_gen_s": round(info["gen_s"], 3),
                       "voxels_per_s": round(info["voxels"] / info["build_s"], 1)},
             "kernel_ms": {"primary": round(t_prim_avg, 3), "shadow": round(sum(t_shadow) / len(t_shadow), 3)},
@@ -350,9 +416,92 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def config3_views(n_views, seed=3):
+    """96 (octree, view) pairs: depth U{7..11}, even index -> sphere-union
+    generator (48 spheres), odd -> terrain generator (200 spheres), scene seed
+    = index; one orbit camera each, pixel count log-uniform in
+    [256x256, 1920x1080] at 16:9 clipped to [256, 1920] x [256, 1080]."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for i in range(1, n_views + 1):
+        depth = int(rng.integers(7, 12))
+        pix = float(np.exp(rng.uniform(np.log(256 * 256), np.log(1920 * 1080))))
+        W = int(min(1920, max(256, round((pix * 16 / 9) ** 0.5))))
+        H = int(min(1080, max(256, round(pix / W))))
+        specs.append((i, 1 << depth, "sphere" if i % 2 == 0 else "terrain", W, H))
+    return specs
+
+
+def run_config3(args, torch, svo, scenes, tune_cache=None):
+    """Batched persistent launch (graph-captured, autotuned) against the plain
+    per-view kernel over the config-3 views; checks exact parity."""
+    t0 = time.perf_counter()
+    views, plain_out, rays_list = [], [], []
+    trees = []
+    total_rays = 0
+    for (i, side, gen, W, H) in config3_views(args.views):
+        grid = scenes.gpu_sphere_scene(side, 48, i) if gen == "sphere" else scenes.gpu_terrain_scene(side, 200, i)
+        tree = svo.VoxelOctree(svo.VoxelData(grid))
+        del grid
+        trees.append(tree)
+        cam = scenes.orbit_cameras(1, 5000 + i, tree.center(), radius=2.0)[0]
+        rays = scenes.gpu_camera_rays(cam, W, H)
+        light = scenes.headlight(cam)
+        n = W * H
+        mk = lambda: {"t": torch.empty(n, dtype=torch.float32, device="cuda"),
+                      "leaf": torch.empty(n, dtype=torch.int32, device="cuda"),
+                      "rgb": torch.empty((n, 3), dtype=torch.float32, device="cuda")}
+        out_b, out_p = mk(), mk()
+        views.append({"octree": tree, "rays": rays, "width": W, "height": H, "light": light, "out": out_b})
+        plain_out.append((tree, rays, light, out_p))
+        total_rays += n
+    torch.cuda.empty_cache()
+    setup_s = time.perf_counter() - t0
+    batch = svo.Batch(views)
+    if tune_cache:
+        os.environ.setdefault("SVO_AUTOTUNE_CACHE", tune_cache)
+    t0 = time.perf_counter()
+    cfg, tune_ms = batch.autotune()
+    tune_s = time.perf_counter() - t0
+    batch.capture_graph(cfg)
+    stream = torch.cuda.current_stream()
+
+    def plain_step():
+        for tree, rays, light, out in plain_out:
+            tree.trace(rays, out=out, light=light, stream=stream)
+
+    def batched_step():
+        batch.launch_graph(stream)
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / args.steps
+
+    ms_plain = timed(plain_step)
+    ms_batched = timed(batched_step)
+    exact = all(torch.equal(v["out"][k], po[3][k]) for v, po in zip(views, plain_out) for k in ("t", "leaf", "rgb"))
+    return {"workload": "%d octrees (depth 7-11, sphere/terrain generators, seeds 1..%d), one view each, "
+                        "256x256..1920x1080 log-uniform pixels" % (len(views), len(views)),
+            "rays_per_step": total_rays, "octree_words": int(sum(t.num_words() for t in trees)),
+            "plain_ms": round(ms_plain, 3), "batched_ms": round(ms_batched, 3),
+            "plain_mrays_s": round(total_rays / ms_plain / 1e3, 1),
+            "batched_mrays_s": round(total_rays / ms_batched / 1e3, 1),
+            "speedup": round(ms_plain / ms_batched, 3), "exact_hit_parity": bool(exact),
+            "config": cfg.as_dict(), "autotune_s": round(tune_s, 1), "setup_s": round(setup_s, 1),
+            "launches": {"plain": len(views), "batched": 1}}
+
+
 def profiled_traffic(rays):
     """DRAM bytes per launch from the committed ncu summary (scaled per ray), or None."""
-    path = os.path.join(ROOT, "profiles", "trace_plain_config1.txt")
+    path = os.path.join(ROOT, "profiles", "trace_image_config1.txt")
     try:
         for line in open(path):
             if line.startswith("dram_bytes_per_ray:"):

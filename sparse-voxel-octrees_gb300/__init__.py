@@ -92,6 +92,10 @@ def _load():
         "svo_trace_host": (ctypes.c_int, [_vp, _vp, ctypes.c_uint64, ctypes.c_float, _f32p,
                                           ctypes.POINTER(TraceOut)]),
         "svo_trace_count_loads": (ctypes.c_int, [_vp, _vp, ctypes.c_uint64, ctypes.c_float, _vp, _vp]),
+        "svo_trace_image": (ctypes.c_int, [_vp, _vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float, _f32p,
+                                           ctypes.POINTER(TraceOut), _vp]),
+        "svo_trace_image_host": (ctypes.c_int, [_vp, _vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float, _f32p,
+                                                ctypes.POINTER(TraceOut)]),
         "svo_batch_create": (ctypes.c_int, [ctypes.POINTER(View), ctypes.c_int, ctypes.POINTER(_vp)]),
         "svo_batch_default_config": (ctypes.c_int, [ctypes.POINTER(TraceConfig)]),
         "svo_batch_num_slots": (ctypes.c_int, [_vp, _u64p]),
@@ -303,6 +307,33 @@ class VoxelOctree:
         lt = np.ascontiguousarray(light, dtype=np.float32)
         check(lib.svo_trace_host(self._h, _np_ptr(rays), R, float(ray_scale), lt.ctypes.data_as(_f32p),
                                  ctypes.byref(o)))
+        return res
+
+    def trace_image(self, rays, width, height, ray_scale=0.0, light=(0.0, 0.0, 1.0), out=None, stream=None):
+        """Device form for row-major image rays (R = width*height)."""
+        o = TraceOut()
+        for k in ("hit", "t", "leaf", "word", "rgb"):
+            v = (out or {}).get(k)
+            setattr(o, k, _dev_ptr(v).value if v is not None else None)
+        lt = np.ascontiguousarray(light, dtype=np.float32)
+        check(lib.svo_trace_image(self._h, _dev_ptr(rays), int(width), int(height), float(ray_scale),
+                                  lt.ctypes.data_as(_f32p), ctypes.byref(o), _stream_ptr(stream)))
+
+    def trace_image_host(self, rays, width, height, ray_scale=0.0, light=(0.0, 0.0, 1.0),
+                         outputs=("hit", "t", "leaf", "word", "rgb"), out=None):
+        rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 6)
+        R = rays.shape[0]
+        assert R == width * height
+        shapes = {"hit": ((R,), np.uint8), "t": ((R,), np.float32), "leaf": ((R,), np.uint32),
+                  "word": ((R,), np.uint32), "rgb": ((R, 3), np.float32)}
+        res = out if out is not None else {k: np.empty(*shapes[k]) for k in outputs}
+        o = TraceOut()
+        for k in ("hit", "t", "leaf", "word", "rgb"):
+            v = res.get(k)
+            setattr(o, k, v.ctypes.data if v is not None else None)
+        lt = np.ascontiguousarray(light, dtype=np.float32)
+        check(lib.svo_trace_image_host(self._h, _np_ptr(rays), int(width), int(height), float(ray_scale),
+                                       lt.ctypes.data_as(_f32p), ctypes.byref(o)))
         return res
 
     def count_loads(self, rays, n=None, ray_scale=0.0, loads=None, stream=None):

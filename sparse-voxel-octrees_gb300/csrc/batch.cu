@@ -65,6 +65,105 @@ __device__ __forceinline__ int find_job(const uint64_t *beg, int n_jobs, uint64_
     return lo;
 }
 
+// Maps a work slot to its view and ray, initialises the traversal state and
+// returns false for the padding slots of partial pixel tiles.
+__device__ __forceinline__ bool setup_slot(const BatchArgs &a, const uint64_t *beg, uint64_t slot, RayState &st,
+                                           int &job, uint32_t &out_idx, const uint32_t *&oct, uint32_t &nw,
+                                           float &rs, float &rdx, float &rdy, float &rdz) {
+    int j = find_job(beg, a.n_jobs, slot);
+    const JobDev &J = a.jobs[j];
+    uint64_t local = slot - beg[j];
+    uint32_t px = 0, py = 0;
+    if (J.width) {
+        uint64_t tile = local >> 5;
+        uint32_t r = (uint32_t)(local & 31);
+        px = (uint32_t)(tile % J.tiles_x) * (1u << a.log_tile_w) + (r & ((1u << a.log_tile_w) - 1u));
+        py = (uint32_t)(tile / J.tiles_x) * (32u >> a.log_tile_w) + (r >> a.log_tile_w);
+        if (px >= J.width || py >= J.height) return false;
+        out_idx = py * J.width + px;
+    } else {
+        out_idx = (uint32_t)local;
+    }
+    float ox, oy, oz, dx, dy, dz;
+    if (J.rays) {
+        const float2 *r2 = reinterpret_cast<const float2 *>(J.rays) + 3 * (uint64_t)out_idx;
+        float2 p0 = __ldg(r2), p1 = __ldg(r2 + 1), p2 = __ldg(r2 + 2);
+        ox = p0.x; oy = p0.y; oz = p1.x;
+        dx = p1.y; dy = p2.x; dz = p2.y;
+    } else {
+        // The viewer's camera ray (Main.cpp:167-176), as scenes.camera_rays.
+        const float *c = J.cam;
+        float sx = -1.0f + (float)px * c[12];
+        float sy = c[13] - (float)py * c[12];
+        float vx = (sx * c[0] + sy * c[1]) + c[14];
+        float vy = (sx * c[3] + sy * c[4]) + c[15];
+        float vz = (sx * c[6] + sy * c[7]) + c[16];
+        float n = inv_sqrt((vx * vx + vy * vy) + vz * vz);
+        ox = c[9]; oy = c[10]; oz = c[11];
+        dx = vx * n; dy = vy * n; dz = vz * n;
+    }
+    ray_init(st, J.oct, ox, oy, oz, dx, dy, dz);
+    rdx = dx; rdy = dy; rdz = dz;
+    job = j;
+    oct = J.oct;
+    nw = J.n_words;
+    rs = J.ray_scale;
+    return true;
+}
+
+__device__ __forceinline__ void write_result(const BatchArgs &a, int job, uint32_t out_idx, const RayResult &res,
+                                             float rdx, float rdy, float rdz) {
+    const JobDev &J = a.jobs[job];
+    if (res.status == kFault) atomicOr(a.status, 1u);
+    uint8_t hs = res.status == kFault ? 0 : (uint8_t)res.status;
+    bool leaf = res.status == kLeafHit;
+    if (J.hit) J.hit[out_idx] = hs;
+    if (J.t) J.t[out_idx] = hs == 0 ? __int_as_float(0x7f800000) : res.t;
+    if (J.leaf) J.leaf[out_idx] = leaf ? res.leaf : 0xFFFFFFFFu;
+    if (J.word) J.word[out_idx] = leaf ? res.word : 0u;
+    if (J.rgb) {
+        float g = leaf ? shade_grey(res.word, rdx, rdy, rdz, J.lx, J.ly, J.lz) : 0.0f;
+        J.rgb[3 * (uint64_t)out_idx + 0] = g;
+        J.rgb[3 * (uint64_t)out_idx + 1] = g;
+        J.rgb[3 * (uint64_t)out_idx + 2] = g;
+    }
+}
+
+// refill_idle == 0: a warp takes `chunk` slots at once and runs them 32 at a
+// time, each lane to completion, before it takes the next chunk.
+template <bool kLod>
+__global__ void k_trace_tiles(BatchArgs a) {
+    extern __shared__ uint64_t s_begin[];
+    const bool staged = a.n_jobs + 1 <= kMaxSmemJobs;
+    if (staged)
+        for (int i = threadIdx.x; i <= a.n_jobs; i += blockDim.x) s_begin[i] = a.begin[i];
+    __syncthreads();
+    const uint64_t *beg = staged ? s_begin : a.begin;
+    const int lane = threadIdx.x & 31;
+    RayStack stk;
+    while (true) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(a.queue, (unsigned long long)a.chunk);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= a.total) break;
+        unsigned long long end = min(base + (unsigned long long)a.chunk, (unsigned long long)a.total);
+        for (unsigned long long s0 = base; s0 < end; s0 += 32) {
+            uint64_t slot = s0 + lane;
+            if (slot >= end) continue;
+            RayState st;
+            int job;
+            uint32_t out_idx, nw;
+            const uint32_t *oct;
+            float rs, rdx, rdy, rdz;
+            if (!setup_slot(a, beg, slot, st, job, out_idx, oct, nw, rs, rdx, rdy, rdz)) continue;
+            RayResult res;
+            while (!ray_step<false, kLod>(st, stk, oct, nw, rs, res)) {
+            }
+            write_result(a, job, out_idx, res, rdx, rdy, rdz);
+        }
+    }
+}
+
 template <bool kLod>
 __global__ void k_trace_persistent(BatchArgs a) {
     extern __shared__ uint64_t s_begin[];
@@ -77,8 +176,6 @@ __global__ void k_trace_persistent(BatchArgs a) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;
-    const int tile_w = 1 << a.log_tile_w;
-
     RayState st;
     RayStack stk;
     bool active = false;
@@ -108,51 +205,8 @@ __global__ void k_trace_persistent(BatchArgs a) {
                 uint32_t avail = (uint32_t)(pool_end - pool_next);
                 uint32_t rank = __popc(idle & lt_mask);
                 bool mine = ((idle >> lane) & 1u) && rank < avail;
-                if (mine) {
-                    uint64_t slot = pool_next + rank;
-                    int j = find_job(beg, a.n_jobs, slot);
-                    const JobDev &J = a.jobs[j];
-                    uint64_t local = slot - beg[j];
-                    uint32_t px = 0, py = 0;
-                    bool live = true;
-                    if (J.width) {
-                        uint64_t tile = local >> 5;
-                        uint32_t r = (uint32_t)(local & 31);
-                        px = (uint32_t)(tile % J.tiles_x) * tile_w + (r & (tile_w - 1));
-                        py = (uint32_t)(tile / J.tiles_x) * (32 >> a.log_tile_w) + (r >> a.log_tile_w);
-                        live = px < J.width && py < J.height;
-                        out_idx = py * J.width + px;
-                    } else {
-                        out_idx = (uint32_t)local;
-                    }
-                    if (live) {
-                        float ox, oy, oz, dx, dy, dz;
-                        if (J.rays) {
-                            const float2 *r2 = reinterpret_cast<const float2 *>(J.rays) + 3 * (uint64_t)out_idx;
-                            float2 p0 = __ldg(r2), p1 = __ldg(r2 + 1), p2 = __ldg(r2 + 2);
-                            ox = p0.x; oy = p0.y; oz = p1.x;
-                            dx = p1.y; dy = p2.x; dz = p2.y;
-                        } else {
-                            // The viewer's camera ray (Main.cpp:167-176), as scenes.camera_rays.
-                            const float *c = J.cam;
-                            float sx = -1.0f + (float)px * c[12];
-                            float sy = c[13] - (float)py * c[12];
-                            float vx = (sx * c[0] + sy * c[1]) + c[14];
-                            float vy = (sx * c[3] + sy * c[4]) + c[15];
-                            float vz = (sx * c[6] + sy * c[7]) + c[16];
-                            float n = inv_sqrt((vx * vx + vy * vy) + vz * vz);
-                            ox = c[9]; oy = c[10]; oz = c[11];
-                            dx = vx * n; dy = vy * n; dz = vz * n;
-                        }
-                        ray_init(st, J.oct, ox, oy, oz, dx, dy, dz);
-                        rdx = dx; rdy = dy; rdz = dz;
-                        job = j;
-                        oct = J.oct;
-                        nw = J.n_words;
-                        rs = J.ray_scale;
-                        active = true;
-                    }
-                }
+                if (mine)
+                    active = setup_slot(a, beg, pool_next + rank, st, job, out_idx, oct, nw, rs, rdx, rdy, rdz);
                 unsigned taken = __ballot_sync(FULL, mine);
                 pool_next += __popc(taken);
                 idle &= ~taken;
@@ -166,24 +220,48 @@ __global__ void k_trace_persistent(BatchArgs a) {
             for (int k = 0; k < a.steps_per_round; ++k) {
                 RayResult res;
                 if (ray_step<false, kLod>(st, stk, oct, nw, rs, res)) {
-                    const JobDev &J = a.jobs[job];
-                    if (res.status == kFault) atomicOr(a.status, 1u);
-                    uint8_t hs = res.status == kFault ? 0 : (uint8_t)res.status;
-                    bool leaf = res.status == kLeafHit;
-                    if (J.hit) J.hit[out_idx] = hs;
-                    if (J.t) J.t[out_idx] = hs == 0 ? __int_as_float(0x7f800000) : res.t;
-                    if (J.leaf) J.leaf[out_idx] = leaf ? res.leaf : 0xFFFFFFFFu;
-                    if (J.word) J.word[out_idx] = leaf ? res.word : 0u;
-                    if (J.rgb) {
-                        float g = leaf ? shade_grey(res.word, rdx, rdy, rdz, J.lx, J.ly, J.lz) : 0.0f;
-                        J.rgb[3 * (uint64_t)out_idx + 0] = g;
-                        J.rgb[3 * (uint64_t)out_idx + 1] = g;
-                        J.rgb[3 * (uint64_t)out_idx + 2] = g;
-                    }
+                    write_result(a, job, out_idx, res, rdx, rdy, rdz);
                     active = false;
                     break;
                 }
             }
+        }
+    }
+}
+
+// One image view, passed by value (svo_trace_image): the tile kernel's loop
+// without a job table.
+template <bool kLod>
+__global__ void k_trace_single(JobDev J, uint64_t total, unsigned long long *queue, uint32_t *status, int log_tile_w,
+                               int chunk) {
+    const int lane = threadIdx.x & 31;
+    RayStack stk;
+    BatchArgs a;  // only the fields write_result reads
+    a.jobs = &J;
+    a.status = status;
+    while (true) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(queue, (unsigned long long)chunk);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= total) break;
+        unsigned long long end = min(base + (unsigned long long)chunk, (unsigned long long)total);
+        for (unsigned long long s0 = base; s0 < end; s0 += 32) {
+            uint64_t local = s0 + lane;
+            if (local >= end) continue;
+            uint64_t tile = local >> 5;
+            uint32_t r = (uint32_t)(local & 31);
+            uint32_t px = (uint32_t)(tile % J.tiles_x) * (1u << log_tile_w) + (r & ((1u << log_tile_w) - 1u));
+            uint32_t py = (uint32_t)(tile / J.tiles_x) * (32u >> log_tile_w) + (r >> log_tile_w);
+            if (px >= J.width || py >= J.height) continue;
+            uint32_t out_idx = py * J.width + px;
+            const float2 *r2 = reinterpret_cast<const float2 *>(J.rays) + 3 * (uint64_t)out_idx;
+            float2 p0 = __ldg(r2), p1 = __ldg(r2 + 1), p2 = __ldg(r2 + 2);
+            RayState st;
+            ray_init(st, J.oct, p0.x, p0.y, p1.x, p1.y, p2.x, p2.y);
+            RayResult res;
+            while (!ray_step<false, kLod>(st, stk, J.oct, J.n_words, J.ray_scale, res)) {
+            }
+            write_result(a, 0, out_idx, res, p1.y, p2.x, p2.y);
         }
     }
 }
@@ -196,12 +274,50 @@ int log2_of(int v) {
 
 bool config_ok(const svo_trace_config &c) {
     return c.block_threads >= 32 && c.block_threads <= 1024 && c.block_threads % 32 == 0 && c.blocks_per_sm >= 1 &&
-           c.blocks_per_sm <= 32 && c.refill_idle >= 1 && c.refill_idle <= 32 && c.steps_per_round >= 1 &&
+           c.blocks_per_sm <= 32 && c.refill_idle >= 0 && c.refill_idle <= 32 && c.steps_per_round >= 1 &&
            c.steps_per_round <= 4096 && (c.tile_w == 4 || c.tile_w == 8 || c.tile_w == 16 || c.tile_w == 32) &&
            c.chunk >= 32 && c.chunk <= 8192 && c.chunk % 32 == 0;
 }
 
 }  // namespace
+
+// svo_trace_image: rays in row-major image order, traced in tile_w x (32 /
+// tile_w) pixel tiles by one persistent launch.
+int launch_trace_image(const svo_octree *oct, const float *d_rays, uint32_t width, uint32_t height, float ray_scale,
+                       const float light[3], const svo_trace_out &out, cudaStream_t st) {
+    if (width == 0 || height == 0) return SVO_OK;
+    const int tile_w = 8, log_tw = 3, chunk = 32, threads = 256;
+    JobDev J;
+    std::memset(&J, 0, sizeof(J));
+    J.oct = oct->d_words;
+    J.n_words = (uint32_t)oct->n_words;
+    J.width = width;
+    J.height = height;
+    J.tiles_x = (width + tile_w - 1) / tile_w;
+    J.rays = d_rays;
+    J.ray_scale = ray_scale;
+    J.lx = light ? light[0] : 0.0f;
+    J.ly = light ? light[1] : 0.0f;
+    J.lz = light ? light[2] : 0.0f;
+    J.hit = out.hit;
+    J.t = out.t;
+    J.leaf = out.leaf;
+    J.word = out.word;
+    J.rgb = out.rgb;
+    uint64_t total = (uint64_t)J.tiles_x * ((height + (32 / tile_w) - 1) / (32 / tile_w)) * 32;
+    void (*kern)(JobDev, uint64_t, unsigned long long *, uint32_t *, int, int) =
+        ray_scale != 0.0f ? k_trace_single<true> : k_trace_single<false>;
+    int dev = 0, sms = 0, resident = 0;
+    SVO_CUDA_TRY(cudaGetDevice(&dev));
+    SVO_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    SVO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, kern, threads, 0));
+    SVO_CUDA_TRY(cudaMemsetAsync(oct->d_queue, 0, sizeof(unsigned long long), st));
+    kern<<<(unsigned)(sms * std::max(1, resident)), threads, 0, st>>>(J, total, oct->d_queue, oct->d_status, log_tw,
+                                                                   chunk);
+    SVO_CUDA_TRY(cudaGetLastError());
+    return SVO_OK;
+}
+
 }  // namespace svo
 
 struct svo_batch {
@@ -276,20 +392,17 @@ int enqueue_trace(svo_batch *b, const svo_trace_config &c, cudaStream_t st) {
     size_t smem = (a.n_jobs + 1 <= kMaxSmemJobs) ? (size_t)(a.n_jobs + 1) * sizeof(uint64_t) : 0;
     // A persistent grid larger than what is resident only adds CTAs that
     // start after the queue is drained: clamp to the occupancy limit.
-    int resident = 0;
-    if (b->any_lod)
-        SVO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k_trace_persistent<true>,
-                                                                   c.block_threads, smem));
+    void (*kern)(BatchArgs);
+    if (c.refill_idle == 0)
+        kern = b->any_lod ? k_trace_tiles<true> : k_trace_tiles<false>;
     else
-        SVO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k_trace_persistent<false>,
-                                                                   c.block_threads, smem));
+        kern = b->any_lod ? k_trace_persistent<true> : k_trace_persistent<false>;
+    int resident = 0;
+    SVO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, kern, c.block_threads, smem));
     int per_sm = std::max(1, std::min(c.blocks_per_sm, resident));
     SVO_CUDA_TRY(cudaMemsetAsync(b->queue_d, 0, sizeof(unsigned long long), st));
     dim3 grid((unsigned)(b->num_sms * per_sm));
-    if (b->any_lod)
-        k_trace_persistent<true><<<grid, c.block_threads, smem, st>>>(a);
-    else
-        k_trace_persistent<false><<<grid, c.block_threads, smem, st>>>(a);
+    kern<<<grid, c.block_threads, smem, st>>>(a);
     SVO_CUDA_TRY(cudaGetLastError());
     return SVO_OK;
 }
@@ -479,19 +592,23 @@ int svo_batch_autotune(svo_batch *b, svo_trace_config *best, float *best_ms, svo
         return prepare_jobs(b, best->tile_w);
     }
     std::vector<svo_trace_config> cands;
+    auto add = [&](int bt, int refill, int steps, int tw, int chunk) {
+        svo_trace_config c;
+        c.block_threads = bt;
+        c.blocks_per_sm = 2048 / bt;
+        c.refill_idle = refill;
+        c.steps_per_round = steps;
+        c.tile_w = tw;
+        c.chunk = chunk;
+        cands.push_back(c);
+    };
+    for (int bt : {128, 256, 512})
+        for (int tw : {4, 8, 16})
+            for (int chunk : {32, 128}) add(bt, 0, 1, tw, chunk);  // whole-warp tiles, no refill
     for (int bt : {128, 256})
-        for (int refill : {8, 16, 24})
-            for (int steps : {4, 8, 16})
-                for (int tw : {8, 4, 16}) {
-                    svo_trace_config c;
-                    c.block_threads = bt;
-                    c.blocks_per_sm = bt == 128 ? 12 : 6;
-                    c.refill_idle = refill;
-                    c.steps_per_round = steps;
-                    c.tile_w = tw;
-                    c.chunk = 64;
-                    cands.push_back(c);
-                }
+        for (int refill : {8, 16, 32})
+            for (int steps : {16, 64})
+                for (int tw : {4, 8}) add(bt, refill, steps, tw, 64);
     cudaEvent_t e0, e1;
     SVO_CUDA_TRY(cudaEventCreate(&e0));
     SVO_CUDA_TRY(cudaEventCreate(&e1));

@@ -67,6 +67,10 @@ int cache_block_log2(int w, int h, int d, uint64_t mem, uint64_t cell_cost) {
     return largest;
 }
 
+}  // namespace svo
+extern "C" int svo_octree_destroy(svo_octree *oct);
+namespace svo {
+
 int make_handle(uint32_t *d_words, uint64_t n_words, const float center[3], svo_octree **out) {
     std::unique_ptr<svo_octree> h(new svo_octree());
     h->d_words = d_words;
@@ -81,6 +85,11 @@ int make_handle(uint32_t *d_words, uint64_t n_words, const float center[3], svo_
     }
     e = cudaMemset(h->d_status, 0, sizeof(uint32_t));
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemset(status)");
+    e = cudaMalloc((void **)&h->d_queue, sizeof(unsigned long long));
+    if (e != cudaSuccess) {
+        svo_octree_destroy(h.release());
+        return cuda_fail(e, "cudaMalloc(queue)");
+    }
     *out = h.release();
     return SVO_OK;
 }
@@ -226,9 +235,17 @@ int svo_octree_destroy(svo_octree *oct) {
     if (!oct) return SVO_OK;
     if (oct->d_words) cudaFree(oct->d_words);
     if (oct->d_status) cudaFree(oct->d_status);
+    if (oct->d_queue) cudaFree(oct->d_queue);
     if (oct->stage_dev) cudaFree(oct->stage_dev);
     for (auto &s : oct->stage_streams)
         if (s) cudaStreamDestroy(s);
+    for (auto &s : oct->img_streams)
+        if (s) cudaStreamDestroy(s);
+    for (int k = 0; k < 2; ++k) {
+        if (oct->img_in[k]) cudaEventDestroy(oct->img_in[k]);
+        if (oct->img_traced[k]) cudaEventDestroy(oct->img_traced[k]);
+        if (oct->img_out[k]) cudaEventDestroy(oct->img_out[k]);
+    }
     delete oct;
     return SVO_OK;
 }
@@ -382,6 +399,13 @@ int svo_trace(const svo_octree *oct, const float *rays, uint64_t n, float ray_sc
     return launch_trace(oct, rays, n, ray_scale, light, *out, (cudaStream_t)stream);
 }
 
+int svo_trace_image(const svo_octree *oct, const float *rays, uint32_t width, uint32_t height, float ray_scale,
+                    const float light[3], const svo_trace_out *out, svo_stream stream) {
+    if (!oct || (!rays && width && height) || !out) return set_error(SVO_ERR_INVALID, "null argument");
+    if ((uint64_t)width * height > 0xFFFFFFFFull) return set_error(SVO_ERR_LIMIT, "more than 2^32-1 pixels");
+    return launch_trace_image(oct, rays, width, height, ray_scale, light, *out, (cudaStream_t)stream);
+}
+
 int svo_trace_count_loads(const svo_octree *oct, const float *rays, uint64_t n, float ray_scale, uint32_t *loads,
                           svo_stream stream) {
     if (!oct || (!rays && n) || (!loads && n)) return set_error(SVO_ERR_INVALID, "null argument");
@@ -426,6 +450,74 @@ int svo_trace_host(svo_octree *oct, const float *rays, uint64_t n, float ray_sca
     }
     SVO_CUDA_TRY(cudaStreamSynchronize(oct->stage_streams[0]));
     SVO_CUDA_TRY(cudaStreamSynchronize(oct->stage_streams[1]));
+    return check_device_status(oct);
+}
+
+int svo_trace_image_host(svo_octree *oct, const float *rays, uint32_t width, uint32_t height, float ray_scale,
+                         const float light[3], const svo_trace_out *out) {
+    if (!oct || (!rays && width && height) || !out) return set_error(SVO_ERR_INVALID, "null argument");
+    if ((uint64_t)width * height > 0xFFFFFFFFull) return set_error(SVO_ERR_LIMIT, "more than 2^32-1 pixels");
+    if (width == 0 || height == 0) return SVO_OK;
+    std::lock_guard<std::mutex> lock(oct->staging_mtx);
+    // Chunks of whole rows (a multiple of the 4-row tile height), about
+    // kStageRays rays each, alternating between two streams.
+    uint64_t rows = std::max<uint64_t>(4, (kStageRays / width) & ~uint64_t(3));
+    const uint64_t C = rows * width;
+    auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+    const size_t half = al(C * 24) + al(C) + al(C * 4) * 3 + al(C * 12);
+    int rc = ensure_staging(oct, 2 * half);
+    if (rc) return rc;
+    // The persistent launch uses the handle's single work counter, so traces
+    // run one after another on the trace stream while the next chunk's rays
+    // come in and the previous chunk's results go out on two copy streams.
+    if (!oct->img_streams[0]) {
+        for (auto &st : oct->img_streams) SVO_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        for (int k = 0; k < 2; ++k) {
+            SVO_CUDA_TRY(cudaEventCreateWithFlags(&oct->img_in[k], cudaEventDisableTiming));
+            SVO_CUDA_TRY(cudaEventCreateWithFlags(&oct->img_traced[k], cudaEventDisableTiming));
+            SVO_CUDA_TRY(cudaEventCreateWithFlags(&oct->img_out[k], cudaEventDisableTiming));
+        }
+    }
+    cudaStream_t si = oct->img_streams[0], sk = oct->img_streams[1], so = oct->img_streams[2];
+    uint64_t j = 0;
+    for (uint64_t y0 = 0; y0 < height; y0 += rows, ++j) {
+        const int h = (int)(j & 1);
+        uint64_t nr = std::min<uint64_t>(rows, height - y0);
+        uint64_t m = nr * width, c0 = y0 * width;
+        uint8_t *base = (uint8_t *)oct->stage_dev + h * half;
+        float *d_rays = (float *)base;
+        uint8_t *d_hit = base + al(C * 24);
+        float *d_t = (float *)(d_hit + al(C));
+        uint32_t *d_leaf = (uint32_t *)((uint8_t *)d_t + al(C * 4));
+        uint32_t *d_word = (uint32_t *)((uint8_t *)d_leaf + al(C * 4));
+        float *d_rgb = (float *)((uint8_t *)d_word + al(C * 4));
+        // rays of this half are free once the trace two chunks back is done
+        if (j >= 2) SVO_CUDA_TRY(cudaStreamWaitEvent(si, oct->img_traced[h], 0));
+        SVO_CUDA_TRY(cudaMemcpyAsync(d_rays, rays + 6 * c0, m * 24, cudaMemcpyHostToDevice, si));
+        SVO_CUDA_TRY(cudaEventRecord(oct->img_in[h], si));
+        // outputs of this half are free once their copy two chunks back is done
+        SVO_CUDA_TRY(cudaStreamWaitEvent(sk, oct->img_in[h], 0));
+        if (j >= 2) SVO_CUDA_TRY(cudaStreamWaitEvent(sk, oct->img_out[h], 0));
+        svo_trace_out o;
+        o.hit = out->hit ? d_hit : nullptr;
+        o.t = out->t ? d_t : nullptr;
+        o.leaf = out->leaf ? d_leaf : nullptr;
+        o.word = out->word ? d_word : nullptr;
+        o.rgb = out->rgb ? d_rgb : nullptr;
+        rc = launch_trace_image(oct, d_rays, width, (uint32_t)nr, ray_scale, light, o, sk);
+        if (rc) return rc;
+        SVO_CUDA_TRY(cudaEventRecord(oct->img_traced[h], sk));
+        SVO_CUDA_TRY(cudaStreamWaitEvent(so, oct->img_traced[h], 0));
+        if (out->hit) SVO_CUDA_TRY(cudaMemcpyAsync(out->hit + c0, d_hit, m, cudaMemcpyDeviceToHost, so));
+        if (out->t) SVO_CUDA_TRY(cudaMemcpyAsync(out->t + c0, d_t, m * 4, cudaMemcpyDeviceToHost, so));
+        if (out->leaf) SVO_CUDA_TRY(cudaMemcpyAsync(out->leaf + c0, d_leaf, m * 4, cudaMemcpyDeviceToHost, so));
+        if (out->word) SVO_CUDA_TRY(cudaMemcpyAsync(out->word + c0, d_word, m * 4, cudaMemcpyDeviceToHost, so));
+        if (out->rgb) SVO_CUDA_TRY(cudaMemcpyAsync(out->rgb + 3 * c0, d_rgb, m * 12, cudaMemcpyDeviceToHost, so));
+        SVO_CUDA_TRY(cudaEventRecord(oct->img_out[h], so));
+    }
+    SVO_CUDA_TRY(cudaStreamSynchronize(si));
+    SVO_CUDA_TRY(cudaStreamSynchronize(sk));
+    SVO_CUDA_TRY(cudaStreamSynchronize(so));
     return check_device_status(oct);
 }
 

@@ -19,6 +19,7 @@ struct svo_octree {
     float center[3] = {0.0f, 0.0f, 0.0f};
     int device = 0;
     uint32_t *d_status = nullptr;  // device error word: bit 0 = a ray ended with kFault
+    unsigned long long *d_queue = nullptr;  // work counter of svo_trace_image's persistent launch
 
     // Staging for svo_trace_host: one device arena and one pinned host arena,
     // split into two halves that alternate between two streams.
@@ -28,6 +29,10 @@ struct svo_octree {
     void *stage_host = nullptr;
     size_t stage_host_bytes = 0;
     cudaStream_t stage_streams[2] = {nullptr, nullptr};
+    // svo_trace_image_host pipeline: copy-in, trace and copy-out streams and
+    // per-half events (inputs landed, trace done, outputs copied).
+    cudaStream_t img_streams[3] = {nullptr, nullptr, nullptr};
+    cudaEvent_t img_in[2] = {nullptr, nullptr}, img_traced[2] = {nullptr, nullptr}, img_out[2] = {nullptr, nullptr};
 };
 
 namespace svo {
@@ -60,6 +65,8 @@ int build_dense_device(const uint32_t *d_grid, int w, int h, int d, int log_side
 // Trace launchers (trace.cu).
 int launch_trace(const svo_octree *oct, const float *d_rays, uint64_t n, float ray_scale, const float light[3],
                  const svo_trace_out &out, cudaStream_t st);
+int launch_trace_image(const svo_octree *oct, const float *d_rays, uint32_t width, uint32_t height, float ray_scale,
+                       const float light[3], const svo_trace_out &out, cudaStream_t st);
 int launch_count_loads(const svo_octree *oct, const float *d_rays, uint64_t n, float ray_scale, uint32_t *loads,
                        cudaStream_t st);
 

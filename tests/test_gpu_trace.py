@@ -134,3 +134,39 @@ def test_corrupt_tree_raises_device_flag(cuda, svo):
     with pytest.raises(svo.SvoError) as e:
         tree.trace_host(rays)
     assert e.value.code == svo.SVO_ERR_DEVICE
+
+
+@pytest.mark.parametrize("W,H", [(320, 240), (37, 23), (1, 1), (1000, 3), (7, 401)])
+def test_trace_image_matches_oracle(cuda, svo, golden, oracle, scenes, W, H):
+    torch = cuda
+    g = golden["dragon"]
+    tree = svo.VoxelOctree.from_words(g["words"], g["center"])
+    cam = scenes.orbit_cameras(1, W * 7 + H, g["center"], radius=1.4)[0]
+    rays = scenes.camera_rays(cam, W, H)
+    light = scenes.headlight(cam)
+    R = rays.shape[0]
+    out = {"hit": torch.empty(R, dtype=torch.uint8, device="cuda"),
+           "t": torch.empty(R, dtype=torch.float32, device="cuda"),
+           "leaf": torch.empty(R, dtype=torch.int32, device="cuda"),
+           "word": torch.empty(R, dtype=torch.int32, device="cuda"),
+           "rgb": torch.empty((R, 3), dtype=torch.float32, device="cuda")}
+    for scale in (0.0, 0.01):
+        tree.trace_image(torch.from_numpy(rays).cuda(), W, H, ray_scale=scale, light=light, out=out)
+        torch.cuda.synchronize()
+        res = {k: v.cpu().numpy() for k, v in out.items()}
+        res["leaf"] = res["leaf"].view(np.uint32)
+        res["word"] = res["word"].view(np.uint32)
+        _assert_same(res, oracle.raymarch(g["words"], rays, ray_scale=scale, light=light, threads=4), grey=scale == 0)
+    assert tree.device_status() == 0
+
+
+def test_trace_image_host_matches_oracle(svo, oracle, scenes):
+    grid = scenes.sphere_scene(128, 24, 5)
+    words, center = oracle.build_dense(grid)
+    tree = svo.VoxelOctree.from_words(words, center)
+    cams = scenes.orbit_cameras(4, 3, center)
+    W, H = 1003, 777  # 2.2 M rays: several staged chunks of whole rows
+    rays = np.concatenate([scenes.camera_rays(c, W, H // 4 + 1)[:W * (H // 4)] for c in cams] +
+                          [scenes.camera_rays(cams[0], W, H - 4 * (H // 4))])
+    host = tree.trace_image_host(rays, W, H, light=(0.0, 1.0, 0.0))
+    _assert_same(host, oracle.raymarch(words, rays, light=(0.0, 1.0, 0.0), threads=8))
