@@ -59,8 +59,9 @@ def parse():
     p.add_argument("--height", type=int, default=H_PIX)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--config", type=int, default=1, choices=[1, 3],
-                   help="1: plain traversal (headline); 3: batched vs plain over 96 octrees and views")
+    p.add_argument("--config", type=int, default=1, choices=[1, 3, 4],
+                   help="1: plain traversal (headline); 3: batched vs plain over 96 octrees and views; "
+                        "4: differentiable shading fwd+bwd")
     p.add_argument("--no-extra", action="store_true", help="skip the config-3 batched comparison in the default run")
     p.add_argument("--views", type=int, default=96)
     return p.parse_args()
@@ -232,6 +233,17 @@ def run_ours(args):
     import svo_gb300.scenes as scenes
     os.environ.setdefault("SVO_AUTOTUNE_CACHE", os.path.join(ROOT, "gpurun_out", "autotune.jsonl"))
 
+    if args.config == 4:
+        r4 = run_config4(args, torch, svo, scenes)
+        if rank == 0:
+            print(json.dumps({"metric": "fwd+bwd Mrays/s", "value": r4["fwd_bwd_mrays_s"], "unit": "Mrays/s",
+                              "n_gpus": world, "steps": r4["steps"], "warmup": 0,
+                              "ms_per_step": r4["step_ms_with_adam"], "higher_is_better": True, "scaling": "weak",
+                              "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                              "config": {"workload": "differentiable: " + r4["workload"]}, "fwd_bwd": r4,
+                              "gpu_launches": 2 * r4["steps"]}))
+        return
+
     if args.config == 3:
         r3 = run_config3(args, torch, svo, scenes)
         if rank == 0:
@@ -377,11 +389,13 @@ def run_ours(args):
                          "VoxelOctree::raymarch, %d threads)" % (ncam, len(cam_slices), n, secs, thr)}
         del words
 
-    extra = None
+    extra = extra4 = None
     if not args.no_extra and world == 1:
         del prim, shadow, out_p, out_s, ref_p, ref_s, tree
         torch.cuda.empty_cache()
         extra = run_config3(args, torch, svo, scenes)
+        torch.cuda.empty_cache()
+        extra4 = run_config4(args, torch, svo, scenes)
 
     if rank == 0:
         line = {
@@ -407,6 +421,7 @@ def run_ours(args):
                         "ms_per_step": round(ms_batched, 3), "mrays_s": round(rays_per_step / ms_batched / 1e3, 1),
                         "config": cfg.as_dict(), "exact_vs_value_path": bool(exact_batched)},
             "batched_vs_plain": extra,
+            "fwd_bwd": extra4,
             "build": {"build_s": round(info["build_s"], 3), "scene_gen_s": round(info["gen_s"], 3),
                       "voxels_per_s": round(info["voxels"] / info["build_s"], 1)},
             "kernel_ms": {"primary": round(t_prim_avg, 3), "shadow": round(sum(t_shadow) / len(t_shadow), 3)},
@@ -497,6 +512,91 @@ def run_config3(args, torch, svo, scenes, tune_cache=None):
             "speedup": round(ms_plain / ms_batched, 3), "exact_hit_parity": bool(exact),
             "config": cfg.as_dict(), "autotune_s": round(tune_s, 1), "setup_s": round(setup_s, 1),
             "launches": {"plain": len(views), "batched": 1}}
+
+
+def run_config4(args, torch, svo, scenes, n_steps=200):
+    """Differentiable leaf shading: 512^3 sphere union (160 spheres, seed 7),
+    per-leaf FP32 rgb and normal parameters ~U[0,1], 24 views 512x512 against
+    targets from a seeded 3-octave noise colour field; L2 loss, forward +
+    hand-written adjoint, Adam lr 1e-2, 200 steps."""
+    side, W, H, V = 512, 512, 512, 24
+    t0 = time.perf_counter()
+    grid = scenes.gpu_sphere_scene(side, 160, 7)
+    tree = svo.VoxelOctree(svo.VoxelData(grid))
+    del grid
+    center = tree.center()
+    cams = scenes.orbit_cameras(V, 7, center, radius=2.0)
+    rays = torch.empty((V * W * H, 6), dtype=torch.float32, device="cuda")
+    for i, c in enumerate(cams):
+        scenes.gpu_camera_rays(c, W, H, out=rays[i * W * H:(i + 1) * W * H])
+    lights = torch.from_numpy(np.stack([scenes.headlight(c) for c in cams]).astype(np.float32)).cuda()
+    R = rays.shape[0]
+    nw = tree.num_words()
+    # targets: noise colour at the hit point, lit with the leaf's own normal
+    t = torch.empty(R, dtype=torch.float32, device="cuda")
+    word = torch.empty(R, dtype=torch.int32, device="cuda")
+    hit = torch.empty(R, dtype=torch.uint8, device="cuda")
+    for v in range(V):
+        sl = slice(v * W * H, (v + 1) * W * H)
+        tree.trace(rays[sl], out={"t": t[sl], "word": word[sl], "hit": hit[sl]})
+    torch.cuda.synchronize()
+    h = hit == 1
+    p = rays[h, :3] + t[h, None] * rays[h, 3:]
+    gt = torch.stack([scenes.noise3(p, 7 + k) for k in range(3)], 1)
+    n = scenes.decompress_normal(word[h].to(torch.int64) & 0xFFFFFFFF)
+    d = rays[h, 3:]
+    l = lights.repeat_interleave(W * H, 0)[h]
+    ln = (l * n).sum(1)
+    r = d - 2 * (n * d).sum(1, keepdim=True) * n
+    spec = torch.clamp((l * r).sum(1), min=0) ** 2 * 0.2
+    target = torch.zeros((R, 3), dtype=torch.float32, device="cuda")
+    target[h] = gt * 0.9 * ln.abs()[:, None] + spec[:, None]
+    del t, word, p, gt, n, d, l, ln, r, spec
+    gen = torch.Generator(device="cuda").manual_seed(7)
+    p_rgb = torch.rand((nw, 3), generator=gen, device="cuda").requires_grad_()
+    p_n = torch.rand((nw, 3), generator=gen, device="cuda").requires_grad_()
+    opt = torch.optim.Adam([p_rgb, p_n], lr=1e-2)
+    rgb = torch.empty((R, 3), dtype=torch.float32, device="cuda")
+    leaf = torch.empty(R, dtype=torch.int32, device="cuda")
+    d_rgb = torch.empty((R, 3), dtype=torch.float32, device="cuda")
+    g_rgb = torch.zeros_like(p_rgb)
+    g_n = torch.zeros_like(p_n)
+    scale = 2.0 / (3 * R)
+    setup_s = time.perf_counter() - t0
+    stream = torch.cuda.current_stream()
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(n_steps)]
+    losses = []
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for k in range(n_steps):
+        ev[k][0].record(stream)
+        tree.diff_forward(rays, W, H, V, lights, p_rgb.detach(), p_n.detach(), rgb, hit_leaf=leaf, stream=stream)
+        ev[k][1].record(stream)
+        torch.sub(rgb, target, out=d_rgb)
+        if k % 20 == 0 or k == n_steps - 1:
+            losses.append((k, d_rgb.square().sum() / (3 * R)))
+        d_rgb.mul_(scale)
+        g_rgb.zero_()
+        g_n.zero_()
+        tree.diff_backward(rays, W, H, V, lights, p_rgb.detach(), p_n.detach(), d_rgb, g_rgb, g_n, hit_leaf=leaf,
+                           stream=stream)
+        ev[k][2].record(stream)
+        p_rgb.grad = g_rgb
+        p_n.grad = g_n
+        opt.step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    fwd = [e[0].elapsed_time(e[1]) for e in ev]
+    bwd = [e[1].elapsed_time(e[2]) for e in ev]  # includes the dL/drgb elementwise ops
+    step_ms = e0.elapsed_time(e1) / n_steps
+    fb = (sum(fwd) + sum(bwd)) / n_steps
+    return {"workload": "512^3 sphere union (160 spheres, seed 7), %d octree words; 24 views 512x512; per-leaf FP32 "
+                        "rgb+normal params; L2 loss vs 3-octave noise colour field; Adam lr 1e-2" % nw,
+            "rays_per_step": R, "steps": n_steps, "fwd_ms": round(sum(fwd) / n_steps, 3),
+            "bwd_ms": round(sum(bwd) / n_steps, 3), "fwd_bwd_mrays_s": round(R / fb / 1e3, 1),
+            "step_ms_with_adam": round(step_ms, 3),
+            "loss": [[k, round(float(v.item()), 6)] for k, v in losses], "setup_s": round(setup_s, 1)}
 
 
 def profiled_traffic(rays):

@@ -204,6 +204,35 @@ int svo_trace_image_host(svo_octree *oct, const float *rays, uint32_t width, uin
 int svo_trace_count_loads(const svo_octree *oct, const float *rays, uint64_t n, float ray_scale,
                           uint32_t *loads, svo_stream stream);
 
+/* ---------------------------------------------------- differentiable shading */
+
+/* No counterpart in the reference.  The viewer's shade() (Main.cpp:81-90)
+ * with FP32 per-leaf parameters instead of the packed leaf word:
+ *   n = p/|p| (p = leaf_normal[3*i..]),  rgb_k = c_k 0.9 |l.n| + 0.2 max(l.r, 0)^2,
+ *   r = d - 2 (n.d) n,  c = leaf_rgb[3*i..],
+ * for the leaf i a ray hits (i = the word index svo_trace reports as `leaf`;
+ * the arrays hold 3 floats per octree word, only leaf entries are used).
+ * Rays are a stack of n_views row-major images of width x height, all device
+ * memory; view v (rows [v*height, (v+1)*height)) uses lights[3*v..] (device).
+ *
+ * svo_diff_forward traces every ray (the unchanged discrete raymarch) and
+ * writes rgb (3 floats per ray, 0 on a miss) and, when hit_leaf != NULL, the
+ * hit leaf's word index per ray (0xFFFFFFFF on a miss). */
+int svo_diff_forward(const svo_octree *oct, const float *rays, uint32_t width, uint32_t height, uint32_t n_views,
+                     const float *lights, const float *leaf_rgb, const float *leaf_normal, uint32_t *hit_leaf,
+                     float *rgb, svo_stream stream);
+
+/* Adjoint of svo_diff_forward: adds dL/dleaf_rgb and dL/dleaf_normal for
+ * the given dL/drgb (3 floats per ray) into grad_rgb / grad_normal (same
+ * layout as the parameters; zero them first for a fresh gradient).  Hit
+ * leaves come from hit_leaf, or, when hit_leaf == NULL, from re-tracing the
+ * rays (no per-ray buffer kept between the passes).  Lanes of a warp hitting
+ * the same leaf are summed in registers before one set of atomics per leaf;
+ * the summation order across warps is not fixed. */
+int svo_diff_backward(const svo_octree *oct, const float *rays, uint32_t width, uint32_t height, uint32_t n_views,
+                      const float *lights, const float *leaf_rgb, const float *leaf_normal, const uint32_t *hit_leaf,
+                      const float *d_rgb, float *grad_rgb, float *grad_normal, svo_stream stream);
+
 /* ----------------------------------------------------------------- batched */
 
 /* One (octree, view) pair of a batched trace.  A view is either

@@ -96,6 +96,10 @@ def _load():
                                            ctypes.POINTER(TraceOut), _vp]),
         "svo_trace_image_host": (ctypes.c_int, [_vp, _vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float, _f32p,
                                                 ctypes.POINTER(TraceOut)]),
+        "svo_diff_forward": (ctypes.c_int, [_vp, _vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _vp, _vp, _vp,
+                                            _vp, _vp, _vp]),
+        "svo_diff_backward": (ctypes.c_int, [_vp, _vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _vp, _vp, _vp,
+                                             _vp, _vp, _vp, _vp, _vp]),
         "svo_batch_create": (ctypes.c_int, [ctypes.POINTER(View), ctypes.c_int, ctypes.POINTER(_vp)]),
         "svo_batch_default_config": (ctypes.c_int, [ctypes.POINTER(TraceConfig)]),
         "svo_batch_num_slots": (ctypes.c_int, [_vp, _u64p]),
@@ -335,6 +339,20 @@ class VoxelOctree:
         check(lib.svo_trace_image_host(self._h, _np_ptr(rays), int(width), int(height), float(ray_scale),
                                        lt.ctypes.data_as(_f32p), ctypes.byref(o)))
         return res
+
+    def diff_forward(self, rays, width, height, n_views, lights, leaf_rgb, leaf_normal, rgb, hit_leaf=None,
+                     stream=None):
+        """Differentiable shading forward (all CUDA tensors); see svo_diff_forward."""
+        check(lib.svo_diff_forward(self._h, _dev_ptr(rays), int(width), int(height), int(n_views), _dev_ptr(lights),
+                                   _dev_ptr(leaf_rgb), _dev_ptr(leaf_normal), _dev_ptr(hit_leaf), _dev_ptr(rgb),
+                                   _stream_ptr(stream)))
+
+    def diff_backward(self, rays, width, height, n_views, lights, leaf_rgb, leaf_normal, d_rgb, grad_rgb,
+                      grad_normal, hit_leaf=None, stream=None):
+        """Adjoint: accumulates parameter gradients; hit_leaf=None re-traces."""
+        check(lib.svo_diff_backward(self._h, _dev_ptr(rays), int(width), int(height), int(n_views), _dev_ptr(lights),
+                                    _dev_ptr(leaf_rgb), _dev_ptr(leaf_normal), _dev_ptr(hit_leaf), _dev_ptr(d_rgb),
+                                    _dev_ptr(grad_rgb), _dev_ptr(grad_normal), _stream_ptr(stream)))
 
     def count_loads(self, rays, n=None, ray_scale=0.0, loads=None, stream=None):
         if n is None:

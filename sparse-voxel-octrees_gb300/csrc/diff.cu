@@ -1,0 +1,280 @@
+// diff.cu — differentiable leaf shading over the octree (no counterpart in
+// the reference; the shading model is the viewer's shade(), Main.cpp:81-90,
+// with per-leaf parameters in place of the packed leaf word).
+//
+// Parameters are FP32 arrays indexed by the leaf's word index (the `leaf`
+// output of svo_trace): rgb[3*i..] and normal[3*i..].  For a ray with
+// direction d, hitting leaf i, under light l:
+//   n     = p / |p|                 (p = normal parameters; n = 0 when p = 0)
+//   a     = |l.n|
+//   r     = d - 2 (n.d) n           (Vec3::reflect, math/Vec3.hpp:63-71)
+//   s     = max(l.r, 0)
+//   rgb_k = c_k * 0.9 * a + 0.2 * s^2          (c = rgb parameters)
+// Rays that hit no leaf produce 0 and no gradient.  Traversal is the discrete
+// ESVO raymarch, unchanged; only the shading is differentiated:
+//   dL/dc_k = g_k 0.9 a
+//   dL/dn   = (0.9 sgn(l.n) sum_k g_k c_k) l - 0.8 G s [s > 0] ((n.d) l + (n.l) d),  G = sum_k g_k
+//   dL/dp   = (dL/dn - n (n.dL/dn)) / |p|
+// with g = dL/drgb.  Gradients are summed over rays with atomics; lanes of a
+// warp that hit the same leaf are first reduced in registers (match_any +
+// a rank-ordered shuffle tree), so one lane per distinct leaf issues the six
+// atomicAdds.  Summation order across warps is not fixed, so gradients can
+// differ in the last bits between runs.
+#include "svo_device.cuh"
+#include "svo_internal.h"
+
+namespace svo {
+namespace {
+
+struct DiffArgs {
+    const uint32_t *oct;
+    uint32_t n_words;
+    const float *rays;
+    uint32_t width, height, n_views;  // image = width x (height * n_views), view v = rows [v*height, (v+1)*height)
+    uint32_t tiles_x;
+    uint64_t total;
+    const float *lights;  // 3 per view (device)
+    const float *p_rgb, *p_n;
+    uint32_t *hit_leaf;
+    float *rgb;
+    const float *d_rgb;
+    float *g_rgb, *g_n;
+    unsigned long long *queue;
+    uint32_t *status;
+};
+
+__device__ __forceinline__ bool tile_pixel(const DiffArgs &a, uint64_t slot, uint32_t &idx, uint32_t &view) {
+    uint64_t tile = slot >> 5;
+    uint32_t r = (uint32_t)(slot & 31);
+    uint32_t px = (uint32_t)(tile % a.tiles_x) * 8u + (r & 7u);
+    uint32_t py = (uint32_t)(tile / a.tiles_x) * 4u + (r >> 3);
+    if (px >= a.width || py >= a.height * a.n_views) return false;
+    idx = py * a.width + px;
+    view = py / a.height;
+    return true;
+}
+
+struct Shading {
+    float nx, ny, nz, inv_len, ln, a, nd, s;
+};
+
+__device__ __forceinline__ Shading shade_terms(const float *p_n, uint32_t leaf, float dx, float dy, float dz, float lx,
+                                               float ly, float lz) {
+    Shading sh;
+    float px = p_n[3 * (uint64_t)leaf], py = p_n[3 * (uint64_t)leaf + 1], pz = p_n[3 * (uint64_t)leaf + 2];
+    float len2 = px * px + py * py + pz * pz;
+    sh.inv_len = len2 > 0.0f ? 1.0f / sqrtf(len2) : 0.0f;
+    sh.nx = px * sh.inv_len;
+    sh.ny = py * sh.inv_len;
+    sh.nz = pz * sh.inv_len;
+    sh.ln = lx * sh.nx + ly * sh.ny + lz * sh.nz;
+    sh.a = fabsf(sh.ln);
+    sh.nd = sh.nx * dx + sh.ny * dy + sh.nz * dz;
+    float proj = sh.nd * 2.0f;
+    float rx = dx - sh.nx * proj, ry = dy - sh.ny * proj, rz = dz - sh.nz * proj;
+    sh.s = fmaxf(lx * rx + ly * ry + lz * rz, 0.0f);
+    return sh;
+}
+
+template <bool kRecord>
+__global__ void k_diff_forward(DiffArgs a) {
+    const int lane = threadIdx.x & 31;
+    RayStack stk;
+    while (true) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(a.queue, 32ull);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= a.total) break;
+        uint32_t idx, view;
+        if (!tile_pixel(a, base + lane, idx, view)) continue;
+        const float2 *r2 = reinterpret_cast<const float2 *>(a.rays) + 3 * (uint64_t)idx;
+        float2 p0 = __ldg(r2), p1 = __ldg(r2 + 1), p2 = __ldg(r2 + 2);
+        RayState st;
+        ray_init(st, a.oct, p0.x, p0.y, p1.x, p1.y, p2.x, p2.y);
+        RayResult res;
+        while (!ray_step<false, false>(st, stk, a.oct, a.n_words, 0.0f, res)) {
+        }
+        if (res.status == kFault) atomicOr(a.status, 1u);
+        bool hit = res.status == kLeafHit;
+        if (kRecord) a.hit_leaf[idx] = hit ? res.leaf : 0xFFFFFFFFu;
+        float c0 = 0.0f, c1 = 0.0f, c2 = 0.0f;
+        if (hit) {
+            float lx = a.lights[3 * view], ly = a.lights[3 * view + 1], lz = a.lights[3 * view + 2];
+            Shading sh = shade_terms(a.p_n, res.leaf, p1.y, p2.x, p2.y, lx, ly, lz);
+            float spec = sh.s * sh.s * 0.2f;
+            const float *c = a.p_rgb + 3 * (uint64_t)res.leaf;
+            c0 = c[0] * 0.9f * sh.a + spec;
+            c1 = c[1] * 0.9f * sh.a + spec;
+            c2 = c[2] * 0.9f * sh.a + spec;
+        }
+        a.rgb[3 * (uint64_t)idx] = c0;
+        a.rgb[3 * (uint64_t)idx + 1] = c1;
+        a.rgb[3 * (uint64_t)idx + 2] = c2;
+    }
+}
+
+// Sum of v over the lanes in `peers` (the lanes holding the same key), left
+// in the group's lowest lane.  Lane ranks within the group form a binary
+// tree: at distance k a lane whose rank is a multiple of 2k adds the value of
+// the group member k ranks above it.  All 32 lanes execute every shuffle.
+__device__ __forceinline__ float group_sum(unsigned peers, unsigned rank, unsigned size, float v) {
+    for (unsigned k = 1; k < 32; k <<= 1) {
+        unsigned src_rank = rank + k;
+        bool take = (rank % (2 * k)) == 0 && src_rank < size;
+        int src = take ? (int)__fns(peers, 0, (int)src_rank + 1) : (int)(threadIdx.x & 31);
+        float o = __shfl_sync(0xffffffffu, v, src);
+        if (take) v += o;
+    }
+    return v;
+}
+
+// kRetrace: recompute the hit leaf by traversal instead of reading hit_leaf.
+template <bool kRetrace>
+__global__ void k_diff_backward(DiffArgs a) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    RayStack stk;
+    while (true) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(a.queue, 32ull);
+        base = __shfl_sync(FULL, base, 0);
+        if (base >= a.total) break;
+        uint32_t idx = 0, view = 0;
+        bool live = tile_pixel(a, base + lane, idx, view);
+        uint32_t leaf = 0xFFFFFFFFu;
+        float dx = 0.f, dy = 0.f, dz = 0.f;
+        if (live) {
+            const float2 *r2 = reinterpret_cast<const float2 *>(a.rays) + 3 * (uint64_t)idx;
+            float2 p1 = __ldg(r2 + 1), p2 = __ldg(r2 + 2);
+            dx = p1.y;
+            dy = p2.x;
+            dz = p2.y;
+            if (kRetrace) {
+                float2 p0 = __ldg(r2);
+                RayState st;
+                ray_init(st, a.oct, p0.x, p0.y, p1.x, dx, dy, dz);
+                RayResult res;
+                while (!ray_step<false, false>(st, stk, a.oct, a.n_words, 0.0f, res)) {
+                }
+                if (res.status == kFault) atomicOr(a.status, 1u);
+                if (res.status == kLeafHit) leaf = res.leaf;
+            } else {
+                leaf = a.hit_leaf[idx];
+            }
+        }
+        float gc0 = 0.f, gc1 = 0.f, gc2 = 0.f, gp0 = 0.f, gp1 = 0.f, gp2 = 0.f;
+        bool contrib = leaf != 0xFFFFFFFFu;
+        if (contrib) {
+            float lx = a.lights[3 * view], ly = a.lights[3 * view + 1], lz = a.lights[3 * view + 2];
+            Shading sh = shade_terms(a.p_n, leaf, dx, dy, dz, lx, ly, lz);
+            const float *c = a.p_rgb + 3 * (uint64_t)leaf;
+            float g0 = a.d_rgb[3 * (uint64_t)idx], g1 = a.d_rgb[3 * (uint64_t)idx + 1],
+                  g2 = a.d_rgb[3 * (uint64_t)idx + 2];
+            gc0 = g0 * 0.9f * sh.a;
+            gc1 = g1 * 0.9f * sh.a;
+            gc2 = g2 * 0.9f * sh.a;
+            float sgn = sh.ln > 0.0f ? 1.0f : (sh.ln < 0.0f ? -1.0f : 0.0f);
+            float wl = 0.9f * sgn * (g0 * c[0] + g1 * c[1] + g2 * c[2]);
+            float ws = sh.s > 0.0f ? -0.8f * (g0 + g1 + g2) * sh.s : 0.0f;
+            // dL/dn = wl l + ws ((n.d) l + (n.l) d)
+            float gnx = wl * lx + ws * (sh.nd * lx + sh.ln * dx);
+            float gny = wl * ly + ws * (sh.nd * ly + sh.ln * dy);
+            float gnz = wl * lz + ws * (sh.nd * lz + sh.ln * dz);
+            float ndg = sh.nx * gnx + sh.ny * gny + sh.nz * gnz;
+            gp0 = (gnx - sh.nx * ndg) * sh.inv_len;
+            gp1 = (gny - sh.ny * ndg) * sh.inv_len;
+            gp2 = (gnz - sh.nz * ndg) * sh.inv_len;
+        }
+        // warp aggregation by leaf: one set of atomics per distinct leaf
+        unsigned peers = __match_any_sync(FULL, leaf);
+        unsigned rank = __popc(peers & lt), size = __popc(peers);
+        gc0 = group_sum(peers, rank, size, gc0);
+        gc1 = group_sum(peers, rank, size, gc1);
+        gc2 = group_sum(peers, rank, size, gc2);
+        gp0 = group_sum(peers, rank, size, gp0);
+        gp1 = group_sum(peers, rank, size, gp1);
+        gp2 = group_sum(peers, rank, size, gp2);
+        if (contrib && rank == 0) {
+            float *gr = a.g_rgb + 3 * (uint64_t)leaf;
+            float *gn = a.g_n + 3 * (uint64_t)leaf;
+            atomicAdd(gr, gc0);
+            atomicAdd(gr + 1, gc1);
+            atomicAdd(gr + 2, gc2);
+            atomicAdd(gn, gp0);
+            atomicAdd(gn + 1, gp1);
+            atomicAdd(gn + 2, gp2);
+        }
+    }
+}
+
+int prepare(const svo_octree *oct, const float *rays, uint32_t width, uint32_t height, uint32_t n_views,
+            const float *lights, const float *p_rgb, const float *p_n, DiffArgs &a) {
+    if (!oct || !rays || !lights || !p_rgb || !p_n || width == 0 || height == 0 || n_views == 0)
+        return set_error(SVO_ERR_INVALID, "bad arguments");
+    if ((uint64_t)width * height * n_views > 0xFFFFFFFFull) return set_error(SVO_ERR_LIMIT, "more than 2^32-1 rays");
+    std::memset(&a, 0, sizeof(a));
+    a.oct = oct->d_words;
+    a.n_words = (uint32_t)oct->n_words;
+    a.rays = rays;
+    a.width = width;
+    a.height = height;
+    a.n_views = n_views;
+    a.tiles_x = (width + 7) / 8;
+    a.total = (uint64_t)a.tiles_x * ((height * n_views + 3) / 4) * 32;
+    a.lights = lights;
+    a.p_rgb = p_rgb;
+    a.p_n = p_n;
+    a.queue = oct->d_queue;
+    a.status = oct->d_status;
+    return SVO_OK;
+}
+
+template <typename K>
+int launch_persistent(K kern, const DiffArgs &a, cudaStream_t st) {
+    int dev = 0, sms = 0, resident = 0;
+    SVO_CUDA_TRY(cudaGetDevice(&dev));
+    SVO_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    SVO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, kern, 256, 0));
+    SVO_CUDA_TRY(cudaMemsetAsync(a.queue, 0, sizeof(unsigned long long), st));
+    kern<<<(unsigned)(sms * (resident > 0 ? resident : 1)), 256, 0, st>>>(a);
+    SVO_CUDA_TRY(cudaGetLastError());
+    return SVO_OK;
+}
+
+}  // namespace
+}  // namespace svo
+
+using namespace svo;
+
+extern "C" {
+
+int svo_diff_forward(const svo_octree *oct, const float *rays, uint32_t width, uint32_t height, uint32_t n_views,
+                     const float *lights, const float *leaf_rgb, const float *leaf_normal, uint32_t *hit_leaf,
+                     float *rgb, svo_stream stream) {
+    DiffArgs a;
+    int rc = prepare(oct, rays, width, height, n_views, lights, leaf_rgb, leaf_normal, a);
+    if (rc) return rc;
+    if (!rgb) return set_error(SVO_ERR_INVALID, "rgb output required");
+    a.hit_leaf = hit_leaf;
+    a.rgb = rgb;
+    return hit_leaf ? launch_persistent(k_diff_forward<true>, a, (cudaStream_t)stream)
+                    : launch_persistent(k_diff_forward<false>, a, (cudaStream_t)stream);
+}
+
+int svo_diff_backward(const svo_octree *oct, const float *rays, uint32_t width, uint32_t height, uint32_t n_views,
+                      const float *lights, const float *leaf_rgb, const float *leaf_normal, const uint32_t *hit_leaf,
+                      const float *d_rgb, float *grad_rgb, float *grad_normal, svo_stream stream) {
+    DiffArgs a;
+    int rc = prepare(oct, rays, width, height, n_views, lights, leaf_rgb, leaf_normal, a);
+    if (rc) return rc;
+    if (!d_rgb || !grad_rgb || !grad_normal) return set_error(SVO_ERR_INVALID, "gradient buffers required");
+    a.hit_leaf = const_cast<uint32_t *>(hit_leaf);
+    a.d_rgb = d_rgb;
+    a.g_rgb = grad_rgb;
+    a.g_n = grad_normal;
+    return hit_leaf ? launch_persistent(k_diff_backward<false>, a, (cudaStream_t)stream)
+                    : launch_persistent(k_diff_backward<true>, a, (cudaStream_t)stream);
+}
+
+}  // extern "C"

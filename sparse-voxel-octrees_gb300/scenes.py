@@ -404,3 +404,58 @@ def gpu_camera_rays(cam, W, H, out=None):
     _chk(_scene_lib().svo_scene_camera_rays(c.data_ptr(), 0, 0, W, H, out.data_ptr(), None))
     torch.cuda.synchronize()
     return out
+
+
+# ---------------------------------------------------------------- colour field (torch)
+
+def _lattice_value(ix, iy, iz, seed):
+    """Hash of integer lattice points to [0, 1) (int64 tensors)."""
+    import torch
+    m = 0xFFFFFFFF
+    h = (ix * 73856093) ^ (iy * 19349663) ^ (iz * 83492791) ^ (seed * 2654435761)
+    h = h & m
+    h = ((h ^ (h >> 16)) * 0x45D9F3B) & m
+    h = ((h ^ (h >> 16)) * 0x45D9F3B) & m
+    h = h ^ (h >> 16)
+    return (h & 0xFFFFFF).to(torch.float32) / float(1 << 24)
+
+
+def noise3(p, seed, octaves=3, freq=4.0):
+    """Seeded 3-octave value noise in [0, 1) at points p (CUDA float tensor
+    (N, 3) in the octree's [1, 2]^3 frame): trilinear smoothstep
+    interpolation of hashed lattice values, octave k at frequency freq*2^k
+    with amplitude 2^-k."""
+    import torch
+    total = torch.zeros(p.shape[0], dtype=torch.float32, device=p.device)
+    norm = 0.0
+    for k in range(octaves):
+        q = (p - 1.0) * (freq * (2 ** k))
+        qf = torch.floor(q)
+        i = qf.to(torch.int64)
+        f = q - qf
+        s = f * f * (3.0 - 2.0 * f)
+        v = 0.0
+        for dz in (0, 1):
+            for dy in (0, 1):
+                for dx in (0, 1):
+                    w = (s[:, 0] if dx else 1 - s[:, 0]) * (s[:, 1] if dy else 1 - s[:, 1]) * \
+                        (s[:, 2] if dz else 1 - s[:, 2])
+                    v = v + w * _lattice_value(i[:, 0] + dx, i[:, 1] + dy, i[:, 2] + dz, seed * 31 + k)
+        total += v * (0.5 ** k)
+        norm += 0.5 ** k
+    return total / norm
+
+
+def decompress_normal(word):
+    """Leaf normal of packed words (Util.hpp:86-100 layout), exact
+    normalisation; CUDA int64 tensor in, (N, 3) float tensor out."""
+    import torch
+    sign = ((word >> 31) & 1).to(torch.float32)
+    face = (word >> 29) & 3
+    u = ((word >> 18) & 0x7FF).to(torch.float32) * 4.8852e-4 * 2.0 - 1.0
+    v = ((word >> 7) & 0x7FF).to(torch.float32) * 4.8852e-4 * 2.0 - 1.0
+    s = 1.0 - 2.0 * sign
+    n = torch.stack([s, u, v], 1)
+    n = torch.where((face == 1)[:, None], torch.stack([v, s, u], 1), n)
+    n = torch.where((face >= 2)[:, None], torch.stack([u, v, s], 1), n)
+    return n / n.norm(dim=1, keepdim=True)
