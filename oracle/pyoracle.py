@@ -10,6 +10,7 @@ TEST INFRASTRUCTURE ONLY: imported by tests/, by ``__graft_entry__.smoke()``
                  the reference sources are present.
 """
 import ctypes
+import multiprocessing
 import os
 import subprocess
 
@@ -188,14 +189,75 @@ class Oracle:
         return words, c
 
 
+def _ref_worker_main(conn, path, threads):
+    """Child process: runs reference builds sent over `conn`."""
+    ref = Reference(path, isolated=False)
+    ref.start_threads(threads)
+    while True:
+        msg = conn.recv()
+        if msg is None:
+            return
+        name, args = msg
+        try:
+            conn.send(("ok", getattr(ref, name)(*args)))
+        except Exception as e:  # report, keep serving
+            conn.send(("err", repr(e)))
+
+
+class _RefBuildWorker:
+    """Runs the reference's VoxelOctree(VoxelData*) builds in a spawned child.
+
+    The reference's TaskGroup (thread/TaskGroup.hpp) sets its done flag and
+    notifies its condition variable without holding the waiter's mutex, so a
+    notification can land between the waiter's predicate check and its wait
+    and be lost; VoxelData's enqueue()->wait() calls then block forever now
+    and then.  A build that does not answer within `timeout` seconds is
+    retried in a fresh process."""
+
+    def __init__(self, path, threads, timeout=5.0, retries=6):
+        self.path, self.threads, self.timeout, self.retries = path, threads, timeout, retries
+        self.ctx = multiprocessing.get_context("spawn")
+        self.proc = None
+
+    def _start(self):
+        self.conn, child = self.ctx.Pipe()
+        self.proc = self.ctx.Process(target=_ref_worker_main, args=(child, self.path, self.threads), daemon=True)
+        self.proc.start()
+
+    def _stop(self):
+        if self.proc is not None:
+            self.proc.kill()
+            self.proc.join(5)
+            self.proc = None
+
+    def call(self, name, *args):
+        for _ in range(self.retries):
+            if self.proc is None or not self.proc.is_alive():
+                self._start()
+            self.conn.send((name, args))
+            if self.conn.poll(self.timeout):
+                status, value = self.conn.recv()
+                if status == "err":
+                    raise RuntimeError(value)
+                return value
+            self._stop()  # lost wakeup in the reference's thread pool: retry in a new process
+        raise RuntimeError("reference build did not finish after %d attempts" % self.retries)
+
+
 class Reference:
-    """The reference's own code, compiled in place from its sources."""
+    """The reference's own code, compiled in place from its sources.
+
+    Builds (whose VoxelData waits on the reference's thread pool) run in a
+    spawned worker process with a timeout; loads, saves and raymarches run
+    in-process."""
 
     _threads_started = None
 
-    def __init__(self, path=REF_SO):
+    def __init__(self, path=REF_SO, isolated=True):
         if not os.path.exists(path):
             raise FileNotFoundError(path)
+        self.path = path
+        self._worker = _RefBuildWorker(path, 4) if isolated else None
         L = ctypes.CDLL(path)
         self.L = L
         L.ref_start_threads.argtypes = [ctypes.c_int]
@@ -250,21 +312,62 @@ class Reference:
     def save(self, tree, path):
         self.L.ref_save(tree, path.encode())
 
-    def build_voxel_file(self, path, mem=1 << 30, threads=1, keep=False):
-        self.start_threads(threads)
-        tree = self.L.ref_build_voxel_file(path.encode(), int(mem))
-        out = self._take(tree)
+    def build_voxel_file(self, path, mem=1 << 30, threads=None, keep=False):
+        """(words, center); with keep=True also a loaded in-process tree
+        handle of the result (for raymarching)."""
+        if self._worker is not None:
+            out = self._worker.call("build_voxel_file", path, mem)
+        else:
+            tree = self.L.ref_build_voxel_file(path.encode(), int(mem))
+            out = self._take(tree)
+            self.L.ref_free(tree)
         if keep:
-            return out, tree
-        self.L.ref_free(tree)
+            words, center = out
+            return out, self.tree_from_words(words, center)
         return out
 
-    def build_ply(self, path, side, mem=1 << 30, threads=1):
-        self.start_threads(threads)
+    def build_ply(self, path, side, mem=1 << 30, threads=None):
+        if self._worker is not None:
+            return self._worker.call("build_ply", path, side, mem)
         tree = self.L.ref_build_ply(path.encode(), int(side), int(mem))
         out = self._take(tree)
         self.L.ref_free(tree)
         return out
+
+    def ply_to_voxel_file(self, ply_path, voxel_path, side, mem=1 << 30):
+        if self._worker is not None:
+            return self._worker.call("ply_to_voxel_file", ply_path, voxel_path, side, mem)
+        return self.L.ref_ply_to_voxel_file(ply_path.encode(), voxel_path.encode(), int(side), int(mem))
+
+    def tree_from_words(self, words, center):
+        """An in-process reference tree holding `words` (written to a
+        temporary .oct and loaded by VoxelOctree(const char*))."""
+        import tempfile
+        from_words_path = tempfile.mktemp(suffix=".oct")
+        with open(from_words_path, "wb") as f:
+            f.write(np.asarray(center, np.float32).tobytes())
+            f.write(np.uint64(words.size).tobytes())
+            # a single uncompressed-literal LZ4 block per 64 MiB of payload
+            raw = np.ascontiguousarray(words, np.uint32).tobytes()
+            block = 64 << 20
+            for off in range(0, len(raw), block):
+                chunk = raw[off:off + block]
+                lit = len(chunk)
+                if lit < 15:
+                    hdr = bytearray([lit << 4])
+                else:
+                    hdr = bytearray([0xF0])
+                    rem = lit - 15
+                    while rem >= 255:
+                        hdr.append(255)
+                        rem -= 255
+                    hdr.append(rem)
+                f.write(np.uint64(len(hdr) + lit).tobytes())
+                f.write(bytes(hdr))
+                f.write(chunk)
+        tree = self.load(from_words_path)
+        os.unlink(from_words_path)
+        return tree
 
     def raymarch(self, tree, rays, ray_scale=0.0, threads=1):
         rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 6)
