@@ -150,6 +150,54 @@ int svo_octree_build_voxel_file(const char *path, uint64_t mem, svo_stream strea
 int svo_octree_build_dense_noalloc(const uint32_t *d_grid, int w, int h, int d, uint64_t mem, uint32_t *d_words,
                                    uint64_t capacity, uint64_t *n_words, float center[3], svo_stream stream);
 
+/* -------------------------------------------------------------- mesh build */
+
+/* A triangle mesh on the current device: PlyLoader(const char *path)
+ * (PlyLoader.cpp:66-79) after readVertices, rescaleVertices and
+ * readTriangles (:122-224).  Vertex x y z [nx ny nz] [red green blue]
+ * as FP32 (a missing colour channel is 255), polygons fan-triangulated,
+ * flat face normals when the file has no normals. */
+typedef struct svo_mesh svo_mesh;
+
+/* Parses a PLY file (ascii, binary_little_endian or binary_big_endian, the
+ * formats of the reference's plyfile reader, with its value conversions) on
+ * the host and uploads the triangles.  SVO_ERR_FORMAT for a file the
+ * reference cannot read (no vertex/face element, no vertex_indices), a face
+ * index outside the vertex array or a non-finite vertex coordinate (the
+ * reference's undefined cases); SVO_ERR_IO when the file cannot be read. */
+int svo_mesh_load_ply(const char *path, svo_mesh **out);
+
+/* The same from arrays: n_vertices positions (3 floats each), optional
+ * normals and colours (3 floats each, NULL = absent / 255), and faces as
+ * n_face_ints ints holding, per polygon, its vertex count then its indices. */
+int svo_mesh_from_arrays(const float *positions, const float *normals, const float *colors, uint64_t n_vertices,
+                         const int32_t *faces, uint64_t n_face_ints, svo_mesh **out);
+
+uint64_t svo_mesh_num_triangles(const svo_mesh *mesh);
+
+/* PlyLoader::suggestedDimensions (PlyLoader.cpp:499-504): the volume
+ * W, H, D for a side length. */
+int svo_mesh_dimensions(const svo_mesh *mesh, int side, int dims[3]);
+
+void svo_mesh_destroy(svo_mesh *mesh);
+
+/* Replaces VoxelOctree(VoxelData *) over VoxelData(PlyLoader *, side, mem)
+ * (VoxelData.cpp:50-56): the mesh voxelized on the GPU by the reference's
+ * per-voxel triangle/box rule and running-average material blend, then the
+ * octree built as svo_octree_build_dense does.  The reference's result
+ * depends on its thread-pool size, which cuts each cache block into
+ * `threads` sub-blocks with their own culled triangle lists
+ * (PlyLoader.cpp:381-437), and on `mem`, which sets the cache block; both
+ * are parameters here and the words match the reference's for the same
+ * pair.  side in [5, 2^20]. */
+int svo_octree_build_mesh(const svo_mesh *mesh, int side, int threads, uint64_t mem, svo_stream stream,
+                          svo_octree **out);
+
+/* svo_mesh_load_ply + svo_octree_build_mesh + svo_mesh_destroy: the
+ * builder's in-memory mode (Main.cpp -builder with a .ply input). */
+int svo_octree_build_ply(const char *path, int side, int threads, uint64_t mem, svo_stream stream,
+                         svo_octree **out);
+
 /* ------------------------------------------------------------------- trace */
 
 /* Per-ray outputs; any pointer may be NULL to skip that output.

@@ -74,6 +74,18 @@ class Oracle:
         L.svo_oracle_scene_voxels.argtypes = [ctypes.c_int, _f32p, ctypes.c_float, ctypes.POINTER(ctypes.c_int),
                                               _f32p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_u64p),
                                               ctypes.POINTER(_u32p), _u64p]
+        L.svo_oracle_mesh_create.restype = _vp
+        L.svo_oracle_mesh_create.argtypes = [_f32p, _f32p, _f32p, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                             ctypes.c_int]
+        L.svo_oracle_mesh_destroy.argtypes = [_vp]
+        L.svo_oracle_mesh_num_tris.restype = ctypes.c_int
+        L.svo_oracle_mesh_num_tris.argtypes = [_vp]
+        L.svo_oracle_mesh_dims.argtypes = [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+        L.svo_oracle_build_mesh.restype = ctypes.c_int
+        L.svo_oracle_build_mesh.argtypes = [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(_u32p),
+                                            _u64p, _f32p]
+        L.svo_oracle_tri_box_overlap.restype = ctypes.c_int
+        L.svo_oracle_tri_box_overlap.argtypes = [_f32p, _f32p, _f32p]
         L.svo_oracle_build_sorted.restype = ctypes.c_int
         L.svo_oracle_build_sorted.argtypes = [_u64p, _u32p, ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(_u32p),
                                               _u64p]
@@ -172,6 +184,50 @@ class Oracle:
         self.L.svo_oracle_free(ctypes.cast(p, _vp))
         return words
 
+    def build_mesh(self, pos, faces, side, threads, mem=1 << 30, normals=None, colors=None):
+        """VoxelData(PlyLoader*, side, mem) + VoxelOctree for a parsed mesh:
+        pos (V, 3) float32, faces (F, k) int or a list of index lists,
+        optional per-vertex normals and colours (float, colour default 255).
+        `threads` is the reference's thread-pool size, which selects the
+        sub-block partition.  Returns (words, center)."""
+        pos = np.ascontiguousarray(pos, dtype=np.float32).reshape(-1, 3)
+        nrm = None if normals is None else np.ascontiguousarray(normals, dtype=np.float32).reshape(-1, 3)
+        col = None if colors is None else np.ascontiguousarray(colors, dtype=np.float32).reshape(-1, 3)
+        flat = flatten_faces(faces)
+        n_faces = len(faces)
+        m = self.L.svo_oracle_mesh_create(_ptr(pos, _f32p), _ptr(nrm, _f32p), _ptr(col, _f32p), pos.shape[0],
+                                          flat.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), n_faces)
+        if not m:
+            raise MemoryError("svo_oracle_mesh_create")
+        try:
+            p, n = _u32p(), ctypes.c_uint64()
+            c = np.zeros(3, np.float32)
+            rc = self.L.svo_oracle_build_mesh(m, int(side), int(threads), int(mem), ctypes.byref(p), ctypes.byref(n),
+                                              _ptr(c, _f32p))
+            if rc != 0:
+                raise RuntimeError("svo_oracle_build_mesh failed: %d" % rc)
+            words = np.ctypeslib.as_array(p, shape=(n.value,)).copy()
+            self.L.svo_oracle_free(ctypes.cast(p, _vp))
+            return words, c
+        finally:
+            self.L.svo_oracle_mesh_destroy(m)
+
+    def mesh_dims(self, pos, faces, side):
+        pos = np.ascontiguousarray(pos, dtype=np.float32).reshape(-1, 3)
+        flat = flatten_faces(faces)
+        m = self.L.svo_oracle_mesh_create(_ptr(pos, _f32p), None, None, pos.shape[0],
+                                          flat.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), len(faces))
+        dims = (ctypes.c_int * 3)()
+        self.L.svo_oracle_mesh_dims(m, int(side), dims)
+        self.L.svo_oracle_mesh_destroy(m)
+        return tuple(dims)
+
+    def tri_box_overlap(self, center, half, verts):
+        c = np.ascontiguousarray(center, dtype=np.float32)
+        h = np.ascontiguousarray(half, dtype=np.float32)
+        v = np.ascontiguousarray(verts, dtype=np.float32).reshape(9)
+        return int(self.L.svo_oracle_tri_box_overlap(_ptr(c, _f32p), _ptr(h, _f32p), _ptr(v, _f32p)))
+
     def cache_block(self, w, h, d, mem, cell_cost=4):
         return int(self.L.svo_oracle_cache_block(w, h, d, int(mem), int(cell_cost)))
 
@@ -189,12 +245,30 @@ class Oracle:
         return words, c
 
 
+def flatten_faces(faces):
+    """[count, idx...] runs as int32 (the layout svo_oracle_mesh_create takes)."""
+    if isinstance(faces, np.ndarray) and faces.ndim == 2:
+        f = np.asarray(faces, dtype=np.int32)
+        return np.ascontiguousarray(np.concatenate([np.full((f.shape[0], 1), f.shape[1], np.int32), f], 1).ravel())
+    out = []
+    for f in faces:
+        out.append(len(f))
+        out.extend(int(i) for i in f)
+    return np.asarray(out if out else [0], dtype=np.int32)
+
+
 def _ref_worker_main(conn, path, threads):
-    """Child process: runs reference builds sent over `conn`."""
+    """Child process: runs reference builds sent over `conn` (the
+    reference's progress output goes to /dev/null)."""
+    devnull = os.open(os.devnull, os.O_WRONLY)
+    os.dup2(devnull, 1)
     ref = Reference(path, isolated=False)
     ref.start_threads(threads)
     while True:
-        msg = conn.recv()
+        try:
+            msg = conn.recv()
+        except (EOFError, OSError):  # the parent went away
+            return
         if msg is None:
             return
         name, args = msg
@@ -230,12 +304,12 @@ class _RefBuildWorker:
             self.proc.join(5)
             self.proc = None
 
-    def call(self, name, *args):
+    def call(self, name, *args, timeout=None):
         for _ in range(self.retries):
             if self.proc is None or not self.proc.is_alive():
                 self._start()
             self.conn.send((name, args))
-            if self.conn.poll(self.timeout):
+            if self.conn.poll(timeout or self.timeout):
                 status, value = self.conn.recv()
                 if status == "err":
                     raise RuntimeError(value)
@@ -257,7 +331,9 @@ class Reference:
         if not os.path.exists(path):
             raise FileNotFoundError(path)
         self.path = path
-        self._worker = _RefBuildWorker(path, 4) if isolated else None
+        self._isolated = isolated
+        self._workers = {}
+        self._worker = self._worker_for(4)
         L = ctypes.CDLL(path)
         self.L = L
         L.ref_start_threads.argtypes = [ctypes.c_int]
@@ -284,6 +360,15 @@ class Reference:
         L.ref_inv_sqrt.argtypes = [ctypes.c_float]
         L.ref_tri_box_overlap.restype = ctypes.c_int
         L.ref_tri_box_overlap.argtypes = [_f32p, _f32p, _f32p]
+
+    def _worker_for(self, threads):
+        """The spawned build worker whose reference thread pool has `threads`
+        threads (None in-process)."""
+        if not self._isolated:
+            return None
+        if threads not in self._workers:
+            self._workers[threads] = _RefBuildWorker(self.path, threads)
+        return self._workers[threads]
 
     def start_threads(self, n):
         if Reference._threads_started != n:
@@ -326,17 +411,19 @@ class Reference:
             return out, self.tree_from_words(words, center)
         return out
 
-    def build_ply(self, path, side, mem=1 << 30, threads=None):
-        if self._worker is not None:
-            return self._worker.call("build_ply", path, side, mem)
+    def build_ply(self, path, side, mem=1 << 30, threads=4):
+        """VoxelData(PlyLoader*, side, mem) + VoxelOctree with a `threads`-thread
+        pool (the pool size selects the sub-block partition)."""
+        if self._isolated:
+            return self._worker_for(threads).call("build_ply", path, side, mem, timeout=60.0)
         tree = self.L.ref_build_ply(path.encode(), int(side), int(mem))
         out = self._take(tree)
         self.L.ref_free(tree)
         return out
 
-    def ply_to_voxel_file(self, ply_path, voxel_path, side, mem=1 << 30):
-        if self._worker is not None:
-            return self._worker.call("ply_to_voxel_file", ply_path, voxel_path, side, mem)
+    def ply_to_voxel_file(self, ply_path, voxel_path, side, mem=1 << 30, threads=4):
+        if self._isolated:
+            return self._worker_for(threads).call("ply_to_voxel_file", ply_path, voxel_path, side, mem, timeout=60.0)
         return self.L.ref_ply_to_voxel_file(ply_path.encode(), voxel_path.encode(), int(side), int(mem))
 
     def tree_from_words(self, words, center):

@@ -41,6 +41,13 @@ float svo_oracle_inv_sqrt(float x) {
     return y;
 }
 
+/* float -> int32 truncation with x86-64 cvttss2si semantics (the reference's
+ * platform): NaN and out-of-range values give INT32_MIN.  A plain C cast is
+ * undefined there, and Arm's conversion saturates and maps NaN to 0. */
+static inline int32_t f2i_x86(float f) {
+    return (f < 2147483648.0f && f >= -2147483648.0f) ? (int32_t)f : INT32_MIN;
+}
+
 /* Util.hpp:64-84 */
 uint32_t svo_oracle_compress_material(const float n[3], float shade) {
     const int32_t uScale = (1 << 11) - 1;
@@ -52,9 +59,9 @@ uint32_t svo_oracle_compress_material(const float n[3], float shade) {
     uint32_t sign = n[face] < 0.0f;
     float n1 = n[MOD3[face + 1]] / dominant;
     float n2 = n[MOD3[face + 2]] / dominant;
-    uint32_t u = (uint32_t)imin((int32_t)((n1 * 0.5f + 0.5f) * (float)uScale), 0x7FF);
-    uint32_t v = (uint32_t)imin((int32_t)((n2 * 0.5f + 0.5f) * (float)vScale), 0x7FF);
-    uint32_t c = (uint32_t)imin((int32_t)(shade * 127.0f), 0x7F);
+    uint32_t u = (uint32_t)imin(f2i_x86((n1 * 0.5f + 0.5f) * (float)uScale), 0x7FF);
+    uint32_t v = (uint32_t)imin(f2i_x86((n2 * 0.5f + 0.5f) * (float)vScale), 0x7FF);
+    uint32_t c = (uint32_t)imin(f2i_x86(shade * 127.0f), 0x7F);
     return (sign << 31) | (face << 29) | (u << 18) | (v << 7) | c;
 }
 
@@ -318,8 +325,16 @@ static uint64_t cells_in_pyramid(int levels) {
     return result;
 }
 
-/* State of VoxelData (VoxelData.hpp:38-99) for the .voxel-file source. */
+/* ply_oracle.c: the PlyLoader side of VoxelData's loader mode */
+void svo_oracle_mesh_process_block(void *mesh, uint32_t *data, int x, int y, int z, int w, int h, int d);
+int svo_oracle_mesh_block_empty(void *mesh, int x, int y, int z);
+void svo_oracle_mesh_dims(void *mesh, int side, int dims[3]);
+int svo_oracle_mesh_setup(void *mesh, int side, int block, const int dims[3], int threads);
+
+/* State of VoxelData (VoxelData.hpp:38-99): a .voxel payload in memory
+ * (`grid`) or a PlyLoader (`loader`). */
 typedef struct {
+    void *loader;
     const uint32_t *grid;
     int dataW, dataH, dataD;
     int virtW, virtH, virtD;
@@ -371,8 +386,14 @@ static void upsample(uint8_t **table, int l) {
             }
 }
 
-/* VoxelData::cacheData file branch, VoxelData.cpp:177-209. */
+/* VoxelData::cacheData, VoxelData.cpp:177-209: the loader writes into the
+ * buffer as it stands (it is never cleared between blocks); the file branch
+ * overwrites the block's w*h*d words. */
 static void cache_data(voxel_source *s, int x, int y, int z, int w, int h, int d) {
+    if (s->loader) {
+        svo_oracle_mesh_process_block(s->loader, s->buffered, x, y, z, w, h, d);
+        return;
+    }
     for (uint64_t vz = 0; vz < (uint64_t)d; vz++)
         for (uint64_t vy = 0; vy < (uint64_t)h; vy++) {
             const uint32_t *src = s->grid + (uint64_t)x + (uint64_t)s->dataW * ((uint64_t)y + vy +
@@ -402,10 +423,14 @@ static void build_top_lut(voxel_source *s) {
             for (int x = 0; x < s->virtW; x += size) {
                 int bw = imin(size, s->dataW - x), bh = imin(size, s->dataH - y), bd = imin(size, s->dataD - z);
                 if (bw <= 0 || bh <= 0 || bd <= 0) continue;
-                cache_data(s, x, y, z, bw, bh, bd);
                 int empty = 1;
-                for (uint64_t i = 0; i < (uint64_t)bw * bh * bd; ++i)
-                    if (s->buffered[i]) { empty = 0; break; }
+                if (s->loader) {
+                    empty = svo_oracle_mesh_block_empty(s->loader, x, y, z);
+                } else {
+                    cache_data(s, x, y, z, bw, bh, bd);
+                    for (uint64_t i = 0; i < (uint64_t)bw * bh * bd; ++i)
+                        if (s->buffered[i]) { empty = 0; break; }
+                }
                 if (!empty) {
                     int l = s->topLutLevels - 1;
                     s->topTable[l][lut_idx(l, x >> s->lowLutLevels, y >> s->lowLutLevels, z >> s->lowLutLevels)] = 1;
@@ -574,45 +599,48 @@ static uint64_t build_node(voxel_source *s, word_stream *ws, int x, int y, int z
     return childOffset;
 }
 
-int svo_oracle_build_dense(const uint32_t *grid, int w, int h, int d, uint64_t mem,
-                           uint32_t **words, uint64_t *nwords, float center[3]) {
-    voxel_source s;
-    memset(&s, 0, sizeof(s));
-    s.grid = grid;
-    s.dataW = w; s.dataH = h; s.dataD = d;
-    s.virtW = round_to_pow2(w);
-    s.virtH = round_to_pow2(h);
-    s.virtD = round_to_pow2(d);
-    int side = s.virtW > s.virtH ? s.virtW : s.virtH;
-    side = side > s.virtD ? side : s.virtD;
+/* VoxelData::init + buildTopLut, then VoxelOctree(VoxelData*). */
+static int build_from_source(voxel_source *s, int w, int h, int d, uint64_t mem, uint64_t cell_cost, int side_arg,
+                             int threads, uint32_t **words, uint64_t *nwords, float center[3]) {
+    s->dataW = w; s->dataH = h; s->dataD = d;
+    s->virtW = round_to_pow2(w);
+    s->virtH = round_to_pow2(h);
+    s->virtD = round_to_pow2(d);
+    int side = s->virtW > s->virtH ? s->virtW : s->virtH;
+    side = side > s->virtD ? side : s->virtD;
     if (side < 2) return -2;
-    s.highestVirtualBit = find_highest_bit((uint32_t)side);
-    int lower = choose_lower_level(s.highestVirtualBit, 4, mem);
+    s->highestVirtualBit = find_highest_bit((uint32_t)side);
+    int lower = choose_lower_level(s->highestVirtualBit, cell_cost, mem);
     if (lower < 0) return -1;
     /* lowLutLevels == 0 makes the reference index lowTable[-1]; reject it. */
     if (lower < 1) return -1;
-    s.lowLutLevels = lower;
-    s.topLutLevels = s.highestVirtualBit - lower + 1;
-    s.maxCacheable = (uint64_t)1 << lower;
-    s.topLut = (uint8_t *)calloc((size_t)cells_in_pyramid(s.topLutLevels), 1);
-    s.lowLut = (uint8_t *)calloc((size_t)cells_in_pyramid(s.lowLutLevels), 1);
-    s.buffered = (uint32_t *)calloc((size_t)1 << (3 * lower), 4);
-    if (!s.topLut || !s.lowLut || !s.buffered) {
-        free(s.topLut); free(s.lowLut); free(s.buffered);
+    s->lowLutLevels = lower;
+    s->topLutLevels = s->highestVirtualBit - lower + 1;
+    s->maxCacheable = (uint64_t)1 << lower;
+    if (s->loader) {  /* VoxelData.cpp:53-54 */
+        int dims[3] = {w, h, d};
+        int rc = svo_oracle_mesh_setup(s->loader, side_arg, (int)s->maxCacheable, dims, threads);
+        if (rc) return rc;
+    }
+    s->topLut = (uint8_t *)calloc((size_t)cells_in_pyramid(s->topLutLevels), 1);
+    s->lowLut = (uint8_t *)calloc((size_t)cells_in_pyramid(s->lowLutLevels), 1);
+    s->buffered = (uint32_t *)calloc((size_t)1 << (3 * lower), 4);
+    if (!s->topLut || !s->lowLut || !s->buffered) {
+        free(s->topLut); free(s->lowLut); free(s->buffered);
         return -3;
     }
     /* VoxelData.cpp:76-85 */
     uint64_t off = 0, sz = 1;
-    for (int i = 0; i < s.topLutLevels; ++i) { s.topTable[i] = s.topLut + off; off += sz; sz *= 8; }
+    for (int i = 0; i < s->topLutLevels; ++i) { s->topTable[i] = s->topLut + off; off += sz; sz *= 8; }
     off = 0; sz = 1;
-    for (int i = 0; i < s.lowLutLevels; ++i) { s.lowTable[i] = s.lowLut + off; off += sz; sz *= 8; }
+    for (int i = 0; i < s->lowLutLevels; ++i) { s->lowTable[i] = s->lowLut + off; off += sz; sz *= 8; }
 
-    build_top_lut(&s);
+    build_top_lut(s);
 
     word_stream ws;
     memset(&ws, 0, sizeof(ws));
     ws_push(&ws, 0);
-    build_node(&s, &ws, 0, 0, 0, side, 0);
+    build_node(s, &ws, 0, 0, 0, side, 0);
     ws.data[0] |= 1u << 18;
     int rc = 0;
     if (ws.oom) {
@@ -629,8 +657,29 @@ int svo_oracle_build_dense(const uint32_t *grid, int w, int h, int d, uint64_t m
         center[2] = (float)d * 0.5f / (float)side;
     }
     free(ws.data); free(ws.ins);
-    free(s.topLut); free(s.lowLut); free(s.buffered);
+    free(s->topLut); free(s->lowLut); free(s->buffered);
     return rc;
+}
+
+int svo_oracle_build_dense(const uint32_t *grid, int w, int h, int d, uint64_t mem,
+                           uint32_t **words, uint64_t *nwords, float center[3]) {
+    voxel_source s;
+    memset(&s, 0, sizeof(s));
+    s.grid = grid;
+    return build_from_source(&s, w, h, d, mem, 4, 0, 0, words, nwords, center);
+}
+
+/* VoxelData(PlyLoader*, side, mem) (VoxelData.cpp:50-56) + VoxelOctree:
+ * cell cost 4 + 1 (blockMemRequirement, PlyLoader.cpp:376-379), dims from
+ * suggestedDimensions, sub-block partition for `threads` threads. */
+int svo_oracle_build_mesh(void *mesh, int side, int threads, uint64_t mem, uint32_t **words, uint64_t *nwords,
+                          float center[3]) {
+    voxel_source s;
+    memset(&s, 0, sizeof(s));
+    s.loader = mesh;
+    int dims[3];
+    svo_oracle_mesh_dims(mesh, side, dims);
+    return build_from_source(&s, dims[0], dims[1], dims[2], mem, 5, side, threads, words, nwords, center);
 }
 
 /* --------------------------------------------------------------- .oct I/O */

@@ -82,6 +82,23 @@ int svo_oracle_scene_voxels(int side, const float *heights, float thickness, con
 int svo_oracle_build_sorted(const uint64_t *keys, const uint32_t *payload, uint64_t n, int log_side,
                             uint32_t **words, uint64_t *n_words);
 
+/* ply_oracle.c: the reference's mesh path.  svo_oracle_mesh_create takes a
+ * parsed PLY (positions, optional vertex normals and colours as floats,
+ * faces as [count, idx...] runs) and restates PlyLoader's rescale and
+ * triangulation; svo_oracle_build_mesh then runs VoxelData(PlyLoader*,
+ * side, mem) with `threads` sub-block partitions and VoxelOctree(VoxelData*).
+ * Returns 0, or -1 (mem too small), -2 (side < 2), -3 (allocation),
+ * -5 (a triangle's block cell lies outside the block grid). */
+void *svo_oracle_mesh_create(const float *pos, const float *nrm, const float *col, int n_verts, const int *faces,
+                             int n_faces);
+void svo_oracle_mesh_dims(void *mesh, int side, int dims[3]);
+int svo_oracle_mesh_num_tris(void *mesh);
+void svo_oracle_mesh_destroy(void *mesh);
+int svo_oracle_build_mesh(void *mesh, int side, int threads, uint64_t mem, uint32_t **words, uint64_t *nwords,
+                          float center[3]);
+/* Triangle/box overlap (separating axes), third-party/tribox3.c:132-206. */
+int svo_oracle_tri_box_overlap(const float center[3], const float half[3], const float verts[9]);
+
 #ifdef __cplusplus
 }
 #endif

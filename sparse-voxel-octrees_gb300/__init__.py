@@ -88,6 +88,16 @@ def _load():
         "svo_octree_build_dense": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_uint64,
                                                   ctypes.c_int, _vp, ctypes.POINTER(_vp)]),
         "svo_octree_build_voxel_file": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_uint64, _vp, ctypes.POINTER(_vp)]),
+        "svo_mesh_load_ply": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_vp)]),
+        "svo_mesh_from_arrays": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_uint64, _vp, ctypes.c_uint64,
+                                                ctypes.POINTER(_vp)]),
+        "svo_mesh_num_triangles": (ctypes.c_uint64, [_vp]),
+        "svo_mesh_dimensions": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
+        "svo_mesh_destroy": (None, [_vp]),
+        "svo_octree_build_mesh": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_uint64, _vp,
+                                                 ctypes.POINTER(_vp)]),
+        "svo_octree_build_ply": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_uint64, _vp,
+                                                ctypes.POINTER(_vp)]),
         "svo_trace": (ctypes.c_int, [_vp, _vp, ctypes.c_uint64, ctypes.c_float, _f32p, ctypes.POINTER(TraceOut), _vp]),
         "svo_trace_host": (ctypes.c_int, [_vp, _vp, ctypes.c_uint64, ctypes.c_float, _f32p,
                                           ctypes.POINTER(TraceOut)]),
@@ -165,15 +175,79 @@ def oct_write(path, words, center):
     check(lib.svo_oct_write(os.fsencode(path), _np_ptr(words), words.size, c.ctypes.data_as(_f32p)))
 
 
+class PlyLoader:
+    """A triangle mesh on the current device: PlyLoader(const char *path)
+    (PlyLoader.cpp:66-79), or PlyLoader.from_arrays(positions, faces,
+    normals=None, colors=None) for a mesh already in memory (faces: (F, k)
+    array or a list of index lists; colours as floats, 255 when absent)."""
+
+    def __init__(self, path=None, _handle=None):
+        self._h = _vp()
+        if _handle is not None:
+            self._h = _handle
+        else:
+            check(lib.svo_mesh_load_ply(os.fsencode(path), ctypes.byref(self._h)))
+
+    @classmethod
+    def from_arrays(cls, positions, faces, normals=None, colors=None):
+        pos = np.ascontiguousarray(positions, dtype=np.float32).reshape(-1, 3)
+        nrm = None if normals is None else np.ascontiguousarray(normals, dtype=np.float32).reshape(-1, 3)
+        col = None if colors is None else np.ascontiguousarray(colors, dtype=np.float32).reshape(-1, 3)
+        if isinstance(faces, np.ndarray) and faces.ndim == 2:
+            f = np.asarray(faces, dtype=np.int32)
+            flat = np.concatenate([np.full((f.shape[0], 1), f.shape[1], np.int32), f], 1).ravel()
+        else:
+            flat = np.asarray([x for fc in faces for x in (len(fc), *fc)], dtype=np.int32)
+        flat = np.ascontiguousarray(flat, dtype=np.int32)
+        h = _vp()
+        check(lib.svo_mesh_from_arrays(_np_ptr(pos), _np_ptr(nrm), _np_ptr(col), pos.shape[0], _np_ptr(flat),
+                                       flat.size, ctypes.byref(h)))
+        return cls(_handle=h)
+
+    @property
+    def num_triangles(self):
+        return int(lib.svo_mesh_num_triangles(self._h))
+
+    def suggested_dimensions(self, side):
+        """PlyLoader::suggestedDimensions (PlyLoader.cpp:499-504)."""
+        dims = (ctypes.c_int * 3)()
+        check(lib.svo_mesh_dimensions(self._h, int(side), dims))
+        return tuple(dims)
+
+    def close(self):
+        if self._h:
+            lib.svo_mesh_destroy(self._h)
+            self._h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class VoxelData:
     """Input of the octree build: VoxelData(const char *path, size_t mem)
-    (VoxelData.cpp:37-48) or an in-memory dense grid of shape (d, h, w),
-    x fastest, 0 = empty.  `grid` may be a numpy array or a CUDA tensor."""
+    (VoxelData.cpp:37-48), VoxelData(PlyLoader, side, mem, threads)
+    (VoxelData.cpp:50-56; `threads` is the reference's thread-pool size,
+    which its voxelization depends on), or an in-memory dense grid of shape
+    (d, h, w), x fastest, 0 = empty (a numpy array or a CUDA tensor)."""
 
-    def __init__(self, source, mem=DEFAULT_MEM):
-        self.mem = int(mem)
+    def __init__(self, source, side=None, mem=DEFAULT_MEM, threads=None):
         self.path = None
         self.grid = None
+        self.loader = None
+        if isinstance(source, PlyLoader):
+            if side is None:
+                raise TypeError("VoxelData(PlyLoader, side, mem, threads)")
+            self.loader = source
+            self.side = int(side)
+            self.threads = int(threads if threads is not None else (os.cpu_count() or 1))
+            self.mem = int(mem)
+            return
+        if side is not None:  # VoxelData(path_or_grid, mem)
+            mem = side
+        self.mem = int(mem)
         if isinstance(source, (str, bytes, os.PathLike)):
             self.path = os.fsdecode(source)
         else:
@@ -194,7 +268,10 @@ class VoxelOctree:
         elif isinstance(source, (str, bytes, os.PathLike)):
             check(lib.svo_octree_load(os.fsencode(source), ctypes.byref(self._h)))
         elif isinstance(source, VoxelData):
-            if source.path is not None:
+            if source.loader is not None:
+                check(lib.svo_octree_build_mesh(source.loader._h, source.side, source.threads, source.mem,
+                                                _stream_ptr(stream), ctypes.byref(self._h)))
+            elif source.path is not None:
                 check(lib.svo_octree_build_voxel_file(os.fsencode(source.path), source.mem, _stream_ptr(stream),
                                                       ctypes.byref(self._h)))
             else:

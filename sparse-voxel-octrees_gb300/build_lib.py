@@ -22,7 +22,7 @@ SCENES_SRC = os.path.join(HERE, "scenes_gpu.cu")
 SCENES_LIB = os.path.join(HERE, "libsvo_scenes.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC]
+COMMON = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-I", INCLUDE, "-I", CSRC]
 
 
 def _nvcc():

@@ -33,6 +33,7 @@
 #include <cstdio>
 #include <mutex>
 
+#include "morton.cuh"
 #include "scan.cuh"
 #include "svo_internal.h"
 
@@ -41,30 +42,6 @@ namespace {
 
 constexpr int kBrickThreads = 256;
 
-__device__ __forceinline__ uint64_t spread3(uint32_t v) {
-    uint64_t x = v & 0x1fffffu;
-    x = (x | x << 32) & 0x1f00000000ffffull;
-    x = (x | x << 16) & 0x1f0000ff0000ffull;
-    x = (x | x << 8) & 0x100f00f00f00f00full;
-    x = (x | x << 4) & 0x10c30c30c30c30c3ull;
-    x = (x | x << 2) & 0x1249249249249249ull;
-    return x;
-}
-
-__device__ __forceinline__ uint32_t compact3(uint64_t x) {
-    x &= 0x1249249249249249ull;
-    x = (x ^ (x >> 2)) & 0x10c30c30c30c30c3ull;
-    x = (x ^ (x >> 4)) & 0x100f00f00f00f00full;
-    x = (x ^ (x >> 8)) & 0x1f0000ff0000ffull;
-    x = (x ^ (x >> 16)) & 0x1f00000000ffffull;
-    x = (x ^ (x >> 32)) & 0x1fffffull;
-    return (uint32_t)x;
-}
-
-__device__ __forceinline__ uint64_t morton3(uint32_t x, uint32_t y, uint32_t z) {
-    return spread3(x) | (spread3(y) << 1) | (spread3(z) << 2);
-}
-
 struct GridGeom {
     const uint32_t *grid;
     int w, h, d;
@@ -72,6 +49,8 @@ struct GridGeom {
     int drop_last_z;    // 1: voxels at z == d-1 are excluded from the output
     int log_block;      // cache-block edge M = 1 << log_block
     uint8_t *topflag;   // per M-block "has any voxel" (Morton-indexed), or null
+    uint64_t key_base;  // added to every emitted Morton key
+    uint32_t *clear;    // when set (== grid), emitted words are zeroed in place
 };
 
 // Phase 1a: per brick, count voxels that survive (V') and flag M-blocks that
@@ -128,8 +107,10 @@ __global__ void __launch_bounds__(kBrickThreads) k_brick_emit(GridGeom g, uint64
         for (int c = threadIdx.x; c < cells; c += kBrickThreads) {
             int gx = gx0 + (c & (E - 1)), gy = gy0 + ((c >> g.log_brick) & (E - 1)), gz = gz0 + (c >> (2 * g.log_brick));
             uint32_t v = 0;
-            if (gx < g.w && gy < g.h && gz < g.d && !(g.drop_last_z && gz == g.d - 1))
-                v = __ldg(g.grid + (uint64_t)gx + (uint64_t)g.w * ((uint64_t)gy + (uint64_t)g.h * gz));
+            if (gx < g.w && gy < g.h && gz < g.d && !(g.drop_last_z && gz == g.d - 1)) {
+                uint64_t gi = (uint64_t)gx + (uint64_t)g.w * ((uint64_t)gy + (uint64_t)g.h * gz);
+                v = g.clear ? g.clear[gi] : __ldg(g.grid + gi);  // no read-only path for a grid this launch writes
+            }
             tile[c] = v;
         }
         __syncthreads();
@@ -145,7 +126,7 @@ __global__ void __launch_bounds__(kBrickThreads) k_brick_emit(GridGeom g, uint64
         uint32_t total;
         uint32_t pre = block_excl_scan<uint32_t>(cnt, &total);
         uint64_t out = offsets[b] + pre;
-        uint64_t kbase = b << (3 * g.log_brick);
+        uint64_t kbase = g.key_base + (b << (3 * g.log_brick));
         for (int k = 0; k < per; ++k) {
             int m = m0 + k;
             if (m < cells) {
@@ -155,6 +136,9 @@ __global__ void __launch_bounds__(kBrickThreads) k_brick_emit(GridGeom g, uint64
                     keys[out] = kbase | (uint64_t)m;
                     payload[out] = v;
                     ++out;
+                    if (g.clear)
+                        g.clear[(uint64_t)(gx0 + (int)lx) +
+                                (uint64_t)g.w * ((uint64_t)(gy0 + (int)ly) + (uint64_t)g.h * (uint64_t)(gz0 + (int)lz))] = 0;
                 }
             }
         }
@@ -384,62 +368,20 @@ int scan_to(const uint32_t *in, TO *out, uint64_t n, TO *total_host, cudaStream_
 
 }  // namespace
 
-int build_dense_device(const uint32_t *d_grid, int w, int h, int d, int log_side, int log_block, cudaStream_t st,
-                       uint32_t **d_words_out, uint64_t *n_words_out) {
+int build_from_sorted_device(const uint64_t *d_keys, const uint32_t *d_payload, uint64_t N, int log_side,
+                             int log_block, const uint8_t *d_topflag, cudaStream_t st, uint32_t **d_words_out,
+                             uint64_t *n_words_out) {
     const int D = log_side;
-    const int log_brick = D < 4 ? D : 4;
-    const uint64_t n_bricks = 1ull << (3 * (D - log_brick));
     const bool multi_block = log_block < D;
-
-    GridGeom g;
-    g.grid = d_grid;
-    g.w = w;
-    g.h = h;
-    g.d = d;
-    g.log_brick = log_brick;
-    g.drop_last_z = ((d & 1) && log_block >= 2) ? 1 : 0;
-    g.log_block = log_block;
-    g.topflag = nullptr;
-
     const uint64_t n_blocks = multi_block ? (1ull << (3 * (D - log_block))) : 0;
-    if (n_blocks > (1ull << 27))
-        return set_error(SVO_ERR_LIMIT, "memory budget gives %llu cache blocks; the GPU build supports at most 2^27",
-                         (unsigned long long)n_blocks);
-    DevBuf<uint8_t> topflag;
-    if (multi_block) {
-        SVO_TRY_ALLOC(topflag.alloc(n_blocks, st));
-        SVO_CUDA_TRY(cudaMemsetAsync(topflag.p, 0, n_blocks, st));
-        g.topflag = topflag.p;
-    }
-
-    // Phase 1: extraction in Morton order.
-    DevBuf<uint32_t> bcount;
-    DevBuf<uint64_t> boff;
-    SVO_TRY_ALLOC(bcount.alloc(n_bricks, st));
-    SVO_TRY_ALLOC(boff.alloc(n_bricks, st));
-    unsigned grid1 = (unsigned)(n_bricks < (1ull << 20) ? n_bricks : (1ull << 20));
-    k_brick_count<<<grid1, kBrickThreads, 0, st>>>(g, n_bricks, bcount.p);
-    SVO_LAUNCH_CHECK("k_brick_count");
-    uint64_t N = 0;
-    int rc = scan_to<uint64_t>(bcount.p, boff.p, n_bricks, &N, st);
-    if (rc) return rc;
+    if (multi_block && !d_topflag) return set_error(SVO_ERR_INVALID, "build: missing cache-block flags");
     if (N >= 0xFFFFFFFFull) return set_error(SVO_ERR_LIMIT, "%llu occupied voxels exceed 2^32-1", (unsigned long long)N);
-
-    DevBuf<uint64_t> lkey;
-    DevBuf<uint32_t> lpay;
-    SVO_TRY_ALLOC(lkey.alloc(N, st));
-    SVO_TRY_ALLOC(lpay.alloc(N, st));
-    if (N) {
-        k_brick_emit<<<grid1, kBrickThreads, 0, st>>>(g, n_bricks, bcount.p, boff.p, lkey.p, lpay.p);
-        SVO_LAUNCH_CHECK("k_brick_emit");
-    }
-    bcount.release();
-    boff.release();
+    int rc = SVO_OK;
 
     // Phase 2: levels e = 1..D (node edge 2^e); level 0 is the leaves.
     std::vector<LevelArrays> lv(D + 1);
     DevBuf<uint32_t> leaf_pidx;
-    const uint64_t *ckey = lkey.p;
+    const uint64_t *ckey = d_keys;
     uint64_t nc = N;
     for (int e = 1; e <= D; ++e) {
         LevelArrays &L = lv[e];
@@ -459,7 +401,7 @@ int build_dense_device(const uint32_t *d_grid, int w, int h, int d, int log_side
             SVO_TRY_ALLOC(bidx.alloc(n_blocks, st));
             SVO_CUDA_TRY(cudaMemsetAsync(first.p, 0xFF, n_blocks * sizeof(uint32_t), st));
             if (nc) k_block_first<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, head.p, first.p);
-            k_block_present<<<blocks_for(n_blocks), 256, 0, st>>>(first.p, topflag.p, n_blocks, present.p);
+            k_block_present<<<blocks_for(n_blocks), 256, 0, st>>>(first.p, d_topflag, n_blocks, present.p);
             SVO_LAUNCH_CHECK("k_block_present");
             uint32_t np = 0;
             rc = scan_to<uint32_t>(present.p, bidx.p, n_blocks, &np, st);
@@ -504,7 +446,6 @@ int build_dense_device(const uint32_t *d_grid, int w, int h, int d, int log_side
         ckey = L.key.p;
         nc = L.n;
     }
-    lkey.release();
 
     // Subtree sizes, bottom-up.
     for (int e = 1; e <= D; ++e) {
@@ -541,7 +482,7 @@ int build_dense_device(const uint32_t *d_grid, int w, int h, int d, int log_side
         SVO_LAUNCH_CHECK("k_place");
     }
     if (N) {
-        k_place_leaves<<<blocks_for(N), 256, 0, st>>>(N, leaf_pidx.p, lv[1].n, lv[1].start.p, lv[1].B.p, lpay.p,
+        k_place_leaves<<<blocks_for(N), 256, 0, st>>>(N, leaf_pidx.p, lv[1].n, lv[1].start.p, lv[1].B.p, d_payload,
                                                       words, W, err.p);
         SVO_LAUNCH_CHECK("k_place_leaves");
     }
@@ -559,6 +500,106 @@ int build_dense_device(const uint32_t *d_grid, int w, int h, int d, int log_side
     *d_words_out = words;
     *n_words_out = W;
     return SVO_OK;
+}
+
+int extract_voxels_device(uint32_t *d_grid, int w, int h, int d, int log_extent, uint64_t key_base, int drop_last_z,
+                          int clear, cudaStream_t st, uint64_t **d_keys, uint32_t **d_payload, uint64_t *n) {
+    const int log_brick = log_extent < 4 ? log_extent : 4;
+    const uint64_t n_bricks = 1ull << (3 * (log_extent - log_brick));
+    GridGeom g;
+    g.grid = d_grid;
+    g.w = w;
+    g.h = h;
+    g.d = d;
+    g.log_brick = log_brick;
+    g.drop_last_z = drop_last_z;
+    g.log_block = log_extent;
+    g.topflag = nullptr;
+    g.key_base = key_base;
+    g.clear = clear ? d_grid : nullptr;
+    *d_keys = nullptr;
+    *d_payload = nullptr;
+    *n = 0;
+    DevBuf<uint32_t> bcount;
+    DevBuf<uint64_t> boff;
+    SVO_TRY_ALLOC(bcount.alloc(n_bricks, st));
+    SVO_TRY_ALLOC(boff.alloc(n_bricks, st));
+    unsigned grid1 = (unsigned)(n_bricks < (1ull << 20) ? n_bricks : (1ull << 20));
+    k_brick_count<<<grid1, kBrickThreads, 0, st>>>(g, n_bricks, bcount.p);
+    SVO_LAUNCH_CHECK("k_brick_count");
+    uint64_t N = 0;
+    int rc = scan_to<uint64_t>(bcount.p, boff.p, n_bricks, &N, st);
+    if (rc) return rc;
+    if (N == 0) return SVO_OK;
+    SVO_CUDA_TRY(cudaMallocAsync((void **)d_keys, N * sizeof(uint64_t), st));
+    cudaError_t e = cudaMallocAsync((void **)d_payload, N * sizeof(uint32_t), st);
+    if (e != cudaSuccess) {
+        cudaFreeAsync(*d_keys, st);
+        *d_keys = nullptr;
+        return cuda_fail(e, "device allocation in extraction");
+    }
+    k_brick_emit<<<grid1, kBrickThreads, 0, st>>>(g, n_bricks, bcount.p, boff.p, *d_keys, *d_payload);
+    SVO_LAUNCH_CHECK("k_brick_emit");
+    *n = N;
+    return SVO_OK;
+}
+
+int build_dense_device(const uint32_t *d_grid, int w, int h, int d, int log_side, int log_block, cudaStream_t st,
+                       uint32_t **d_words_out, uint64_t *n_words_out) {
+    const int D = log_side;
+    const int log_brick = D < 4 ? D : 4;
+    const uint64_t n_bricks = 1ull << (3 * (D - log_brick));
+    const bool multi_block = log_block < D;
+
+    GridGeom g;
+    g.grid = d_grid;
+    g.w = w;
+    g.h = h;
+    g.d = d;
+    g.log_brick = log_brick;
+    g.drop_last_z = ((d & 1) && log_block >= 2) ? 1 : 0;
+    g.log_block = log_block;
+    g.topflag = nullptr;
+    g.key_base = 0;
+    g.clear = nullptr;
+
+    const uint64_t n_blocks = multi_block ? (1ull << (3 * (D - log_block))) : 0;
+    if (n_blocks > (1ull << 27))
+        return set_error(SVO_ERR_LIMIT, "memory budget gives %llu cache blocks; the GPU build supports at most 2^27",
+                         (unsigned long long)n_blocks);
+    DevBuf<uint8_t> topflag;
+    if (multi_block) {
+        SVO_TRY_ALLOC(topflag.alloc(n_blocks, st));
+        SVO_CUDA_TRY(cudaMemsetAsync(topflag.p, 0, n_blocks, st));
+        g.topflag = topflag.p;
+    }
+
+    // Phase 1: extraction in Morton order.
+    DevBuf<uint32_t> bcount;
+    DevBuf<uint64_t> boff;
+    SVO_TRY_ALLOC(bcount.alloc(n_bricks, st));
+    SVO_TRY_ALLOC(boff.alloc(n_bricks, st));
+    unsigned grid1 = (unsigned)(n_bricks < (1ull << 20) ? n_bricks : (1ull << 20));
+    k_brick_count<<<grid1, kBrickThreads, 0, st>>>(g, n_bricks, bcount.p);
+    SVO_LAUNCH_CHECK("k_brick_count");
+    uint64_t N = 0;
+    int rc = scan_to<uint64_t>(bcount.p, boff.p, n_bricks, &N, st);
+    if (rc) return rc;
+    if (N >= 0xFFFFFFFFull) return set_error(SVO_ERR_LIMIT, "%llu occupied voxels exceed 2^32-1", (unsigned long long)N);
+
+    DevBuf<uint64_t> lkey;
+    DevBuf<uint32_t> lpay;
+    SVO_TRY_ALLOC(lkey.alloc(N, st));
+    SVO_TRY_ALLOC(lpay.alloc(N, st));
+    if (N) {
+        k_brick_emit<<<grid1, kBrickThreads, 0, st>>>(g, n_bricks, bcount.p, boff.p, lkey.p, lpay.p);
+        SVO_LAUNCH_CHECK("k_brick_emit");
+    }
+    bcount.release();
+    boff.release();
+
+    // Phases 2 and 3.
+    return build_from_sorted_device(lkey.p, lpay.p, N, D, log_block, topflag.p, st, d_words_out, n_words_out);
 }
 
 }  // namespace svo
@@ -656,6 +697,8 @@ int build_dense_noalloc(const uint32_t *d_grid, int w, int h, int d, int log_sid
     g.drop_last_z = ((d & 1) && log_block >= 2) ? 1 : 0;
     g.log_block = log_block;
     g.topflag = nullptr;
+    g.key_base = 0;
+    g.clear = nullptr;
     if (multi_block) {
         SVO_ARENA_TAKE(tf, uint8_t, n_blocks);
         SVO_CUDA_TRY(cudaMemsetAsync(tf, 0, n_blocks, st));  // the arena keeps the previous call's bytes

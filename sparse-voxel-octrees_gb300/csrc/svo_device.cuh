@@ -45,6 +45,15 @@ __device__ __forceinline__ void decompress_material(uint32_t word, float &nx, fl
     shade = (float)(word & 0x7Fu) * 1.0f / 127.0f;
 }
 
+// float -> int32 truncation as x86-64's cvttss2si performs it (the platform
+// the reference is built for): NaN and values outside the int32 range give
+// INT32_MIN.  A plain cast on the GPU saturates and maps NaN to 0 instead,
+// which changes compressMaterial's word for a NaN normal or shade (a
+// degenerate triangle's interpolation weights).
+__device__ __forceinline__ int32_t f2i_x86(float f) {
+    return (f < 2147483648.0f && f >= -2147483648.0f) ? (int32_t)f : (int32_t)0x80000000u;
+}
+
 // Util.hpp:64-84.
 __device__ __forceinline__ uint32_t compress_material(float nx, float ny, float nz, float shade) {
     const float scale = (float)((1 << 11) - 1);
@@ -57,9 +66,9 @@ __device__ __forceinline__ uint32_t compress_material(float nx, float ny, float 
     uint32_t f1 = face == 2 ? 0 : face + 1, f2 = face == 0 ? 2 : face - 1;
     float n1 = n[f1] / dominant;
     float n2 = n[f2] / dominant;
-    int32_t ui = (int32_t)((n1 * 0.5f + 0.5f) * scale);
-    int32_t vi = (int32_t)((n2 * 0.5f + 0.5f) * scale);
-    int32_t ci = (int32_t)(shade * 127.0f);
+    int32_t ui = f2i_x86((n1 * 0.5f + 0.5f) * scale);
+    int32_t vi = f2i_x86((n2 * 0.5f + 0.5f) * scale);
+    int32_t ci = f2i_x86(shade * 127.0f);
     uint32_t u = (uint32_t)(ui < 0x7FF ? ui : 0x7FF);
     uint32_t v = (uint32_t)(vi < 0x7FF ? vi : 0x7FF);
     uint32_t c = (uint32_t)(ci < 0x7F ? ci : 0x7F);

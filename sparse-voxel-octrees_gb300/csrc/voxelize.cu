@@ -1,0 +1,971 @@
+// voxelize.cu — GPU mesh-to-octree build: PlyLoader + VoxelData(PlyLoader*,
+// side, mem) + VoxelOctree(VoxelData*) (PlyLoader.cpp:226-504,
+// VoxelData.cpp:50-56, 120-175, 262-289, VoxelOctree.cpp:125-205).
+//
+// The reference voxelizes one cache block at a time into a buffer that is
+// never cleared between blocks: each block's triangles are taken from the
+// lists of its sub-blocks (the cache block cut into one part per worker
+// thread), every voxel of a triangle's clamped bounding box that passes the
+// triangle/box test receives a running-average material write, and the
+// octree walk then reads the block's voxels destructively, which leaves only
+// voxels the walk never reaches (the dropped last z slice of an odd-depth
+// block) behind for later blocks.  This file computes the same result:
+//
+//  1. Triangle setup (one thread per triangle): rescale to the unit cube,
+//     gather the fan triangle's vertices, flat normal when the file has none,
+//     bounds (PlyLoader.cpp:40-53, 167-224).
+//  2. Sub-block lists (one thread per triangle): the cells of
+//     iterateOverlappingBlocks (PlyLoader.cpp:233-270), culled by the same
+//     triangle/box test with the same incrementally accumulated centres; each
+//     member cell marks its cache block non-empty (isBlockEmpty) and emits
+//     one (brick, triangle) pair per 8^3 brick (smaller when sub-blocks are)
+//     of the cell that the triangle's clamped voxel box touches.
+//  3. A stable radix sort of the pairs by brick (sort.cuh): each brick's
+//     triangles in ascending index, the order a sub-block list holds them.
+//  4. Cache blocks in the reference's visiting order (ascending Morton code
+//     of the blocks the lists mark), each against the one persistent
+//     buffer: one CTA per brick, one thread per voxel, folding the brick's
+//     triangles in order with writeTriangleCell's blend
+//     (PlyLoader.cpp:296-336); voxel-box centres are the reference's running
+//     sums (lo - 0.5) * h + h + ... + h, read from a table of those sums.
+//     Then the block's nonzero words are extracted in Morton order and
+//     cleared (build.cu), except a dropped odd last slice.
+//  5. The octree from the Morton-ordered voxels and the block flags
+//     (build_from_sorted_device).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <vector>
+
+#include "mesh.h"
+#include "morton.cuh"
+#include "scan.cuh"
+#include "sort.cuh"
+#include "svo_device.cuh"
+#include "svo_internal.h"
+
+// Device-resident triangle mesh (after PlyLoader's rescale and
+// triangulation).
+struct svo_mesh {
+    float *d_tris = nullptr;  // kTriFloats per triangle, see TriLayout
+    uint64_t n_tris = 0;
+    float lower[3] = {0, 0, 0}, upper[3] = {0, 0, 0};  // PlyLoader::_lower/_upper after rescale
+    int has_normals = 0;
+    int device = 0;
+};
+
+namespace svo {
+namespace {
+
+// Per triangle: p0 p1 p2 (9), n0 n1 n2 (9), c0 c1 c2 (9), lower (3),
+// upper (3), padding (3).
+constexpr int kTriFloats = 36;
+constexpr int kTriP = 0, kTriN = 9, kTriC = 18, kTriLo = 27, kTriHi = 30;
+constexpr int kStageFloats = 27;  // p, n, c: what the brick kernel stages
+constexpr int kChunk = 64;        // triangles staged per round in the brick kernel
+constexpr int kBrickCta = 512;    // one thread per voxel of an 8^3 brick
+
+#define SVO_LAUNCH_OK(name)                                                    \
+    do {                                                                       \
+        cudaError_t _e = cudaGetLastError();                                   \
+        if (_e != cudaSuccess) return ::svo::cuda_fail(_e, "launch of " name); \
+    } while (0)
+
+inline unsigned grid_for(uint64_t n, int t = 256) {
+    uint64_t b = (n + t - 1) / t;
+    if (b == 0) b = 1;
+    return (unsigned)(b < (1u << 30) ? b : (1u << 30));
+}
+
+template <typename T>
+struct Dev {
+    T *p = nullptr;
+    cudaStream_t st = nullptr;
+    Dev() = default;
+    Dev(const Dev &) = delete;
+    Dev &operator=(const Dev &) = delete;
+    cudaError_t alloc(uint64_t n, cudaStream_t s) {
+        st = s;
+        return cudaMallocAsync((void **)&p, (size_t)(n ? n : 1) * sizeof(T), s);
+    }
+    void release() {
+        if (p) cudaFreeAsync(p, st);
+        p = nullptr;
+    }
+    ~Dev() { release(); }
+};
+
+#define SVO_ALLOC(buf, n)                                                          \
+    do {                                                                           \
+        cudaError_t _e = (buf).alloc((n), st);                                     \
+        if (_e != cudaSuccess) return ::svo::cuda_fail(_e, "device allocation in mesh build"); \
+    } while (0)
+
+// ---- triangle/box overlap ---------------------------------------------------
+
+// Separating-axis triangle/box test of Akenine-Moller ("Fast 3D
+// triangle-box overlap testing", 2001) in the form third-party/tribox3.c:
+// 132-206 evaluates it: the nine edge-axis tests first (projections of two
+// vertices per axis, with that code's choice of which vertex is tested
+// first for the min), then the box axes, then the triangle's plane.
+__device__ __forceinline__ bool axis_sep(float pa, float pb, bool a_first, float rad) {
+    float mn, mx;
+    if (a_first) {
+        if (pa < pb) { mn = pa; mx = pb; } else { mn = pb; mx = pa; }
+    } else {
+        if (pb < pa) { mn = pb; mx = pa; } else { mn = pa; mx = pb; }
+    }
+    return mn > rad || mx < -rad;
+}
+
+__device__ __forceinline__ bool plane_box(const float n[3], const float v[3], const float h[3]) {
+    float vmin[3], vmax[3];
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+        if (n[q] > 0.0f) {
+            vmin[q] = -h[q] - v[q];
+            vmax[q] = h[q] - v[q];
+        } else {
+            vmin[q] = h[q] - v[q];
+            vmax[q] = -h[q] - v[q];
+        }
+    }
+    if (n[0] * vmin[0] + n[1] * vmin[1] + n[2] * vmin[2] > 0.0f) return false;
+    if (n[0] * vmax[0] + n[1] * vmax[1] + n[2] * vmax[2] >= 0.0f) return true;
+    return false;
+}
+
+__device__ __forceinline__ bool tri_box(float cx, float cy, float cz, const float h[3], const float *tv) {
+    const float v0[3] = {tv[0] - cx, tv[1] - cy, tv[2] - cz};
+    const float v1[3] = {tv[3] - cx, tv[4] - cy, tv[5] - cz};
+    const float v2[3] = {tv[6] - cx, tv[7] - cy, tv[8] - cz};
+    const float e0[3] = {v1[0] - v0[0], v1[1] - v0[1], v1[2] - v0[2]};
+    const float e1[3] = {v2[0] - v1[0], v2[1] - v1[1], v2[2] - v1[2]};
+    const float e2[3] = {v0[0] - v2[0], v0[1] - v2[1], v0[2] - v2[2]};
+    float fex, fey, fez, a, b;
+
+    fex = fabsf(e0[0]); fey = fabsf(e0[1]); fez = fabsf(e0[2]);
+    a = e0[2]; b = e0[1];
+    if (axis_sep(a * v0[1] - b * v0[2], a * v2[1] - b * v2[2], true, fez * h[1] + fey * h[2])) return false;
+    a = e0[2]; b = e0[0];
+    if (axis_sep(-a * v0[0] + b * v0[2], -a * v2[0] + b * v2[2], true, fez * h[0] + fex * h[2])) return false;
+    a = e0[1]; b = e0[0];
+    if (axis_sep(a * v1[0] - b * v1[1], a * v2[0] - b * v2[1], false, fey * h[0] + fex * h[1])) return false;
+
+    fex = fabsf(e1[0]); fey = fabsf(e1[1]); fez = fabsf(e1[2]);
+    a = e1[2]; b = e1[1];
+    if (axis_sep(a * v0[1] - b * v0[2], a * v2[1] - b * v2[2], true, fez * h[1] + fey * h[2])) return false;
+    a = e1[2]; b = e1[0];
+    if (axis_sep(-a * v0[0] + b * v0[2], -a * v2[0] + b * v2[2], true, fez * h[0] + fex * h[2])) return false;
+    a = e1[1]; b = e1[0];
+    if (axis_sep(a * v0[0] - b * v0[1], a * v1[0] - b * v1[1], true, fey * h[0] + fex * h[1])) return false;
+
+    fex = fabsf(e2[0]); fey = fabsf(e2[1]); fez = fabsf(e2[2]);
+    a = e2[2]; b = e2[1];
+    if (axis_sep(a * v0[1] - b * v0[2], a * v1[1] - b * v1[2], true, fez * h[1] + fey * h[2])) return false;
+    a = e2[2]; b = e2[0];
+    if (axis_sep(-a * v0[0] + b * v0[2], -a * v1[0] + b * v1[2], true, fez * h[0] + fex * h[2])) return false;
+    a = e2[1]; b = e2[0];
+    if (axis_sep(a * v1[0] - b * v1[1], a * v2[0] - b * v2[1], false, fey * h[0] + fex * h[1])) return false;
+
+    const float *vv[3] = {v0, v1, v2};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        float mn = vv[0][k], mx = vv[0][k];
+        if (vv[1][k] < mn) mn = vv[1][k];
+        if (vv[1][k] > mx) mx = vv[1][k];
+        if (vv[2][k] < mn) mn = vv[2][k];
+        if (vv[2][k] > mx) mx = vv[2][k];
+        if (mn > h[k] || mx < -h[k]) return false;
+    }
+    const float n[3] = {e0[1] * e1[2] - e0[2] * e1[1], e0[2] * e1[0] - e0[0] * e1[2], e0[0] * e1[1] - e0[1] * e1[0]};
+    return plane_box(n, v0, h);
+}
+
+// ---- 1. triangle setup ---------------------------------------------------------
+
+__global__ void k_mesh_setup(uint64_t n_tris, const int32_t *__restrict__ tri_idx, const float *__restrict__ pos,
+                             const float *__restrict__ nrm, const float *__restrict__ col, float lx, float ly,
+                             float lz, float factor, float *__restrict__ out) {
+    uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_tris) return;
+    const float low[3] = {lx, ly, lz};
+    float p[9], n[9], c[9];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        uint64_t v = (uint64_t)tri_idx[3 * t + j];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            p[3 * j + k] = (pos[3 * v + k] - low[k]) * factor;  // (pos - _lower) * factor
+            c[3 * j + k] = col[3 * v + k];
+            n[3 * j + k] = nrm ? nrm[3 * v + k] : 0.0f;
+        }
+    }
+    if (!nrm) {  // (v1 - v0).cross(v2 - v0).normalize(), PlyLoader.cpp:213-218
+        float ax = p[3] - p[0], ay = p[4] - p[1], az = p[5] - p[2];
+        float bx = p[6] - p[0], by = p[7] - p[1], bz = p[8] - p[2];
+        float cx = ay * bz - az * by, cy = az * bx - ax * bz, cz = ax * by - ay * bx;
+        float inv = 1.0f / sqrtf(cx * cx + cy * cy + cz * cz);
+        cx *= inv;
+        cy *= inv;
+        cz *= inv;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            n[3 * j] = cx;
+            n[3 * j + 1] = cy;
+            n[3 * j + 2] = cz;
+        }
+    }
+    float *o = out + t * kTriFloats;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        o[kTriP + k] = p[k];
+        o[kTriN + k] = n[k];
+        o[kTriC + k] = c[k];
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        o[kTriLo + k] = smin(p[k], smin(p[3 + k], p[6 + k]));
+        o[kTriHi + k] = smax(p[k], smax(p[3 + k], p[6 + k]));
+    }
+    o[33] = o[34] = o[35] = 0.0f;
+}
+
+// ---- 2. sub-block lists -> (brick, triangle) pairs -------------------------------
+
+struct ListGeom {
+    float grid_scale;        // float(sideLength - 2) of PlyLoader::pointToGrid
+    float cell_h[3];         // _subBlock{W,H,D} / float(sideLength - 2)
+    int sub[3];              // sub-block edges
+    int part[3];             // partitions per cache block and axis
+    int grid[3];             // _gridW/H/D
+    int dims[3];             // volume W/H/D
+    int log_e;               // brick edge 2^log_e
+    int log_block;           // cache-block edge 2^log_block
+    uint64_t n_blocks;       // Morton-indexed block flags
+};
+
+__device__ __forceinline__ int point_to_grid(float p, float s) { return (int)(p * s + 1.0f); }
+
+// mode 0: count pairs per triangle (and store the triangle's voxel box,
+// mark blocks); mode 1: emit pairs at out_off[t].
+template <int kMode>
+__global__ void k_tri_pairs(uint64_t n_tris, const float *__restrict__ tris, ListGeom g, int32_t *__restrict__ box,
+                            uint8_t *__restrict__ block_flag, uint32_t *__restrict__ count,
+                            const uint64_t *__restrict__ out_off, uint32_t *__restrict__ pair_key,
+                            uint32_t *__restrict__ pair_tri, uint32_t *__restrict__ err) {
+    uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_tris) return;
+    const float *T = tris + t * kTriFloats;
+    int lo[3], hi[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        lo[k] = point_to_grid(T[kTriLo + k], g.grid_scale);
+        hi[k] = point_to_grid(T[kTriHi + k], g.grid_scale);
+    }
+    if (kMode == 0) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            box[6 * t + k] = lo[k];
+            box[6 * t + 3 + k] = hi[k];
+        }
+    }
+    float tv[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) tv[k] = T[kTriP + k];
+    int lg[3], ug[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        lg[k] = lo[k] / g.sub[k];
+        ug[k] = (hi[k] + 1) / g.sub[k];
+    }
+    const int max_side = max(ug[0] - lg[0], max(ug[1] - lg[1], ug[2] - lg[2]));
+    uint32_t n = 0;
+    uint64_t o = kMode == 1 ? out_off[t] : 0;
+
+    auto member = [&](int gx, int gy, int gz) {
+        if (gx < 0 || gy < 0 || gz < 0 || gx >= g.grid[0] || gy >= g.grid[1] || gz >= g.grid[2]) {
+            atomicOr(err, 1u);  // the reference would index past its block offsets
+            return;
+        }
+        if (kMode == 0) {
+            uint64_t blk = morton3((uint32_t)(gx / g.part[0]), (uint32_t)(gy / g.part[1]), (uint32_t)(gz / g.part[2]));
+            if (blk < g.n_blocks) block_flag[blk] = 1;
+            else atomicOr(err, 2u);
+        }
+        const int c0[3] = {gx * g.sub[0], gy * g.sub[1], gz * g.sub[2]};
+        int a[3], b[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            a[k] = max(lo[k], c0[k]);
+            b[k] = min(hi[k], min(c0[k] + g.sub[k] - 1, g.dims[k] - 1));
+        }
+        if (a[0] > b[0] || a[1] > b[1] || a[2] > b[2]) return;
+        for (int bz = a[2] >> g.log_e; bz <= (b[2] >> g.log_e); ++bz)
+            for (int by = a[1] >> g.log_e; by <= (b[1] >> g.log_e); ++by)
+                for (int bx = a[0] >> g.log_e; bx <= (b[0] >> g.log_e); ++bx) {
+                    if (kMode == 1) {
+                        pair_key[o + n] = (uint32_t)morton3((uint32_t)bx, (uint32_t)by, (uint32_t)bz);
+                        pair_tri[o + n] = (uint32_t)t;
+                    }
+                    ++n;
+                }
+    };
+
+    if (max_side > 0) {
+        const float half[3] = {0.5f * g.cell_h[0], 0.5f * g.cell_h[1], 0.5f * g.cell_h[2]};
+        float cz = ((float)lg[2] + 0.5f) * g.cell_h[2];
+        for (int z = lg[2]; z <= ug[2]; ++z, cz += g.cell_h[2]) {
+            float cy = ((float)lg[1] + 0.5f) * g.cell_h[1];
+            for (int y = lg[1]; y <= ug[1]; ++y, cy += g.cell_h[1]) {
+                float cx = ((float)lg[0] + 0.5f) * g.cell_h[0];
+                for (int x = lg[0]; x <= ug[0]; ++x, cx += g.cell_h[0])
+                    if (tri_box(cx, cy, cz, half, tv)) member(x, y, z);
+            }
+        }
+    } else {
+        member(lg[0], lg[1], lg[2]);
+    }
+    if (kMode == 0) count[t] = n;
+}
+
+// Unique bricks of the sorted pairs.
+__global__ void k_heads_u32(const uint32_t *__restrict__ key, uint64_t n, uint32_t *__restrict__ head) {
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) head[i] = (i == 0 || key[i] != key[i - 1]) ? 1u : 0u;
+}
+
+__global__ void k_brick_table(const uint32_t *__restrict__ key, uint64_t n, const uint32_t *__restrict__ head,
+                              const uint32_t *__restrict__ hidx, uint32_t *__restrict__ bkey,
+                              uint32_t *__restrict__ bstart) {
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !head[i]) return;
+    bkey[hidx[i]] = key[i];
+    bstart[hidx[i]] = (uint32_t)i;
+}
+
+// Per cache block: [first, last) of its bricks in the unique-brick table.
+__global__ void k_block_ranges(const uint32_t *__restrict__ bkey, uint32_t nb, int shift, uint64_t n_blocks,
+                               uint32_t *__restrict__ rfirst, uint32_t *__restrict__ rlast, uint32_t *__restrict__ err) {
+    uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nb) return;
+    uint32_t blk = bkey[j] >> shift;
+    if (blk >= n_blocks) {
+        atomicOr(err, 4u);
+        return;
+    }
+    if (j == 0 || (bkey[j - 1] >> shift) != blk) rfirst[blk] = j;
+    if (j == nb - 1 || (bkey[j + 1] >> shift) != blk) rlast[blk] = j + 1;
+}
+
+__global__ void k_flag_to_u32(const uint8_t *__restrict__ f, uint64_t n, uint32_t *__restrict__ out) {
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = f[i] ? 1u : 0u;
+}
+
+__global__ void k_gather_blocks(const uint8_t *__restrict__ flag, uint64_t n, const uint32_t *__restrict__ idx,
+                                const uint32_t *__restrict__ rfirst, const uint32_t *__restrict__ rlast,
+                                uint32_t *__restrict__ out) {
+    uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= n || !flag[b]) return;
+    uint32_t k = idx[b];
+    out[3 * k] = (uint32_t)b;
+    out[3 * k + 1] = rfirst[b];
+    out[3 * k + 2] = rlast[b];
+}
+
+// Running centres: acc[l * K + k] = ((l - 0.5) * h) + h + ... (k additions),
+// the value the reference's loop holds at voxel l + k (PlyLoader.cpp:363-368).
+__global__ void k_center_table(int n_l, int K, float h, float *__restrict__ acc) {
+    int l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= n_l) return;
+    float c = ((float)l - 0.5f) * h;
+    float *row = acc + (uint64_t)l * K;
+    for (int k = 0; k < K; ++k) {
+        row[k] = c;
+        c += h;
+    }
+}
+
+// ---- 4. per-block brick fold ------------------------------------------------------
+
+struct BlockArgs {
+    const float *tris;
+    const int32_t *box;
+    const uint32_t *pair_tri;
+    const uint32_t *bkey;
+    const uint32_t *bstart;  // nb + 1 entries
+    uint32_t b_first, b_last;
+    int log_e;
+    int sub[3];
+    int org[3];   // block origin
+    int buf[3];   // clamped block dims (the buffer's W/H/D for this block)
+    const float *acc;
+    int K;
+    float half;
+    uint32_t *data;
+    uint8_t *counts;
+};
+
+// PlyLoader::writeTriangleCell on a register copy of one buffer cell.
+__device__ __forceinline__ void write_cell(uint32_t &w, uint32_t &cnt, float cx, float cy, float cz, const float *T) {
+    const float *p = T + kTriP, *nv = T + kTriN, *cv = T + kTriC;
+    // Triangle::barycentric (PlyLoader.cpp:55-64)
+    float f1x = p[0] - cx, f1y = p[1] - cy, f1z = p[2] - cz;
+    float f2x = p[3] - cx, f2y = p[4] - cy, f2z = p[5] - cz;
+    float f3x = p[6] - cx, f3y = p[7] - cy, f3z = p[8] - cz;
+    float ax = p[0] - p[3], ay = p[1] - p[4], az = p[2] - p[5];
+    float bx = p[0] - p[6], by = p[1] - p[7], bz = p[2] - p[8];
+    float qx = ay * bz - az * by, qy = az * bx - ax * bz, qz = ax * by - ay * bx;
+    float area = sqrtf(qx * qx + qy * qy + qz * qz);
+    qx = f2y * f3z - f2z * f3y;
+    qy = f2z * f3x - f2x * f3z;
+    qz = f2x * f3y - f2y * f3x;
+    float l1 = sqrtf(qx * qx + qy * qy + qz * qz) / area;
+    qx = f3y * f1z - f3z * f1y;
+    qy = f3z * f1x - f3x * f1z;
+    qz = f3x * f1y - f3y * f1x;
+    float l2 = sqrtf(qx * qx + qy * qy + qz * qz) / area;
+    if (!(l1 >= 0.0f && l2 >= 0.0f && l1 + l2 <= 1.0f)) {
+        l1 = smin(smax(l1, 0.0f), 1.0f);
+        l2 = smin(smax(l2, 0.0f), 1.0f);
+        float tau = l1 + l2;
+        if (tau > 1.0f) {
+            l1 /= tau;
+            l2 /= tau;
+        }
+    }
+    float l3 = 1.0f - l1 - l2;
+    float nx = nv[0] * l1 + nv[3] * l2 + nv[6] * l3;
+    float ny = nv[1] * l1 + nv[4] * l2 + nv[7] * l3;
+    float nz = nv[2] * l1 + nv[5] * l2 + nv[8] * l3;
+    float inv = 1.0f / sqrtf(nx * nx + ny * ny + nz * nz);
+    nx *= inv;
+    ny *= inv;
+    nz *= inv;
+    float r = cv[0] * l1 + cv[3] * l2 + cv[6] * l3;
+    float gg = cv[1] * l1 + cv[4] * l2 + cv[7] * l3;
+    float b = cv[2] * l1 + cv[5] * l2 + cv[8] * l3;
+    float shade = (r * 0.2126f + gg * 0.7152f + b * 0.0722f) * (1.0f / 256.0f);
+    if (w == 0) {
+        cnt = 1;
+        w = compress_material(nx, ny, nz, shade);
+    } else {
+        float cur = (float)cnt / ((float)cnt + 1.0f);
+        float nr = 1.0f - cur;
+        float cnx, cny, cnz, cs;
+        decompress_material(w, cnx, cny, cnz, cs);
+        float mx = cnx * cur + nx * nr, my = cny * cur + ny * nr, mz = cnz * cur + nz * nr;
+        float ms = cs * cur + shade * nr;
+        if (mx * mx + my * my + mz * mz < 1e-3f) {
+            mx = cnx;
+            my = cny;
+            mz = cnz;
+        }
+        w = compress_material(mx, my, mz, ms);
+        cnt = cnt + 1 < 255 ? cnt + 1 : 255;
+    }
+}
+
+__global__ void __launch_bounds__(kBrickCta) k_block_bricks(BlockArgs a) {
+    __shared__ float sT[kChunk][kStageFloats];
+    __shared__ int sB[kChunk][6];
+    const int E = 1 << a.log_e;
+    const int tid = threadIdx.x;
+    const bool lane_used = tid < E * E * E;
+    const int tx = tid & (E - 1), ty = (tid >> a.log_e) & (E - 1), tz = tid >> (2 * a.log_e);
+    const float hv[3] = {a.half, a.half, a.half};
+    for (uint32_t j = a.b_first + blockIdx.x; j < a.b_last; j += gridDim.x) {
+        const uint32_t key = a.bkey[j];
+        const int x = (int)(compact3(key) << a.log_e) + tx;
+        const int y = (int)(compact3((uint64_t)key >> 1) << a.log_e) + ty;
+        const int z = (int)(compact3((uint64_t)key >> 2) << a.log_e) + tz;
+        const bool active = lane_used && x < a.org[0] + a.buf[0] && y < a.org[1] + a.buf[1] &&
+                            z < a.org[2] + a.buf[2] && x >= a.org[0] && y >= a.org[1] && z >= a.org[2];
+        // start of this voxel's sub-block: PlyLoader's clamp _bufferX + offX
+        const int cx0 = (x / a.sub[0]) * a.sub[0], cy0 = (y / a.sub[1]) * a.sub[1], cz0 = (z / a.sub[2]) * a.sub[2];
+        const uint64_t bi = (uint64_t)(x - a.org[0]) +
+                            (uint64_t)a.buf[0] * ((uint64_t)(y - a.org[1]) + (uint64_t)a.buf[1] * (uint64_t)(z - a.org[2]));
+        uint32_t w = 0, cnt = 0;
+        bool loaded = false;
+        const uint32_t s0 = a.bstart[j], s1 = a.bstart[j + 1];
+        for (uint32_t c0 = s0; c0 < s1; c0 += kChunk) {
+            const int nc = (int)min((uint32_t)kChunk, s1 - c0);
+            __syncthreads();
+            for (int i = tid; i < nc * kStageFloats; i += blockDim.x) {
+                int q = i / kStageFloats, f = i - q * kStageFloats;
+                sT[q][f] = a.tris[(uint64_t)a.pair_tri[c0 + q] * kTriFloats + f];
+            }
+            for (int i = tid; i < nc * 6; i += blockDim.x) {
+                int q = i / 6, f = i - q * 6;
+                sB[q][f] = a.box[(uint64_t)a.pair_tri[c0 + q] * 6 + f];
+            }
+            __syncthreads();
+            if (!active) continue;
+            for (int q = 0; q < nc; ++q) {
+                const int lx = max(sB[q][0], cx0), ly = max(sB[q][1], cy0), lz = max(sB[q][2], cz0);
+                if (x < lx || y < ly || z < lz || x > sB[q][3] || y > sB[q][4] || z > sB[q][5]) continue;
+                const float fx = a.acc[(uint64_t)lx * a.K + (x - lx)];
+                const float fy = a.acc[(uint64_t)ly * a.K + (y - ly)];
+                const float fz = a.acc[(uint64_t)lz * a.K + (z - lz)];
+                if (!tri_box(fx, fy, fz, hv, &sT[q][kTriP])) continue;
+                if (!loaded) {
+                    w = a.data[bi];
+                    cnt = a.counts[bi];
+                    loaded = true;
+                }
+                write_cell(w, cnt, fx, fy, fz, &sT[q][0]);
+            }
+        }
+        if (loaded) {
+            a.data[bi] = w;
+            a.counts[bi] = (uint8_t)cnt;
+        }
+    }
+}
+
+// findBestBlockPartition (PlyLoader.cpp:381-405).
+void best_partition(int &w, int &h, int &d, int threads) {
+    auto maximum = [&]() -> int & { if (w > h && w > d) return w; else if (h > d) return h; else return d; };
+    auto median = [&]() -> int & {
+        int mx = std::max(w, std::max(h, d)), mn = std::min(w, std::min(h, d));
+        if (w != mn && w != mx) return w; else if (h != mn && h != mx) return h; else return d;
+    };
+    auto minimum = [&]() -> int & { if (w < h && w < d) return w; else if (h < d) return h; else return d; };
+    int used = 1;
+    while (used < threads) {
+        if ((maximum() % 2) == 0) maximum() /= 2;
+        else if ((median() % 2) == 0) median() /= 2;
+        else if ((minimum() % 2) == 0) minimum() /= 2;
+        else break;
+        used *= 2;
+    }
+}
+
+template <typename TI, typename TO>
+int scan_total(const TI *in, TO *out, uint64_t n, TO *total_host, cudaStream_t st) {
+    Dev<TO> scratch, tot;
+    SVO_ALLOC(scratch, scan_scratch_elems(n));
+    SVO_ALLOC(tot, 1);
+    SVO_CUDA_TRY((exclusive_scan<TI, TO>(in, out, n, tot.p, scratch.p, st)));
+    SVO_CUDA_TRY(cudaMemcpyAsync(total_host, tot.p, sizeof(TO), cudaMemcpyDeviceToHost, st));
+    SVO_CUDA_TRY(cudaStreamSynchronize(st));
+    return SVO_OK;
+}
+
+int log2_floor(uint64_t v) {
+    int r = -1;
+    while (v) {
+        v >>= 1;
+        ++r;
+    }
+    return r;
+}
+
+uint64_t round_pow2(uint64_t v) {
+    uint64_t p = 1;
+    while (p < v) p <<= 1;
+    return p;
+}
+
+struct BlockJob {
+    uint32_t morton, first, last;
+};
+
+}  // namespace
+
+// Mesh dimensions for a side length: PlyLoader::suggestedDimensions
+// (PlyLoader.cpp:499-504).
+static void mesh_dims(const svo_mesh *m, int side, int dims[3]) {
+    const float s = (float)(side - 2);
+    for (int k = 0; k < 3; ++k) dims[k] = (int)((m->upper[k] - m->lower[k]) * s) + 2;
+}
+
+int mesh_upload(const MeshHost &h, svo_mesh **out) {
+    *out = nullptr;
+    const uint64_t nv = h.pos.size() / 3, nt = h.tris.size() / 3;
+    if (nv == 0) return set_error(SVO_ERR_FORMAT, "mesh has no vertices");
+    std::unique_ptr<svo_mesh> m(new svo_mesh());
+    SVO_CUDA_TRY(cudaGetDevice(&m->device));
+    // PlyLoader::rescaleVertices (PlyLoader.cpp:167-181)
+    float diff[3] = {h.upper[0] - h.lower[0], h.upper[1] - h.lower[1], h.upper[2] - h.lower[2]};
+    int largest = 2;
+    if (diff[0] > diff[1] && diff[0] > diff[2]) largest = 0;
+    else if (diff[1] > diff[2]) largest = 1;
+    const float factor = 1.0f / diff[largest];
+    for (int k = 0; k < 3; ++k) {
+        m->upper[k] = h.upper[k] * factor;
+        m->lower[k] = h.lower[k] * factor;
+    }
+    m->has_normals = h.nrm.empty() ? 0 : 1;
+    m->n_tris = nt;
+    if (nt == 0) {
+        *out = m.release();
+        return SVO_OK;
+    }
+    cudaStream_t st = nullptr;
+    SVO_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    struct StreamGuard {
+        cudaStream_t s;
+        ~StreamGuard() { cudaStreamDestroy(s); }
+    } guard{st};
+    Dev<float> pos, nrm, col;
+    Dev<int32_t> idx;
+    SVO_ALLOC(pos, nv * 3);
+    SVO_ALLOC(col, nv * 3);
+    SVO_ALLOC(idx, nt * 3);
+    if (m->has_normals) SVO_ALLOC(nrm, nv * 3);
+    SVO_CUDA_TRY(cudaMemcpyAsync(pos.p, h.pos.data(), nv * 3 * sizeof(float), cudaMemcpyHostToDevice, st));
+    SVO_CUDA_TRY(cudaMemcpyAsync(col.p, h.col.data(), nv * 3 * sizeof(float), cudaMemcpyHostToDevice, st));
+    SVO_CUDA_TRY(cudaMemcpyAsync(idx.p, h.tris.data(), nt * 3 * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    if (m->has_normals)
+        SVO_CUDA_TRY(cudaMemcpyAsync(nrm.p, h.nrm.data(), nv * 3 * sizeof(float), cudaMemcpyHostToDevice, st));
+    SVO_CUDA_TRY(cudaMalloc((void **)&m->d_tris, nt * kTriFloats * sizeof(float)));
+    k_mesh_setup<<<grid_for(nt), 256, 0, st>>>(nt, idx.p, pos.p, m->has_normals ? nrm.p : nullptr, col.p, h.lower[0],
+                                               h.lower[1], h.lower[2], factor, m->d_tris);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        cudaFree(m->d_tris);
+        m->d_tris = nullptr;
+        return cuda_fail(e, "mesh setup");
+    }
+    *out = m.release();
+    return SVO_OK;
+}
+
+int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cudaStream_t st, uint32_t **d_words,
+                      uint64_t *n_words, float center[3]) {
+    if (side < 5 || side > (1 << 20)) return set_error(SVO_ERR_INVALID, "side %d outside [5, 2^20]", side);
+    if (threads < 1) return set_error(SVO_ERR_INVALID, "threads must be >= 1");
+    int dims[3];
+    mesh_dims(m, side, dims);
+    // VoxelData::init (VoxelData.cpp:211-262) with the loader's cell cost 4 + 1
+    const int lb = cache_block_log2(dims[0], dims[1], dims[2], mem, 5);
+    if (lb < 1)
+        return set_error(SVO_ERR_MEMORY, "memory budget %llu too small for a %dx%dx%d volume",
+                         (unsigned long long)mem, dims[0], dims[1], dims[2]);
+    const uint64_t V = round_pow2((uint64_t)std::max(dims[0], std::max(dims[1], dims[2])));
+    const int D = log2_floor(V);
+    const int B = 1 << lb;
+    // VoxelData::getCenter (VoxelData.cpp:297-303)
+    for (int k = 0; k < 3; ++k) center[k] = (float)dims[k] * 0.5f / (float)V;
+
+    // PlyLoader::setupBlockProcessing (PlyLoader.cpp:407-437)
+    ListGeom g;
+    int sub[3] = {B, B, B};
+    best_partition(sub[0], sub[1], sub[2], threads);
+    for (int k = 0; k < 3; ++k) {
+        g.sub[k] = sub[k];
+        g.part[k] = B / sub[k];
+        g.grid[k] = g.part[k] * (dims[k] + B - 1) / B;
+        g.dims[k] = dims[k];
+        g.cell_h[k] = (float)sub[k] / (float)(side - 4);
+    }
+    g.grid_scale = (float)(side - 4);
+    const int min_sub = std::min(sub[0], std::min(sub[1], sub[2]));
+    g.log_e = std::min(3, log2_floor((uint64_t)min_sub));
+    g.log_block = lb;
+    const int lbv = D - lb;  // log2 of blocks per axis
+    g.n_blocks = 1ull << (3 * lbv);
+    if (g.n_blocks > (1ull << 27))
+        return set_error(SVO_ERR_LIMIT, "memory budget gives %llu cache blocks; the GPU build supports at most 2^27",
+                         (unsigned long long)g.n_blocks);
+    const int key_bits = 3 * (D - g.log_e);
+    if (key_bits > 32) return set_error(SVO_ERR_LIMIT, "side %d with %d^3 bricks needs more than 32-bit brick keys",
+                                        side, 1 << g.log_e);
+    const int K = std::max(sub[0], std::max(sub[1], sub[2]));
+    const int n_l = std::max(dims[0], std::max(dims[1], dims[2])) + 1;
+    if ((uint64_t)n_l * (uint64_t)K > (1ull << 28))
+        return set_error(SVO_ERR_LIMIT, "voxel-centre table of %d x %d entries is too large", n_l, K);
+
+    const uint64_t nt = m->n_tris;
+    Dev<uint32_t> err;
+    SVO_ALLOC(err, 1);
+    SVO_CUDA_TRY(cudaMemsetAsync(err.p, 0, sizeof(uint32_t), st));
+    Dev<uint8_t> bflag;
+    SVO_ALLOC(bflag, g.n_blocks);
+    SVO_CUDA_TRY(cudaMemsetAsync(bflag.p, 0, g.n_blocks, st));
+
+    // 2. pairs: count, offsets, emit (triangle-major order)
+    Dev<int32_t> box;
+    Dev<uint32_t> pcount;
+    Dev<uint64_t> poff;
+    SVO_ALLOC(box, nt * 6);
+    SVO_ALLOC(pcount, nt);
+    SVO_ALLOC(poff, nt);
+    uint64_t n_pairs = 0;
+    if (nt) {
+        k_tri_pairs<0><<<grid_for(nt, 128), 128, 0, st>>>(nt, m->d_tris, g, box.p, bflag.p, pcount.p, nullptr,
+                                                          nullptr, nullptr, err.p);
+        SVO_LAUNCH_OK("k_tri_pairs<count>");
+        int rc = scan_total<uint32_t, uint64_t>(pcount.p, poff.p, nt, &n_pairs, st);
+        if (rc) return rc;
+    }
+    if (n_pairs >= 0xFFFFFFFFull)
+        return set_error(SVO_ERR_LIMIT, "%llu brick/triangle pairs exceed 2^32-1", (unsigned long long)n_pairs);
+    Dev<uint32_t> pk, pt, pk2, pt2, sort_scratch;
+    SVO_ALLOC(pk, n_pairs);
+    SVO_ALLOC(pt, n_pairs);
+    SVO_ALLOC(pk2, n_pairs);
+    SVO_ALLOC(pt2, n_pairs);
+    if (n_pairs) {
+        k_tri_pairs<1><<<grid_for(nt, 128), 128, 0, st>>>(nt, m->d_tris, g, box.p, bflag.p, pcount.p, poff.p, pk.p,
+                                                          pt.p, err.p);
+        SVO_LAUNCH_OK("k_tri_pairs<emit>");
+    }
+    pcount.release();
+    poff.release();
+
+    // 3. stable sort by brick
+    SVO_ALLOC(sort_scratch, radix_scratch_elems(n_pairs));
+    bool in_alt = false;
+    SVO_CUDA_TRY(radix_sort_pairs(pk.p, pt.p, pk2.p, pt2.p, n_pairs, key_bits, sort_scratch.p, st, &in_alt));
+    sort_scratch.release();
+    const uint32_t *skey = in_alt ? pk2.p : pk.p;
+    const uint32_t *stri = in_alt ? pt2.p : pt.p;
+
+    // unique bricks and per-block brick ranges
+    Dev<uint32_t> head, hidx, bkey, bstart, rfirst, rlast;
+    SVO_ALLOC(head, n_pairs);
+    SVO_ALLOC(hidx, n_pairs);
+    uint32_t nb = 0;
+    if (n_pairs) {
+        k_heads_u32<<<grid_for(n_pairs), 256, 0, st>>>(skey, n_pairs, head.p);
+        SVO_LAUNCH_OK("k_heads_u32");
+        int rc = scan_total<uint32_t, uint32_t>(head.p, hidx.p, n_pairs, &nb, st);
+        if (rc) return rc;
+    }
+    SVO_ALLOC(bkey, nb);
+    SVO_ALLOC(bstart, (uint64_t)nb + 1);
+    SVO_ALLOC(rfirst, g.n_blocks);
+    SVO_ALLOC(rlast, g.n_blocks);
+    SVO_CUDA_TRY(cudaMemsetAsync(rfirst.p, 0, g.n_blocks * sizeof(uint32_t), st));
+    SVO_CUDA_TRY(cudaMemsetAsync(rlast.p, 0, g.n_blocks * sizeof(uint32_t), st));
+    {
+        uint32_t np32 = (uint32_t)n_pairs;
+        SVO_CUDA_TRY(cudaMemcpyAsync(bstart.p + nb, &np32, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    }
+    if (nb) {
+        k_brick_table<<<grid_for(n_pairs), 256, 0, st>>>(skey, n_pairs, head.p, hidx.p, bkey.p, bstart.p);
+        k_block_ranges<<<grid_for(nb), 256, 0, st>>>(bkey.p, nb, 3 * (lb - g.log_e), g.n_blocks, rfirst.p, rlast.p,
+                                                    err.p);
+        SVO_LAUNCH_OK("k_block_ranges");
+    }
+    head.release();
+    hidx.release();
+
+    // cache blocks the lists mark, in Morton (visiting) order
+    std::vector<BlockJob> jobs;
+    {
+        Dev<uint32_t> f32, fidx, packed;
+        SVO_ALLOC(f32, g.n_blocks);
+        SVO_ALLOC(fidx, g.n_blocks);
+        k_flag_to_u32<<<grid_for(g.n_blocks), 256, 0, st>>>(bflag.p, g.n_blocks, f32.p);
+        SVO_LAUNCH_OK("k_flag_to_u32");
+        uint32_t n_jobs = 0;
+        int rc = scan_total<uint32_t, uint32_t>(f32.p, fidx.p, g.n_blocks, &n_jobs, st);
+        if (rc) return rc;
+        SVO_ALLOC(packed, (uint64_t)n_jobs * 3);
+        if (n_jobs) {
+            k_gather_blocks<<<grid_for(g.n_blocks), 256, 0, st>>>(bflag.p, g.n_blocks, fidx.p, rfirst.p, rlast.p,
+                                                                 packed.p);
+            SVO_LAUNCH_OK("k_gather_blocks");
+        }
+        jobs.resize(n_jobs);
+        if (n_jobs)
+            SVO_CUDA_TRY(cudaMemcpyAsync(jobs.data(), packed.p, (size_t)n_jobs * 3 * sizeof(uint32_t),
+                                         cudaMemcpyDeviceToHost, st));
+        uint32_t e_h = 0;
+        SVO_CUDA_TRY(cudaMemcpyAsync(&e_h, err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        SVO_CUDA_TRY(cudaStreamSynchronize(st));
+        if (e_h) return set_error(SVO_ERR_DEVICE, "mesh build: sub-block lists out of range (flags %u)", e_h);
+    }
+    rfirst.release();
+    rlast.release();
+
+    // the persistent block buffer (VoxelData::_bufferedData, zeroed) and the
+    // loader's per-cell counts, sized for the largest block volume
+    uint64_t buf_cells = 1;
+    for (const BlockJob &j : jobs) {
+        int o[3] = {(int)(compact3(j.morton) << lb), (int)(compact3((uint64_t)j.morton >> 1) << lb),
+                    (int)(compact3((uint64_t)j.morton >> 2) << lb)};
+        uint64_t v = 1;
+        for (int k = 0; k < 3; ++k) v *= (uint64_t)std::max(0, std::min(B, dims[k] - o[k]));
+        buf_cells = std::max(buf_cells, v);
+    }
+    Dev<uint32_t> data;
+    Dev<uint8_t> counts;
+    Dev<float> acc;
+    SVO_ALLOC(data, buf_cells);
+    SVO_ALLOC(counts, buf_cells);
+    SVO_ALLOC(acc, (uint64_t)n_l * K);
+    SVO_CUDA_TRY(cudaMemsetAsync(data.p, 0, buf_cells * sizeof(uint32_t), st));
+    SVO_CUDA_TRY(cudaMemsetAsync(counts.p, 0, buf_cells, st));
+    const float hx = 1.0f / (float)(side - 4);
+    k_center_table<<<grid_for(n_l), 256, 0, st>>>(n_l, K, hx, acc.p);
+    SVO_LAUNCH_OK("k_center_table");
+
+    int dev = 0, sms = 0;
+    SVO_CUDA_TRY(cudaGetDevice(&dev));
+    SVO_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+
+    // 4. blocks in order: fold, then extract (and clear) the block's voxels
+    std::vector<uint64_t *> part_keys;
+    std::vector<uint32_t *> part_pay;
+    std::vector<uint64_t> part_n;
+    struct PartsGuard {
+        std::vector<uint64_t *> &k;
+        std::vector<uint32_t *> &p;
+        cudaStream_t st;
+        ~PartsGuard() {
+            for (auto x : k) cudaFreeAsync(x, st);
+            for (auto x : p) cudaFreeAsync(x, st);
+        }
+    } parts_guard{part_keys, part_pay, st};
+    uint64_t N = 0;
+    for (const BlockJob &j : jobs) {
+        BlockArgs ba;
+        ba.org[0] = (int)(compact3(j.morton) << lb);
+        ba.org[1] = (int)(compact3((uint64_t)j.morton >> 1) << lb);
+        ba.org[2] = (int)(compact3((uint64_t)j.morton >> 2) << lb);
+        bool inside = true;
+        for (int k = 0; k < 3; ++k) {
+            ba.buf[k] = std::min(B, dims[k] - ba.org[k]);
+            ba.sub[k] = sub[k];
+            if (ba.buf[k] <= 0) inside = false;
+        }
+        if (!inside) continue;  // VoxelData::prepareDataAccess returns early
+        if (j.last > j.first) {
+            ba.tris = m->d_tris;
+            ba.box = box.p;
+            ba.pair_tri = stri;
+            ba.bkey = bkey.p;
+            ba.bstart = bstart.p;
+            ba.b_first = j.first;
+            ba.b_last = j.last;
+            ba.log_e = g.log_e;
+            ba.acc = acc.p;
+            ba.K = K;
+            ba.half = 0.5f * hx;
+            ba.data = data.p;
+            ba.counts = counts.p;
+            uint32_t nbricks = j.last - j.first;
+            unsigned grid = (unsigned)std::min<uint64_t>(nbricks, (uint64_t)sms * 4);
+            k_block_bricks<<<grid, kBrickCta, 0, st>>>(ba);
+            SVO_LAUNCH_OK("k_block_bricks");
+        }
+        uint64_t *bk = nullptr;
+        uint32_t *bp = nullptr;
+        uint64_t bn = 0;
+        const int drop = ((ba.buf[2] & 1) && lb >= 2) ? 1 : 0;
+        int rc = extract_voxels_device(data.p, ba.buf[0], ba.buf[1], ba.buf[2], lb, (uint64_t)j.morton << (3 * lb),
+                                       drop, 1, st, &bk, &bp, &bn);
+        if (rc) return rc;
+        if (bn) {
+            part_keys.push_back(bk);
+            part_pay.push_back(bp);
+            part_n.push_back(bn);
+            N += bn;
+        }
+    }
+    data.release();
+    counts.release();
+    acc.release();
+    if (N >= 0xFFFFFFFFull) return set_error(SVO_ERR_LIMIT, "%llu voxels exceed 2^32-1", (unsigned long long)N);
+
+    // 5. octree from the concatenated (already Morton-ordered) voxels
+    Dev<uint64_t> keys;
+    Dev<uint32_t> pay;
+    SVO_ALLOC(keys, N);
+    SVO_ALLOC(pay, N);
+    uint64_t at = 0;
+    for (size_t i = 0; i < part_n.size(); ++i) {
+        SVO_CUDA_TRY(cudaMemcpyAsync(keys.p + at, part_keys[i], part_n[i] * sizeof(uint64_t), cudaMemcpyDeviceToDevice, st));
+        SVO_CUDA_TRY(cudaMemcpyAsync(pay.p + at, part_pay[i], part_n[i] * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
+        at += part_n[i];
+    }
+    return build_from_sorted_device(keys.p, pay.p, N, D, lb, lb < D ? bflag.p : nullptr, st, d_words, n_words);
+}
+
+}  // namespace svo
+
+// ---- C ABI ---------------------------------------------------------------------
+
+using namespace svo;
+
+extern "C" int svo_mesh_load_ply(const char *path, svo_mesh **out) {
+    clear_error();
+    if (!path || !out) return set_error(SVO_ERR_INVALID, "null argument");
+    *out = nullptr;
+    MeshHost h;
+    int rc = ply_read(path, h);
+    if (rc) return rc;
+    return mesh_upload(h, out);
+}
+
+extern "C" int svo_mesh_from_arrays(const float *positions, const float *normals, const float *colors,
+                                    uint64_t n_vertices, const int32_t *faces, uint64_t n_face_ints, svo_mesh **out) {
+    clear_error();
+    if (!positions || !out || (!faces && n_face_ints)) return set_error(SVO_ERR_INVALID, "null argument");
+    *out = nullptr;
+    MeshHost h;
+    h.pos.reserve(n_vertices * 3);
+    h.col.reserve(n_vertices * 3);
+    const float white[3] = {255.0f, 255.0f, 255.0f};
+    for (uint64_t v = 0; v < n_vertices; ++v) {
+        for (int k = 0; k < 3; ++k)
+            if (!std::isfinite(positions[3 * v + k]))
+                return set_error(SVO_ERR_FORMAT, "vertex %llu has a non-finite coordinate", (unsigned long long)v);
+        mesh_add_vertex(h, positions + 3 * v, normals ? normals + 3 * v : nullptr, colors ? colors + 3 * v : white);
+    }
+    for (uint64_t o = 0; o < n_face_ints;) {
+        int32_t c = faces[o];
+        if (c < 0 || o + 1 + (uint64_t)c > n_face_ints) return set_error(SVO_ERR_FORMAT, "face list truncated");
+        int rc = mesh_add_face(h, faces + o + 1, c, n_vertices);
+        if (rc) return rc;
+        o += 1 + (uint64_t)c;
+    }
+    return mesh_upload(h, out);
+}
+
+extern "C" uint64_t svo_mesh_num_triangles(const svo_mesh *m) { return m ? m->n_tris : 0; }
+
+extern "C" int svo_mesh_dimensions(const svo_mesh *m, int side, int dims[3]) {
+    clear_error();
+    if (!m || !dims) return set_error(SVO_ERR_INVALID, "null argument");
+    mesh_dims(m, side, dims);
+    return SVO_OK;
+}
+
+extern "C" void svo_mesh_destroy(svo_mesh *m) {
+    if (!m) return;
+    if (m->d_tris) cudaFree(m->d_tris);
+    delete m;
+}
+
+extern "C" int svo_octree_build_mesh(const svo_mesh *m, int side, int threads, uint64_t mem, svo_stream stream,
+                                     svo_octree **out) {
+    clear_error();
+    if (!m || !out) return set_error(SVO_ERR_INVALID, "null argument");
+    *out = nullptr;
+    int cur = 0;
+    SVO_CUDA_TRY(cudaGetDevice(&cur));
+    if (cur != m->device) return set_error(SVO_ERR_INVALID, "mesh lives on device %d, current device is %d", m->device, cur);
+    uint32_t *dw = nullptr;
+    uint64_t nw = 0;
+    float center[3];
+    int rc = build_mesh_device(m, side, threads, mem, (cudaStream_t)stream, &dw, &nw, center);
+    if (rc) return rc;
+    return make_handle(dw, nw, center, out);
+}
+
+extern "C" int svo_octree_build_ply(const char *path, int side, int threads, uint64_t mem, svo_stream stream,
+                                    svo_octree **out) {
+    svo_mesh *m = nullptr;
+    int rc = svo_mesh_load_ply(path, &m);
+    if (rc) return rc;
+    rc = svo_octree_build_mesh(m, side, threads, mem, stream, out);
+    svo_mesh_destroy(m);
+    return rc;
+}

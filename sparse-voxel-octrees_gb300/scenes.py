@@ -459,3 +459,143 @@ def decompress_normal(word):
     n = torch.where((face == 1)[:, None], torch.stack([v, s, u], 1), n)
     n = torch.where((face >= 2)[:, None], torch.stack([u, v, s], 1), n)
     return n / n.norm(dim=1, keepdim=True)
+
+
+# ---------------------------------------------------------------- triangle meshes (PLY source)
+
+def icosphere(level):
+    """Unit icosphere: the icosahedron with every triangle split into four
+    `level` times, new vertices pushed out to the sphere (float64).  Level 7
+    has 163,842 vertices and 327,680 triangles."""
+    t = (1.0 + 5.0 ** 0.5) / 2.0
+    v = np.array([[-1, t, 0], [1, t, 0], [-1, -t, 0], [1, -t, 0], [0, -1, t], [0, 1, t], [0, -1, -t], [0, 1, -t],
+                  [t, 0, -1], [t, 0, 1], [-t, 0, -1], [-t, 0, 1]], np.float64)
+    f = np.array([[0, 11, 5], [0, 5, 1], [0, 1, 7], [0, 7, 10], [0, 10, 11], [1, 5, 9], [5, 11, 4], [11, 10, 2],
+                  [10, 7, 6], [7, 1, 8], [3, 9, 4], [3, 4, 2], [3, 2, 6], [3, 6, 8], [3, 8, 9], [4, 9, 5],
+                  [2, 4, 11], [6, 2, 10], [8, 6, 7], [9, 8, 1]], np.int64)
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    for _ in range(level):
+        e = np.concatenate([f[:, [0, 1]], f[:, [1, 2]], f[:, [2, 0]]])
+        key = np.minimum(e[:, 0], e[:, 1]) * v.shape[0] + np.maximum(e[:, 0], e[:, 1])
+        uniq, inv = np.unique(key, return_inverse=True)
+        a, b = uniq // v.shape[0], uniq % v.shape[0]
+        mid = v[a] + v[b]
+        mid /= np.linalg.norm(mid, axis=1, keepdims=True)
+        m = inv.reshape(3, -1) + v.shape[0]  # midpoints of edges 01, 12, 20
+        v = np.concatenate([v, mid])
+        f = np.concatenate([np.stack([f[:, 0], m[0], m[2]], 1), np.stack([f[:, 1], m[1], m[0]], 1),
+                            np.stack([f[:, 2], m[2], m[1]], 1), np.stack([m[0], m[1], m[2]], 1)])
+    return v, f.astype(np.int32)
+
+
+def _hash_lattice(ix, iy, iz, seed):
+    m = np.uint64(0xFFFFFFFF)
+    h = ((ix.astype(np.uint64) * np.uint64(73856093)) ^ (iy.astype(np.uint64) * np.uint64(19349663)) ^
+         (iz.astype(np.uint64) * np.uint64(83492791)) ^ np.uint64((seed * 2654435761) & 0xFFFFFFFF)) & m
+    h = ((h ^ (h >> np.uint64(16))) * np.uint64(0x45D9F3B)) & m
+    h = ((h ^ (h >> np.uint64(16))) * np.uint64(0x45D9F3B)) & m
+    h = h ^ (h >> np.uint64(16))
+    return (h & np.uint64(0xFFFFFF)).astype(np.float64) / float(1 << 24)
+
+
+def value_noise3(p, seed, octaves=4, freq=2.0):
+    """Seeded fractal value noise in [0, 1) at points p (N, 3) float64:
+    smoothstep-trilinear hashed lattice values, octave k at frequency
+    freq*2^k with amplitude 2^-k."""
+    total = np.zeros(p.shape[0])
+    norm = 0.0
+    for k in range(octaves):
+        q = (p + 4.0) * (freq * 2 ** k)
+        i = np.floor(q).astype(np.int64)
+        f = q - i
+        s = f * f * (3.0 - 2.0 * f)
+        v = 0.0
+        for dz in (0, 1):
+            for dy in (0, 1):
+                for dx in (0, 1):
+                    w = (s[:, 0] if dx else 1 - s[:, 0]) * (s[:, 1] if dy else 1 - s[:, 1]) * \
+                        (s[:, 2] if dz else 1 - s[:, 2])
+                    v = v + w * _hash_lattice(i[:, 0] + dx, i[:, 1] + dy, i[:, 2] + dz, seed * 31 + k)
+        total += v * 0.5 ** k
+        norm += 0.5 ** k
+    return total / norm
+
+
+def displaced_icosphere(level, seed, amplitude=0.15, octaves=4):
+    """The PLY-build workload's mesh: a level-`level` icosphere radially
+    displaced by `octaves`-octave seeded value noise (amplitude a fraction
+    of the radius), per-vertex RGB uniform in [0, 255].  Returns
+    (positions float32 (V, 3), faces int32 (F, 3), colours uint8 (V, 3))."""
+    v, f = icosphere(level)
+    r = 1.0 + amplitude * (2.0 * value_noise3(v, seed, octaves) - 1.0)
+    pos = (v * r[:, None]).astype(np.float32)
+    col = np.random.default_rng(seed).integers(0, 256, size=(v.shape[0], 3), dtype=np.uint8)
+    return pos, f, col
+
+
+def write_ply(path, pos, faces, colors=None, normals=None, binary=True, big_endian=False):
+    """Write a PLY mesh: float x, y, z [, nx, ny, nz] [, uchar red, green,
+    blue] per vertex and a `list uchar int vertex_indices` per face, as
+    binary (little- or big-endian) or ASCII.  faces is (F, k) or a list of
+    index lists."""
+    pos = np.asarray(pos, np.float32)
+    V = pos.shape[0]
+    cols = [("x", "f4"), ("y", "f4"), ("z", "f4")]
+    if normals is not None:
+        cols += [("nx", "f4"), ("ny", "f4"), ("nz", "f4")]
+    if colors is not None:
+        cols += [("red", "u1"), ("green", "u1"), ("blue", "u1")]
+    polys = [list(map(int, fc)) for fc in faces] if not isinstance(faces, np.ndarray) else None
+    nf = len(polys) if polys is not None else faces.shape[0]
+    fmt = ("binary_big_endian" if big_endian else "binary_little_endian") if binary else "ascii"
+    bo = ">" if big_endian else "<"
+    hdr = ["ply", "format %s 1.0" % fmt, "element vertex %d" % V]
+    hdr += ["property %s %s" % ("float" if t == "f4" else "uchar", n) for n, t in cols]
+    hdr += ["element face %d" % nf, "property list uchar int vertex_indices", "end_header"]
+    rec = np.zeros(V, dtype=[(n, bo + t if t != "u1" else t) for n, t in cols])
+    rec["x"], rec["y"], rec["z"] = pos[:, 0], pos[:, 1], pos[:, 2]
+    if normals is not None:
+        nrm = np.asarray(normals, np.float32)
+        rec["nx"], rec["ny"], rec["nz"] = nrm[:, 0], nrm[:, 1], nrm[:, 2]
+    if colors is not None:
+        c = np.asarray(colors, np.uint8)
+        rec["red"], rec["green"], rec["blue"] = c[:, 0], c[:, 1], c[:, 2]
+    with open(path, "wb") as fp:
+        fp.write(("\n".join(hdr) + "\n").encode())
+        if binary:
+            fp.write(rec.tobytes())
+            if polys is None:
+                fr = np.zeros(nf, dtype=[("n", "u1"), ("i", bo + "i4", (faces.shape[1],))])
+                fr["n"] = faces.shape[1]
+                fr["i"] = faces
+                fp.write(fr.tobytes())
+            else:
+                for fc in polys:
+                    fp.write(np.uint8(len(fc)).tobytes() + np.asarray(fc, bo + "i4").tobytes())
+        else:
+            lines = []
+            for i in range(V):
+                lines.append(" ".join(repr(float(rec[n][i])) if t == "f4" else str(int(rec[n][i])) for n, t in cols))
+            for fc in (polys if polys is not None else faces.tolist()):
+                lines.append(" ".join([str(len(fc))] + [str(int(x)) for x in fc]))
+            fp.write(("\n".join(lines) + "\n").encode())
+
+
+def edge_case_mesh(level, seed):
+    """A displaced icosphere plus the polygon cases PlyLoader meets: a
+    triangle with a repeated vertex and a collinear triangle (zero area: NaN
+    weights and normals), a quad and a pentagon (fan-triangulated), and
+    faces with 1 and 2 indices (no triangles).  Returns (positions float32,
+    faces as a list of index lists, colours uint8)."""
+    pos, f, col = displaced_icosphere(level, seed)
+    V = pos.shape[0]
+    line = np.array([[0.05, 0.1, 0.2], [0.15, 0.2, 0.3], [0.35, 0.4, 0.5]], np.float32)
+    pos = np.concatenate([pos, line])
+    rng = np.random.default_rng(seed + 1)
+    col = np.concatenate([col, rng.integers(0, 256, (3, 3), dtype=np.uint8)])
+    faces = [list(map(int, t)) for t in f]
+    faces += [[0, 0, 5], [V, V + 1, V + 2]]
+    faces += [[int(f[7, 0]), int(f[7, 1]), int(f[7, 2]), int(f[9, 1])]]
+    faces += [[int(f[11, 0]), int(f[11, 1]), int(f[11, 2]), int(f[13, 2]), int(f[15, 0])]]
+    faces += [[3], [4, 6]]
+    return pos, faces, col

@@ -54,9 +54,7 @@ def scenes():
 @pytest.fixture(scope="session")
 def oracle():
     import pyoracle
-    if not os.path.exists(pyoracle.ORACLE_SO) or \
-            os.path.getmtime(pyoracle.ORACLE_SO) < os.path.getmtime(os.path.join(ORACLE_DIR, "svo_oracle.c")):
-        subprocess.run(["make", "-s", "-C", ORACLE_DIR, "liboracle.so"], check=True)
+    subprocess.run(["make", "-s", "-C", ORACLE_DIR, "liboracle.so"], check=True)  # make decides staleness
     return pyoracle.Oracle()
 
 
@@ -78,6 +76,7 @@ def golden():
         "dragon": np.load(os.path.join(GOLDEN, "dragon.npz")),
         "builds": np.load(os.path.join(GOLDEN, "builds.npz")),
         "codec": np.load(os.path.join(GOLDEN, "codec.npz")),
+        "ply": np.load(os.path.join(GOLDEN, "ply.npz")),
     }
 
 
@@ -96,3 +95,19 @@ def cuda():
     if not torch.cuda.is_available():
         pytest.fail("CUDA device required for gpu-marked tests")
     return torch
+
+
+def golden_ply(golden):
+    """Yields (mesh, side, threads, mem, words, center) for ply.npz; mesh
+    holds pos, faces (index lists), colors (float) and normals (or None)."""
+    g = golden["ply"]
+    flat = g["faces"].tolist()
+    faces, i = [], 0
+    while i < len(flat):
+        faces.append(flat[i + 1:i + 1 + flat[i]])
+        i += 1 + flat[i]
+    wo = g["word_offsets"]
+    for k, (side, threads, mem, with_n, binary) in enumerate(g["meta"].tolist()):
+        mesh = {"pos": g["pos"], "faces": faces, "colors": g["colors"].astype(np.float32),
+                "colors_u8": g["colors"], "normals": g["normals"] if with_n else None, "binary": bool(binary)}
+        yield mesh, int(side), int(threads), int(mem), g["words"][wo[k]:wo[k + 1]], g["centers"][k]

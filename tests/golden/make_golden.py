@@ -12,6 +12,10 @@ Outputs (all produced by the reference's own code through oracle/_ref):
                grids covering odd dimensions, small memory budgets (several
                cache blocks, an odd last slice, far pointers) and empty grids
   codec.npz    compressMaterial / decompressMaterial / invSqrt samples
+  ply.npz      VoxelOctree(VoxelData(PlyLoader(path), side, mem)) word streams
+               for a seeded edge-case mesh (displaced icosphere plus
+               degenerate triangles and polygons; the mesh arrays are stored
+               too) over thread counts, sides and memory budgets
 """
 import hashlib
 import importlib.util
@@ -30,6 +34,16 @@ scenes = importlib.util.module_from_spec(spec)
 spec.loader.exec_module(scenes)
 
 OUT = os.path.dirname(os.path.abspath(__file__))
+
+# (side, threads, mem, with_normals, binary): PLY builds of the edge-case mesh
+PLY_CASES = [
+    (64, 4, 1 << 30, False, True),
+    (64, 16, 5 * 16 ** 3 + 3000, False, True),   # 16^3 cache blocks
+    (96, 3, 5 * 32 ** 3 + 40000, True, True),    # file normals, 32^3 blocks
+    (37, 8, 1 << 30, False, False),              # ascii, odd side
+    (44, 8, 5 * 8 ** 3 + 2000, False, True),     # 8^3 blocks, odd depth (dropped slices)
+    (65, 1, 5 * 16 ** 3 + 3000, True, False),
+]
 
 # (w, h, d, density, mem, seed)
 BUILD_CASES = [
@@ -110,7 +124,24 @@ def main():
                         dec_n=np.array([d[0] for d in dec], np.float32),
                         dec_shade=np.array([d[1] for d in dec], np.float32),
                         isqrt_x=xs, isqrt_y=np.array([R.inv_sqrt(x) for x in xs], np.float32))
-    for f in ("dragon.npz", "builds.npz", "codec.npz"):
+    # ---- PLY builds
+    pos, faces, col = scenes.edge_case_mesh(3, 4)
+    nrm = np.random.default_rng(17).normal(size=pos.shape).astype(np.float32)
+    flat = np.asarray([x for fc in faces for x in (len(fc), *fc)], np.int32)
+    wlist, centers, meta = [], [], []
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "m.ply")
+        for (side, threads, mem, with_n, binary) in PLY_CASES:
+            scenes.write_ply(path, pos, faces, colors=col, normals=nrm if with_n else None, binary=binary)
+            ws, c = R.build_ply(path, side, mem, threads=threads)
+            wlist.append(ws)
+            centers.append(c)
+            meta.append((side, threads, mem, int(with_n), int(binary)))
+    np.savez_compressed(os.path.join(OUT, "ply.npz"), pos=pos, faces=flat, colors=col, normals=nrm,
+                        meta=np.array(meta, np.uint64),
+                        word_offsets=np.cumsum([0] + [x.size for x in wlist]).astype(np.uint64),
+                        words=np.concatenate(wlist), centers=np.array(centers, np.float32))
+    for f in ("dragon.npz", "builds.npz", "codec.npz", "ply.npz"):
         print(f, os.path.getsize(os.path.join(OUT, f)))
 
 

@@ -57,6 +57,28 @@ def test_build_argument_checks_before_device_use(svo):
                                           ctypes.byref(h)) == svo.SVO_ERR_MEMORY
 
 
+def test_ply_errors_before_device_use(svo, scenes, tmp_path):
+    h = ctypes.c_void_p()
+    assert svo.lib.svo_mesh_load_ply(str(tmp_path / "missing.ply").encode(), ctypes.byref(h)) == svo.SVO_ERR_IO
+    bad = tmp_path / "bad.ply"
+    bad.write_bytes(b"ply\nformat ascii 1.0\nelement vertex 1\nproperty float x\nend_header\n0\n")
+    assert svo.lib.svo_mesh_load_ply(str(bad).encode(), ctypes.byref(h)) == svo.SVO_ERR_FORMAT
+    assert b"triangles and vertices" in svo.lib.svo_last_error()
+    trunc = tmp_path / "trunc.ply"
+    pos, faces, col = scenes.edge_case_mesh(1, 1)
+    scenes.write_ply(str(trunc), pos, faces, colors=col)
+    trunc.write_bytes(trunc.read_bytes()[:-7])
+    assert svo.lib.svo_mesh_load_ply(str(trunc).encode(), ctypes.byref(h)) == svo.SVO_ERR_FORMAT
+    with pytest.raises(svo.SvoError) as e:  # index past the vertex array
+        svo.PlyLoader.from_arrays(pos, faces + [[0, 1, pos.shape[0]]])
+    assert e.value.code == svo.SVO_ERR_FORMAT
+    nan = pos.copy()
+    nan[3, 1] = np.nan
+    with pytest.raises(svo.SvoError) as e:
+        svo.PlyLoader.from_arrays(nan, faces)
+    assert e.value.code == svo.SVO_ERR_FORMAT
+
+
 def test_oct_read_reference_dragon_fixture_roundtrip(svo, oracle, golden, tmp_path):
     g = golden["dragon"]
     p = str(tmp_path / "d.oct")

@@ -1,0 +1,123 @@
+"""GPU mesh build (svo_octree_build_ply / svo_octree_build_mesh) against the
+oracle's restatement of PlyLoader + VoxelData(PlyLoader*) + VoxelOctree and
+against the reference's own words in tests/golden/ply.npz: bit-exact word
+streams and centres."""
+import numpy as np
+import pytest
+
+from conftest import golden_ply
+
+pytestmark = pytest.mark.gpu
+
+
+def _swap_floats(v):
+    return np.asarray(v, np.float32).astype(">f4").view("<f4").astype(np.float32)
+
+
+def _be_floats(v):
+    g = np.asarray(v, np.float32).astype(">f4").view("<f4")
+    with np.errstate(invalid="ignore"):
+        g = g.astype(np.float64).astype(np.float32)
+    return g.view(">f4").astype(np.float32)
+
+
+def _gpu_build(svo, path, side, threads, mem):
+    tree = svo.VoxelOctree(svo.VoxelData(svo.PlyLoader(path), side, mem, threads))
+    return tree.words(), tree.center(), tree
+
+
+def test_golden_ply_builds(cuda, svo, scenes, golden, tmp_path):
+    n = 0
+    for mesh, side, threads, mem, words, center in golden_ply(golden):
+        path = str(tmp_path / "g.ply")
+        scenes.write_ply(path, mesh["pos"], mesh["faces"], colors=mesh["colors_u8"], normals=mesh["normals"],
+                         binary=mesh["binary"])
+        w, c, tree = _gpu_build(svo, path, side, threads, mem)
+        assert np.array_equal(w, words), (side, threads, mem)
+        assert np.array_equal(c, center)
+        n += 1
+    assert n == 6
+
+
+@pytest.mark.parametrize("level,side,threads,mem", [
+    (3, 64, 4, 1 << 30), (3, 64, 1, 1 << 30), (4, 128, 16, 1 << 30), (4, 128, 8, 5 * 16 ** 3 + 3000),
+    (4, 200, 6, 3 << 20), (3, 45, 8, 5 * 8 ** 3 + 2000), (5, 256, 16, 1 << 30), (5, 256, 8, 1 << 20),
+    (2, 16, 2, 1 << 30), (3, 9, 3, 1 << 30),
+])
+def test_build_matches_oracle(cuda, svo, oracle, scenes, tmp_path, level, side, threads, mem):
+    pos, faces, col = scenes.edge_case_mesh(level, side + threads)
+    path = str(tmp_path / "m.ply")
+    scenes.write_ply(path, pos, faces, colors=col)
+    w, c, tree = _gpu_build(svo, path, side, threads, mem)
+    ow, oc = oracle.build_mesh(pos, faces, side, threads, mem, colors=col.astype(np.float32))
+    assert np.array_equal(w, ow), (w.size, ow.size)
+    assert np.array_equal(c, oc)
+    nd, nl = tree.validate()
+    assert nl > 0
+
+
+def test_formats_and_normals(cuda, svo, oracle, scenes, tmp_path):
+    pos, faces, col = scenes.edge_case_mesh(3, 21)
+    nrm = np.random.default_rng(4).normal(size=pos.shape).astype(np.float32)
+    ow, oc = oracle.build_mesh(pos, faces, 96, 8, 1 << 30, colors=col.astype(np.float32), normals=nrm)
+    for binary in (True, False):
+        path = str(tmp_path / ("b.ply" if binary else "a.ply"))
+        scenes.write_ply(path, pos, faces, colors=col, normals=nrm, binary=binary)
+        w, c, _ = _gpu_build(svo, path, 96, 8, 1 << 30)
+        assert np.array_equal(w, ow) and np.array_equal(c, oc)
+    # big-endian: the reference's double conversion, swapped colours
+    path = str(tmp_path / "be.ply")
+    scenes.write_ply(path, pos, faces, colors=col, big_endian=True)
+    w, c, _ = _gpu_build(svo, path, 64, 4, 1 << 30)
+    bw, bc = oracle.build_mesh(_be_floats(pos), faces, 64, 4, 1 << 30, colors=_swap_floats(col.astype(np.float32)))
+    assert np.array_equal(w, bw) and np.array_equal(c, bc)
+    # no colour channels: 255
+    path = str(tmp_path / "nc.ply")
+    scenes.write_ply(path, pos, faces)
+    w, c, _ = _gpu_build(svo, path, 64, 4, 1 << 30)
+    nw, _ = oracle.build_mesh(pos, faces, 64, 4, 1 << 30)
+    assert np.array_equal(w, nw)
+
+
+def test_from_arrays_matches_file(cuda, svo, scenes, tmp_path):
+    pos, faces, col = scenes.edge_case_mesh(3, 5)
+    path = str(tmp_path / "m.ply")
+    scenes.write_ply(path, pos, faces, colors=col)
+    w, c, _ = _gpu_build(svo, path, 80, 4, 1 << 30)
+    loader = svo.PlyLoader.from_arrays(pos, faces, colors=col.astype(np.float32))
+    assert loader.num_triangles == svo.PlyLoader(path).num_triangles
+    tree = svo.VoxelOctree(svo.VoxelData(loader, 80, 1 << 30, 4))
+    assert np.array_equal(tree.words(), w) and np.array_equal(tree.center(), c)
+
+
+def test_workload_mesh_matches_oracle(cuda, svo, oracle, scenes, tmp_path):
+    """The bench's mesh (level-7 displaced icosphere, 327,680 triangles) at
+    1024^3 with 16 sub-blocks per 512^3 cache block (1 GiB budget)."""
+    pos, f, col = scenes.displaced_icosphere(7, 3)
+    path = str(tmp_path / "ico7.ply")
+    scenes.write_ply(path, pos, f, colors=col)
+    w, c, tree = _gpu_build(svo, path, 1024, 16, 1 << 30)
+    ow, oc = oracle.build_mesh(pos, f, 1024, 16, 1 << 30, colors=col.astype(np.float32))
+    assert np.array_equal(w, ow) and np.array_equal(c, oc)
+    assert w.size > 1_000_000
+
+
+def test_build_then_trace(cuda, svo, oracle, scenes, tmp_path):
+    pos, f, col = scenes.displaced_icosphere(5, 8)
+    path = str(tmp_path / "m.ply")
+    scenes.write_ply(path, pos, f, colors=col)
+    w, c, tree = _gpu_build(svo, path, 256, 8, 1 << 30)
+    cam = scenes.orbit_cameras(1, 3, c, radius=1.5)[0]
+    rays = scenes.camera_rays(cam, 160, 120)
+    host = tree.trace_host(rays, light=scenes.headlight(cam))
+    ref = oracle.raymarch(w, rays, light=scenes.headlight(cam), threads=4)
+    assert np.array_equal(host["hit"], ref["hit"]) and np.array_equal(host["word"], ref["word"])
+    assert (ref["hit"] == 1).mean() > 0.2
+
+
+def test_budget_too_small(cuda, svo, scenes):
+    pos, faces, col = scenes.edge_case_mesh(2, 1)
+    loader = svo.PlyLoader.from_arrays(pos, faces)
+    with pytest.raises(svo.SvoError) as e:
+        svo.VoxelOctree(svo.VoxelData(loader, 64, 10, 4))
+    assert e.value.code == svo.SVO_ERR_MEMORY
