@@ -59,7 +59,7 @@ def parse():
     p.add_argument("--height", type=int, default=H_PIX)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--config", type=int, default=1, choices=[1, 3, 4],
+    p.add_argument("--config", type=int, default=1, choices=[1, 2, 3, 4],
                    help="1: plain traversal (headline); 3: batched vs plain over 96 octrees and views; "
                         "4: differentiable shading fwd+bwd")
     p.add_argument("--no-extra", action="store_true", help="skip the config-3 batched comparison in the default run")
@@ -244,6 +244,20 @@ def run_ours(args):
                               "gpu_launches": 2 * r4["steps"]}))
         return
 
+    if args.config == 2:
+        r2 = run_config2(args, torch, svo, scenes, check=not args.no_cpu)
+        if rank == 0:
+            print(json.dumps({"metric": "voxels/s", "value": r2["voxels_per_s"], "unit": "voxels/s",
+                              "n_gpus": world, "steps": r2["steps"], "warmup": r2["warmup"],
+                              "ms_per_step": r2["build_ms"], "higher_is_better": True, "scaling": "weak",
+                              "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                              "config": {"workload": "mesh build: " + r2["workload"]},
+                              "e2e": {"value": r2["e2e_voxels_per_s"], "unit": "voxels/s",
+                                      "h2d_bytes_per_step": r2["ply_bytes"], "d2h_bytes_per_step": 0},
+                              "mesh_build": r2, "cpu_baseline": r2["cpu_baseline"],
+                              "gpu_launches": r2["launches_per_build"] * r2["steps"]}))
+        return
+
     if args.config == 3:
         r3 = run_config3(args, torch, svo, scenes)
         if rank == 0:
@@ -389,13 +403,15 @@ def run_ours(args):
                          "VoxelOctree::raymarch, %d threads)" % (ncam, len(cam_slices), n, secs, thr)}
         del words
 
-    extra = extra4 = None
+    extra = extra2 = extra4 = None
     if not args.no_extra and world == 1:
         del prim, shadow, out_p, out_s, ref_p, ref_s, tree
         torch.cuda.empty_cache()
         extra = run_config3(args, torch, svo, scenes)
         torch.cuda.empty_cache()
         extra4 = run_config4(args, torch, svo, scenes)
+        torch.cuda.empty_cache()
+        extra2 = run_config2(args, torch, svo, scenes, steps=3, warmup=1, check=not args.no_cpu)
 
     if rank == 0:
         line = {
@@ -422,6 +438,7 @@ def run_ours(args):
                         "config": cfg.as_dict(), "exact_vs_value_path": bool(exact_batched)},
             "batched_vs_plain": extra,
             "fwd_bwd": extra4,
+            "mesh_build": extra2,
             "build": {"build_s": round(info["build_s"], 3), "scene_gen_s": round(info["gen_s"], 3),
                       "voxels_per_s": round(info["voxels"] / info["build_s"], 1)},
             "kernel_ms": {"primary": round(t_prim_avg, 3), "shadow": round(sum(t_shadow) / len(t_shadow), 3)},
@@ -512,6 +529,109 @@ def run_config3(args, torch, svo, scenes, tune_cache=None):
             "speedup": round(ms_plain / ms_batched, 3), "exact_hit_parity": bool(exact),
             "config": cfg.as_dict(), "autotune_s": round(tune_s, 1), "setup_s": round(setup_s, 1),
             "launches": {"plain": len(views), "batched": 1}}
+
+
+MESH_LEVEL, MESH_SEED, MESH_SIDE, MESH_THREADS, MESH_MEM = 7, 3, 1024, 16, 1 << 30
+
+
+def profile_kernels(torch, fn):
+    """Kernel launches of one untimed call of fn, from the CUDA activity
+    trace: (launch count, {kernel: [launches, device ms]}) for the ten
+    longest kernels; memcpy and memset records are not kernels."""
+    try:
+        from torch.profiler import ProfilerActivity, profile
+        torch.cuda.synchronize()
+        with profile(activities=[ProfilerActivity.CUDA]) as prof:
+            r = fn()
+            torch.cuda.synchronize()
+        del r
+        from torch.autograd import DeviceType
+        rows = {}
+        for ev in prof.key_averages():
+            name = ev.key
+            if ev.device_type != DeviceType.CUDA or name.startswith(("Memcpy", "Memset")):
+                continue
+            t = getattr(ev, "device_time_total", None)
+            if t is None:
+                t = getattr(ev, "cuda_time_total", 0.0)
+            rows[name] = [int(ev.count), round(t / 1e3, 4)]
+        total = sum(v[0] for v in rows.values())
+        top = dict(sorted(rows.items(), key=lambda kv: -kv[1][1])[:10])
+        return total, {(k[:60] + ".." if len(k) > 62 else k): v for k, v in top.items()}
+    except Exception as e:  # the profiler is optional here
+        return None, {"unavailable": repr(e)[:120]}
+
+
+def run_config2(args, torch, svo, scenes, steps=None, warmup=None, check=True):
+    """Mesh build: a level-7 icosphere (327,680 triangles) radially displaced
+    by 4-octave seeded noise (15% of the radius), per-vertex RGB ~U[0,255],
+    written as a binary little-endian PLY (float xyz, uchar rgb); voxelized at
+    1024^3 with the reference's triangle/box rule and built into an octree,
+    with the reference's result parameters pinned: 16 worker threads (16
+    sub-blocks per cache block) and a 1 GiB budget (512^3 cache blocks).
+    Each step is one VoxelOctree(VoxelData(PlyLoader, side, mem, threads))
+    from the device-resident mesh; e2e adds reading, parsing and uploading
+    the PLY file (svo_octree_build_ply)."""
+    import tempfile
+    steps = steps or args.steps
+    warmup = args.warmup if warmup is None else warmup
+    pos, faces, col = scenes.displaced_icosphere(MESH_LEVEL, MESH_SEED)
+    tmp = tempfile.mkdtemp(prefix="svo_mesh_")
+    path = os.path.join(tmp, "icosphere7.ply")
+    scenes.write_ply(path, pos, faces, colors=col)
+    ply_bytes = os.path.getsize(path)
+    t0 = time.perf_counter()
+    loader = svo.PlyLoader(path)
+    load_s = time.perf_counter() - t0
+    data = svo.VoxelData(loader, MESH_SIDE, MESH_MEM, MESH_THREADS)
+    times, tree = [], None
+    for k in range(warmup + steps):
+        tree = None
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        tree = svo.VoxelOctree(data)
+        torch.cuda.synchronize()
+        if k >= warmup:
+            times.append(time.perf_counter() - t0)
+    n_desc, n_leaves = tree.validate()
+    words = tree.words()
+    e2e = []
+    for k in range(warmup + steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        t2 = svo.VoxelOctree(svo.VoxelData(svo.PlyLoader(path), MESH_SIDE, MESH_MEM, MESH_THREADS))
+        torch.cuda.synchronize()
+        if k >= warmup:
+            e2e.append(time.perf_counter() - t0)
+        del t2
+    build_s = sorted(times)[len(times) // 2]
+    e2e_s = sorted(e2e)[len(e2e) // 2]
+    launches, kernels = profile_kernels(torch, lambda: svo.VoxelOctree(data))
+    out = {"workload": "level-7 displaced icosphere (327,680 triangles, seed %d) as binary PLY, %d^3, %d threads, "
+                       "1 GiB budget" % (MESH_SEED, MESH_SIDE, MESH_THREADS),
+           "triangles": loader.num_triangles, "voxels": int(n_leaves), "octree_words": int(words.size),
+           "descriptors": int(n_desc), "steps": steps, "warmup": warmup,
+           "build_ms": round(build_s * 1e3, 3), "build_ms_all": [round(t * 1e3, 3) for t in times],
+           "voxels_per_s": round(n_leaves / build_s, 1), "e2e_ms": round(e2e_s * 1e3, 3),
+           "e2e_voxels_per_s": round(n_leaves / e2e_s, 1), "ply_load_ms": round(load_s * 1e3, 3),
+           "ply_bytes": ply_bytes, "launches_per_build": launches, "kernels": kernels, "cpu_baseline": None,
+           "exact_vs_oracle": None}
+    if check:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import pyoracle
+        pyoracle.build_oracle(with_reference=False)
+        oracle = pyoracle.Oracle()
+        t0 = time.perf_counter()
+        ow, oc = oracle.build_mesh(pos, faces, MESH_SIDE, MESH_THREADS, MESH_MEM, colors=col.astype(np.float32))
+        cpu_s = time.perf_counter() - t0
+        out["exact_vs_oracle"] = bool(np.array_equal(ow, words) and np.array_equal(oc, tree.center()))
+        out["cpu_baseline"] = {"value": round(n_leaves / cpu_s, 1), "unit": "voxels/s", "cores": 1, "kind": "port",
+                               "sample": "the full build (oracle/ply_oracle.c, single-threaded restatement of "
+                                         "PlyLoader + VoxelData + VoxelOctree) on the same mesh",
+                               "build_s": round(cpu_s, 3)}
+    os.unlink(path)
+    os.rmdir(tmp)
+    return out
 
 
 def run_config4(args, torch, svo, scenes, n_steps=200):

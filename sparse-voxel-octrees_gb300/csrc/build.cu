@@ -49,8 +49,6 @@ struct GridGeom {
     int drop_last_z;    // 1: voxels at z == d-1 are excluded from the output
     int log_block;      // cache-block edge M = 1 << log_block
     uint8_t *topflag;   // per M-block "has any voxel" (Morton-indexed), or null
-    uint64_t key_base;  // added to every emitted Morton key
-    uint32_t *clear;    // when set (== grid), emitted words are zeroed in place
 };
 
 // Phase 1a: per brick, count voxels that survive (V') and flag M-blocks that
@@ -107,10 +105,8 @@ __global__ void __launch_bounds__(kBrickThreads) k_brick_emit(GridGeom g, uint64
         for (int c = threadIdx.x; c < cells; c += kBrickThreads) {
             int gx = gx0 + (c & (E - 1)), gy = gy0 + ((c >> g.log_brick) & (E - 1)), gz = gz0 + (c >> (2 * g.log_brick));
             uint32_t v = 0;
-            if (gx < g.w && gy < g.h && gz < g.d && !(g.drop_last_z && gz == g.d - 1)) {
-                uint64_t gi = (uint64_t)gx + (uint64_t)g.w * ((uint64_t)gy + (uint64_t)g.h * gz);
-                v = g.clear ? g.clear[gi] : __ldg(g.grid + gi);  // no read-only path for a grid this launch writes
-            }
+            if (gx < g.w && gy < g.h && gz < g.d && !(g.drop_last_z && gz == g.d - 1))
+                v = __ldg(g.grid + (uint64_t)gx + (uint64_t)g.w * ((uint64_t)gy + (uint64_t)g.h * gz));
             tile[c] = v;
         }
         __syncthreads();
@@ -126,7 +122,7 @@ __global__ void __launch_bounds__(kBrickThreads) k_brick_emit(GridGeom g, uint64
         uint32_t total;
         uint32_t pre = block_excl_scan<uint32_t>(cnt, &total);
         uint64_t out = offsets[b] + pre;
-        uint64_t kbase = g.key_base + (b << (3 * g.log_brick));
+        uint64_t kbase = b << (3 * g.log_brick);
         for (int k = 0; k < per; ++k) {
             int m = m0 + k;
             if (m < cells) {
@@ -136,9 +132,6 @@ __global__ void __launch_bounds__(kBrickThreads) k_brick_emit(GridGeom g, uint64
                     keys[out] = kbase | (uint64_t)m;
                     payload[out] = v;
                     ++out;
-                    if (g.clear)
-                        g.clear[(uint64_t)(gx0 + (int)lx) +
-                                (uint64_t)g.w * ((uint64_t)(gy0 + (int)ly) + (uint64_t)g.h * (uint64_t)(gz0 + (int)lz))] = 0;
                 }
             }
         }
@@ -502,48 +495,6 @@ int build_from_sorted_device(const uint64_t *d_keys, const uint32_t *d_payload, 
     return SVO_OK;
 }
 
-int extract_voxels_device(uint32_t *d_grid, int w, int h, int d, int log_extent, uint64_t key_base, int drop_last_z,
-                          int clear, cudaStream_t st, uint64_t **d_keys, uint32_t **d_payload, uint64_t *n) {
-    const int log_brick = log_extent < 4 ? log_extent : 4;
-    const uint64_t n_bricks = 1ull << (3 * (log_extent - log_brick));
-    GridGeom g;
-    g.grid = d_grid;
-    g.w = w;
-    g.h = h;
-    g.d = d;
-    g.log_brick = log_brick;
-    g.drop_last_z = drop_last_z;
-    g.log_block = log_extent;
-    g.topflag = nullptr;
-    g.key_base = key_base;
-    g.clear = clear ? d_grid : nullptr;
-    *d_keys = nullptr;
-    *d_payload = nullptr;
-    *n = 0;
-    DevBuf<uint32_t> bcount;
-    DevBuf<uint64_t> boff;
-    SVO_TRY_ALLOC(bcount.alloc(n_bricks, st));
-    SVO_TRY_ALLOC(boff.alloc(n_bricks, st));
-    unsigned grid1 = (unsigned)(n_bricks < (1ull << 20) ? n_bricks : (1ull << 20));
-    k_brick_count<<<grid1, kBrickThreads, 0, st>>>(g, n_bricks, bcount.p);
-    SVO_LAUNCH_CHECK("k_brick_count");
-    uint64_t N = 0;
-    int rc = scan_to<uint64_t>(bcount.p, boff.p, n_bricks, &N, st);
-    if (rc) return rc;
-    if (N == 0) return SVO_OK;
-    SVO_CUDA_TRY(cudaMallocAsync((void **)d_keys, N * sizeof(uint64_t), st));
-    cudaError_t e = cudaMallocAsync((void **)d_payload, N * sizeof(uint32_t), st);
-    if (e != cudaSuccess) {
-        cudaFreeAsync(*d_keys, st);
-        *d_keys = nullptr;
-        return cuda_fail(e, "device allocation in extraction");
-    }
-    k_brick_emit<<<grid1, kBrickThreads, 0, st>>>(g, n_bricks, bcount.p, boff.p, *d_keys, *d_payload);
-    SVO_LAUNCH_CHECK("k_brick_emit");
-    *n = N;
-    return SVO_OK;
-}
-
 int build_dense_device(const uint32_t *d_grid, int w, int h, int d, int log_side, int log_block, cudaStream_t st,
                        uint32_t **d_words_out, uint64_t *n_words_out) {
     const int D = log_side;
@@ -560,8 +511,6 @@ int build_dense_device(const uint32_t *d_grid, int w, int h, int d, int log_side
     g.drop_last_z = ((d & 1) && log_block >= 2) ? 1 : 0;
     g.log_block = log_block;
     g.topflag = nullptr;
-    g.key_base = 0;
-    g.clear = nullptr;
 
     const uint64_t n_blocks = multi_block ? (1ull << (3 * (D - log_block))) : 0;
     if (n_blocks > (1ull << 27))
@@ -697,8 +646,6 @@ int build_dense_noalloc(const uint32_t *d_grid, int w, int h, int d, int log_sid
     g.drop_last_z = ((d & 1) && log_block >= 2) ? 1 : 0;
     g.log_block = log_block;
     g.topflag = nullptr;
-    g.key_base = 0;
-    g.clear = nullptr;
     if (multi_block) {
         SVO_ARENA_TAKE(tf, uint8_t, n_blocks);
         SVO_CUDA_TRY(cudaMemsetAsync(tf, 0, n_blocks, st));  // the arena keeps the previous call's bytes

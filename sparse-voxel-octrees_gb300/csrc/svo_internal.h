@@ -71,14 +71,6 @@ int build_from_sorted_device(const uint64_t *d_keys, const uint32_t *d_payload, 
                              int log_block, const uint8_t *d_topflag, cudaStream_t st, uint32_t **d_words,
                              uint64_t *n_words);
 
-// Phase 1 of the build over one w x h x d grid (x fastest) inside a
-// 2^log_extent cube: the nonzero words in Morton order, each key offset by
-// key_base; with drop_last_z the z == d-1 slice is left out; with clear the
-// emitted words are zeroed in the grid.  *d_keys / *d_payload are
-// cudaMallocAsync'd on `st` (null when *n == 0); the caller frees them.
-int extract_voxels_device(uint32_t *d_grid, int w, int h, int d, int log_extent, uint64_t key_base, int drop_last_z,
-                          int clear, cudaStream_t st, uint64_t **d_keys, uint32_t **d_payload, uint64_t *n);
-
 // Trace launchers (trace.cu).
 int launch_trace(const svo_octree *oct, const float *d_rays, uint64_t n, float ray_scale, const float light[3],
                  const svo_trace_out &out, cudaStream_t st);

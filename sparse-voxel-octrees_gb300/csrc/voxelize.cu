@@ -24,12 +24,14 @@
 //     triangles in ascending index, the order a sub-block list holds them.
 //  4. Cache blocks in the reference's visiting order (ascending Morton code
 //     of the blocks the lists mark), each against the one persistent
-//     buffer: one CTA per brick, one thread per voxel, folding the brick's
-//     triangles in order with writeTriangleCell's blend
-//     (PlyLoader.cpp:296-336); voxel-box centres are the reference's running
-//     sums (lo - 0.5) * h + h + ... + h, read from a table of those sums.
-//     Then the block's nonzero words are extracted in Morton order and
-//     cleared (build.cu), except a dropped odd last slice.
+//     buffer: one warp per brick folds the brick's triangles in order with
+//     writeTriangleCell's blend (PlyLoader.cpp:296-336), its lanes covering
+//     each triangle's clamped box inside the brick; voxel-box centres are
+//     the reference's running sums (lo - 0.5) * h + h + ... + h, read from a
+//     table of those sums.  Then the block's nonzero words are extracted in
+//     Morton order and cleared, except a dropped odd last slice, from the
+//     bricks that can hold any: the folded ones and those under earlier
+//     blocks' dropped slices.
 //  5. The octree from the Morton-ordered voxels and the block flags
 //     (build_from_sorted_device).
 #include <algorithm>
@@ -61,9 +63,7 @@ namespace {
 // upper (3), padding (3).
 constexpr int kTriFloats = 36;
 constexpr int kTriP = 0, kTriN = 9, kTriC = 18, kTriLo = 27, kTriHi = 30;
-constexpr int kStageFloats = 27;  // p, n, c: what the brick kernel stages
-constexpr int kChunk = 64;        // triangles staged per round in the brick kernel
-constexpr int kBrickCta = 512;    // one thread per voxel of an 8^3 brick
+constexpr int kStageFloats = 27;  // p, n, c: what the fold kernel stages
 
 #define SVO_LAUNCH_OK(name)                                                    \
     do {                                                                       \
@@ -389,7 +389,7 @@ __global__ void k_center_table(int n_l, int K, float h, float *__restrict__ acc)
 
 // ---- 4. per-block brick fold ------------------------------------------------------
 
-struct BlockArgs {
+struct FoldArgs {
     const float *tris;
     const int32_t *box;
     const uint32_t *pair_tri;
@@ -398,8 +398,8 @@ struct BlockArgs {
     uint32_t b_first, b_last;
     int log_e;
     int sub[3];
-    int org[3];   // block origin
-    int buf[3];   // clamped block dims (the buffer's W/H/D for this block)
+    int org[3];  // block origin
+    int buf[3];  // clamped block dims (the buffer's W/H/D for this block)
     const float *acc;
     int K;
     float half;
@@ -467,60 +467,205 @@ __device__ __forceinline__ void write_cell(uint32_t &w, uint32_t &cnt, float cx,
     }
 }
 
-__global__ void __launch_bounds__(kBrickCta) k_block_bricks(BlockArgs a) {
-    __shared__ float sT[kChunk][kStageFloats];
-    __shared__ int sB[kChunk][6];
-    const int E = 1 << a.log_e;
-    const int tid = threadIdx.x;
-    const bool lane_used = tid < E * E * E;
-    const int tx = tid & (E - 1), ty = (tid >> a.log_e) & (E - 1), tz = tid >> (2 * a.log_e);
+constexpr int kFoldWarps = 4;   // warps per CTA of the fold kernel
+constexpr int kFoldChunk = 16;  // triangles a warp stages per round
+
+struct FoldSmem {
+    float T[kFoldChunk][kStageFloats];  // p, n, c
+    int lo[kFoldChunk][3];              // running-sum start: max(triangle box low, sub-block start)
+    int box[kFoldChunk][6];             // brick-local inclusive range of the clamped box
+    float C[kFoldChunk][3][8];          // running centres of the brick's E coordinates per axis
+    uint32_t w[512];                    // the brick's buffer words ...
+    uint8_t cnt[512];                   // ... and counts (PlyLoader::_counts)
+    uint32_t touched[16];
+};
+
+// One warp per brick.  The warp loads the brick's buffer cells, then takes
+// the brick's triangles in list order; for each, its lanes cover the voxels
+// of the triangle's clamped box inside the brick (triangleToVolume's loop
+// nest, PlyLoader.cpp:338-374), test them and fold the hits into the
+// brick's cells (a voxel is folded by one lane per triangle, triangles in
+// order), and finally writes the touched cells back.
+__global__ void __launch_bounds__(kFoldWarps * 32) k_fold_bricks(FoldArgs a) {
+    __shared__ FoldSmem smem[kFoldWarps];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    FoldSmem &sm = smem[wid];
+    const int le = a.log_e, E = 1 << le, E3 = 1 << (3 * le);
     const float hv[3] = {a.half, a.half, a.half};
-    for (uint32_t j = a.b_first + blockIdx.x; j < a.b_last; j += gridDim.x) {
+    const int end0 = a.org[0] + a.buf[0], end1 = a.org[1] + a.buf[1], end2 = a.org[2] + a.buf[2];
+    const uint32_t nwarps = gridDim.x * kFoldWarps;
+    for (uint32_t j = a.b_first + blockIdx.x * kFoldWarps + wid; j < a.b_last; j += nwarps) {
         const uint32_t key = a.bkey[j];
-        const int x = (int)(compact3(key) << a.log_e) + tx;
-        const int y = (int)(compact3((uint64_t)key >> 1) << a.log_e) + ty;
-        const int z = (int)(compact3((uint64_t)key >> 2) << a.log_e) + tz;
-        const bool active = lane_used && x < a.org[0] + a.buf[0] && y < a.org[1] + a.buf[1] &&
-                            z < a.org[2] + a.buf[2] && x >= a.org[0] && y >= a.org[1] && z >= a.org[2];
-        // start of this voxel's sub-block: PlyLoader's clamp _bufferX + offX
-        const int cx0 = (x / a.sub[0]) * a.sub[0], cy0 = (y / a.sub[1]) * a.sub[1], cz0 = (z / a.sub[2]) * a.sub[2];
-        const uint64_t bi = (uint64_t)(x - a.org[0]) +
-                            (uint64_t)a.buf[0] * ((uint64_t)(y - a.org[1]) + (uint64_t)a.buf[1] * (uint64_t)(z - a.org[2]));
-        uint32_t w = 0, cnt = 0;
-        bool loaded = false;
+        const int ox = (int)(compact3(key) << le), oy = (int)(compact3((uint64_t)key >> 1) << le),
+                  oz = (int)(compact3((uint64_t)key >> 2) << le);
+        const int sx = (ox / a.sub[0]) * a.sub[0], sy = (oy / a.sub[1]) * a.sub[1], sz = (oz / a.sub[2]) * a.sub[2];
+        __syncwarp();
+        for (int i = lane; i < E3; i += 32) {
+            int x = ox + (i & (E - 1)), y = oy + ((i >> le) & (E - 1)), z = oz + (i >> (2 * le));
+            uint32_t wv = 0, cv = 0;
+            if (x < end0 && y < end1 && z < end2) {
+                uint64_t bi = (uint64_t)(x - a.org[0]) +
+                              (uint64_t)a.buf[0] * ((uint64_t)(y - a.org[1]) + (uint64_t)a.buf[1] * (uint64_t)(z - a.org[2]));
+                wv = a.data[bi];
+                cv = a.counts[bi];
+            }
+            sm.w[i] = wv;
+            sm.cnt[i] = (uint8_t)cv;
+        }
+        if (lane < 16) sm.touched[lane] = 0;
         const uint32_t s0 = a.bstart[j], s1 = a.bstart[j + 1];
-        for (uint32_t c0 = s0; c0 < s1; c0 += kChunk) {
-            const int nc = (int)min((uint32_t)kChunk, s1 - c0);
-            __syncthreads();
-            for (int i = tid; i < nc * kStageFloats; i += blockDim.x) {
+        for (uint32_t c0 = s0; c0 < s1; c0 += kFoldChunk) {
+            const int nc = (int)min((uint32_t)kFoldChunk, s1 - c0);
+            __syncwarp();
+            for (int i = lane; i < nc * kStageFloats; i += 32) {
                 int q = i / kStageFloats, f = i - q * kStageFloats;
-                sT[q][f] = a.tris[(uint64_t)a.pair_tri[c0 + q] * kTriFloats + f];
+                sm.T[q][f] = a.tris[(uint64_t)a.pair_tri[c0 + q] * kTriFloats + f];
             }
-            for (int i = tid; i < nc * 6; i += blockDim.x) {
-                int q = i / 6, f = i - q * 6;
-                sB[q][f] = a.box[(uint64_t)a.pair_tri[c0 + q] * 6 + f];
-            }
-            __syncthreads();
-            if (!active) continue;
-            for (int q = 0; q < nc; ++q) {
-                const int lx = max(sB[q][0], cx0), ly = max(sB[q][1], cy0), lz = max(sB[q][2], cz0);
-                if (x < lx || y < ly || z < lz || x > sB[q][3] || y > sB[q][4] || z > sB[q][5]) continue;
-                const float fx = a.acc[(uint64_t)lx * a.K + (x - lx)];
-                const float fy = a.acc[(uint64_t)ly * a.K + (y - ly)];
-                const float fz = a.acc[(uint64_t)lz * a.K + (z - lz)];
-                if (!tri_box(fx, fy, fz, hv, &sT[q][kTriP])) continue;
-                if (!loaded) {
-                    w = a.data[bi];
-                    cnt = a.counts[bi];
-                    loaded = true;
+            if (lane < nc) {
+                const int32_t *bx = a.box + (uint64_t)a.pair_tri[c0 + lane] * 6;
+                const int o[3] = {ox, oy, oz}, st3[3] = {sx, sy, sz}, en[3] = {end0, end1, end2};
+#pragma unroll
+                for (int ax = 0; ax < 3; ++ax) {
+                    int lo = max(bx[ax], st3[ax]);       // PlyLoader.cpp:344-346
+                    int hi = min(bx[3 + ax], en[ax] - 1);  // :347-349 (the sub-block end lies past the brick)
+                    sm.lo[lane][ax] = lo;
+                    sm.box[lane][ax] = max(lo, o[ax]) - o[ax];
+                    sm.box[lane][3 + ax] = min(hi, o[ax] + E - 1) - o[ax];
                 }
-                write_cell(w, cnt, fx, fy, fz, &sT[q][0]);
+            }
+            __syncwarp();
+            for (int i = lane; i < nc * 3 * E; i += 32) {
+                int q = i / (3 * E), r = i - q * 3 * E, ax = r / E, k = r - ax * E;
+                int ov = ax == 0 ? ox : (ax == 1 ? oy : oz);
+                int lo = sm.lo[q][ax];
+                float c = 0.0f;
+                if (k >= sm.box[q][ax] && k <= sm.box[q][3 + ax]) c = a.acc[(uint64_t)lo * a.K + (ov + k - lo)];
+                sm.C[q][ax][k] = c;
+            }
+            __syncwarp();
+            for (int q = 0; q < nc; ++q) {
+                const int bx0 = sm.box[q][0], by0 = sm.box[q][1], bz0 = sm.box[q][2];
+                const int nx = sm.box[q][3] - bx0 + 1, ny = sm.box[q][4] - by0 + 1, nz = sm.box[q][5] - bz0 + 1;
+                if (nx <= 0 || ny <= 0 || nz <= 0) continue;  // warp-uniform
+                const int n = nx * ny * nz;
+                for (int v = lane; v < n; v += 32) {
+                    const int r = v / nx;
+                    const int ix = bx0 + (v - r * nx), iy = by0 + r % ny, iz = bz0 + r / ny;
+                    const float fx = sm.C[q][0][ix], fy = sm.C[q][1][iy], fz = sm.C[q][2][iz];
+                    if (!tri_box(fx, fy, fz, hv, &sm.T[q][kTriP])) continue;
+                    const int idx = ix + (iy << le) + (iz << (2 * le));
+                    uint32_t wv = sm.w[idx], cv = sm.cnt[idx];
+                    write_cell(wv, cv, fx, fy, fz, &sm.T[q][0]);
+                    sm.w[idx] = wv;
+                    sm.cnt[idx] = (uint8_t)cv;
+                    atomicOr(&sm.touched[idx >> 5], 1u << (idx & 31));
+                }
+                __syncwarp();
             }
         }
-        if (loaded) {
-            a.data[bi] = w;
-            a.counts[bi] = (uint8_t)cnt;
+        __syncwarp();
+        for (int i = lane; i < E3; i += 32) {
+            if (!((sm.touched[i >> 5] >> (i & 31)) & 1u)) continue;
+            int x = ox + (i & (E - 1)), y = oy + ((i >> le) & (E - 1)), z = oz + (i >> (2 * le));
+            uint64_t bi = (uint64_t)(x - a.org[0]) +
+                          (uint64_t)a.buf[0] * ((uint64_t)(y - a.org[1]) + (uint64_t)a.buf[1] * (uint64_t)(z - a.org[2]));
+            a.data[bi] = sm.w[i];
+            a.counts[bi] = sm.cnt[i];
         }
+    }
+}
+
+// Bricks of the block (edge E, Morton-indexed within the block) that may
+// hold a nonzero buffer word: those this block folded ...
+__global__ void k_mark_folded(const uint32_t *__restrict__ bkey, uint32_t first, uint32_t last, int log_e, int ox,
+                              int oy, int oz, uint8_t *__restrict__ dirty, uint64_t n_dirty) {
+    uint32_t j = first + blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= last) return;
+    uint32_t key = bkey[j];
+    uint32_t x = ((compact3(key) << log_e) - ox) >> log_e;
+    uint32_t y = ((compact3((uint64_t)key >> 1) << log_e) - oy) >> log_e;
+    uint32_t z = ((compact3((uint64_t)key >> 2) << log_e) - oz) >> log_e;
+    uint64_t m = morton3(x, y, z);
+    if (m < n_dirty) dirty[m] = 1;
+}
+
+// ... and those holding a buffer index of an earlier block's dropped slice
+// ([s0, s1) flat), read in this block's w x h x d layout.
+__global__ void k_mark_range(uint64_t s0, uint64_t s1, int w, int h, int d, int log_e, uint8_t *__restrict__ dirty,
+                             uint64_t n_dirty) {
+    uint64_t i = s0 + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= s1) return;
+    uint64_t x = i % (uint64_t)w, y = (i / (uint64_t)w) % (uint64_t)h, z = i / ((uint64_t)w * (uint64_t)h);
+    if (z >= (uint64_t)d) return;
+    uint64_t m = morton3((uint32_t)(x >> log_e), (uint32_t)(y >> log_e), (uint32_t)(z >> log_e));
+    if (m < n_dirty) dirty[m] = 1;
+}
+
+__global__ void k_compact_u8(const uint8_t *__restrict__ flag, uint64_t n, const uint32_t *__restrict__ idx,
+                             uint32_t *__restrict__ out) {
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && flag[i]) out[idx[i]] = (uint32_t)i;
+}
+
+struct ExtractArgs {
+    const uint32_t *cand;  // candidate bricks (Morton index within the block), ascending
+    uint32_t n_cand;
+    int log_e;
+    int buf[3];
+    int drop;              // the z == buf[2]-1 slice is never read (VoxelData.cpp:163-170)
+    uint64_t key_base;     // Morton key of the block's first voxel
+    uint32_t *data;
+};
+
+// Voxel m (local Morton index) of candidate brick c: buffer index, or
+// ~0 when the voxel lies outside the block or in a dropped slice.
+__device__ __forceinline__ uint64_t cand_cell(const ExtractArgs &a, uint32_t c, uint32_t m) {
+    const int le = a.log_e;
+    int x = (int)((compact3(c) << le) + compact3(m)), y = (int)((compact3((uint64_t)c >> 1) << le) + compact3((uint64_t)m >> 1));
+    int z = (int)((compact3((uint64_t)c >> 2) << le) + compact3((uint64_t)m >> 2));
+    if (x >= a.buf[0] || y >= a.buf[1] || z >= a.buf[2] || (a.drop && z == a.buf[2] - 1)) return ~0ull;
+    return (uint64_t)x + (uint64_t)a.buf[0] * ((uint64_t)y + (uint64_t)a.buf[1] * (uint64_t)z);
+}
+
+// One warp per candidate brick: its occupied voxels.
+__global__ void k_cand_count(ExtractArgs a, uint32_t *__restrict__ count) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (c >= a.n_cand) return;
+    const uint32_t key = a.cand[c], E3 = 1u << (3 * a.log_e);
+    uint32_t n = 0;
+    for (uint32_t m = lane; m < E3; m += 32) {
+        uint64_t bi = cand_cell(a, key, m);
+        if (bi != ~0ull && a.data[bi]) ++n;
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
+    if (lane == 0) count[c] = n;
+}
+
+// One warp per candidate brick: (key, word) of its occupied voxels in
+// Morton order at off[c], and the emitted cells cleared (the walk reads
+// them with getVoxelDestructive).
+__global__ void k_cand_emit(ExtractArgs a, const uint64_t *__restrict__ off, uint64_t *__restrict__ keys,
+                            uint32_t *__restrict__ payload) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (c >= a.n_cand) return;
+    const uint32_t key = a.cand[c], E3 = 1u << (3 * a.log_e);
+    uint64_t base = off[c];
+    const uint32_t lt = (1u << lane) - 1u;
+    for (uint32_t m0 = 0; m0 < E3; m0 += 32) {
+        const uint32_t m = m0 + lane;
+        uint64_t bi = m < E3 ? cand_cell(a, key, m) : ~0ull;
+        uint32_t v = bi != ~0ull ? a.data[bi] : 0u;
+        uint32_t ball = __ballot_sync(0xffffffffu, v != 0);
+        if (v) {
+            uint64_t o = base + __popc(ball & lt);
+            keys[o] = a.key_base + ((uint64_t)key << (3 * a.log_e)) + m;
+            payload[o] = v;
+            a.data[bi] = 0;
+        }
+        base += __popc(ball);
     }
 }
 
@@ -811,62 +956,119 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
     SVO_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
 
     // 4. blocks in order: fold, then extract (and clear) the block's voxels
-    std::vector<uint64_t *> part_keys;
-    std::vector<uint32_t *> part_pay;
-    std::vector<uint64_t> part_n;
-    struct PartsGuard {
-        std::vector<uint64_t *> &k;
-        std::vector<uint32_t *> &p;
-        cudaStream_t st;
-        ~PartsGuard() {
-            for (auto x : k) cudaFreeAsync(x, st);
-            for (auto x : p) cudaFreeAsync(x, st);
-        }
-    } parts_guard{part_keys, part_pay, st};
-    uint64_t N = 0;
+    const uint64_t n_e = 1ull << (3 * (lb - g.log_e));  // bricks per block
+    Dev<uint8_t> dirty;
+    Dev<uint32_t> d32, didx, cand, ccount;
+    Dev<uint64_t> coff;
+    SVO_ALLOC(dirty, n_e);
+    SVO_ALLOC(d32, n_e);
+    SVO_ALLOC(didx, n_e);
+    SVO_ALLOC(cand, n_e);
+    SVO_ALLOC(ccount, n_e);
+    SVO_ALLOC(coff, n_e);
+    std::vector<std::pair<uint64_t, uint64_t>> ghosts;  // flat ranges of the dropped slices so far
+    uint64_t ghost_len = 0;
+    Dev<uint64_t> keys;
+    Dev<uint32_t> pay;
+    uint64_t cap = std::max<uint64_t>(1 << 20, n_pairs * 8), N = 0;
+    SVO_ALLOC(keys, cap);
+    SVO_ALLOC(pay, cap);
+    const unsigned fold_grid = (unsigned)sms * 8;
     for (const BlockJob &j : jobs) {
-        BlockArgs ba;
-        ba.org[0] = (int)(compact3(j.morton) << lb);
-        ba.org[1] = (int)(compact3((uint64_t)j.morton >> 1) << lb);
-        ba.org[2] = (int)(compact3((uint64_t)j.morton >> 2) << lb);
+        FoldArgs fa;
+        fa.org[0] = (int)(compact3(j.morton) << lb);
+        fa.org[1] = (int)(compact3((uint64_t)j.morton >> 1) << lb);
+        fa.org[2] = (int)(compact3((uint64_t)j.morton >> 2) << lb);
         bool inside = true;
         for (int k = 0; k < 3; ++k) {
-            ba.buf[k] = std::min(B, dims[k] - ba.org[k]);
-            ba.sub[k] = sub[k];
-            if (ba.buf[k] <= 0) inside = false;
+            fa.buf[k] = std::min(B, dims[k] - fa.org[k]);
+            fa.sub[k] = sub[k];
+            if (fa.buf[k] <= 0) inside = false;
         }
         if (!inside) continue;  // VoxelData::prepareDataAccess returns early
         if (j.last > j.first) {
-            ba.tris = m->d_tris;
-            ba.box = box.p;
-            ba.pair_tri = stri;
-            ba.bkey = bkey.p;
-            ba.bstart = bstart.p;
-            ba.b_first = j.first;
-            ba.b_last = j.last;
-            ba.log_e = g.log_e;
-            ba.acc = acc.p;
-            ba.K = K;
-            ba.half = 0.5f * hx;
-            ba.data = data.p;
-            ba.counts = counts.p;
-            uint32_t nbricks = j.last - j.first;
-            unsigned grid = (unsigned)std::min<uint64_t>(nbricks, (uint64_t)sms * 4);
-            k_block_bricks<<<grid, kBrickCta, 0, st>>>(ba);
-            SVO_LAUNCH_OK("k_block_bricks");
+            fa.tris = m->d_tris;
+            fa.box = box.p;
+            fa.pair_tri = stri;
+            fa.bkey = bkey.p;
+            fa.bstart = bstart.p;
+            fa.b_first = j.first;
+            fa.b_last = j.last;
+            fa.log_e = g.log_e;
+            fa.acc = acc.p;
+            fa.K = K;
+            fa.half = 0.5f * hx;
+            fa.data = data.p;
+            fa.counts = counts.p;
+            unsigned grid = (unsigned)std::min<uint64_t>((j.last - j.first + kFoldWarps - 1) / kFoldWarps, fold_grid);
+            k_fold_bricks<<<grid, kFoldWarps * 32, 0, st>>>(fa);
+            SVO_LAUNCH_OK("k_fold_bricks");
         }
-        uint64_t *bk = nullptr;
-        uint32_t *bp = nullptr;
-        uint64_t bn = 0;
-        const int drop = ((ba.buf[2] & 1) && lb >= 2) ? 1 : 0;
-        int rc = extract_voxels_device(data.p, ba.buf[0], ba.buf[1], ba.buf[2], lb, (uint64_t)j.morton << (3 * lb),
-                                       drop, 1, st, &bk, &bp, &bn);
+        // candidate bricks: folded here, or under an earlier block's dropped
+        // slice (all bricks, when those slices are large)
+        const uint64_t vol = (uint64_t)fa.buf[0] * fa.buf[1] * fa.buf[2];
+        if (ghost_len * 4 > vol) {
+            SVO_CUDA_TRY(cudaMemsetAsync(dirty.p, 1, n_e, st));
+        } else {
+            SVO_CUDA_TRY(cudaMemsetAsync(dirty.p, 0, n_e, st));
+            if (j.last > j.first) {
+                k_mark_folded<<<grid_for(j.last - j.first), 256, 0, st>>>(bkey.p, j.first, j.last, g.log_e, fa.org[0],
+                                                                         fa.org[1], fa.org[2], dirty.p, n_e);
+                SVO_LAUNCH_OK("k_mark_folded");
+            }
+            for (const auto &r : ghosts) {
+                uint64_t s1 = std::min(r.second, vol);
+                if (r.first >= s1) continue;
+                k_mark_range<<<grid_for(s1 - r.first), 256, 0, st>>>(r.first, s1, fa.buf[0], fa.buf[1], fa.buf[2],
+                                                                    g.log_e, dirty.p, n_e);
+                SVO_LAUNCH_OK("k_mark_range");
+            }
+        }
+        k_flag_to_u32<<<grid_for(n_e), 256, 0, st>>>(dirty.p, n_e, d32.p);
+        SVO_LAUNCH_OK("k_flag_to_u32");
+        uint32_t n_cand = 0;
+        int rc = scan_total<uint32_t, uint32_t>(d32.p, didx.p, n_e, &n_cand, st);
         if (rc) return rc;
-        if (bn) {
-            part_keys.push_back(bk);
-            part_pay.push_back(bp);
-            part_n.push_back(bn);
+        const int drop = ((fa.buf[2] & 1) && lb >= 2) ? 1 : 0;
+        if (n_cand) {
+            k_compact_u8<<<grid_for(n_e), 256, 0, st>>>(dirty.p, n_e, didx.p, cand.p);
+            ExtractArgs ea;
+            ea.cand = cand.p;
+            ea.n_cand = n_cand;
+            ea.log_e = g.log_e;
+            for (int k = 0; k < 3; ++k) ea.buf[k] = fa.buf[k];
+            ea.drop = drop;
+            ea.key_base = (uint64_t)j.morton << (3 * lb);
+            ea.data = data.p;
+            k_cand_count<<<grid_for((uint64_t)n_cand * 32), 256, 0, st>>>(ea, ccount.p);
+            SVO_LAUNCH_OK("k_cand_count");
+            uint64_t bn = 0;
+            rc = scan_total<uint32_t, uint64_t>(ccount.p, coff.p, n_cand, &bn, st);
+            if (rc) return rc;
+            if (N + bn > cap) {  // grow the voxel arrays
+                uint64_t nc = std::max(cap * 2, N + bn);
+                Dev<uint64_t> k2;
+                Dev<uint32_t> p2;
+                SVO_ALLOC(k2, nc);
+                SVO_ALLOC(p2, nc);
+                if (N) {
+                    SVO_CUDA_TRY(cudaMemcpyAsync(k2.p, keys.p, N * sizeof(uint64_t), cudaMemcpyDeviceToDevice, st));
+                    SVO_CUDA_TRY(cudaMemcpyAsync(p2.p, pay.p, N * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
+                }
+                std::swap(keys.p, k2.p);
+                std::swap(pay.p, p2.p);
+                cap = nc;
+            }
+            if (bn) {
+                k_cand_emit<<<grid_for((uint64_t)n_cand * 32), 256, 0, st>>>(ea, coff.p, keys.p + N, pay.p + N);
+                SVO_LAUNCH_OK("k_cand_emit");
+            }
             N += bn;
+        }
+        if (drop) {  // the walk never reads this slice; it stays in the buffer
+            uint64_t plane = (uint64_t)fa.buf[0] * fa.buf[1];
+            ghosts.emplace_back(plane * (uint64_t)(fa.buf[2] - 1), plane * (uint64_t)fa.buf[2]);
+            ghost_len += plane;
         }
     }
     data.release();
@@ -874,17 +1076,7 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
     acc.release();
     if (N >= 0xFFFFFFFFull) return set_error(SVO_ERR_LIMIT, "%llu voxels exceed 2^32-1", (unsigned long long)N);
 
-    // 5. octree from the concatenated (already Morton-ordered) voxels
-    Dev<uint64_t> keys;
-    Dev<uint32_t> pay;
-    SVO_ALLOC(keys, N);
-    SVO_ALLOC(pay, N);
-    uint64_t at = 0;
-    for (size_t i = 0; i < part_n.size(); ++i) {
-        SVO_CUDA_TRY(cudaMemcpyAsync(keys.p + at, part_keys[i], part_n[i] * sizeof(uint64_t), cudaMemcpyDeviceToDevice, st));
-        SVO_CUDA_TRY(cudaMemcpyAsync(pay.p + at, part_pay[i], part_n[i] * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
-        at += part_n[i];
-    }
+    // 5. octree from the (already Morton-ordered) voxels
     return build_from_sorted_device(keys.p, pay.p, N, D, lb, lb < D ? bflag.p : nullptr, st, d_words, n_words);
 }
 
