@@ -79,6 +79,11 @@ void svo_free(void *p);
  * copied to the device.  Used to trace octrees produced elsewhere. */
 int svo_octree_from_words(const uint32_t *words, uint64_t n_words, const float center[3], svo_octree **out);
 
+/* The builds keep their freed scratch memory in a per-device pool of the
+ * library for the next build; this returns that memory to the driver (after
+ * a device synchronisation). */
+int svo_trim_memory(void);
+
 /* Frees the handle and its device memory. */
 int svo_octree_destroy(svo_octree *oct);
 
@@ -172,6 +177,14 @@ int svo_mesh_load_ply(const char *path, svo_mesh **out);
  * n_face_ints ints holding, per polygon, its vertex count then its indices. */
 int svo_mesh_from_arrays(const float *positions, const float *normals, const float *colors, uint64_t n_vertices,
                          const int32_t *faces, uint64_t n_face_ints, svo_mesh **out);
+
+/* Host only: the parse step of svo_mesh_load_ply, before rescaling.  On
+ * success *positions, *colors (3 floats per vertex), *normals (3 floats per
+ * vertex, or NULL when the file has none) and *triangles (3 indices per fan
+ * triangle) are malloc'd arrays to release with svo_free; lower/upper are
+ * PlyLoader's vertex bounds (PlyLoader.cpp:160-163). */
+int svo_ply_parse(const char *path, float **positions, float **normals, float **colors, uint64_t *n_vertices,
+                  int32_t **triangles, uint64_t *n_triangles, float lower[3], float upper[3]);
 
 uint64_t svo_mesh_num_triangles(const svo_mesh *mesh);
 

@@ -77,6 +77,7 @@ def _load():
         "svo_oct_read": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_u32p), _u64p, _f32p]),
         "svo_oct_write": (ctypes.c_int, [ctypes.c_char_p, _vp, ctypes.c_uint64, _f32p]),
         "svo_free": (None, [_vp]),
+        "svo_trim_memory": (ctypes.c_int, []),
         "svo_octree_from_words": (ctypes.c_int, [_vp, ctypes.c_uint64, _f32p, ctypes.POINTER(_vp)]),
         "svo_octree_destroy": (ctypes.c_int, [_vp]),
         "svo_octree_num_words": (ctypes.c_int, [_vp, _u64p]),
@@ -92,6 +93,9 @@ def _load():
         "svo_mesh_from_arrays": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_uint64, _vp, ctypes.c_uint64,
                                                 ctypes.POINTER(_vp)]),
         "svo_mesh_num_triangles": (ctypes.c_uint64, [_vp]),
+        "svo_ply_parse": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_f32p), ctypes.POINTER(_f32p),
+                                         ctypes.POINTER(_f32p), _u64p, ctypes.POINTER(ctypes.POINTER(ctypes.c_int32)),
+                                         _u64p, _f32p, _f32p]),
         "svo_mesh_dimensions": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
         "svo_mesh_destroy": (None, [_vp]),
         "svo_octree_build_mesh": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_uint64, _vp,
@@ -173,6 +177,27 @@ def oct_write(path, words, center):
     words = np.ascontiguousarray(words, dtype=np.uint32)
     c = np.ascontiguousarray(center, dtype=np.float32)
     check(lib.svo_oct_write(os.fsencode(path), _np_ptr(words), words.size, c.ctypes.data_as(_f32p)))
+
+
+def ply_parse(path):
+    """Host-only PLY parse (svo_ply_parse): dict with positions, normals (or
+    None), colors (V x 3 float32), triangles (T x 3 int32), lower, upper."""
+    pp, pn, pc, pt = _f32p(), _f32p(), _f32p(), ctypes.POINTER(ctypes.c_int32)()
+    nv, nt = ctypes.c_uint64(), ctypes.c_uint64()
+    lo, hi = np.zeros(3, np.float32), np.zeros(3, np.float32)
+    check(lib.svo_ply_parse(os.fsencode(path), ctypes.byref(pp), ctypes.byref(pn), ctypes.byref(pc), ctypes.byref(nv),
+                            ctypes.byref(pt), ctypes.byref(nt), lo.ctypes.data_as(_f32p), hi.ctypes.data_as(_f32p)))
+
+    def take(p, n, k):
+        if not p:
+            return None
+        a = np.ctypeslib.as_array(p, shape=(n * k,)).copy().reshape(n, k) if n else np.zeros((0, k), np.float32)
+        lib.svo_free(ctypes.cast(p, _vp))
+        return a
+
+    V, T = nv.value, nt.value
+    return {"positions": take(pp, V, 3), "normals": take(pn, V, 3), "colors": take(pc, V, 3),
+            "triangles": take(pt, T, 3), "lower": lo, "upper": hi}
 
 
 class PlyLoader:

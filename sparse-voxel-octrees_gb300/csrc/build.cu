@@ -325,7 +325,7 @@ struct DevBuf {
     DevBuf &operator=(const DevBuf &) = delete;
     cudaError_t alloc(uint64_t n, cudaStream_t s) {
         st = s;
-        return cudaMallocAsync((void **)&p, (size_t)(n ? n : 1) * sizeof(T), s);
+        return scratch_alloc((void **)&p, (size_t)(n ? n : 1) * sizeof(T), s);
     }
     void release() {
         if (p) cudaFreeAsync(p, st);

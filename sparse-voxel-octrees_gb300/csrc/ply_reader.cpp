@@ -16,12 +16,20 @@
 // Errors the reference meets with ASSERT/exit or undefined behaviour
 // (missing elements, an index outside the vertex array, a truncated file)
 // return SVO_ERR_FORMAT or SVO_ERR_IO.
+#include <fcntl.h>
+#include <sys/mman.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
+#include <algorithm>
+#include <atomic>
 #include <cerrno>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "mesh.h"
@@ -73,6 +81,19 @@ T load_le(const unsigned char *p) {
     T v;
     std::memcpy(&v, p, sizeof(T));  // both supported hosts are little-endian
     return v;
+}
+
+// A stored float after plyfile's float -> double -> float round trip
+// (get_binary_item then store_item): identity, except that a signalling NaN
+// comes back quiet with its payload kept (IEEE 754 conversion, as x86 and
+// Arm perform it).  Written out so no compiler folds the round trip away.
+float float_round_trip(const unsigned char *p) {
+    uint32_t u;
+    std::memcpy(&u, p, 4);
+    if ((u & 0x7F800000u) == 0x7F800000u && (u & 0x007FFFFFu)) u |= 0x00400000u;
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
 }
 
 // get_binary_item (plyfile.c:2132-2196)
@@ -134,21 +155,77 @@ void split_words(const std::string &line, std::vector<std::string> &out) {
     }
 }
 
+// The file's bytes: mapped read-only (no copy), or read into memory where
+// mapping fails.
 struct Reader {
-    std::vector<unsigned char> buf;
-    size_t pos = 0;
+    const unsigned char *data = nullptr;
+    size_t size = 0, pos = 0;
+    void *map = nullptr;
+    std::vector<unsigned char> copy;
+    ~Reader() {
+        if (map) munmap(map, size);
+    }
     bool line(std::string &out) {
-        if (pos >= buf.size()) return false;
+        if (pos >= size) return false;
         size_t e = pos;
-        while (e < buf.size() && buf[e] != '\n') ++e;
-        out.assign((const char *)buf.data() + pos, e - pos);
-        pos = e < buf.size() ? e + 1 : e;
+        while (e < size && data[e] != '\n') ++e;
+        out.assign((const char *)data + pos, e - pos);
+        pos = e < size ? e + 1 : e;
         return true;
     }
 };
 
+// Runs fn(begin, end, part) over [0, n) in `parts` contiguous pieces on
+// worker threads (inline when there is one part).
+template <typename Fn>
+void parallel_parts(uint64_t n, int parts, Fn fn) {
+    if (parts <= 1) {
+        fn((uint64_t)0, n, 0);
+        return;
+    }
+    std::vector<std::thread> th;
+    for (int p = 0; p < parts; ++p)
+        th.emplace_back([=, &fn] { fn(n * p / parts, n * (p + 1) / parts, p); });
+    for (auto &t : th) t.join();
+}
+
+int worker_count(uint64_t n) {
+    if (n < (1u << 15)) return 1;
+    unsigned hw = std::thread::hardware_concurrency();
+    return (int)std::max(1u, std::min(hw ? hw : 1u, 16u));
+}
+
 const int kVertexProps = 9;
 const char *const kVertexNames[kVertexProps] = {"x", "y", "z", "nx", "ny", "nz", "red", "green", "blue"};
+
+// Float value of one stored binary item, as binary_item(...).d converted to
+// float (plyfile's store_item for PLY_FLOAT).
+inline float binary_float(const unsigned char *p, int type) {
+    switch (type) {
+        case kFloat: return float_round_trip(p);
+        case kUChar: return (float)p[0];
+        case kChar: return (float)(int8_t)p[0];
+        case kShort: return (float)load_le<int16_t>(p);
+        case kUShort: return (float)load_le<uint16_t>(p);
+        case kInt: return (float)(double)load_le<int32_t>(p);
+        case kUInt: return (float)(double)load_le<uint32_t>(p);
+        case kDouble: return (float)load_le<double>(p);
+        default: return 0.0f;
+    }
+}
+
+// Int value of one stored binary item (binary_item(...).i).
+inline int32_t binary_int(const unsigned char *p, int type) {
+    switch (type) {
+        case kInt: return load_le<int32_t>(p);
+        case kUInt: return (int32_t)load_le<uint32_t>(p);
+        case kUChar: return p[0];
+        case kUShort: return load_le<uint16_t>(p);
+        case kShort: return load_le<int16_t>(p);
+        case kChar: return (int8_t)p[0];
+        default: return binary_item(p, type).i;
+    }
+}
 
 }  // namespace
 
@@ -181,19 +258,35 @@ int mesh_add_face(MeshHost &m, const int32_t *idx, int count, uint64_t n_vertice
 int ply_read(const char *path, MeshHost &out) {
     Reader rd;
     {
-        FILE *fp = std::fopen(path, "rb");
-        if (!fp) return set_error(SVO_ERR_IO, "cannot open PLY %s: %s", path, std::strerror(errno));
-        std::fseek(fp, 0, SEEK_END);
-        long sz = std::ftell(fp);
-        std::fseek(fp, 0, SEEK_SET);
-        if (sz < 0) {
-            std::fclose(fp);
+        int fd = open(path, O_RDONLY);
+        if (fd < 0) return set_error(SVO_ERR_IO, "cannot open PLY %s: %s", path, std::strerror(errno));
+        struct stat stt;
+        if (fstat(fd, &stt) != 0) {
+            close(fd);
             return set_error(SVO_ERR_IO, "cannot size PLY %s", path);
         }
-        rd.buf.resize((size_t)sz);
-        size_t got = sz ? std::fread(rd.buf.data(), 1, (size_t)sz, fp) : 0;
-        std::fclose(fp);
-        if (got != (size_t)sz) return set_error(SVO_ERR_IO, "short read on PLY %s", path);
+        rd.size = (size_t)stt.st_size;
+        if (rd.size) {
+            void *mp = mmap(nullptr, rd.size, PROT_READ, MAP_PRIVATE | MAP_POPULATE, fd, 0);
+            if (mp != MAP_FAILED) {
+                rd.map = mp;
+                rd.data = (const unsigned char *)mp;
+            } else {
+                rd.copy.resize(rd.size);
+                size_t got = 0;
+                while (got < rd.size) {
+                    ssize_t r = read(fd, rd.copy.data() + got, rd.size - got);
+                    if (r <= 0) break;
+                    got += (size_t)r;
+                }
+                if (got != rd.size) {
+                    close(fd);
+                    return set_error(SVO_ERR_IO, "short read on PLY %s", path);
+                }
+                rd.data = rd.copy.data();
+            }
+        }
+        close(fd);
     }
 
     // Header (plyfile.c ply_read, :700-790).
@@ -281,6 +374,166 @@ int ply_read(const char *path, MeshHost &out) {
     std::vector<int32_t> idx;
     for (const Elem &e : elems) {
         const bool is_v = &e == ve, is_f = &e == fe;
+        bool scalar_only = true;
+        size_t stride = 0;
+        for (const Prop &p : e.props) {
+            if (p.count_type != kInvalid) scalar_only = false;
+            else stride += type_size(p.type);
+        }
+        if (format != 0 && is_v && scalar_only) {
+            // Fixed-size vertex records: convert the wanted properties in place.
+            if (rd.pos + stride * e.count > rd.size) return set_error(SVO_ERR_FORMAT, "%s: truncated PLY", path);
+            int off[kVertexProps], typ[kVertexProps];
+            for (int t = 0; t < kVertexProps; ++t) off[t] = -1, typ[t] = kInvalid;
+            size_t o = 0;
+            for (size_t pi = 0; pi < e.props.size(); ++pi) {
+                if (vslot[pi] >= 0) {
+                    off[vslot[pi]] = (int)o;
+                    typ[vslot[pi]] = e.props[pi].type;
+                }
+                o += type_size(e.props[pi].type);
+            }
+            const uint64_t n = e.count;
+            out.pos.resize(n * 3);
+            out.col.resize(n * 3);
+            if (has_normals) out.nrm.resize(n * 3);
+            const unsigned char *base0 = rd.data + rd.pos;
+            const int parts = worker_count(n);
+            // per-part bounds, folded in part order afterwards: std::min keeps
+            // the first of equal values, and so does this in-order fold
+            std::vector<float> plo(3 * parts, 1e30f), phi(3 * parts, -1e30f);
+            std::atomic<uint64_t> bad{~0ull};
+            parallel_parts(n, parts, [&](uint64_t b, uint64_t e_, int part) {
+                float lo[3] = {1e30f, 1e30f, 1e30f}, hi[3] = {-1e30f, -1e30f, -1e30f};
+                const unsigned char *base = base0 + b * stride;
+                for (uint64_t k = b; k < e_; ++k, base += stride) {
+                    float vd[kVertexProps];
+                    for (int t = 0; t < kVertexProps; ++t) {
+                        if (off[t] < 0) {
+                            vd[t] = vdefault[t];
+                        } else {
+                            float f = binary_float(base + off[t], typ[t]);
+                            vd[t] = be ? swap_f32(f) : f;
+                        }
+                    }
+                    for (int t = 0; t < 3; ++t) {
+                        if (!std::isfinite(vd[t])) {
+                            uint64_t cur = bad.load();
+                            while (k < cur && !bad.compare_exchange_weak(cur, k)) {
+                            }
+                        }
+                        out.pos[3 * k + t] = vd[t];
+                        out.col[3 * k + t] = vd[6 + t];
+                        if (has_normals) out.nrm[3 * k + t] = vd[3 + t];
+                        lo[t] = (vd[t] < lo[t]) ? vd[t] : lo[t];
+                        hi[t] = (hi[t] < vd[t]) ? vd[t] : hi[t];
+                    }
+                }
+                for (int t = 0; t < 3; ++t) {
+                    plo[3 * part + t] = lo[t];
+                    phi[3 * part + t] = hi[t];
+                }
+            });
+            if (bad.load() != ~0ull)
+                return set_error(SVO_ERR_FORMAT, "%s: vertex %llu has a non-finite coordinate", path,
+                                 (unsigned long long)bad.load());
+            for (int part = 0; part < parts; ++part)
+                for (int t = 0; t < 3; ++t) {
+                    float l = plo[3 * part + t], h = phi[3 * part + t];
+                    out.lower[t] = (l < out.lower[t]) ? l : out.lower[t];
+                    out.upper[t] = (out.upper[t] < h) ? h : out.upper[t];
+                }
+            rd.pos += stride * e.count;
+            continue;
+        }
+        if (format != 0 && is_f) {
+            // Faces: scalars skipped by size, the index list read directly.
+            const Prop &lp = e.props[face_prop];
+            const int cs = type_size(lp.count_type), is = type_size(lp.type);
+            size_t pre = 0, post = 0;
+            bool simple = true;
+            for (size_t pi = 0; pi < e.props.size(); ++pi) {
+                if ((int)pi == face_prop) continue;
+                if (e.props[pi].count_type != kInvalid) simple = false;
+                else if ((int)pi < face_prop) pre += type_size(e.props[pi].type);
+                else post += type_size(e.props[pi].type);
+            }
+            if (simple && e.count > 0) {
+                // All faces triangles (checked face by face): fixed-size
+                // records, converted in parallel.
+                const uint64_t nv = ve->count;
+                const size_t rec = pre + cs + 3 * (size_t)is + post;
+                if (rd.pos + rec * e.count <= rd.size) {
+                    const unsigned char *base0 = rd.data + rd.pos;
+                    const uint64_t n = e.count;
+                    const size_t t0 = out.tris.size();
+                    out.tris.resize(t0 + 3 * n);
+                    std::atomic<bool> uniform{true};
+                    std::atomic<uint64_t> bad{~0ull};
+                    parallel_parts(n, worker_count(n), [&](uint64_t b, uint64_t e_, int) {
+                        const unsigned char *r = base0 + b * rec;
+                        for (uint64_t k = b; k < e_; ++k, r += rec) {
+                            if (binary_int(r + pre, lp.count_type) != 3) {
+                                uniform.store(false);
+                                return;
+                            }
+                            for (int c = 0; c < 3; ++c) {
+                                int32_t x = binary_int(r + pre + cs + (size_t)c * is, lp.type);
+                                x = be ? swap_i32(x) : x;
+                                if (x < 0 || (uint64_t)x >= nv) bad.store(k);
+                                out.tris[t0 + 3 * k + c] = x;
+                            }
+                        }
+                    });
+                    if (uniform.load()) {
+                        if (bad.load() != ~0ull)
+                            return set_error(SVO_ERR_FORMAT, "%s: face %llu has an index outside the %llu vertices",
+                                             path, (unsigned long long)bad.load(), (unsigned long long)nv);
+                        rd.pos += rec * e.count;
+                        continue;
+                    }
+                    out.tris.resize(t0);
+                }
+            }
+            if (simple) {
+                const uint64_t nv = ve->count;
+                const unsigned char *buf = rd.data;
+                const size_t size = rd.size;
+                size_t pos = rd.pos;
+                int32_t ib[256];
+                for (uint64_t k = 0; k < e.count; ++k) {
+                    if (pos + pre + cs > size) return set_error(SVO_ERR_FORMAT, "%s: truncated PLY", path);
+                    pos += pre;
+                    int cnt = binary_int(buf + pos, lp.count_type);
+                    pos += cs;
+                    if (cnt < 0 || pos + (size_t)cnt * is + post > size)
+                        return set_error(SVO_ERR_FORMAT, "%s: truncated PLY list", path);
+                    if (cnt >= 3) {
+                        int32_t *v = cnt <= 256 ? ib : nullptr;
+                        std::vector<int32_t> big;
+                        if (!v) {
+                            big.resize(cnt);
+                            v = big.data();
+                        }
+                        for (int c = 0; c < cnt; ++c) {
+                            int32_t x = binary_int(buf + pos + (size_t)c * is, lp.type);
+                            v[c] = be ? swap_i32(x) : x;
+                            if (v[c] < 0 || (uint64_t)v[c] >= nv)
+                                return set_error(SVO_ERR_FORMAT, "PLY face index %d outside the %llu vertices", v[c],
+                                                 (unsigned long long)nv);
+                        }
+                        for (int c = 2; c < cnt; ++c) {  // PlyLoader.cpp:208-220
+                            out.tris.push_back(v[0]);
+                            out.tris.push_back(c == 2 ? v[1] : v[c - 1]);
+                            out.tris.push_back(v[c]);
+                        }
+                    }
+                    pos += (size_t)cnt * is + post;
+                }
+                rd.pos = pos;
+                continue;
+            }
+        }
         for (uint64_t k = 0; k < e.count; ++k) {
             float vd[kVertexProps];
             for (int t = 0; t < kVertexProps; ++t) vd[t] = vdefault[t];
@@ -311,23 +564,23 @@ int ply_read(const char *path, MeshHost &out) {
                     const Prop &p = e.props[pi];
                     if (p.count_type != kInvalid) {
                         int cs = type_size(p.count_type), is = type_size(p.type);
-                        if (rd.pos + cs > rd.buf.size()) return set_error(SVO_ERR_FORMAT, "%s: truncated PLY", path);
-                        int cnt = binary_item(rd.buf.data() + rd.pos, p.count_type).i;
+                        if (rd.pos + cs > rd.size) return set_error(SVO_ERR_FORMAT, "%s: truncated PLY", path);
+                        int cnt = binary_item(rd.data + rd.pos, p.count_type).i;
                         rd.pos += cs;
-                        if (cnt < 0 || rd.pos + (size_t)cnt * is > rd.buf.size())
+                        if (cnt < 0 || rd.pos + (size_t)cnt * is > rd.size)
                             return set_error(SVO_ERR_FORMAT, "%s: truncated PLY list", path);
                         for (int c = 0; c < cnt; ++c) {
                             if (is_f && (int)pi == face_prop) {
-                                int32_t v = binary_item(rd.buf.data() + rd.pos, p.type).i;
+                                int32_t v = binary_item(rd.data + rd.pos, p.type).i;
                                 idx.push_back(be ? swap_i32(v) : v);
                             }
                             rd.pos += is;
                         }
                     } else {
                         int is = type_size(p.type);
-                        if (rd.pos + is > rd.buf.size()) return set_error(SVO_ERR_FORMAT, "%s: truncated PLY", path);
+                        if (rd.pos + is > rd.size) return set_error(SVO_ERR_FORMAT, "%s: truncated PLY", path);
                         if (is_v && vslot[pi] >= 0) {
-                            float f = (float)binary_item(rd.buf.data() + rd.pos, p.type).d;
+                            float f = binary_float(rd.data + rd.pos, p.type);
                             vd[vslot[pi]] = be ? swap_f32(f) : f;
                         }
                         rd.pos += is;

@@ -54,6 +54,10 @@ size_t lz4_compress_bound(size_t n);
 size_t lz4_compress_block(const uint8_t *src, size_t n, uint8_t *dst, size_t cap);
 int lz4_decompress_block(const uint8_t *src, size_t src_len, uint8_t *out, size_t pos0, size_t out_len);
 
+// Stream-ordered scratch from the library's per-device pool (mem_pool.cpp);
+// release with cudaFreeAsync.
+cudaError_t scratch_alloc(void **p, size_t bytes, cudaStream_t st);
+
 // VoxelData::init cache-block search (VoxelData.cpp:211-244): log2 of the
 // cache-block edge, or -1 when no partition fits `mem`.
 int cache_block_log2(int w, int h, int d, uint64_t mem, uint64_t cell_cost);

@@ -37,6 +37,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
+#include <cstring>
 #include <vector>
 
 #include "mesh.h"
@@ -86,7 +88,7 @@ struct Dev {
     Dev &operator=(const Dev &) = delete;
     cudaError_t alloc(uint64_t n, cudaStream_t s) {
         st = s;
-        return cudaMallocAsync((void **)&p, (size_t)(n ? n : 1) * sizeof(T), s);
+        return scratch_alloc((void **)&p, (size_t)(n ? n : 1) * sizeof(T), s);
     }
     void release() {
         if (p) cudaFreeAsync(p, st);
@@ -609,7 +611,6 @@ __global__ void k_compact_u8(const uint8_t *__restrict__ flag, uint64_t n, const
 
 struct ExtractArgs {
     const uint32_t *cand;  // candidate bricks (Morton index within the block), ascending
-    uint32_t n_cand;
     int log_e;
     int buf[3];
     int drop;              // the z == buf[2]-1 slice is never read (VoxelData.cpp:163-170)
@@ -627,47 +628,59 @@ __device__ __forceinline__ uint64_t cand_cell(const ExtractArgs &a, uint32_t c, 
     return (uint64_t)x + (uint64_t)a.buf[0] * ((uint64_t)y + (uint64_t)a.buf[1] * (uint64_t)z);
 }
 
-// One warp per candidate brick: its occupied voxels.
-__global__ void k_cand_count(ExtractArgs a, uint32_t *__restrict__ count) {
+// One warp per candidate brick (grid-stride over *n_cand): its occupied
+// voxels.
+__global__ void k_cand_count(ExtractArgs a, const uint32_t *__restrict__ n_cand, uint32_t *__restrict__ count) {
     const int lane = threadIdx.x & 31;
-    const uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (c >= a.n_cand) return;
-    const uint32_t key = a.cand[c], E3 = 1u << (3 * a.log_e);
-    uint32_t n = 0;
-    for (uint32_t m = lane; m < E3; m += 32) {
-        uint64_t bi = cand_cell(a, key, m);
-        if (bi != ~0ull && a.data[bi]) ++n;
-    }
+    const uint32_t nc = *n_cand, E3 = 1u << (3 * a.log_e);
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < nc; c += nw) {
+        const uint32_t key = a.cand[c];
+        uint32_t n = 0;
+        for (uint32_t m = lane; m < E3; m += 32) {
+            uint64_t bi = cand_cell(a, key, m);
+            if (bi != ~0ull && a.data[bi]) ++n;
+        }
 #pragma unroll
-    for (int o = 16; o; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
-    if (lane == 0) count[c] = n;
+        for (int o = 16; o; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
+        if (lane == 0) count[c] = n;
+    }
 }
 
 // One warp per candidate brick: (key, word) of its occupied voxels in
-// Morton order at off[c], and the emitted cells cleared (the walk reads
-// them with getVoxelDestructive).
-__global__ void k_cand_emit(ExtractArgs a, const uint64_t *__restrict__ off, uint64_t *__restrict__ keys,
-                            uint32_t *__restrict__ payload) {
+// Morton order at *base + off[c] (at most cap), and the emitted cells
+// cleared (the walk reads them with getVoxelDestructive).
+__global__ void k_cand_emit(ExtractArgs a, const uint32_t *__restrict__ n_cand, const uint64_t *__restrict__ off,
+                            const uint64_t *__restrict__ base_p, uint64_t cap, uint64_t *__restrict__ keys,
+                            uint32_t *__restrict__ payload, uint32_t *__restrict__ err) {
     const int lane = threadIdx.x & 31;
-    const uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (c >= a.n_cand) return;
-    const uint32_t key = a.cand[c], E3 = 1u << (3 * a.log_e);
-    uint64_t base = off[c];
+    const uint32_t nc = *n_cand, E3 = 1u << (3 * a.log_e);
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     const uint32_t lt = (1u << lane) - 1u;
-    for (uint32_t m0 = 0; m0 < E3; m0 += 32) {
-        const uint32_t m = m0 + lane;
-        uint64_t bi = m < E3 ? cand_cell(a, key, m) : ~0ull;
-        uint32_t v = bi != ~0ull ? a.data[bi] : 0u;
-        uint32_t ball = __ballot_sync(0xffffffffu, v != 0);
-        if (v) {
-            uint64_t o = base + __popc(ball & lt);
-            keys[o] = a.key_base + ((uint64_t)key << (3 * a.log_e)) + m;
-            payload[o] = v;
-            a.data[bi] = 0;
+    for (uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < nc; c += nw) {
+        const uint32_t key = a.cand[c];
+        uint64_t base = *base_p + off[c];
+        for (uint32_t m0 = 0; m0 < E3; m0 += 32) {
+            const uint32_t m = m0 + lane;
+            uint64_t bi = m < E3 ? cand_cell(a, key, m) : ~0ull;
+            uint32_t v = bi != ~0ull ? a.data[bi] : 0u;
+            uint32_t ball = __ballot_sync(0xffffffffu, v != 0);
+            if (v) {
+                uint64_t o = base + __popc(ball & lt);
+                if (o < cap) {
+                    keys[o] = a.key_base + ((uint64_t)key << (3 * a.log_e)) + m;
+                    payload[o] = v;
+                    a.data[bi] = 0;
+                } else {
+                    atomicOr(err, 8u);
+                }
+            }
+            base += __popc(ball);
         }
-        base += __popc(ball);
     }
 }
+
+__global__ void k_add_u64(uint64_t *__restrict__ acc, const uint64_t *__restrict__ add) { *acc += *add; }
 
 // findBestBlockPartition (PlyLoader.cpp:381-405).
 void best_partition(int &w, int &h, int &d, int threads) {
@@ -955,25 +968,39 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
     SVO_CUDA_TRY(cudaGetDevice(&dev));
     SVO_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
 
-    // 4. blocks in order: fold, then extract (and clear) the block's voxels
+    // 4. blocks in order: fold, then extract (and clear) the block's voxels.
+    // Counts stay on the device, so the loop queues its work without waiting.
     const uint64_t n_e = 1ull << (3 * (lb - g.log_e));  // bricks per block
     Dev<uint8_t> dirty;
-    Dev<uint32_t> d32, didx, cand, ccount;
-    Dev<uint64_t> coff;
+    Dev<uint32_t> d32, didx, cand, ccount, ncand, sc32;
+    Dev<uint64_t> coff, bn, dN, sc64;
     SVO_ALLOC(dirty, n_e);
     SVO_ALLOC(d32, n_e);
     SVO_ALLOC(didx, n_e);
     SVO_ALLOC(cand, n_e);
     SVO_ALLOC(ccount, n_e);
     SVO_ALLOC(coff, n_e);
-    std::vector<std::pair<uint64_t, uint64_t>> ghosts;  // flat ranges of the dropped slices so far
-    uint64_t ghost_len = 0;
+    SVO_ALLOC(ncand, 1);
+    SVO_ALLOC(bn, 1);
+    SVO_ALLOC(dN, 1);
+    SVO_ALLOC(sc32, scan_scratch_elems(n_e));
+    SVO_ALLOC(sc64, scan_scratch_elems(n_e));
+    SVO_CUDA_TRY(cudaMemsetAsync(dN.p, 0, sizeof(uint64_t), st));
+    // Every emitted voxel lies in a brick folded by its block or is a word an
+    // earlier block's dropped slice left behind (each emitted once).
+    uint64_t cap = (uint64_t)nb << (3 * g.log_e);
+    for (const BlockJob &j : jobs) {
+        int oz = (int)(compact3((uint64_t)j.morton >> 2) << lb);
+        int bd = std::min(B, dims[2] - oz);
+        if (bd > 0 && (bd & 1) && lb >= 2) cap += (uint64_t)B * B;
+    }
     Dev<uint64_t> keys;
     Dev<uint32_t> pay;
-    uint64_t cap = std::max<uint64_t>(1 << 20, n_pairs * 8), N = 0;
     SVO_ALLOC(keys, cap);
     SVO_ALLOC(pay, cap);
-    const unsigned fold_grid = (unsigned)sms * 8;
+    std::vector<std::pair<uint64_t, uint64_t>> ghosts;  // flat ranges of the dropped slices so far
+    uint64_t ghost_len = 0;
+    const unsigned fold_grid = (unsigned)sms * 8, warp_grid = (unsigned)sms * 16;
     for (const BlockJob &j : jobs) {
         FoldArgs fa;
         fa.org[0] = (int)(compact3(j.morton) << lb);
@@ -1026,51 +1053,36 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
         }
         k_flag_to_u32<<<grid_for(n_e), 256, 0, st>>>(dirty.p, n_e, d32.p);
         SVO_LAUNCH_OK("k_flag_to_u32");
-        uint32_t n_cand = 0;
-        int rc = scan_total<uint32_t, uint32_t>(d32.p, didx.p, n_e, &n_cand, st);
-        if (rc) return rc;
+        SVO_CUDA_TRY((exclusive_scan<uint32_t, uint32_t>(d32.p, didx.p, n_e, ncand.p, sc32.p, st)));
+        k_compact_u8<<<grid_for(n_e), 256, 0, st>>>(dirty.p, n_e, didx.p, cand.p);
+        SVO_LAUNCH_OK("k_compact_u8");
         const int drop = ((fa.buf[2] & 1) && lb >= 2) ? 1 : 0;
-        if (n_cand) {
-            k_compact_u8<<<grid_for(n_e), 256, 0, st>>>(dirty.p, n_e, didx.p, cand.p);
-            ExtractArgs ea;
-            ea.cand = cand.p;
-            ea.n_cand = n_cand;
-            ea.log_e = g.log_e;
-            for (int k = 0; k < 3; ++k) ea.buf[k] = fa.buf[k];
-            ea.drop = drop;
-            ea.key_base = (uint64_t)j.morton << (3 * lb);
-            ea.data = data.p;
-            k_cand_count<<<grid_for((uint64_t)n_cand * 32), 256, 0, st>>>(ea, ccount.p);
-            SVO_LAUNCH_OK("k_cand_count");
-            uint64_t bn = 0;
-            rc = scan_total<uint32_t, uint64_t>(ccount.p, coff.p, n_cand, &bn, st);
-            if (rc) return rc;
-            if (N + bn > cap) {  // grow the voxel arrays
-                uint64_t nc = std::max(cap * 2, N + bn);
-                Dev<uint64_t> k2;
-                Dev<uint32_t> p2;
-                SVO_ALLOC(k2, nc);
-                SVO_ALLOC(p2, nc);
-                if (N) {
-                    SVO_CUDA_TRY(cudaMemcpyAsync(k2.p, keys.p, N * sizeof(uint64_t), cudaMemcpyDeviceToDevice, st));
-                    SVO_CUDA_TRY(cudaMemcpyAsync(p2.p, pay.p, N * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
-                }
-                std::swap(keys.p, k2.p);
-                std::swap(pay.p, p2.p);
-                cap = nc;
-            }
-            if (bn) {
-                k_cand_emit<<<grid_for((uint64_t)n_cand * 32), 256, 0, st>>>(ea, coff.p, keys.p + N, pay.p + N);
-                SVO_LAUNCH_OK("k_cand_emit");
-            }
-            N += bn;
-        }
+        ExtractArgs ea;
+        ea.cand = cand.p;
+        ea.log_e = g.log_e;
+        for (int k = 0; k < 3; ++k) ea.buf[k] = fa.buf[k];
+        ea.drop = drop;
+        ea.key_base = (uint64_t)j.morton << (3 * lb);
+        ea.data = data.p;
+        SVO_CUDA_TRY(cudaMemsetAsync(ccount.p, 0, n_e * sizeof(uint32_t), st));
+        k_cand_count<<<warp_grid, 256, 0, st>>>(ea, ncand.p, ccount.p);
+        SVO_LAUNCH_OK("k_cand_count");
+        SVO_CUDA_TRY((exclusive_scan<uint32_t, uint64_t>(ccount.p, coff.p, n_e, bn.p, sc64.p, st)));
+        k_cand_emit<<<warp_grid, 256, 0, st>>>(ea, ncand.p, coff.p, dN.p, cap, keys.p, pay.p, err.p);
+        SVO_LAUNCH_OK("k_cand_emit");
+        k_add_u64<<<1, 1, 0, st>>>(dN.p, bn.p);
         if (drop) {  // the walk never reads this slice; it stays in the buffer
             uint64_t plane = (uint64_t)fa.buf[0] * fa.buf[1];
             ghosts.emplace_back(plane * (uint64_t)(fa.buf[2] - 1), plane * (uint64_t)fa.buf[2]);
             ghost_len += plane;
         }
     }
+    uint64_t N = 0;
+    uint32_t e_h = 0;
+    SVO_CUDA_TRY(cudaMemcpyAsync(&N, dN.p, sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+    SVO_CUDA_TRY(cudaMemcpyAsync(&e_h, err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    SVO_CUDA_TRY(cudaStreamSynchronize(st));
+    if (e_h) return set_error(SVO_ERR_DEVICE, "mesh build: voxel extraction check failed (flags %u)", e_h);
     data.release();
     counts.release();
     acc.release();
@@ -1119,6 +1131,44 @@ extern "C" int svo_mesh_from_arrays(const float *positions, const float *normals
         o += 1 + (uint64_t)c;
     }
     return mesh_upload(h, out);
+}
+
+extern "C" int svo_ply_parse(const char *path, float **positions, float **normals, float **colors,
+                             uint64_t *n_vertices, int32_t **triangles, uint64_t *n_triangles, float lower[3],
+                             float upper[3]) {
+    clear_error();
+    if (!path || !positions || !normals || !colors || !n_vertices || !triangles || !n_triangles || !lower || !upper)
+        return set_error(SVO_ERR_INVALID, "null argument");
+    *positions = *normals = *colors = nullptr;
+    *triangles = nullptr;
+    MeshHost h;
+    int rc = ply_read(path, h);
+    if (rc) return rc;
+    auto dup = [](const void *src, size_t bytes) -> void * {
+        void *d = std::malloc(bytes ? bytes : 1);
+        if (d && bytes) std::memcpy(d, src, bytes);
+        return d;
+    };
+    *positions = (float *)dup(h.pos.data(), h.pos.size() * sizeof(float));
+    *colors = (float *)dup(h.col.data(), h.col.size() * sizeof(float));
+    *normals = h.nrm.empty() ? nullptr : (float *)dup(h.nrm.data(), h.nrm.size() * sizeof(float));
+    *triangles = (int32_t *)dup(h.tris.data(), h.tris.size() * sizeof(int32_t));
+    if (!*positions || !*colors || !*triangles || (!h.nrm.empty() && !*normals)) {
+        std::free(*positions);
+        std::free(*colors);
+        std::free(*normals);
+        std::free(*triangles);
+        *positions = *normals = *colors = nullptr;
+        *triangles = nullptr;
+        return set_error(SVO_ERR_MEMORY, "host allocation for the parsed mesh");
+    }
+    *n_vertices = h.pos.size() / 3;
+    *n_triangles = h.tris.size() / 3;
+    for (int k = 0; k < 3; ++k) {
+        lower[k] = h.lower[k];
+        upper[k] = h.upper[k];
+    }
+    return SVO_OK;
 }
 
 extern "C" uint64_t svo_mesh_num_triangles(const svo_mesh *m) { return m ? m->n_tris : 0; }
