@@ -294,6 +294,16 @@ int svo_diff_backward(const svo_octree *oct, const float *rays, uint32_t width, 
                       const float *lights, const float *leaf_rgb, const float *leaf_normal, const uint32_t *hit_leaf,
                       const float *d_rgb, float *grad_rgb, float *grad_normal, svo_stream stream);
 
+/* No counterpart in the reference.  One Adam step (no weight decay, no
+ * amsgrad) over n parameters in one pass: exp_avg = beta1 exp_avg + (1 -
+ * beta1) g, exp_avg_sq = beta2 exp_avg_sq + (1 - beta2) g^2, params -=
+ * lr / (1 - beta1^step) * exp_avg / (sqrt(exp_avg_sq) / sqrt(1 - beta2^step)
+ * + eps); with zero_grad != 0 the gradients are zeroed in the same pass for
+ * the next svo_diff_backward accumulation.  All arrays are device memory;
+ * asynchronous on `stream`.  step >= 1 counts this update. */
+int svo_adam_step(float *params, float *grads, float *exp_avg, float *exp_avg_sq, uint64_t n, float lr, float beta1,
+                  float beta2, float eps, int step, int zero_grad, svo_stream stream);
+
 /* ----------------------------------------------------------------- batched */
 
 /* One (octree, view) pair of a batched trace.  A view is either

@@ -114,6 +114,8 @@ def _load():
                                             _vp, _vp, _vp]),
         "svo_diff_backward": (ctypes.c_int, [_vp, _vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _vp, _vp, _vp,
                                              _vp, _vp, _vp, _vp, _vp]),
+        "svo_adam_step": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_uint64, ctypes.c_float, ctypes.c_float,
+                                         ctypes.c_float, ctypes.c_float, ctypes.c_int, ctypes.c_int, _vp]),
         "svo_batch_create": (ctypes.c_int, [ctypes.POINTER(View), ctypes.c_int, ctypes.POINTER(_vp)]),
         "svo_batch_default_config": (ctypes.c_int, [ctypes.POINTER(TraceConfig)]),
         "svo_batch_num_slots": (ctypes.c_int, [_vp, _u64p]),
@@ -461,6 +463,28 @@ class VoxelOctree:
             n = rays.shape[0]
         check(lib.svo_trace_count_loads(self._h, _dev_ptr(rays), int(n), float(ray_scale), _dev_ptr(loads),
                                         _stream_ptr(stream)))
+
+
+class LeafAdam:
+    """Adam over per-leaf parameter tensors (CUDA float32, contiguous) with
+    svo_adam_step: one fused pass per tensor that also zeroes the gradient
+    (pass zero_grad=False to keep it).  step() reads each tensor's .grad."""
+
+    def __init__(self, params, lr=1e-2, betas=(0.9, 0.999), eps=1e-8, zero_grad=True):
+        import torch
+        self.params = list(params)
+        self.lr, self.betas, self.eps, self.zero_grad = float(lr), betas, float(eps), zero_grad
+        self.state = [(torch.zeros_like(p), torch.zeros_like(p)) for p in self.params]
+        self.t = 0
+
+    def step(self, stream=None):
+        self.t += 1
+        for p, (m, v) in zip(self.params, self.state):
+            g = p.grad
+            assert p.is_contiguous() and g is not None and g.is_contiguous()
+            check(lib.svo_adam_step(_dev_ptr(p), _dev_ptr(g), _dev_ptr(m), _dev_ptr(v), p.numel(), self.lr,
+                                    float(self.betas[0]), float(self.betas[1]), self.eps, self.t,
+                                    1 if self.zero_grad else 0, _stream_ptr(stream)))
 
 
 def default_config(**overrides):
