@@ -391,6 +391,8 @@ def run_ours(args):
                 "bytes_per_ray": round(bytes_prim / Rp, 2), "launch_ms": round(t_prim_avg, 3)}
 
     cpu = None
+    frames = None
+    oracle = words = None
     if rank == 0 and world == 1 and not args.no_cpu:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import pyoracle
@@ -402,7 +404,12 @@ def run_ours(args):
         cpu = {"value": round(n / secs / 1e6, 3), "unit": "Mrays/s", "cores": thr, "kind": "port",
                "sample": "%d of %d cameras: %d primary+shadow rays in %.1f s (oracle C restatement of "
                          "VoxelOctree::raymarch, %d threads)" % (ncam, len(cam_slices), n, secs, thr)}
-        del words
+    if not args.no_extra and world == 1:
+        center = tree.center()
+        cams = scenes.orbit_cameras(args.cams, 1000 + rank, center, radius=1.25, radius_hi=2.0, pitch=45.0)
+        frames = {"scene": run_frames(args, torch, svo, tree, cams, oracle, words),
+                  "dragon": run_dragon_frames(args, torch, svo, scenes, oracle)}
+    del words
 
     extra = extra2 = extra4 = None
     if not args.no_extra and world == 1:
@@ -440,6 +447,7 @@ def run_ours(args):
             "batched_vs_plain": extra,
             "fwd_bwd": extra4,
             "mesh_build": extra2,
+            "viewer_frames": frames,
             "build": {"build_s": round(info["build_s"], 3), "scene_gen_s": round(info["gen_s"], 3),
                       "voxels_per_s": round(info["voxels"] / info["build_s"], 1)},
             "kernel_ms": {"primary": round(t_prim_avg, 3), "shadow": round(sum(t_shadow) / len(t_shadow), 3)},
@@ -530,6 +538,60 @@ def run_config3(args, torch, svo, scenes, tune_cache=None):
             "speedup": round(ms_plain / ms_batched, 3), "exact_hit_parity": bool(exact),
             "config": cfg.as_dict(), "autotune_s": round(tune_s, 1), "setup_s": round(setup_s, 1),
             "launches": {"plain": len(views), "batched": 1}}
+
+
+FRAME_W, FRAME_H, FRAME_STRIPS = 1280, 720, 16  # the viewer's GWidth, GHeight, NumThreads (Main.cpp:47-59)
+
+
+def run_frames(args, torch, svo, tree, cams, oracle=None, words=None, steps=None, label=None):
+    """The viewer's frame loop (svo_render_frame: beam prepass + per-pixel
+    trace + RGBA8, 1280x720 in 16 strips) over the cameras; device time per
+    frame from CUDA events, parity and a CPU time from the oracle's
+    restatement of renderBatch (all host threads)."""
+    steps = steps or args.steps
+    out = torch.empty((FRAME_H, FRAME_W), dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream()
+    for cam in cams[:max(1, args.warmup)]:
+        tree.render_frame(cam[:9], cam[9:12], FRAME_W, FRAME_H, FRAME_STRIPS, 1, out=out, stream=stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        for cam in cams:
+            tree.render_frame(cam[:9], cam[9:12], FRAME_W, FRAME_H, FRAME_STRIPS, 1, out=out, stream=stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / (steps * len(cams))
+    res = {"workload": label or "%d camera views" % len(cams), "frame": "%dx%d, %d strips" % (FRAME_W, FRAME_H,
+                                                                                           FRAME_STRIPS),
+           "frame_ms": round(ms, 4), "fps": round(1e3 / ms, 1), "mpix_s": round(FRAME_W * FRAME_H / ms / 1e3, 1)}
+    assert tree.device_status() == 0
+    if oracle is not None and words is not None:
+        exact = True
+        t_cpu, n_cpu = 0.0, 0
+        for cam in (cams[0], cams[-1]):
+            tree.render_frame(cam[:9], cam[9:12], FRAME_W, FRAME_H, FRAME_STRIPS, 1, out=out, stream=stream)
+            gpu = out.cpu().numpy().view(np.uint32)
+            t0 = time.perf_counter()
+            ref = oracle.render_frame(words, cam[:9], cam[9:12], FRAME_W, FRAME_H, FRAME_STRIPS, 1,
+                                      threads=cpu_threads())
+            t_cpu += time.perf_counter() - t0
+            n_cpu += 1
+            exact = exact and bool(np.array_equal(gpu, ref))
+        res["exact_vs_oracle"] = exact
+        res["cpu_baseline"] = {"fps": round(n_cpu / t_cpu, 2), "cores": cpu_threads(), "kind": "port",
+                               "sample": "%d frames of the oracle's renderBatch restatement" % n_cpu}
+    return res
+
+
+def run_dragon_frames(args, torch, svo, scenes, oracle=None):
+    """The viewer's own model: the shipped XYZRGB dragon octree (words from
+    the committed fixture) at 1280x720 from 16 orbit cameras."""
+    g = np.load(os.path.join(ROOT, "tests", "golden", "dragon.npz"))
+    tree = svo.VoxelOctree.from_words(g["words"], g["center"])
+    cams = scenes.orbit_cameras(16, 77, g["center"], radius=1.0, radius_hi=2.0, pitch=45.0)
+    return run_frames(args, torch, svo, tree, cams, oracle, g["words"] if oracle is not None else None,
+                      steps=max(args.steps, 20), label="XYZRGB dragon (119,887 words), 16 camera views")
 
 
 MESH_LEVEL, MESH_SEED, MESH_SIDE, MESH_THREADS, MESH_MEM = 7, 3, 1024, 16, 1 << 30

@@ -265,6 +265,23 @@ int svo_trace_image_host(svo_octree *oct, const float *rays, uint32_t width, uin
 int svo_trace_count_loads(const svo_octree *oct, const float *rays, uint64_t n, float ray_scale,
                           uint32_t *loads, svo_stream stream);
 
+/* The viewer's frame, headless: renderBatch + renderTile (Main.cpp:92-202)
+ * with its beam prepass.  The frame is cut into n_strips horizontal strips
+ * as the viewer cuts it over its threads (NumThreads = 16, Main.cpp:47,
+ * 349-361); per strip, level-of-detail corner rays every 8 pixels
+ * (coarseScale = 16 / (planeDist * height)) bound each 8x8 tile's start
+ * distance, tiles whose four corners all miss stay 0, and every other pixel
+ * is traced from pos + dir * max(minT - 0.03, 0) and written as the
+ * viewer's RGBA8 (0xFF000000 | grey * 0x010101).  pixel_stride 3 is the
+ * viewer's half-size mode (renderHalfSize).  rot = the viewer's
+ * INV_MODELVIEW rotation a11..a33 (row-major), pos = its camera position in
+ * the octree frame (tform * 0 + center + 1, Main.cpp:145); the headlight is
+ * derived from rot as the viewer does (:158).  rgba: width*height device
+ * words, row-major.  Asynchronous on `stream`; rays that stop at a bounds
+ * check set the handle's error word. */
+int svo_render_frame(const svo_octree *oct, const float rot[9], const float pos[3], uint32_t width, uint32_t height,
+                     uint32_t n_strips, uint32_t pixel_stride, uint32_t *rgba, svo_stream stream);
+
 /* ---------------------------------------------------- differentiable shading */
 
 /* No counterpart in the reference.  The viewer's shade() (Main.cpp:81-90)

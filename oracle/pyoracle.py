@@ -84,6 +84,10 @@ class Oracle:
         L.svo_oracle_build_mesh.restype = ctypes.c_int
         L.svo_oracle_build_mesh.argtypes = [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(_u32p),
                                             _u64p, _f32p]
+        L.svo_oracle_render_frame.restype = ctypes.c_int
+        L.svo_oracle_render_frame.argtypes = [_u32p, ctypes.c_uint64, _f32p, _f32p, ctypes.c_float, ctypes.c_int,
+                                              ctypes.c_int, ctypes.c_int, ctypes.c_int, _u32p, ctypes.c_int]
+        L.svo_oracle_plane_dist.restype = ctypes.c_float
         L.svo_oracle_tri_box_overlap.restype = ctypes.c_int
         L.svo_oracle_tri_box_overlap.argtypes = [_f32p, _f32p, _f32p]
         L.svo_oracle_build_sorted.restype = ctypes.c_int
@@ -211,6 +215,19 @@ class Oracle:
             return words, c
         finally:
             self.L.svo_oracle_mesh_destroy(m)
+
+    def render_frame(self, words, rot, pos, W=1280, H=720, n_strips=16, pixel_stride=1, threads=None):
+        """The viewer's frame (render_oracle.c): (H, W) uint32 RGBA8."""
+        words = np.ascontiguousarray(words, dtype=np.uint32)
+        rot = np.ascontiguousarray(rot, dtype=np.float32).reshape(9)
+        pos = np.ascontiguousarray(pos, dtype=np.float32).reshape(3)
+        out = np.zeros((H, W), np.uint32)
+        rc = self.L.svo_oracle_render_frame(_ptr(words, _u32p), words.size, _ptr(rot, _f32p), _ptr(pos, _f32p),
+                                            self.L.svo_oracle_plane_dist(), W, H, n_strips, pixel_stride,
+                                            _ptr(out, _u32p), threads or os.cpu_count() or 1)
+        if rc:
+            raise RuntimeError("svo_oracle_render_frame failed: %d" % rc)
+        return out
 
     def mesh_dims(self, pos, faces, side):
         pos = np.ascontiguousarray(pos, dtype=np.float32).reshape(-1, 3)

@@ -96,6 +96,15 @@ int svo_oracle_mesh_num_tris(void *mesh);
 void svo_oracle_mesh_destroy(void *mesh);
 int svo_oracle_build_mesh(void *mesh, int side, int threads, uint64_t mem, uint32_t **words, uint64_t *nwords,
                           float center[3]);
+/* render_oracle.c: the viewer's frame (Main.cpp:92-202, n_strips strips as
+ * its threads cut it, pixel_stride 1 or the half-size 3), RGBA8 into out
+ * (W*H words, row-major).  rot = tform a11..a33, pos = the camera position
+ * in the octree frame, plane_dist = svo_oracle_plane_dist(). */
+int svo_oracle_render_frame(const uint32_t *oct, uint64_t nwords, const float rot[9], const float pos[3],
+                            float plane_dist, int W, int H, int n_strips, int pixel_stride, uint32_t *out,
+                            int threads);
+float svo_oracle_plane_dist(void);
+
 /* Triangle/box overlap (separating axes), third-party/tribox3.c:132-206. */
 int svo_oracle_tri_box_overlap(const float center[3], const float half[3], const float verts[9]);
 

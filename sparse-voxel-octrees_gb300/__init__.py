@@ -114,6 +114,8 @@ def _load():
                                             _vp, _vp, _vp]),
         "svo_diff_backward": (ctypes.c_int, [_vp, _vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _vp, _vp, _vp,
                                              _vp, _vp, _vp, _vp, _vp]),
+        "svo_render_frame": (ctypes.c_int, [_vp, _f32p, _f32p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                            ctypes.c_uint32, _vp, _vp]),
         "svo_adam_step": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_uint64, ctypes.c_float, ctypes.c_float,
                                          ctypes.c_float, ctypes.c_float, ctypes.c_int, ctypes.c_int, _vp]),
         "svo_batch_create": (ctypes.c_int, [ctypes.POINTER(View), ctypes.c_int, ctypes.POINTER(_vp)]),
@@ -457,6 +459,19 @@ class VoxelOctree:
         check(lib.svo_diff_backward(self._h, _dev_ptr(rays), int(width), int(height), int(n_views), _dev_ptr(lights),
                                     _dev_ptr(leaf_rgb), _dev_ptr(leaf_normal), _dev_ptr(hit_leaf), _dev_ptr(d_rgb),
                                     _dev_ptr(grad_rgb), _dev_ptr(grad_normal), _stream_ptr(stream)))
+
+    def render_frame(self, rot, pos, width=1280, height=720, n_strips=16, pixel_stride=1, out=None, stream=None):
+        """The viewer's frame (svo_render_frame) into `out`, an int32 CUDA
+        tensor of height*width RGBA8 words (allocated when None)."""
+        import torch
+        r = np.ascontiguousarray(rot, dtype=np.float32).reshape(9)
+        p = np.ascontiguousarray(pos, dtype=np.float32).reshape(3)
+        if out is None:
+            out = torch.empty((height, width), dtype=torch.int32, device="cuda")
+        assert out.is_cuda and out.is_contiguous() and out.numel() == width * height
+        check(lib.svo_render_frame(self._h, r.ctypes.data_as(_f32p), p.ctypes.data_as(_f32p), width, height, n_strips,
+                                   pixel_stride, _dev_ptr(out), _stream_ptr(stream)))
+        return out
 
     def count_loads(self, rays, n=None, ray_scale=0.0, loads=None, stream=None):
         if n is None:
