@@ -387,7 +387,7 @@ def run_ours(args):
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": profiled_traffic(Rp),
                 "kernel": "k_trace_single (svo_trace_image, primary rays)", "peak_kind": peak_kind,
-                "algorithmic_bytes_per_launch": bytes_prim,
+                "algorithmic_bytes_per_launch": bytes_prim, "issue_bound": profiled_issue(),
                 "bytes_per_ray": round(bytes_prim / Rp, 2), "launch_ms": round(t_prim_avg, 3)}
 
     cpu = None
@@ -808,6 +808,29 @@ def profiled_traffic(rays):
     except OSError:
         pass
     return None
+
+
+def profiled_issue():
+    """Issue utilisation of the primary-ray kernel from the committed ncu
+    summary: the bound this kernel actually meets (it is issue-bound on the
+    ALU pipe, with DRAM at about 5% of peak)."""
+    path = os.path.join(ROOT, "profiles", "trace_image_config1.txt")
+    import re
+    out = {}
+    first = lambda line: float(re.findall(r"(?<![\w.])(\d+\.\d+|\d+)(?![\w.])", line.split(")")[-1] if ")" in line
+                                          else line.split(None, 1)[1])[0])
+    try:
+        for line in open(path):
+            if line.startswith("smsp__issue_active"):
+                out["issue_active_pct"] = first(line)
+            elif line.startswith("sm__inst_executed_pipe_alu"):
+                out["alu_pipe_pct"] = first(line)
+            elif line.startswith("smsp__thread_inst_executed_per_inst_executed"):
+                out["simt_lanes_of_32"] = first(line)
+    except (OSError, ValueError, IndexError):
+        return None
+    out["source"] = "profiles/trace_image_config1.txt (ncu --set full, same kernel, smaller case)"
+    return out or None
 
 
 def run_reference(args):

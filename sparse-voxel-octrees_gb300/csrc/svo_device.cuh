@@ -203,29 +203,34 @@ __device__ __forceinline__ bool ray_step(RayState &s, RayStack &stk, const uint3
         float centerTZ = half * s.dTz + cornerTZ;
 
         if (s.minT <= maxTV) {
-            uint64_t childOffset = s.current >> 18;
+            // Word indices are below 2^32 (n_words <= 2^32-1), so a far
+            // offset's high part (the descriptor's top 14 bits) must be 0 and
+            // all index sums fit 32 bits unless they wrap, which the bounds
+            // checks below catch.
+            uint32_t childOffset = s.current >> 18;
             if (s.current & 0x20000u) {
-                if (s.parent + 1u >= n_words) { res.status = kFault; return true; }
-                childOffset = (childOffset << 32) | (uint64_t)__ldg(oct + s.parent + 1);
+                if (childOffset != 0u || s.parent + 1u >= n_words) { res.status = kFault; return true; }
+                childOffset = __ldg(oct + s.parent + 1);
                 if (kCountLoads) ++s.nload;
             }
+            const uint32_t base = s.parent + childOffset;
+            if (base < s.parent) { res.status = kFault; return true; }  // wrapped
             if (!(childMasks & 0x80u)) {
-                uint64_t li = childOffset + s.parent +
-                              (uint64_t)__popc(((childMasks >> (8 + childShift)) << childShift) & 127u);
-                if (li >= n_words) { res.status = kFault; return true; }
+                uint32_t li = base + __popc(((childMasks >> (8 + childShift)) << childShift) & 127u);
+                if (li >= n_words || li < base) { res.status = kFault; return true; }
                 res.word = __ldg(oct + li);
-                res.leaf = (uint32_t)li;
+                res.leaf = li;
                 res.status = kLeafHit;
                 res.t = s.minT;
                 if (kCountLoads) ++s.nload;
                 return true;
             }
             uint32_t siblingCount = __popc(childMasks & 127u);
-            uint64_t np = (uint64_t)s.parent + childOffset + siblingCount;
+            uint32_t np = base + siblingCount;
             if (s.current & 0x10000u) np += siblingCount;
-            if (np >= n_words || s.scale <= 0 || ++s.pushes > kPushCap) { res.status = kFault; return true; }
+            if (np >= n_words || np < base || s.scale <= 0 || ++s.pushes > kPushCap) { res.status = kFault; return true; }
             stk.e[s.scale] = make_uint4(s.parent, __float_as_uint(s.maxT), s.current, 0u);
-            s.parent = (uint32_t)np;
+            s.parent = np;
             s.current = __ldg(oct + np);
             if (kCountLoads) ++s.nload;
 
