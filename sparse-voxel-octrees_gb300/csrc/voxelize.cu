@@ -255,7 +255,8 @@ template <int kMode>
 __global__ void k_tri_pairs(uint64_t n_tris, const float *__restrict__ tris, ListGeom g, int32_t *__restrict__ box,
                             uint8_t *__restrict__ block_flag, uint32_t *__restrict__ count,
                             const uint64_t *__restrict__ out_off, uint32_t *__restrict__ pair_key,
-                            uint32_t *__restrict__ pair_tri, uint32_t *__restrict__ err) {
+                            uint32_t *__restrict__ pair_tri, uint32_t *__restrict__ pair_cell,
+                            uint32_t *__restrict__ err) {
     uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n_tris) return;
     const float *T = tris + t * kTriFloats;
@@ -309,6 +310,7 @@ __global__ void k_tri_pairs(uint64_t n_tris, const float *__restrict__ tris, Lis
                     if (kMode == 1) {
                         pair_key[o + n] = (uint32_t)morton3((uint32_t)bx, (uint32_t)by, (uint32_t)bz);
                         pair_tri[o + n] = (uint32_t)t;
+                        pair_cell[o + n] = (uint32_t)gx + (uint32_t)g.grid[0] * ((uint32_t)gy + (uint32_t)g.grid[1] * (uint32_t)gz);
                     }
                     ++n;
                 }
@@ -329,6 +331,21 @@ __global__ void k_tri_pairs(uint64_t n_tris, const float *__restrict__ tris, Lis
         member(lg[0], lg[1], lg[2]);
     }
     if (kMode == 0) count[t] = n;
+}
+
+__global__ void k_iota(uint32_t *__restrict__ v, uint64_t n) {
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) v[i] = (uint32_t)i;
+}
+
+__global__ void k_gather_pairs(const uint32_t *__restrict__ idx, uint64_t n, const uint32_t *__restrict__ tri,
+                               const uint32_t *__restrict__ cell, uint32_t *__restrict__ stri,
+                               uint32_t *__restrict__ scell) {
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t k = idx[i];
+    stri[i] = tri[k];
+    scell[i] = cell[k];
 }
 
 // Unique bricks of the sorted pairs.
@@ -394,14 +411,16 @@ __global__ void k_center_table(int n_l, int K, float h, float *__restrict__ acc)
 struct FoldArgs {
     const float *tris;
     const int32_t *box;
-    const uint32_t *pair_tri;
+    const uint32_t *pair_tri;   // per sorted pair: triangle ...
+    const uint32_t *pair_cell;  // ... and the sub-block cell whose list it came from
     const uint32_t *bkey;
     const uint32_t *bstart;  // nb + 1 entries
     uint32_t b_first, b_last;
     int log_e;
     int sub[3];
-    int org[3];  // block origin
-    int buf[3];  // clamped block dims (the buffer's W/H/D for this block)
+    int grid[3];  // sub-block cells per axis (PlyLoader::_gridW/H/D)
+    int org[3];   // block origin
+    int buf[3];   // clamped block dims (the buffer's W/H/D for this block)
     const float *acc;
     int K;
     float half;
@@ -470,37 +489,50 @@ __device__ __forceinline__ void write_cell(uint32_t &w, uint32_t &cnt, float cx,
 }
 
 constexpr int kFoldWarps = 4;   // warps per CTA of the fold kernel
-constexpr int kFoldChunk = 16;  // triangles a warp stages per round
+constexpr int kFoldChunk = 8;   // pairs a warp stages per round (8-bit hit masks)
 
 struct FoldSmem {
     float T[kFoldChunk][kStageFloats];  // p, n, c
     int lo[kFoldChunk][3];              // running-sum start: max(triangle box low, sub-block start)
     int box[kFoldChunk][6];             // brick-local inclusive range of the clamped box
+    int pre[kFoldChunk + 1];            // prefix of the boxes' voxel counts
     float C[kFoldChunk][3][8];          // running centres of the brick's E coordinates per axis
     uint32_t w[512];                    // the brick's buffer words ...
     uint8_t cnt[512];                   // ... and counts (PlyLoader::_counts)
+    uint32_t mask[128];                 // per voxel, 8 bits: which staged pairs hit it
+    uint16_t list[512];                 // voxels with any hit in this round
     uint32_t touched[16];
 };
 
+// v / n and v % n for v < 1024, n <= 8 by a 16-bit fixed-point reciprocal
+// (exact: the error v / 2^16 stays below 1/n minus the largest fraction).
+__device__ __forceinline__ void divmod_small(int v, int n, int rcp, int &q, int &r) {
+    q = (v * rcp) >> 16;
+    r = v - q * n;
+}
+
 // One warp per brick.  The warp loads the brick's buffer cells, then takes
-// the brick's triangles in list order; for each, its lanes cover the voxels
-// of the triangle's clamped box inside the brick (triangleToVolume's loop
-// nest, PlyLoader.cpp:338-374), test them and fold the hits into the
-// brick's cells (a voxel is folded by one lane per triangle, triangles in
-// order), and finally writes the touched cells back.
-__global__ void __launch_bounds__(kFoldWarps * 32) k_fold_bricks(FoldArgs a) {
+// the brick's (triangle, sub-block) pairs in list order, 16 per round:
+//   1. every (pair, voxel of the pair's clamped box inside the brick) item of
+//      the round is spread over the lanes and tested (triangleToVolume's loop
+//      nest, PlyLoader.cpp:338-374), hits recorded as a per-voxel bit mask;
+//   2. the voxels with hits are compacted and each lane folds one voxel's
+//      hits in pair order with writeTriangleCell (PlyLoader.cpp:296-336).
+// A voxel lies in exactly one sub-block, so only pairs of its own cell reach
+// it, in ascending triangle order as that cell's list holds them.
+__global__ void __launch_bounds__(kFoldWarps * 32, 8) k_fold_bricks(FoldArgs a) {
     __shared__ FoldSmem smem[kFoldWarps];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     FoldSmem &sm = smem[wid];
     const int le = a.log_e, E = 1 << le, E3 = 1 << (3 * le);
     const float hv[3] = {a.half, a.half, a.half};
     const int end0 = a.org[0] + a.buf[0], end1 = a.org[1] + a.buf[1], end2 = a.org[2] + a.buf[2];
+    const uint32_t lt = (1u << lane) - 1u;
     const uint32_t nwarps = gridDim.x * kFoldWarps;
     for (uint32_t j = a.b_first + blockIdx.x * kFoldWarps + wid; j < a.b_last; j += nwarps) {
         const uint32_t key = a.bkey[j];
         const int ox = (int)(compact3(key) << le), oy = (int)(compact3((uint64_t)key >> 1) << le),
                   oz = (int)(compact3((uint64_t)key >> 2) << le);
-        const int sx = (ox / a.sub[0]) * a.sub[0], sy = (oy / a.sub[1]) * a.sub[1], sz = (oz / a.sub[2]) * a.sub[2];
         __syncwarp();
         for (int i = lane; i < E3; i += 32) {
             int x = ox + (i & (E - 1)), y = oy + ((i >> le) & (E - 1)), z = oz + (i >> (2 * le));
@@ -523,18 +555,36 @@ __global__ void __launch_bounds__(kFoldWarps * 32) k_fold_bricks(FoldArgs a) {
                 int q = i / kStageFloats, f = i - q * kStageFloats;
                 sm.T[q][f] = a.tris[(uint64_t)a.pair_tri[c0 + q] * kTriFloats + f];
             }
+            for (int i = lane; i < ((E3 + 3) >> 2); i += 32) sm.mask[i] = 0;
+            int items = 0;
             if (lane < nc) {
                 const int32_t *bx = a.box + (uint64_t)a.pair_tri[c0 + lane] * 6;
-                const int o[3] = {ox, oy, oz}, st3[3] = {sx, sy, sz}, en[3] = {end0, end1, end2};
+                const uint32_t cell = a.pair_cell[c0 + lane];
+                const int g0 = (int)(cell % (uint32_t)a.grid[0]), g12 = (int)(cell / (uint32_t)a.grid[0]);
+                const int g1 = g12 % a.grid[1], g2 = g12 / a.grid[1];
+                const int o[3] = {ox, oy, oz}, st3[3] = {g0 * a.sub[0], g1 * a.sub[1], g2 * a.sub[2]};
+                const int en[3] = {end0, end1, end2};
+                items = 1;
 #pragma unroll
                 for (int ax = 0; ax < 3; ++ax) {
-                    int lo = max(bx[ax], st3[ax]);       // PlyLoader.cpp:344-346
-                    int hi = min(bx[3 + ax], en[ax] - 1);  // :347-349 (the sub-block end lies past the brick)
+                    int lo = max(bx[ax], st3[ax]);                                // PlyLoader.cpp:344-346
+                    int hi = min(bx[3 + ax], min(st3[ax] + a.sub[ax], en[ax]) - 1);  // :347-349
+                    int b0 = max(lo, o[ax]) - o[ax], b1 = min(hi, o[ax] + E - 1) - o[ax];
                     sm.lo[lane][ax] = lo;
-                    sm.box[lane][ax] = max(lo, o[ax]) - o[ax];
-                    sm.box[lane][3 + ax] = min(hi, o[ax] + E - 1) - o[ax];
+                    sm.box[lane][ax] = b0;
+                    sm.box[lane][3 + ax] = b1;
+                    items *= max(0, b1 - b0 + 1);
                 }
             }
+            // exclusive prefix of the items over the staged pairs
+            int incl = items;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                int n = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += n;
+            }
+            if (lane < nc) sm.pre[lane] = incl - items;
+            const int total = __shfl_sync(0xffffffffu, incl, 31);
             __syncwarp();
             for (int i = lane; i < nc * 3 * E; i += 32) {
                 int q = i / (3 * E), r = i - q * 3 * E, ax = r / E, k = r - ax * E;
@@ -545,24 +595,50 @@ __global__ void __launch_bounds__(kFoldWarps * 32) k_fold_bricks(FoldArgs a) {
                 sm.C[q][ax][k] = c;
             }
             __syncwarp();
-            for (int q = 0; q < nc; ++q) {
+            // 1. tests
+            for (int it = lane; it < total; it += 32) {
+                int q = 0;
+#pragma unroll
+                for (int step = kFoldChunk / 2; step; step >>= 1)
+                    if (q + step < nc && sm.pre[q + step] <= it) q += step;
+                const int v = it - sm.pre[q];
                 const int bx0 = sm.box[q][0], by0 = sm.box[q][1], bz0 = sm.box[q][2];
-                const int nx = sm.box[q][3] - bx0 + 1, ny = sm.box[q][4] - by0 + 1, nz = sm.box[q][5] - bz0 + 1;
-                if (nx <= 0 || ny <= 0 || nz <= 0) continue;  // warp-uniform
-                const int n = nx * ny * nz;
-                for (int v = lane; v < n; v += 32) {
-                    const int r = v / nx;
-                    const int ix = bx0 + (v - r * nx), iy = by0 + r % ny, iz = bz0 + r / ny;
-                    const float fx = sm.C[q][0][ix], fy = sm.C[q][1][iy], fz = sm.C[q][2][iz];
-                    if (!tri_box(fx, fy, fz, hv, &sm.T[q][kTriP])) continue;
+                const int nx = sm.box[q][3] - bx0 + 1, ny = sm.box[q][4] - by0 + 1;
+                int r, ix, iy, iz;
+                divmod_small(v, nx, (65536 + nx - 1) / nx, r, ix);
+                divmod_small(r, ny, (65536 + ny - 1) / ny, iz, iy);
+                ix += bx0;
+                iy += by0;
+                iz += bz0;
+                if (tri_box(sm.C[q][0][ix], sm.C[q][1][iy], sm.C[q][2][iz], hv, &sm.T[q][kTriP])) {
                     const int idx = ix + (iy << le) + (iz << (2 * le));
-                    uint32_t wv = sm.w[idx], cv = sm.cnt[idx];
-                    write_cell(wv, cv, fx, fy, fz, &sm.T[q][0]);
-                    sm.w[idx] = wv;
-                    sm.cnt[idx] = (uint8_t)cv;
-                    atomicOr(&sm.touched[idx >> 5], 1u << (idx & 31));
+                    atomicOr(&sm.mask[idx >> 2], 1u << (q + ((idx & 3) << 3)));
                 }
-                __syncwarp();
+            }
+            __syncwarp();
+            // 2. compaction of the voxels with hits, then the ordered fold
+            int nhit = 0;
+            for (int b0 = 0; b0 < E3; b0 += 32) {
+                const int idx = b0 + lane;
+                const bool hit = idx < E3 && ((sm.mask[idx >> 2] >> ((idx & 3) << 3)) & 0xFFu) != 0;
+                const uint32_t ball = __ballot_sync(0xffffffffu, hit);
+                if (hit) sm.list[nhit + __popc(ball & lt)] = (uint16_t)idx;
+                nhit += __popc(ball);
+            }
+            __syncwarp();
+            for (int k = lane; k < nhit; k += 32) {
+                const int idx = sm.list[k];
+                uint32_t m = (sm.mask[idx >> 2] >> ((idx & 3) << 3)) & 0xFFu;
+                const int ix = idx & (E - 1), iy = (idx >> le) & (E - 1), iz = idx >> (2 * le);
+                uint32_t wv = sm.w[idx], cv = sm.cnt[idx];
+                while (m) {
+                    const int q = __ffs(m) - 1;
+                    m &= m - 1;
+                    write_cell(wv, cv, sm.C[q][0][ix], sm.C[q][1][iy], sm.C[q][2][iz], &sm.T[q][0]);
+                }
+                sm.w[idx] = wv;
+                sm.cnt[idx] = (uint8_t)cv;
+                atomicOr(&sm.touched[idx >> 5], 1u << (idx & 31));
             }
         }
         __syncwarp();
@@ -821,8 +897,7 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
         g.cell_h[k] = (float)sub[k] / (float)(side - 4);
     }
     g.grid_scale = (float)(side - 4);
-    const int min_sub = std::min(sub[0], std::min(sub[1], sub[2]));
-    g.log_e = std::min(3, log2_floor((uint64_t)min_sub));
+    g.log_e = std::min(3, lb);  // 8^3 bricks (the block edge when smaller); pairs carry their sub-block
     g.log_block = lb;
     const int lbv = D - lb;  // log2 of blocks per axis
     g.n_blocks = 1ull << (3 * lbv);
@@ -855,33 +930,45 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
     uint64_t n_pairs = 0;
     if (nt) {
         k_tri_pairs<0><<<grid_for(nt, 128), 128, 0, st>>>(nt, m->d_tris, g, box.p, bflag.p, pcount.p, nullptr,
-                                                          nullptr, nullptr, err.p);
+                                                          nullptr, nullptr, nullptr, err.p);
         SVO_LAUNCH_OK("k_tri_pairs<count>");
         int rc = scan_total<uint32_t, uint64_t>(pcount.p, poff.p, nt, &n_pairs, st);
         if (rc) return rc;
     }
     if (n_pairs >= 0xFFFFFFFFull)
         return set_error(SVO_ERR_LIMIT, "%llu brick/triangle pairs exceed 2^32-1", (unsigned long long)n_pairs);
-    Dev<uint32_t> pk, pt, pk2, pt2, sort_scratch;
+    Dev<uint32_t> pk, pt, pc, pi, pk2, pi2, stri_buf, scell_buf, sort_scratch;
     SVO_ALLOC(pk, n_pairs);
     SVO_ALLOC(pt, n_pairs);
+    SVO_ALLOC(pc, n_pairs);
+    SVO_ALLOC(pi, n_pairs);
     SVO_ALLOC(pk2, n_pairs);
-    SVO_ALLOC(pt2, n_pairs);
+    SVO_ALLOC(pi2, n_pairs);
     if (n_pairs) {
         k_tri_pairs<1><<<grid_for(nt, 128), 128, 0, st>>>(nt, m->d_tris, g, box.p, bflag.p, pcount.p, poff.p, pk.p,
-                                                          pt.p, err.p);
+                                                          pt.p, pc.p, err.p);
         SVO_LAUNCH_OK("k_tri_pairs<emit>");
+        k_iota<<<grid_for(n_pairs), 256, 0, st>>>(pi.p, n_pairs);
+        SVO_LAUNCH_OK("k_iota");
     }
     pcount.release();
     poff.release();
 
-    // 3. stable sort by brick
+    // 3. stable sort by brick, then the pairs' triangles and cells in that order
     SVO_ALLOC(sort_scratch, radix_scratch_elems(n_pairs));
     bool in_alt = false;
-    SVO_CUDA_TRY(radix_sort_pairs(pk.p, pt.p, pk2.p, pt2.p, n_pairs, key_bits, sort_scratch.p, st, &in_alt));
+    SVO_CUDA_TRY(radix_sort_pairs(pk.p, pi.p, pk2.p, pi2.p, n_pairs, key_bits, sort_scratch.p, st, &in_alt));
     sort_scratch.release();
     const uint32_t *skey = in_alt ? pk2.p : pk.p;
-    const uint32_t *stri = in_alt ? pt2.p : pt.p;
+    const uint32_t *sidx = in_alt ? pi2.p : pi.p;
+    SVO_ALLOC(stri_buf, n_pairs);
+    SVO_ALLOC(scell_buf, n_pairs);
+    if (n_pairs) {
+        k_gather_pairs<<<grid_for(n_pairs), 256, 0, st>>>(sidx, n_pairs, pt.p, pc.p, stri_buf.p, scell_buf.p);
+        SVO_LAUNCH_OK("k_gather_pairs");
+    }
+    const uint32_t *stri = stri_buf.p;
+    const uint32_t *scell = scell_buf.p;
 
     // unique bricks and per-block brick ranges
     Dev<uint32_t> head, hidx, bkey, bstart, rfirst, rlast;
@@ -1017,6 +1104,8 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
             fa.tris = m->d_tris;
             fa.box = box.p;
             fa.pair_tri = stri;
+            fa.pair_cell = scell;
+            for (int k = 0; k < 3; ++k) fa.grid[k] = g.grid[k];
             fa.bkey = bkey.p;
             fa.bstart = bstart.p;
             fa.b_first = j.first;
