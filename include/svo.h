@@ -131,8 +131,18 @@ int svo_octree_build_dense(const uint32_t *grid, int w, int h, int d, uint64_t m
                            svo_stream stream, svo_octree **out);
 
 /* Same as svo_octree_build_dense, reading a .voxel file (int32 w, h, d then
- * w*h*d uint32, x fastest), i.e. VoxelData(const char *path, size_t mem). */
+ * w*h*d uint32, x fastest), i.e. VoxelData(const char *path, size_t mem).
+ * A grid larger than half the free device memory is not loaded whole: the
+ * file is streamed in z slabs (as VoxelData reads it block by block,
+ * VoxelData.cpp:177-209), only occupied voxels are kept on the device, and a
+ * radix sort restores their Morton order; the words are the same. */
 int svo_octree_build_voxel_file(const char *path, uint64_t mem, svo_stream stream, svo_octree **out);
+
+/* svo_octree_build_voxel_file with the streamed form forced and slabs of
+ * about slab_bytes of device memory (at least 16 slices): for a bounded
+ * device footprint.  Needs a virtual side of at least 16. */
+int svo_octree_build_voxel_file_streamed(const char *path, uint64_t mem, uint64_t slab_bytes, svo_stream stream,
+                                         svo_octree **out);
 
 /* No counterpart in the reference.  The GPU build of svo_octree_build_dense
  * for callers that cannot allocate device memory while they run: a host

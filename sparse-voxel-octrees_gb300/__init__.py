@@ -89,6 +89,8 @@ def _load():
         "svo_octree_build_dense": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_uint64,
                                                   ctypes.c_int, _vp, ctypes.POINTER(_vp)]),
         "svo_octree_build_voxel_file": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_uint64, _vp, ctypes.POINTER(_vp)]),
+        "svo_octree_build_voxel_file_streamed": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_uint64, ctypes.c_uint64, _vp,
+                                                                ctypes.POINTER(_vp)]),
         "svo_mesh_load_ply": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_vp)]),
         "svo_mesh_from_arrays": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_uint64, _vp, ctypes.c_uint64,
                                                 ctypes.POINTER(_vp)]),
@@ -262,7 +264,8 @@ class VoxelData:
     which its voxelization depends on), or an in-memory dense grid of shape
     (d, h, w), x fastest, 0 = empty (a numpy array or a CUDA tensor)."""
 
-    def __init__(self, source, side=None, mem=DEFAULT_MEM, threads=None):
+    def __init__(self, source, side=None, mem=DEFAULT_MEM, threads=None, slab_bytes=0):
+        self.slab_bytes = int(slab_bytes)  # > 0: stream a .voxel file in slabs of about this many device bytes
         self.path = None
         self.grid = None
         self.loader = None
@@ -300,6 +303,9 @@ class VoxelOctree:
             if source.loader is not None:
                 check(lib.svo_octree_build_mesh(source.loader._h, source.side, source.threads, source.mem,
                                                 _stream_ptr(stream), ctypes.byref(self._h)))
+            elif source.path is not None and source.slab_bytes > 0:
+                check(lib.svo_octree_build_voxel_file_streamed(os.fsencode(source.path), source.mem, source.slab_bytes,
+                                                               _stream_ptr(stream), ctypes.byref(self._h)))
             elif source.path is not None:
                 check(lib.svo_octree_build_voxel_file(os.fsencode(source.path), source.mem, _stream_ptr(stream),
                                                       ctypes.byref(self._h)))

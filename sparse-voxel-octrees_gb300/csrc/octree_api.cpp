@@ -364,7 +364,12 @@ int svo_octree_build_dense(const uint32_t *grid, int w, int h, int d, uint64_t m
     return make_handle(dw, nw, center, out);
 }
 
-int svo_octree_build_voxel_file(const char *path, uint64_t mem, svo_stream stream, svo_octree **out) {
+// The .voxel build: the whole grid on the device when it fits in half the
+// free device memory, else streamed in z slabs (voxel_stream.cu).  Both give
+// the same words.  slab_bytes > 0 forces the streamed form with slabs of
+// about that many bytes.
+static int build_voxel_file_impl(const char *path, uint64_t mem, uint64_t slab_bytes, svo_stream stream,
+                                 svo_octree **out) {
     if (!path || !out) return set_error(SVO_ERR_INVALID, "null argument");
     FILE *fp = fopen(path, "rb");
     if (!fp) return set_error(SVO_ERR_IO, "cannot open %s", path);
@@ -374,6 +379,26 @@ int svo_octree_build_voxel_file(const char *path, uint64_t mem, svo_stream strea
     int w = dims[0], h = dims[1], d = dims[2];
     if (w <= 0 || h <= 0 || d <= 0) return set_error(SVO_ERR_FORMAT, "%s: bad dimensions", path);
     const uint64_t slab = (uint64_t)w * h;
+    const int side = std::max(round_to_pow2(w), std::max(round_to_pow2(h), round_to_pow2(d)));
+    if (side > 65536) return set_error(SVO_ERR_LIMIT, "virtual side %d above 65536", side);
+    bool streamed = slab_bytes > 0 && side >= 16;
+    if (!streamed && side >= 16) {
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && slab * d * 4 > free_b / 2) {
+            streamed = true;
+            slab_bytes = std::min<uint64_t>(free_b / 8, 8ull << 30);
+        }
+    }
+    if (streamed) {
+        int lb = cache_block_log2(w, h, d, mem, 4);
+        if (lb < 1) return set_error(SVO_ERR_MEMORY, "memory budget %llu admits no cache block", (unsigned long long)mem);
+        uint32_t *dw = nullptr;
+        uint64_t nw = 0;
+        float center[3];
+        int rc = build_voxel_file_streamed(fp, w, h, d, mem, slab_bytes, (cudaStream_t)stream, &dw, &nw, center);
+        if (rc) return rc;
+        return make_handle(dw, nw, center, out);
+    }
     uint32_t *dg = nullptr;
     SVO_CUDA_TRY(cudaMalloc((void **)&dg, slab * d * 4));
     std::unique_ptr<uint32_t, cudaError_t (*)(void *)> dguard(dg, cudaFree);
@@ -390,6 +415,16 @@ int svo_octree_build_voxel_file(const char *path, uint64_t mem, svo_stream strea
         SVO_CUDA_TRY(cudaMemcpy(dg + z * slab, pin, want * 4, cudaMemcpyHostToDevice));
     }
     return svo_octree_build_dense(dg, w, h, d, mem, 1, stream, out);
+}
+
+int svo_octree_build_voxel_file(const char *path, uint64_t mem, svo_stream stream, svo_octree **out) {
+    return build_voxel_file_impl(path, mem, 0, stream, out);
+}
+
+int svo_octree_build_voxel_file_streamed(const char *path, uint64_t mem, uint64_t slab_bytes, svo_stream stream,
+                                         svo_octree **out) {
+    if (slab_bytes == 0) return set_error(SVO_ERR_INVALID, "slab_bytes must be > 0");
+    return build_voxel_file_impl(path, mem, slab_bytes, stream, out);
 }
 
 int svo_trace(const svo_octree *oct, const float *rays, uint64_t n, float ray_scale, const float light[3],

@@ -1,4 +1,4 @@
-// sort.cuh — stable LSD radix sort of (uint32 key, uint32 value) pairs.
+// sort.cuh — stable LSD radix sort of (uint32 or uint64 key, uint32 value) pairs.
 //
 // Eight-bit digits, three launches per digit:
 //   1. per 4096-item tile, a digit histogram written digit-major
@@ -22,7 +22,8 @@ constexpr int kSortWarps = 8;
 constexpr int kSortPerLane = 16;
 constexpr int kSortTile = kSortWarps * 32 * kSortPerLane;  // 4096
 
-__global__ void __launch_bounds__(kSortWarps * 32) k_radix_hist(const uint32_t *__restrict__ keys, uint64_t n,
+template <typename K>
+__global__ void __launch_bounds__(kSortWarps * 32) k_radix_hist(const K *__restrict__ keys, uint64_t n,
                                                                int shift, uint32_t tiles, uint32_t *__restrict__ hist) {
     __shared__ uint32_t cnt[256];
     for (int i = threadIdx.x; i < 256; i += blockDim.x) cnt[i] = 0;
@@ -30,17 +31,18 @@ __global__ void __launch_bounds__(kSortWarps * 32) k_radix_hist(const uint32_t *
     const uint64_t base = (uint64_t)blockIdx.x * kSortTile;
     for (int i = threadIdx.x; i < kSortTile; i += blockDim.x) {
         uint64_t k = base + (uint64_t)i;
-        if (k < n) atomicAdd(&cnt[(keys[k] >> shift) & 255u], 1u);
+        if (k < n) atomicAdd(&cnt[(uint32_t)(keys[k] >> shift) & 255u], 1u);
     }
     __syncthreads();
     for (int d = threadIdx.x; d < 256; d += blockDim.x) hist[(uint64_t)d * tiles + blockIdx.x] = cnt[d];
 }
 
-__global__ void __launch_bounds__(kSortWarps * 32) k_radix_scatter(const uint32_t *__restrict__ kin,
+template <typename K>
+__global__ void __launch_bounds__(kSortWarps * 32) k_radix_scatter(const K *__restrict__ kin,
                                                                   const uint32_t *__restrict__ vin, uint64_t n,
                                                                   int shift, uint32_t tiles,
                                                                   const uint32_t *__restrict__ slot,
-                                                                  uint32_t *__restrict__ kout,
+                                                                  K *__restrict__ kout,
                                                                   uint32_t *__restrict__ vout) {
     __shared__ uint32_t wcnt[kSortWarps][256];
     __shared__ uint32_t gbase[256];
@@ -51,13 +53,14 @@ __global__ void __launch_bounds__(kSortWarps * 32) k_radix_scatter(const uint32_
 
     const uint64_t base = (uint64_t)blockIdx.x * kSortTile + (uint64_t)warp * (32 * kSortPerLane);
     const uint32_t lt = (1u << lane) - 1u;
-    uint32_t key[kSortPerLane], rank[kSortPerLane];
+    K key[kSortPerLane];
+    uint32_t rank[kSortPerLane];
 #pragma unroll
     for (int j = 0; j < kSortPerLane; ++j) {
         uint64_t i = base + (uint64_t)j * 32 + lane;
         bool valid = i < n;
-        key[j] = valid ? kin[i] : 0u;
-        uint32_t digit = valid ? ((key[j] >> shift) & 255u) : 256u;
+        key[j] = valid ? kin[i] : K(0);
+        uint32_t digit = valid ? ((uint32_t)(key[j] >> shift) & 255u) : 256u;
         uint32_t peers = __match_any_sync(0xffffffffu, digit);
         uint32_t before = valid ? wcnt[warp][digit] : 0u;
         __syncwarp();
@@ -79,7 +82,7 @@ __global__ void __launch_bounds__(kSortWarps * 32) k_radix_scatter(const uint32_
     for (int j = 0; j < kSortPerLane; ++j) {
         uint64_t i = base + (uint64_t)j * 32 + lane;
         if (i < n) {
-            uint32_t digit = (key[j] >> shift) & 255u;
+            uint32_t digit = (uint32_t)(key[j] >> shift) & 255u;
             uint32_t pos = gbase[digit] + wcnt[warp][digit] + rank[j];
             kout[pos] = key[j];
             vout[pos] = vin[i];
@@ -94,27 +97,31 @@ inline uint64_t radix_scratch_elems(uint64_t n) {
     return 2 * h + scan_scratch_elems(h) + 1;
 }
 
-// Sorts n pairs by the low `bits` bits of the keys, stably.  The pairs move
-// between (k, v) and (k_alt, v_alt); *in_alt tells which pair of arrays holds
-// the result.  n < 2^32.
-inline cudaError_t radix_sort_pairs(uint32_t *k, uint32_t *v, uint32_t *k_alt, uint32_t *v_alt, uint64_t n,
+// Sorts n pairs (key K = uint32_t or uint64_t, uint32 value) by the low
+// `bits` bits of the keys, stably.  The pairs move between (k, v) and
+// (k_alt, v_alt); *in_alt tells which pair of arrays holds the result.
+// n < 2^32.
+template <typename K>
+inline cudaError_t radix_sort_pairs(K *k, uint32_t *v, K *k_alt, uint32_t *v_alt, uint64_t n,
                                     int bits, uint32_t *scratch, cudaStream_t st, bool *in_alt) {
     *in_alt = false;
     if (n <= 1 || bits <= 0) return cudaSuccess;
     const uint32_t tiles = (uint32_t)((n + kSortTile - 1) / kSortTile);
     const uint64_t h = 256ull * tiles;
     uint32_t *hist = scratch, *slot = scratch + h, *total = scratch + 2 * h, *sc = scratch + 2 * h + 1;
-    uint32_t *ki = k, *vi = v, *ko = k_alt, *vo = v_alt;
+    K *ki = k, *ko = k_alt;
+    uint32_t *vi = v, *vo = v_alt;
     for (int shift = 0; shift < bits; shift += 8) {
-        k_radix_hist<<<tiles, kSortWarps * 32, 0, st>>>(ki, n, shift, tiles, hist);
+        k_radix_hist<K><<<tiles, kSortWarps * 32, 0, st>>>(ki, n, shift, tiles, hist);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         e = exclusive_scan<uint32_t, uint32_t>(hist, slot, h, total, sc, st);
         if (e != cudaSuccess) return e;
-        k_radix_scatter<<<tiles, kSortWarps * 32, 0, st>>>(ki, vi, n, shift, tiles, slot, ko, vo);
+        k_radix_scatter<K><<<tiles, kSortWarps * 32, 0, st>>>(ki, vi, n, shift, tiles, slot, ko, vo);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
-        uint32_t *tk = ki, *tv = vi;
+        K *tk = ki;
+        uint32_t *tv = vi;
         ki = ko;
         vi = vo;
         ko = tk;

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdarg>
+#include <cstdio>
 #include <cstdint>
 #include <cstring>
 #include <memory>
@@ -74,6 +75,11 @@ int build_dense_device(const uint32_t *d_grid, int w, int h, int d, int log_side
 int build_from_sorted_device(const uint64_t *d_keys, const uint32_t *d_payload, uint64_t n, int log_side,
                              int log_block, const uint8_t *d_topflag, cudaStream_t st, uint32_t **d_words,
                              uint64_t *n_words);
+
+// The .voxel build streamed in z slabs of about slab_bytes (voxel_stream.cu);
+// fp is positioned after the 12-byte header.
+int build_voxel_file_streamed(FILE *fp, int w, int h, int d, uint64_t mem, uint64_t slab_bytes, cudaStream_t st,
+                              uint32_t **d_words, uint64_t *n_words, float center[3]);
 
 // Trace launchers (trace.cu).
 int launch_trace(const svo_octree *oct, const float *d_rays, uint64_t n, float ray_scale, const float light[3],

@@ -113,3 +113,51 @@ def test_voxel_file_build_and_save_load(svo, oracle, scenes, tmp_path):
     assert np.array_equal(back.words(), ow) and np.array_equal(back.center(), oc)
     w2, c2 = oracle.oct_decode(open(p, "rb").read())
     assert np.array_equal(w2, ow)
+
+
+def _streamed(svo, path, mem, slices, plane):
+    tree = svo.VoxelOctree(svo.VoxelData(path, mem, slab_bytes=slices * plane * 4))
+    return tree.words(), tree.center()
+
+
+def test_streamed_voxel_file_golden(svo, golden, tmp_path):
+    """The streamed .voxel build (16-slice slabs) against the reference's own
+    word streams."""
+    n = 0
+    for grid, mem, words, center in golden_builds(golden):
+        d, h, w = grid.shape
+        if max(w, h, d) < 16:
+            continue
+        path = str(tmp_path / "g.voxel")
+        pyoracle.write_voxel_file(path, grid)
+        ws, c = _streamed(svo, path, mem, 16, w * h)
+        assert np.array_equal(ws, words), (grid.shape, mem)
+        assert np.array_equal(c, center)
+        n += 1
+    assert n >= 8
+
+
+@pytest.mark.parametrize("shape,density,mem,slices", [((77, 90, 101), 0.02, 1 << 30, 16),
+                                                        ((64, 64, 63), 0.3, 20000, 32),
+                                                        ((200, 150, 131), 0.001, 100000, 48),
+                                                        ((17, 300, 47), 0.05, 60000, 16)])
+def test_streamed_voxel_file_matches_oracle(svo, oracle, scenes, tmp_path, shape, density, mem, slices):
+    grid = scenes.random_grid(shape, density, sum(shape))
+    d, h, w = grid.shape
+    path = str(tmp_path / "r.voxel")
+    pyoracle.write_voxel_file(path, grid)
+    ow, oc = oracle.build_dense(grid, mem)
+    ws, c = _streamed(svo, path, mem, slices, w * h)
+    assert np.array_equal(ws, ow) and np.array_equal(c, oc)
+    # the whole-grid form of the same file agrees
+    tree = svo.VoxelOctree(svo.VoxelData(path, mem))
+    assert np.array_equal(tree.words(), ow)
+
+
+def test_streamed_terrain_scene(svo, oracle, scenes, tmp_path):
+    grid = scenes.terrain_scene(256, 20, 3)
+    path = str(tmp_path / "t.voxel")
+    pyoracle.write_voxel_file(path, grid)
+    ow, oc = oracle.build_dense(grid, 1 << 20)
+    ws, c = _streamed(svo, path, 1 << 20, 64, 256 * 256)
+    assert np.array_equal(ws, ow) and np.array_equal(c, oc)
