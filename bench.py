@@ -411,7 +411,7 @@ def run_ours(args):
                   "dragon": run_dragon_frames(args, torch, svo, scenes, oracle)}
     del words
 
-    extra = extra2 = extra4 = None
+    extra = extra2 = extra4 = extra_vf = None
     if not args.no_extra and world == 1:
         del prim, shadow, out_p, out_s, ref_p, ref_s, tree
         torch.cuda.empty_cache()
@@ -420,6 +420,8 @@ def run_ours(args):
         extra4 = run_config4(args, torch, svo, scenes)
         torch.cuda.empty_cache()
         extra2 = run_config2(args, torch, svo, scenes, steps=3, warmup=1, check=not args.no_cpu)
+        torch.cuda.empty_cache()
+        extra_vf = run_voxel_file(args, torch, svo, scenes)
 
     if rank == 0:
         line = {
@@ -448,6 +450,7 @@ def run_ours(args):
             "fwd_bwd": extra4,
             "mesh_build": extra2,
             "viewer_frames": frames,
+            "voxel_file_build": extra_vf,
             "build": {"build_s": round(info["build_s"], 3), "scene_gen_s": round(info["gen_s"], 3),
                       "voxels_per_s": round(info["voxels"] / info["build_s"], 1)},
             "kernel_ms": {"primary": round(t_prim_avg, 3), "shadow": round(sum(t_shadow) / len(t_shadow), 3)},
@@ -709,6 +712,48 @@ def run_config2(args, torch, svo, scenes, steps=None, warmup=None, check=True):
     os.unlink(path)
     os.rmdir(tmp)
     return out
+
+
+def run_voxel_file(args, torch, svo, scenes, side=512, slab_mib=64):
+    """VoxelData(path, mem) + VoxelOctree from a .voxel file: the whole grid
+    on the device versus the streamed form (slabs of about slab_mib MiB),
+    both timed from the file (page cache warm) to the resident octree."""
+    import tempfile
+    grid = scenes.gpu_terrain_scene(side, 60, 5)
+    d, h, w = grid.shape
+    tmp = tempfile.mkdtemp(prefix="svo_vox_")
+    path = os.path.join(tmp, "scene.voxel")
+    with open(path, "wb") as f:
+        f.write(np.array([w, h, d], np.int32).tobytes())
+        f.write(grid.cpu().numpy().tobytes())
+    del grid
+    torch.cuda.empty_cache()
+
+    def timed(data):
+        best, tree = None, None
+        for _ in range(3):
+            tree = None
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            tree = svo.VoxelOctree(data)
+            torch.cuda.synchronize()
+            s = time.perf_counter() - t0
+            best = s if best is None else min(best, s)
+        return best, tree
+
+    mem = 1 << 30
+    t_whole, a = timed(svo.VoxelData(path, mem))
+    t_stream, b = timed(svo.VoxelData(path, mem, slab_bytes=slab_mib << 20))
+    nd, nl = a.validate()
+    exact = bool(np.array_equal(a.words(), b.words()))
+    os.unlink(path)
+    os.rmdir(tmp)
+    return {"workload": "%d^3 terrain + 60 spheres as a .voxel file (%.1f GiB), 1 GiB budget" % (side, w * h * d * 4 / 2 ** 30),
+            "voxels": int(nl), "whole_grid_ms": round(t_whole * 1e3, 1), "streamed_ms": round(t_stream * 1e3, 1),
+            "streamed_slab_mib": slab_mib, "streamed_voxels_per_s": round(nl / t_stream, 1),
+            "streamed_equals_whole": exact,
+            "note": "file read from the page cache inside the timed region; the streamed form keeps one slab and "
+                    "the occupied voxels on the device instead of the whole grid"}
 
 
 def run_config4(args, torch, svo, scenes, n_steps=200):
