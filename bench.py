@@ -190,7 +190,16 @@ def setup_scene(args, rank, torch, svo, scenes):
     hit = torch.empty(R, dtype=torch.uint8, device="cuda")
     tree.trace(prim, out={"t": t, "hit": hit})
     torch.cuda.synchronize()
-    idx = torch.nonzero(hit == 1).squeeze(1)
+    # one shadow ray per hit, ordered by 8x4 pixel tile within each camera so
+    # that a warp's 32 consecutive shadow rays start at neighbouring pixels
+    pix = torch.arange(npix, device="cuda")
+    px, py = pix % args.width, pix // args.width
+    tiles_x = (args.width + 7) // 8
+    tile_key = ((py // 4) * tiles_x + px // 8) * 32 + (py % 4) * 8 + px % 8
+    order = torch.argsort(tile_key)
+    perm = (torch.arange(len(cams), device="cuda")[:, None] * npix + order[None, :]).reshape(-1)
+    idx = perm[hit[perm] == 1]
+    del pix, px, py, tile_key, order, perm
     o = prim[idx, :3]
     d = prim[idx, 3:]
     p = o + t[idx, None] * d
@@ -432,6 +441,7 @@ def run_ours(args):
             "config": {"workload": "plain traversal: %d^3 octree (terrain + %d spheres), %d cams %dx%d primary rays "
                                    "+ 1 shadow ray per hit" % (args.side, N_SPHERES, args.cams, args.width,
                                                                args.height),
+                       "shadow_ray_order": "per camera, by 8x4 pixel tile",
                        "api": "svo_trace_image (primary, 8x4-pixel tiles, persistent) + svo_trace (shadow)",
                        "octree_words": info["words"], "voxels": info["voxels"], "primary_rays": Rp,
                        "shadow_rays": Rs, "rays_per_step": rays_per_step,
