@@ -284,7 +284,7 @@ bool config_ok(const svo_trace_config &c) {
 // svo_trace_image: rays in row-major image order, traced in tile_w x (32 /
 // tile_w) pixel tiles by one persistent launch.
 int launch_trace_image(const svo_octree *oct, const float *d_rays, uint32_t width, uint32_t height, float ray_scale,
-                       const float light[3], const svo_trace_out &out, cudaStream_t st) {
+                       const float light[3], const svo_trace_out &out, cudaStream_t st, int queue) {
     if (width == 0 || height == 0) return SVO_OK;
     const int tile_w = 8, log_tw = 3, chunk = 32, threads = 256;
     JobDev J;
@@ -311,9 +311,9 @@ int launch_trace_image(const svo_octree *oct, const float *d_rays, uint32_t widt
     SVO_CUDA_TRY(cudaGetDevice(&dev));
     SVO_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     SVO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, kern, threads, 0));
-    SVO_CUDA_TRY(cudaMemsetAsync(oct->d_queue, 0, sizeof(unsigned long long), st));
-    kern<<<(unsigned)(sms * std::max(1, resident)), threads, 0, st>>>(J, total, oct->d_queue, oct->d_status, log_tw,
-                                                                   chunk);
+    unsigned long long *q = oct->d_queue + queue;
+    SVO_CUDA_TRY(cudaMemsetAsync(q, 0, sizeof(unsigned long long), st));
+    kern<<<(unsigned)(sms * std::max(1, resident)), threads, 0, st>>>(J, total, q, oct->d_status, log_tw, chunk);
     SVO_CUDA_TRY(cudaGetLastError());
     return SVO_OK;
 }

@@ -13,7 +13,7 @@ namespace svo {
 namespace {
 thread_local std::string g_last_error;
 constexpr uint64_t kOctBlock = 64ull * 1024 * 1024;  // VoxelOctree.cpp:55
-constexpr uint64_t kStageRays = 1ull << 21;          // rays per staging chunk
+constexpr uint64_t kStageRays = 1ull << 22;          // rays per staging chunk
 }  // namespace
 
 int set_error(int code, const char *fmt, ...) {
@@ -85,7 +85,7 @@ int make_handle(uint32_t *d_words, uint64_t n_words, const float center[3], svo_
     }
     e = cudaMemset(h->d_status, 0, sizeof(uint32_t));
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemset(status)");
-    e = cudaMalloc((void **)&h->d_queue, sizeof(unsigned long long));
+    e = cudaMalloc((void **)&h->d_queue, 3 * sizeof(unsigned long long));
     if (e != cudaSuccess) {
         svo_octree_destroy(h.release());
         return cuda_fail(e, "cudaMalloc(queue)");
@@ -502,9 +502,10 @@ int svo_trace_image_host(svo_octree *oct, const float *rays, uint32_t width, uin
     const size_t half = al(C * 24) + al(C) + al(C * 4) * 3 + al(C * 12);
     int rc = ensure_staging(oct, 2 * half);
     if (rc) return rc;
-    // The persistent launch uses the handle's single work counter, so traces
-    // run one after another on the trace stream while the next chunk's rays
-    // come in and the previous chunk's results go out on two copy streams.
+    // Chunks alternate between two trace streams with their own work
+    // counters, so one chunk's launch fills the tail of the previous one,
+    // while the next chunk's rays come in and the previous chunk's results go
+    // out on two copy streams.
     if (!oct->img_streams[0]) {
         for (auto &st : oct->img_streams) SVO_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
         for (int k = 0; k < 2; ++k) {
@@ -513,10 +514,12 @@ int svo_trace_image_host(svo_octree *oct, const float *rays, uint32_t width, uin
             SVO_CUDA_TRY(cudaEventCreateWithFlags(&oct->img_out[k], cudaEventDisableTiming));
         }
     }
-    cudaStream_t si = oct->img_streams[0], sk = oct->img_streams[1], so = oct->img_streams[2];
+    cudaStream_t si = oct->img_streams[0], so = oct->img_streams[3];
+    cudaStream_t skh[2] = {oct->img_streams[1], oct->img_streams[2]};
     uint64_t j = 0;
     for (uint64_t y0 = 0; y0 < height; y0 += rows, ++j) {
         const int h = (int)(j & 1);
+        cudaStream_t sk = skh[h];
         uint64_t nr = std::min<uint64_t>(rows, height - y0);
         uint64_t m = nr * width, c0 = y0 * width;
         uint8_t *base = (uint8_t *)oct->stage_dev + h * half;
@@ -539,7 +542,7 @@ int svo_trace_image_host(svo_octree *oct, const float *rays, uint32_t width, uin
         o.leaf = out->leaf ? d_leaf : nullptr;
         o.word = out->word ? d_word : nullptr;
         o.rgb = out->rgb ? d_rgb : nullptr;
-        rc = launch_trace_image(oct, d_rays, width, (uint32_t)nr, ray_scale, light, o, sk);
+        rc = launch_trace_image(oct, d_rays, width, (uint32_t)nr, ray_scale, light, o, sk, 1 + h);
         if (rc) return rc;
         SVO_CUDA_TRY(cudaEventRecord(oct->img_traced[h], sk));
         SVO_CUDA_TRY(cudaStreamWaitEvent(so, oct->img_traced[h], 0));
@@ -551,7 +554,8 @@ int svo_trace_image_host(svo_octree *oct, const float *rays, uint32_t width, uin
         SVO_CUDA_TRY(cudaEventRecord(oct->img_out[h], so));
     }
     SVO_CUDA_TRY(cudaStreamSynchronize(si));
-    SVO_CUDA_TRY(cudaStreamSynchronize(sk));
+    SVO_CUDA_TRY(cudaStreamSynchronize(skh[0]));
+    SVO_CUDA_TRY(cudaStreamSynchronize(skh[1]));
     SVO_CUDA_TRY(cudaStreamSynchronize(so));
     return check_device_status(oct);
 }

@@ -21,7 +21,8 @@ struct svo_octree {
     float center[3] = {0.0f, 0.0f, 0.0f};
     int device = 0;
     uint32_t *d_status = nullptr;  // device error word: bit 0 = a ray ended with kFault
-    unsigned long long *d_queue = nullptr;  // work counter of svo_trace_image's persistent launch
+    unsigned long long *d_queue = nullptr;  // work counters: [0] svo_trace_image and the differentiable
+                                            // launches, [1] and [2] svo_trace_image_host's two trace streams
 
     // Staging for svo_trace_host: one device arena and one pinned host arena,
     // split into two halves that alternate between two streams.
@@ -33,7 +34,7 @@ struct svo_octree {
     cudaStream_t stage_streams[2] = {nullptr, nullptr};
     // svo_trace_image_host pipeline: copy-in, trace and copy-out streams and
     // per-half events (inputs landed, trace done, outputs copied).
-    cudaStream_t img_streams[3] = {nullptr, nullptr, nullptr};
+    cudaStream_t img_streams[4] = {nullptr, nullptr, nullptr, nullptr};  // copy in, trace x2, copy out
     cudaEvent_t img_in[2] = {nullptr, nullptr}, img_traced[2] = {nullptr, nullptr}, img_out[2] = {nullptr, nullptr};
 };
 
@@ -85,7 +86,7 @@ int build_voxel_file_streamed(FILE *fp, int w, int h, int d, uint64_t mem, uint6
 int launch_trace(const svo_octree *oct, const float *d_rays, uint64_t n, float ray_scale, const float light[3],
                  const svo_trace_out &out, cudaStream_t st);
 int launch_trace_image(const svo_octree *oct, const float *d_rays, uint32_t width, uint32_t height, float ray_scale,
-                       const float light[3], const svo_trace_out &out, cudaStream_t st);
+                       const float light[3], const svo_trace_out &out, cudaStream_t st, int queue = 0);
 int launch_count_loads(const svo_octree *oct, const float *d_rays, uint64_t n, float ray_scale, uint32_t *loads,
                        cudaStream_t st);
 
