@@ -89,6 +89,12 @@ size_t lz4_compress_block(const uint8_t *src, size_t n, uint8_t *dst, size_t cap
     return (size_t)(op - dst);
 }
 
+static inline void copy8(uint8_t *d, const uint8_t *s) {
+    uint64_t v;
+    std::memcpy(&v, s, 8);
+    std::memcpy(d, &v, 8);
+}
+
 int lz4_decompress_block(const uint8_t *src, size_t src_len, uint8_t *out, size_t pos0, size_t out_len) {
     size_t ip = 0, op = pos0;
     const size_t end = pos0 + out_len;
@@ -105,7 +111,12 @@ int lz4_decompress_block(const uint8_t *src, size_t src_len, uint8_t *out, size_
             } while (b == 255);
         }
         if (lit > src_len - ip || lit > end - op) return -1;
-        std::memcpy(out + op, src + ip, lit);
+        if (lit <= 16 && end - op >= 16 && src_len - ip >= 16) {  // short run with slack on both sides
+            copy8(out + op, src + ip);
+            copy8(out + op + 8, src + ip + 8);
+        } else {
+            std::memcpy(out + op, src + ip, lit);
+        }
         ip += lit;
         op += lit;
         if (op == end) break;
@@ -124,11 +135,15 @@ int lz4_decompress_block(const uint8_t *src, size_t src_len, uint8_t *out, size_
         }
         ml += kMinMatch;
         if (ml > end - op) return -1;
-        const uint8_t *from = out + op - off;
-        if (off >= ml) {
-            std::memcpy(out + op, from, ml);
+        uint8_t *dst = out + op;
+        const uint8_t *from = dst - off;
+        if (off >= 8 && end - op >= ml + 8) {
+            // 8-byte steps: every source chunk lies before its destination
+            for (size_t k = 0; k < ml; k += 8) copy8(dst + k, from + k);
+        } else if (off >= ml) {
+            std::memcpy(dst, from, ml);
         } else {
-            for (size_t k = 0; k < ml; ++k) out[op + k] = from[k];
+            for (size_t k = 0; k < ml; ++k) dst[k] = from[k];
         }
         op += ml;
     }

@@ -1,7 +1,14 @@
 // octree_api.cpp — the C ABI (include/svo.h): handle lifetime, .oct and
 // .voxel I/O, build and trace entry points, validation, errors.
+#include <fcntl.h>
+#include <sys/mman.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
+#include <functional>
 #include <cstring>
 #include <memory>
 #include <thread>
@@ -142,33 +149,80 @@ int svo_version(void) { return 100; }
 
 void svo_free(void *p) { free(p); }
 
+// .oct read: the file is mapped, its block table indexed, and the blocks
+// decoded on worker threads straight into the word array.  Blocks written by
+// svo_oct_write are independent; the reference writes with
+// LZ4_compress_continue (VoxelOctree.cpp:96-119), whose blocks may copy from
+// the previous 64 KiB of output, so a block that reaches back fails its
+// independent attempt and is decoded afterwards, in order, with that history.
 int svo_oct_read(const char *path, uint32_t **words_out, uint64_t *n_out, float center[3]) {
     if (!path || !words_out || !n_out || !center) return set_error(SVO_ERR_INVALID, "null argument");
-    FILE *fp = fopen(path, "rb");
-    if (!fp) return set_error(SVO_ERR_IO, "cannot open %s", path);
-    std::unique_ptr<FILE, int (*)(FILE *)> guard(fp, fclose);
-    uint64_t n = 0;
-    if (fread(center, sizeof(float), 3, fp) != 3 || fread(&n, sizeof(uint64_t), 1, fp) != 1)
+    int fd = open(path, O_RDONLY);
+    if (fd < 0) return set_error(SVO_ERR_IO, "cannot open %s", path);
+    struct stat st;
+    if (fstat(fd, &st) != 0) {
+        close(fd);
+        return set_error(SVO_ERR_IO, "cannot size %s", path);
+    }
+    const size_t fsize = (size_t)st.st_size;
+    if (fsize < 20) {
+        close(fd);
         return set_error(SVO_ERR_FORMAT, "%s: truncated header", path);
+    }
+    void *mp = mmap(nullptr, fsize, PROT_READ, MAP_PRIVATE, fd, 0);
+    close(fd);
+    if (mp == MAP_FAILED) return set_error(SVO_ERR_IO, "cannot map %s", path);
+    std::unique_ptr<void, std::function<void(void *)>> mguard(mp, [fsize](void *q) { munmap(q, fsize); });
+    const uint8_t *file = (const uint8_t *)mp;
+    uint64_t n = 0;
+    std::memcpy(center, file, 12);
+    std::memcpy(&n, file + 12, 8);
     if (n == 0 || n > (1ull << 36))
         return set_error(n ? SVO_ERR_LIMIT : SVO_ERR_FORMAT, "%s: unsupported word count %llu", path,
                          (unsigned long long)n);
+    struct Block {
+        size_t src;
+        uint64_t csize, off, len;
+    };
+    std::vector<Block> blocks;
+    size_t pos = 20;
+    for (uint64_t off = 0; off < n * 4; off += kOctBlock) {
+        uint64_t csize = 0;
+        if (fsize - pos < 8) return set_error(SVO_ERR_FORMAT, "%s: truncated block header", path);
+        std::memcpy(&csize, file + pos, 8);
+        pos += 8;
+        if (csize > lz4_compress_bound(kOctBlock)) return set_error(SVO_ERR_FORMAT, "%s: bad block size", path);
+        if (fsize - pos < csize) return set_error(SVO_ERR_FORMAT, "%s: truncated block", path);
+        blocks.push_back({pos, csize, off, std::min<uint64_t>(n * 4 - off, kOctBlock)});
+        pos += csize;
+    }
     uint32_t *words = (uint32_t *)malloc(n * sizeof(uint32_t));
     if (!words) return set_error(SVO_ERR_MEMORY, "cannot allocate %llu words", (unsigned long long)n);
     std::unique_ptr<uint32_t, void (*)(void *)> wguard(words, free);
-    std::vector<uint8_t> comp;
     uint8_t *dst = reinterpret_cast<uint8_t *>(words);
-    for (uint64_t off = 0; off < n * 4; off += kOctBlock) {
-        uint64_t csize = 0;
-        if (fread(&csize, sizeof(uint64_t), 1, fp) != 1)
-            return set_error(SVO_ERR_FORMAT, "%s: truncated block header", path);
-        if (csize > lz4_compress_bound(kOctBlock)) return set_error(SVO_ERR_FORMAT, "%s: bad block size", path);
-        comp.resize(csize);
-        if (fread(comp.data(), 1, csize, fp) != csize) return set_error(SVO_ERR_FORMAT, "%s: truncated block", path);
-        uint64_t out_len = std::min<uint64_t>(n * 4 - off, kOctBlock);
-        if (lz4_decompress_block(comp.data(), csize, dst, off, out_len) != 0)
+    // independent attempts in parallel (no history: pos0 = 0 at the block start)
+    std::vector<uint8_t> done(blocks.size(), 0);
+    std::atomic<size_t> next{0};
+    const unsigned nt = std::max(1u, std::min<unsigned>(std::min(std::thread::hardware_concurrency(), 16u),
+                                                        (unsigned)blocks.size()));
+    auto worker = [&] {
+        for (size_t k; (k = next.fetch_add(1)) < blocks.size();) {
+            const Block &b = blocks[k];
+            done[k] = lz4_decompress_block(file + b.src, b.csize, dst + b.off, 0, b.len) == 0;
+        }
+    };
+    std::vector<std::thread> pool;
+    for (unsigned t = 1; t < nt; ++t) pool.emplace_back(worker);
+    worker();
+    for (auto &t : pool) t.join();
+    // the rest in order, each with the preceding output as history
+    for (size_t k = 0; k < blocks.size(); ++k) {
+        if (done[k]) continue;
+        const Block &b = blocks[k];
+        const uint64_t hist = std::min<uint64_t>(b.off, 64 * 1024);
+        if (lz4_decompress_block(file + b.src, b.csize, dst + b.off - hist, hist, b.len) != 0)
             return set_error(SVO_ERR_FORMAT, "%s: corrupt LZ4 block at payload offset %llu", path,
-                             (unsigned long long)off);
+                             (unsigned long long)b.off);
     }
     *words_out = wguard.release();
     *n_out = n;
