@@ -90,6 +90,15 @@ int svo_octree_destroy(svo_octree *oct);
 /* Number of 32-bit words (VoxelOctree::_octreeSize, VoxelOctree.hpp:40). */
 int svo_octree_num_words(const svo_octree *oct, uint64_t *n_words);
 
+/* Index width of svo_trace / svo_trace_host: 32 (the default) or 64.
+ * Octrees above 2^32-1 words always trace with 64-bit word indices (their far
+ * offsets carry bits above 32, VoxelOctree.cpp:190-194, :277-280); 64 selects
+ * that kernel for smaller octrees too, with identical results.  32 is refused
+ * for octrees above 2^32-1 words.  Above 2^32-1 words svo_trace refuses the
+ * 32-bit `leaf` output and the image, batched, load-count, frame and
+ * leaf-shading entry points return SVO_ERR_LIMIT. */
+int svo_octree_set_index_width(svo_octree *oct, int bits);
+
 /* Copies the words to host memory `dst` (n_words entries). */
 int svo_octree_copy_words(const svo_octree *oct, uint32_t *dst, uint64_t n_words);
 

@@ -82,6 +82,7 @@ def _load():
         "svo_octree_destroy": (ctypes.c_int, [_vp]),
         "svo_octree_num_words": (ctypes.c_int, [_vp, _u64p]),
         "svo_octree_copy_words": (ctypes.c_int, [_vp, _vp, ctypes.c_uint64]),
+        "svo_octree_set_index_width": (ctypes.c_int, [_vp, ctypes.c_int]),
         "svo_octree_device_words": (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
         "svo_octree_center": (ctypes.c_int, [_vp, _f32p]),
         "svo_octree_device_status": (ctypes.c_int, [_vp, _u32p]),
@@ -165,6 +166,11 @@ def _stream_ptr(stream):
     if isinstance(stream, int):
         return _vp(stream)
     return _vp(stream.cuda_stream)
+
+
+def trim_memory():
+    """Returns the builds' pooled scratch memory to the driver (svo_trim_memory)."""
+    check(lib.svo_trim_memory())
 
 
 def oct_read(path):
@@ -370,6 +376,11 @@ class VoxelOctree:
         n = ctypes.c_uint64()
         check(lib.svo_octree_num_words(self._h, ctypes.byref(n)))
         return n.value
+
+    def set_index_width(self, bits):
+        """32 or 64-bit word indices for trace()/trace_host(); octrees above
+        2^32-1 words always use 64."""
+        check(lib.svo_octree_set_index_width(self._h, int(bits)))
 
     def words(self):
         n = self.num_words()

@@ -286,6 +286,7 @@ bool config_ok(const svo_trace_config &c) {
 int launch_trace_image(const svo_octree *oct, const float *d_rays, uint32_t width, uint32_t height, float ray_scale,
                        const float light[3], const svo_trace_out &out, cudaStream_t st, int queue) {
     if (width == 0 || height == 0) return SVO_OK;
+    if (wide_octree(oct)) return set_error(SVO_ERR_LIMIT, "image tracing takes octrees of up to 2^32-1 words");
     const int tile_w = 8, log_tw = 3, chunk = 32, threads = 256;
     JobDev J;
     std::memset(&J, 0, sizeof(J));
@@ -501,6 +502,8 @@ int svo_batch_create(const svo_view *views, int n_views, svo_batch **out) {
     for (int i = 0; i < n_views; ++i) {
         const svo_view &v = views[i];
         if (!v.octree) return set_error(SVO_ERR_INVALID, "view %d has no octree", i);
+        if (wide_octree(v.octree))
+            return set_error(SVO_ERR_LIMIT, "view %d: batched tracing takes octrees of up to 2^32-1 words", i);
         if (!v.rays && (v.width == 0 || v.height == 0))
             return set_error(SVO_ERR_INVALID, "view %d: camera rays need width and height", i);
         if (v.width && (uint64_t)v.width * v.height > 0xFFFFFFFFull)

@@ -453,8 +453,6 @@ int build_from_sorted_device(const uint64_t *d_keys, const uint32_t *d_payload, 
     SVO_CUDA_TRY(cudaMemcpyAsync(&S_root, lv[D].S.p, sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
     SVO_CUDA_TRY(cudaStreamSynchronize(st));
     const uint64_t W = 1 + S_root;
-    if (W > 0xFFFFFFFFull)
-        return set_error(SVO_ERR_LIMIT, "octree of %llu words exceeds 2^32-1", (unsigned long long)W);
 
     uint32_t *words = nullptr;
     SVO_CUDA_TRY(cudaMallocAsync((void **)&words, (size_t)W * sizeof(uint32_t), st));

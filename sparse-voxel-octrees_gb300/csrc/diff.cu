@@ -213,6 +213,7 @@ int prepare(const svo_octree *oct, const float *rays, uint32_t width, uint32_t h
     if (!oct || !rays || !lights || !p_rgb || !p_n || width == 0 || height == 0 || n_views == 0)
         return set_error(SVO_ERR_INVALID, "bad arguments");
     if ((uint64_t)width * height * n_views > 0xFFFFFFFFull) return set_error(SVO_ERR_LIMIT, "more than 2^32-1 rays");
+    if (wide_octree(oct)) return set_error(SVO_ERR_LIMIT, "leaf shading takes octrees of up to 2^32-1 words");
     std::memset(&a, 0, sizeof(a));
     a.oct = oct->d_words;
     a.n_words = (uint32_t)oct->n_words;

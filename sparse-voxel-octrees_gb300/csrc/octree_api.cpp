@@ -103,7 +103,6 @@ int make_handle(uint32_t *d_words, uint64_t n_words, const float center[3], svo_
 
 static int upload_words(const uint32_t *words, uint64_t n, const float center[3], svo_octree **out) {
     if (n == 0) return set_error(SVO_ERR_FORMAT, "octree has no words");
-    if (n > 0xFFFFFFFFull) return set_error(SVO_ERR_LIMIT, "octree of %llu words exceeds 2^32-1", (unsigned long long)n);
     uint32_t *d = nullptr;
     SVO_CUDA_TRY(cudaMalloc((void **)&d, n * sizeof(uint32_t)));
     cudaError_t e = cudaMemcpy(d, words, n * sizeof(uint32_t), cudaMemcpyHostToDevice);
@@ -307,6 +306,16 @@ int svo_octree_destroy(svo_octree *oct) {
 int svo_octree_num_words(const svo_octree *oct, uint64_t *n) {
     if (!oct || !n) return set_error(SVO_ERR_INVALID, "null argument");
     *n = oct->n_words;
+    return SVO_OK;
+}
+
+int svo_octree_set_index_width(svo_octree *oct, int bits) {
+    if (!oct) return set_error(SVO_ERR_INVALID, "null argument");
+    if (bits != 32 && bits != 64) return set_error(SVO_ERR_INVALID, "index width %d is neither 32 nor 64", bits);
+    if (bits == 32 && wide_octree(oct))
+        return set_error(SVO_ERR_LIMIT, "an octree of %llu words needs 64-bit word indices",
+                         (unsigned long long)oct->n_words);
+    oct->index_bits = bits;
     return SVO_OK;
 }
 

@@ -153,7 +153,7 @@ extern "C" int svo_render_frame(const svo_octree *oct, const float rot[9], const
         return set_error(SVO_ERR_INVALID, "frame size %ux%u outside [1, 32768]", width, height);
     if (n_strips < 1 || n_strips > height) return set_error(SVO_ERR_INVALID, "n_strips must lie in [1, height]");
     if (pixel_stride < 1 || pixel_stride > kTile) return set_error(SVO_ERR_INVALID, "pixel_stride must lie in [1, 8]");
-    if (oct->n_words > 0xFFFFFFFFull) return set_error(SVO_ERR_LIMIT, "octree exceeds 2^32-1 words");
+    if (wide_octree(oct)) return set_error(SVO_ERR_LIMIT, "frame rendering takes octrees of up to 2^32-1 words");
     cudaStream_t st = (cudaStream_t)stream;
     FrameArgs f;
     f.oct = oct->d_words;

@@ -116,30 +116,38 @@ enum : int { kMiss = 0, kLeafHit = 1, kLodHit = 2, kFault = 3 };
 //   - the POP's highest differing bit is 31 - clz(differing) instead of the
 //     exponent of (float)differing: equal below 2^24, and at or above it both
 //     give a scale >= 23, which leaves the octree.
-struct RayResult {
+// Idx: the word-index type, uint32_t for octrees of up to 2^32-1 words (the
+// common case, 32-bit index arithmetic), uint64_t for larger ones.
+template <typename Idx>
+struct RayResultT {
     int status;
     float t;
-    uint32_t leaf;
+    Idx leaf;
     uint32_t word;
 };
+using RayResult = RayResultT<uint32_t>;
 
 struct RayStack {
-    uint4 e[kMaxScale];  // {parent, maxT bits, descriptor, unused} per scale
+    uint4 e[kMaxScale];  // {parent low word, maxT bits, descriptor, parent high word} per scale
 };
 
-struct RayState {
+template <typename Idx>
+struct RayStateT {
     float dTx, dTy, dTz, bTx, bTy, bTz;
     float minT, maxT, posX, posY, posZ, scaleExp2;
-    uint32_t current, parent, pushes, nload;
+    Idx parent;
+    uint32_t current, pushes, nload;
     int idx, scale, octantMask;
 };
+using RayState = RayStateT<uint32_t>;
 
 constexpr uint32_t kPushCap = 1u << 20;
 
 // Initialises the state for ray (o, d) and fetches the root descriptor
 // (n_words >= 1 for every octree handle).
-__device__ __forceinline__ void ray_init(RayState &s, const uint32_t *__restrict__ oct, float ox, float oy, float oz,
-                                         float dx, float dy, float dz) {
+template <typename Idx>
+__device__ __forceinline__ void ray_init(RayStateT<Idx> &s, const uint32_t *__restrict__ oct, float ox, float oy,
+                                         float oz, float dx, float dy, float dz) {
     if (fabsf(dx) < 1e-4f) dx = 1e-4f;
     if (fabsf(dy) < 1e-4f) dy = 1e-4f;
     if (fabsf(dz) < 1e-4f) dz = 1e-4f;
@@ -177,9 +185,9 @@ __device__ __forceinline__ void ray_init(RayState &s, const uint32_t *__restrict
 // at the start and after every PUSH and POP, far word :279, leaf word :282)
 // in s.nload.  kLod: evaluate the level-of-detail exit (:265-268); with
 // rayScale == 0 that test is always false, so kLod=false skips it.
-template <bool kCountLoads, bool kLod>
-__device__ __forceinline__ bool ray_step(RayState &s, RayStack &stk, const uint32_t *__restrict__ oct,
-                                         uint32_t n_words, float rayScale, RayResult &res) {
+template <bool kCountLoads, bool kLod, typename Idx>
+__device__ __forceinline__ bool ray_step(RayStateT<Idx> &s, RayStack &stk, const uint32_t *__restrict__ oct,
+                                         Idx n_words, float rayScale, RayResultT<Idx> &res) {
     // The loop condition of :252 (scale < MaxScale) holds on entry: scale
     // starts at 22, a PUSH lowers it and a POP past the root returns below.
     float cornerTX = s.posX * s.dTx - s.bTx;
@@ -203,20 +211,32 @@ __device__ __forceinline__ bool ray_step(RayState &s, RayStack &stk, const uint3
         float centerTZ = half * s.dTz + cornerTZ;
 
         if (s.minT <= maxTV) {
-            // Word indices are below 2^32 (n_words <= 2^32-1), so a far
-            // offset's high part (the descriptor's top 14 bits) must be 0 and
-            // all index sums fit 32 bits unless they wrap, which the bounds
-            // checks below catch.
-            uint32_t childOffset = s.current >> 18;
-            if (s.current & 0x20000u) {
-                if (childOffset != 0u || s.parent + 1u >= n_words) { res.status = kFault; return true; }
-                childOffset = __ldg(oct + s.parent + 1);
-                if (kCountLoads) ++s.nload;
+            Idx base, np;
+            if constexpr (sizeof(Idx) == 4) {
+                // Word indices are below 2^32 (n_words <= 2^32-1), so a far
+                // offset's high part (the descriptor's top 14 bits) must be 0
+                // and all index sums fit 32 bits unless they wrap, which the
+                // bounds checks below catch.
+                uint32_t childOffset = s.current >> 18;
+                if (s.current & 0x20000u) {
+                    if (childOffset != 0u || s.parent + 1u >= n_words) { res.status = kFault; return true; }
+                    childOffset = __ldg(oct + s.parent + 1);
+                    if (kCountLoads) ++s.nload;
+                }
+                base = s.parent + childOffset;
+                if (base < s.parent) { res.status = kFault; return true; }  // wrapped
+            } else {
+                // :276-280 with 64-bit indices: offset = (high 14 bits << 32) | far word
+                uint64_t childOffset = s.current >> 18;
+                if (s.current & 0x20000u) {
+                    if (s.parent + 1u >= n_words) { res.status = kFault; return true; }
+                    childOffset = (childOffset << 32) | (uint64_t)__ldg(oct + s.parent + 1);
+                    if (kCountLoads) ++s.nload;
+                }
+                base = s.parent + childOffset;
             }
-            const uint32_t base = s.parent + childOffset;
-            if (base < s.parent) { res.status = kFault; return true; }  // wrapped
             if (!(childMasks & 0x80u)) {
-                uint32_t li = base + __popc(((childMasks >> (8 + childShift)) << childShift) & 127u);
+                Idx li = base + (Idx)__popc(((childMasks >> (8 + childShift)) << childShift) & 127u);
                 if (li >= n_words || li < base) { res.status = kFault; return true; }
                 res.word = __ldg(oct + li);
                 res.leaf = li;
@@ -226,10 +246,14 @@ __device__ __forceinline__ bool ray_step(RayState &s, RayStack &stk, const uint3
                 return true;
             }
             uint32_t siblingCount = __popc(childMasks & 127u);
-            uint32_t np = base + siblingCount;
+            np = base + siblingCount;
             if (s.current & 0x10000u) np += siblingCount;
             if (np >= n_words || np < base || s.scale <= 0 || ++s.pushes > kPushCap) { res.status = kFault; return true; }
-            stk.e[s.scale] = make_uint4(s.parent, __float_as_uint(s.maxT), s.current, 0u);
+            if constexpr (sizeof(Idx) == 4)
+                stk.e[s.scale] = make_uint4(s.parent, __float_as_uint(s.maxT), s.current, 0u);
+            else
+                stk.e[s.scale] = make_uint4((uint32_t)s.parent, __float_as_uint(s.maxT), s.current,
+                                            (uint32_t)((uint64_t)s.parent >> 32));
             s.parent = np;
             s.current = __ldg(oct + np);
             if (kCountLoads) ++s.nload;
@@ -265,7 +289,10 @@ __device__ __forceinline__ bool ray_step(RayState &s, RayStack &stk, const uint3
         }
         s.scaleExp2 = __uint_as_float((uint32_t)(s.scale - kMaxScale + 127) << 23);
         uint4 e = stk.e[s.scale];
-        s.parent = e.x;
+        if constexpr (sizeof(Idx) == 4)
+            s.parent = e.x;
+        else
+            s.parent = (Idx)e.x | ((Idx)e.w << 32);
         s.maxT = __uint_as_float(e.y);
         s.current = e.z;
         if (kCountLoads) ++s.nload;
@@ -280,23 +307,23 @@ __device__ __forceinline__ bool ray_step(RayState &s, RayStack &stk, const uint3
     return false;
 }
 
-template <bool kCountLoads>
-__device__ __forceinline__ RayResult raymarch(const uint32_t *__restrict__ oct, uint32_t n_words, float ox, float oy,
-                                              float oz, float dx, float dy, float dz, float rayScale,
-                                              uint32_t *loads) {
+template <bool kCountLoads, typename Idx = uint32_t>
+__device__ __forceinline__ RayResultT<Idx> raymarch(const uint32_t *__restrict__ oct, Idx n_words, float ox, float oy,
+                                                    float oz, float dx, float dy, float dz, float rayScale,
+                                                    uint32_t *loads) {
     RayStack stk;
-    RayState s;
-    RayResult res;
+    RayStateT<Idx> s;
+    RayResultT<Idx> res;
     res.status = kMiss;
     res.t = __int_as_float(0x7f800000);
-    res.leaf = 0xFFFFFFFFu;
+    res.leaf = (Idx)~(Idx)0;
     res.word = 0;
     ray_init(s, oct, ox, oy, oz, dx, dy, dz);
     if (rayScale != 0.0f) {
-        while (!ray_step<kCountLoads, true>(s, stk, oct, n_words, rayScale, res)) {
+        while (!ray_step<kCountLoads, true, Idx>(s, stk, oct, n_words, rayScale, res)) {
         }
     } else {
-        while (!ray_step<kCountLoads, false>(s, stk, oct, n_words, rayScale, res)) {
+        while (!ray_step<kCountLoads, false, Idx>(s, stk, oct, n_words, rayScale, res)) {
         }
     }
     if (kCountLoads) *loads = s.nload;

@@ -23,6 +23,7 @@ struct svo_octree {
     uint32_t *d_status = nullptr;  // device error word: bit 0 = a ray ended with kFault
     unsigned long long *d_queue = nullptr;  // work counters: [0] svo_trace_image and the differentiable
                                             // launches, [1] and [2] svo_trace_image_host's two trace streams
+    int index_bits = 32;  // 64: svo_trace uses 64-bit word indices even when n_words fits 32 bits
 
     // Staging for svo_trace_host: one device arena and one pinned host arena,
     // split into two halves that alternate between two streams.
@@ -39,6 +40,11 @@ struct svo_octree {
 };
 
 namespace svo {
+
+// Octrees above 2^32-1 words need 64-bit word indices: far offsets then carry
+// bits above 32 in the descriptor's top 14 bits (VoxelOctree.cpp:190-194).
+constexpr uint64_t kMaxNarrowWords = 0xFFFFFFFFull;
+inline bool wide_octree(const svo_octree *o) { return o->n_words > kMaxNarrowWords; }
 
 // Records a formatted message for svo_last_error() and returns `code`.
 int set_error(int code, const char *fmt, ...);

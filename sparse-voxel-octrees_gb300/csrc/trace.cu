@@ -3,7 +3,9 @@
 // k_trace_plain: one thread per ray, the drop-in for a loop of
 // VoxelOctree::raymarch (VoxelOctree.cpp:207-346) plus the viewer's shade()
 // (Main.cpp:81-90).  Rays are 24-byte records (o, d) read as three float2;
-// outputs are structure-of-arrays so every store is coalesced.
+// outputs are structure-of-arrays so every store is coalesced.  It is
+// instantiated for 32-bit word indices (octrees of up to 2^32-1 words) and
+// 64-bit ones (larger octrees, whose far offsets exceed 32 bits).
 #include "svo_device.cuh"
 #include "svo_internal.h"
 
@@ -12,7 +14,7 @@ namespace {
 
 struct TraceArgs {
     const uint32_t *oct;
-    uint32_t n_words;
+    uint64_t n_words;
     const float *rays;
     uint64_t n;
     float ray_scale;
@@ -33,14 +35,15 @@ __device__ __forceinline__ void load_ray(const float *rays, uint64_t i, float &o
     dx = b.y; dy = c.x; dz = c.y;
 }
 
-__device__ __forceinline__ void store_result(const TraceArgs &a, uint64_t i, const RayResult &r, float dx, float dy,
-                                             float dz) {
+template <typename Idx>
+__device__ __forceinline__ void store_result(const TraceArgs &a, uint64_t i, const RayResultT<Idx> &r, float dx,
+                                             float dy, float dz) {
     if (r.status == kFault) atomicOr(a.status, 1u);
     uint8_t hs = r.status == kFault ? 0 : (uint8_t)r.status;
     if (a.hit) a.hit[i] = hs;
     if (a.t) a.t[i] = (hs == 0) ? __int_as_float(0x7f800000) : r.t;
     bool leaf = r.status == kLeafHit;
-    if (a.leaf) a.leaf[i] = leaf ? r.leaf : 0xFFFFFFFFu;
+    if (a.leaf) a.leaf[i] = leaf ? (uint32_t)r.leaf : 0xFFFFFFFFu;  // the host admits it only below 2^32
     if (a.word) a.word[i] = leaf ? r.word : 0u;
     if (a.rgb) {
         float g = leaf ? shade_grey(r.word, dx, dy, dz, a.lx, a.ly, a.lz) : 0.0f;
@@ -50,13 +53,14 @@ __device__ __forceinline__ void store_result(const TraceArgs &a, uint64_t i, con
     }
 }
 
+template <typename Idx>
 __global__ void __launch_bounds__(256) k_trace_plain(TraceArgs a) {
     uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     float ox, oy, oz, dx, dy, dz;
     load_ray(a.rays, i, ox, oy, oz, dx, dy, dz);
-    RayResult r = raymarch<false>(a.oct, a.n_words, ox, oy, oz, dx, dy, dz, a.ray_scale, nullptr);
-    store_result(a, i, r, dx, dy, dz);
+    RayResultT<Idx> r = raymarch<false, Idx>(a.oct, (Idx)a.n_words, ox, oy, oz, dx, dy, dz, a.ray_scale, nullptr);
+    store_result<Idx>(a, i, r, dx, dy, dz);
 }
 
 __global__ void __launch_bounds__(256) k_count_loads(const uint32_t *oct, uint32_t n_words, const float *rays,
@@ -77,9 +81,12 @@ __global__ void __launch_bounds__(256) k_count_loads(const uint32_t *oct, uint32
 int launch_trace(const svo_octree *oct, const float *d_rays, uint64_t n, float ray_scale, const float light[3],
                  const svo_trace_out &out, cudaStream_t st) {
     if (n == 0) return SVO_OK;
+    if (out.leaf && wide_octree(oct))
+        return set_error(SVO_ERR_LIMIT, "leaf indices of an octree of %llu words do not fit the 32-bit leaf output",
+                         (unsigned long long)oct->n_words);
     TraceArgs a;
     a.oct = oct->d_words;
-    a.n_words = (uint32_t)oct->n_words;
+    a.n_words = oct->n_words;
     a.rays = d_rays;
     a.n = n;
     a.ray_scale = ray_scale;
@@ -92,7 +99,10 @@ int launch_trace(const svo_octree *oct, const float *d_rays, uint64_t n, float r
     a.word = out.word;
     a.rgb = out.rgb;
     a.status = oct->d_status;
-    k_trace_plain<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(a);
+    if (wide_octree(oct) || oct->index_bits == 64)
+        k_trace_plain<uint64_t><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(a);
+    else
+        k_trace_plain<uint32_t><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(a);
     SVO_CUDA_TRY(cudaGetLastError());
     return SVO_OK;
 }
@@ -100,6 +110,7 @@ int launch_trace(const svo_octree *oct, const float *d_rays, uint64_t n, float r
 int launch_count_loads(const svo_octree *oct, const float *d_rays, uint64_t n, float ray_scale, uint32_t *loads,
                        cudaStream_t st) {
     if (n == 0) return SVO_OK;
+    if (wide_octree(oct)) return set_error(SVO_ERR_LIMIT, "load counting takes octrees of up to 2^32-1 words");
     k_count_loads<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(oct->d_words, (uint32_t)oct->n_words, d_rays, n,
                                                                ray_scale, loads, oct->d_status);
     SVO_CUDA_TRY(cudaGetLastError());
