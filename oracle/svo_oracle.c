@@ -145,6 +145,16 @@ int svo_oracle_raymarch(const uint32_t *oct, uint64_t nwords, const float o[3], 
     if (1.5f * dTy - bTy > minT) { idx ^= 2; posY = 1.5f; }
     if (1.5f * dTz - bTz > minT) { idx ^= 4; posZ = 1.5f; }
 
+    /* Not in the reference: a ray with a NaN corner distance on some axis
+     * (NaN in o or d, or an infinite o along an infinite d) either never
+     * leaves the loop below (NaN on all three axes: nothing advances or
+     * pops) or follows std::min's operand order around the NaN.  It ends
+     * here as a miss after the root load, as the kernels end it. */
+    if (isnan(dTx + bTx) || isnan(dTy + bTy) || isnan(dTz + bTz)) {
+        if (loads) *loads += 1;
+        return 0;
+    }
+
     int result = 0;
     while (scale < MAX_SCALE) {
         if (current == 0) {

@@ -104,11 +104,11 @@ enum : int { kMiss = 0, kLeafHit = 1, kLodHit = 2, kFault = 3 };
 //   - the reference fetches a node's descriptor at the top of the next pass
 //     (`if (current == 0)`, :253-254); here it is fetched at the PUSH that
 //     enters the node (and at init for the root), the same word;
-//   - word indices are 32-bit (octrees of up to 2^32-1 words) and checked
-//     against n_words; more than kPushCap PUSHes, or a PUSH below scale 0
-//     (both only possible on a corrupt octree), end the ray with kFault.
-//     Every pass that does not PUSH either advances to a sibling or pops
-//     towards the root, so the PUSH cap bounds the whole loop;
+//   - word indices are checked against n_words; more than kPushCap PUSHes,
+//     or a PUSH below scale 0 (both only possible on a corrupt octree), end
+//     the ray with kFault.  Every pass that does not PUSH either advances to
+//     a sibling or pops towards the root (for a ray without NaN corner
+//     distances; ray_init ends those), so the PUSH cap bounds the whole loop;
 //   - the per-pass corner minimum uses fminf: for finite rays no operand is
 //     NaN or -0 (corner t = pos*dT - bT with pos*dT nonzero), where fminf and
 //     the reference's std::min agree bit for bit (a NaN ray never terminates
@@ -177,6 +177,23 @@ __device__ __forceinline__ void ray_init(RayStateT<Idx> &s, const uint32_t *__re
     if (1.5f * s.dTz - s.bTz > s.minT) { s.idx ^= 4; s.posZ = 1.5f; }
     s.pushes = 0;
     s.nload = 1;
+    // A ray with a NaN corner distance on some axis (a NaN origin or
+    // direction component, or an infinite origin along an infinite
+    // direction; dT itself is never infinite) has no result in the
+    // reference: with NaN on all three axes VoxelOctree::raymarch never
+    // leaves its loop (no corner is <= the NaN minimum, so it neither
+    // advances nor pops), otherwise its path hangs on std::min's operand
+    // order around the NaN.  Such a ray ends as a miss: its state becomes
+    // one whose first pass steps out of the root (every corner distance is
+    // -1 at pos 1, so stepMask = 7, and the POP finds scale 23).
+    if (isnan(s.dTx + s.bTx) || isnan(s.dTy + s.bTy) || isnan(s.dTz + s.bTz)) {
+        s.dTx = s.dTy = s.dTz = -1.0f;
+        s.bTx = s.bTy = s.bTz = 0.0f;
+        s.posX = s.posY = s.posZ = 1.0f;
+        s.idx = 0;
+        s.minT = 1.0f;
+        s.maxT = 0.0f;
+    }
 }
 
 // One pass of the loop body.  Returns false while the ray continues; true

@@ -170,3 +170,57 @@ def test_trace_image_host_matches_oracle(svo, oracle, scenes):
                           [scenes.camera_rays(cams[0], W, H - 4 * (H // 4))])
     host = tree.trace_image_host(rays, W, H, light=(0.0, 1.0, 0.0))
     _assert_same(host, oracle.raymarch(words, rays, light=(0.0, 1.0, 0.0), threads=8))
+
+
+def test_nan_and_infinite_rays(cuda, svo, golden, oracle):
+    """Rays with NaN corner distances (NaN components, or an infinite origin
+    along an infinite direction) end as misses after one pass, in every
+    entry point; rays with other infinite components traverse as usual."""
+    torch = cuda
+    nan, inf = np.float32(np.nan), np.float32(np.inf)
+    odd = np.array([[nan, nan, nan, 0.0, 0.0, 1.0], [1.5, 1.5, -1.0, nan, nan, nan],
+                    [1.5, 1.5, -1.0, nan, 0.0, 1.0], [1.5, nan, -1.0, 0.0, 0.0, 1.0],
+                    [inf, 1.5, 1.5, -inf, 0.0, 0.0], [inf, 1.5, 1.5, -1.0, 0.0, 0.0],
+                    [1.5, 1.5, -1.0, 0.0, 0.0, inf]], np.float32)
+    g = golden["dragon"]
+    rays = np.concatenate([odd, g["rays"][:4000], odd])
+    R = rays.shape[0]
+    tree = svo.VoxelOctree.from_words(g["words"], g["center"])
+    ref = oracle.raymarch(g["words"], rays, loads=True, threads=4)
+    assert (ref["hit"][:5] == 0).all()
+    _assert_same(_device_trace(cuda, svo, tree, rays), ref)
+    _assert_same(tree.trace_host(rays), ref)
+    # image form (one row) and the batched persistent kernels
+    d_rays = torch.from_numpy(rays).cuda()
+    out = {"hit": torch.empty(R, dtype=torch.uint8, device="cuda"),
+           "t": torch.empty(R, dtype=torch.float32, device="cuda"),
+           "leaf": torch.empty(R, dtype=torch.int32, device="cuda"),
+           "word": torch.empty(R, dtype=torch.int32, device="cuda"),
+           "rgb": torch.empty((R, 3), dtype=torch.float32, device="cuda")}
+    tree.trace_image(d_rays, R, 1, out=out)
+    torch.cuda.synchronize()
+    res = {k: v.cpu().numpy() for k, v in out.items()}
+    res["leaf"] = res["leaf"].view(np.uint32)
+    res["word"] = res["word"].view(np.uint32)
+    _assert_same(res, ref)
+    for cfg in (dict(refill_idle=0), dict(refill_idle=1)):
+        for v in out.values():
+            v.fill_(7)
+        b = svo.Batch([{"octree": tree, "rays": d_rays, "out": out}])
+        b.trace(svo.default_config(**cfg))
+        torch.cuda.synchronize()
+        res = {k: v.cpu().numpy() for k, v in out.items()}
+        res["leaf"] = res["leaf"].view(np.uint32)
+        res["word"] = res["word"].view(np.uint32)
+        _assert_same(res, ref)
+        assert b.status() == 0
+        b.close()
+    loads = torch.zeros(R, dtype=torch.int32, device="cuda")
+    tree.count_loads(d_rays, loads=loads)
+    torch.cuda.synchronize()
+    assert np.array_equal(loads.cpu().numpy().view(np.uint32), ref["loads"])
+    # a frame from a NaN camera position: every corner and pixel ray is NaN
+    frame = tree.render_frame(np.eye(3, dtype=np.float32).ravel(), (nan, 1.5, -1.0), 64, 48, 4)
+    torch.cuda.synchronize()
+    assert not frame.any()
+    assert tree.device_status() == 0
