@@ -99,6 +99,19 @@ int svo_octree_num_words(const svo_octree *oct, uint64_t *n_words);
  * leaf-shading entry points return SVO_ERR_LIMIT. */
 int svo_octree_set_index_width(svo_octree *oct, int bits);
 
+/* The traversal kernels walk a descriptor table (16 bytes per node: the
+ * descriptor, its children's table position and its child block) that the
+ * first trace call on a handle builds after checking every reachable node;
+ * results are identical to the word traversal of VoxelOctree.cpp:252-339,
+ * which runs instead where the table cannot be built (octrees over 2^32-1
+ * words, or a node whose offsets leave the array) and inside graph capture
+ * before the table exists.  enable = 0 selects the word traversal. */
+int svo_octree_set_table(svo_octree *oct, int enable);
+
+/* Builds the descriptor table now if the octree qualifies (synchronous) and
+ * returns its entry count, or 0 when it does not qualify. */
+int svo_octree_table_size(svo_octree *oct, uint64_t *entries);
+
 /* Copies the words to host memory `dst` (n_words entries). */
 int svo_octree_copy_words(const svo_octree *oct, uint32_t *dst, uint64_t n_words);
 

@@ -83,6 +83,8 @@ def _load():
         "svo_octree_num_words": (ctypes.c_int, [_vp, _u64p]),
         "svo_octree_copy_words": (ctypes.c_int, [_vp, _vp, ctypes.c_uint64]),
         "svo_octree_set_index_width": (ctypes.c_int, [_vp, ctypes.c_int]),
+        "svo_octree_set_table": (ctypes.c_int, [_vp, ctypes.c_int]),
+        "svo_octree_table_size": (ctypes.c_int, [_vp, _u64p]),
         "svo_octree_device_words": (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
         "svo_octree_center": (ctypes.c_int, [_vp, _f32p]),
         "svo_octree_device_status": (ctypes.c_int, [_vp, _u32p]),
@@ -381,6 +383,17 @@ class VoxelOctree:
         """32 or 64-bit word indices for trace()/trace_host(); octrees above
         2^32-1 words always use 64."""
         check(lib.svo_octree_set_index_width(self._h, int(bits)))
+
+    def set_table(self, enable):
+        """Walk the descriptor table (default) or the words directly."""
+        check(lib.svo_octree_set_table(self._h, 1 if enable else 0))
+
+    def table_size(self):
+        """Entries of the descriptor table (built now if needed); 0 when the
+        octree does not qualify for one."""
+        n = ctypes.c_uint64()
+        check(lib.svo_octree_table_size(self._h, ctypes.byref(n)))
+        return n.value
 
     def words(self):
         n = self.num_words()

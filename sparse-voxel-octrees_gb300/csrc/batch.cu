@@ -30,6 +30,7 @@ constexpr int kMaxSmemJobs = 2048;  // views whose slot offsets are staged in sh
 
 struct JobDev {
     const uint32_t *oct;
+    const uint4 *tab;  // the octree's descriptor table (kernels instantiated with kTab)
     uint32_t n_words;
     uint32_t width, height, tiles_x;
     const float *rays;
@@ -67,9 +68,10 @@ __device__ __forceinline__ int find_job(const uint64_t *beg, int n_jobs, uint64_
 
 // Maps a work slot to its view and ray, initialises the traversal state and
 // returns false for the padding slots of partial pixel tiles.
+template <bool kTab>
 __device__ __forceinline__ bool setup_slot(const BatchArgs &a, const uint64_t *beg, uint64_t slot, RayState &st,
-                                           int &job, uint32_t &out_idx, const uint32_t *&oct, uint32_t &nw,
-                                           float &rs, float &rdx, float &rdy, float &rdz) {
+                                           int &job, uint32_t &out_idx, const uint32_t *&oct, const uint4 *&tab,
+                                           uint32_t &nw, float &rs, float &rdx, float &rdy, float &rdz) {
     int j = find_job(beg, a.n_jobs, slot);
     const JobDev &J = a.jobs[j];
     uint64_t local = slot - beg[j];
@@ -102,10 +104,11 @@ __device__ __forceinline__ bool setup_slot(const BatchArgs &a, const uint64_t *b
         ox = c[9]; oy = c[10]; oz = c[11];
         dx = vx * n; dy = vy * n; dz = vz * n;
     }
-    ray_init(st, J.oct, ox, oy, oz, dx, dy, dz);
+    ray_init_any<kTab>(st, J.oct, J.tab, ox, oy, oz, dx, dy, dz);
     rdx = dx; rdy = dy; rdz = dz;
     job = j;
     oct = J.oct;
+    tab = J.tab;
     nw = J.n_words;
     rs = J.ray_scale;
     return true;
@@ -131,7 +134,7 @@ __device__ __forceinline__ void write_result(const BatchArgs &a, int job, uint32
 
 // refill_idle == 0: a warp takes `chunk` slots at once and runs them 32 at a
 // time, each lane to completion, before it takes the next chunk.
-template <bool kLod>
+template <bool kTab, bool kLod>
 __global__ void k_trace_tiles(BatchArgs a) {
     extern __shared__ uint64_t s_begin[];
     const bool staged = a.n_jobs + 1 <= kMaxSmemJobs;
@@ -154,17 +157,18 @@ __global__ void k_trace_tiles(BatchArgs a) {
             int job;
             uint32_t out_idx, nw;
             const uint32_t *oct;
+            const uint4 *tab;
             float rs, rdx, rdy, rdz;
-            if (!setup_slot(a, beg, slot, st, job, out_idx, oct, nw, rs, rdx, rdy, rdz)) continue;
+            if (!setup_slot<kTab>(a, beg, slot, st, job, out_idx, oct, tab, nw, rs, rdx, rdy, rdz)) continue;
             RayResult res;
-            while (!ray_step<false, kLod>(st, stk, oct, nw, rs, res)) {
+            while (!ray_step_any<kTab, kLod>(st, stk, oct, tab, nw, rs, res)) {
             }
             write_result(a, job, out_idx, res, rdx, rdy, rdz);
         }
     }
 }
 
-template <bool kLod>
+template <bool kTab, bool kLod>
 __global__ void k_trace_persistent(BatchArgs a) {
     extern __shared__ uint64_t s_begin[];
     const bool staged = a.n_jobs + 1 <= kMaxSmemJobs;
@@ -182,6 +186,7 @@ __global__ void k_trace_persistent(BatchArgs a) {
     int job = 0;
     uint32_t out_idx = 0, nw = 0;
     const uint32_t *oct = nullptr;
+    const uint4 *tab = nullptr;
     float rdx = 0.f, rdy = 0.f, rdz = 0.f, rs = 0.f;
     uint64_t pool_next = 0, pool_end = 0;
     bool exhausted = false;
@@ -206,7 +211,8 @@ __global__ void k_trace_persistent(BatchArgs a) {
                 uint32_t rank = __popc(idle & lt_mask);
                 bool mine = ((idle >> lane) & 1u) && rank < avail;
                 if (mine)
-                    active = setup_slot(a, beg, pool_next + rank, st, job, out_idx, oct, nw, rs, rdx, rdy, rdz);
+                    active = setup_slot<kTab>(a, beg, pool_next + rank, st, job, out_idx, oct, tab, nw, rs, rdx, rdy,
+                                              rdz);
                 unsigned taken = __ballot_sync(FULL, mine);
                 pool_next += __popc(taken);
                 idle &= ~taken;
@@ -219,7 +225,7 @@ __global__ void k_trace_persistent(BatchArgs a) {
         if (active) {
             for (int k = 0; k < a.steps_per_round; ++k) {
                 RayResult res;
-                if (ray_step<false, kLod>(st, stk, oct, nw, rs, res)) {
+                if (ray_step_any<kTab, kLod>(st, stk, oct, tab, nw, rs, res)) {
                     write_result(a, job, out_idx, res, rdx, rdy, rdz);
                     active = false;
                     break;
@@ -231,7 +237,7 @@ __global__ void k_trace_persistent(BatchArgs a) {
 
 // One image view, passed by value (svo_trace_image): the tile kernel's loop
 // without a job table.
-template <bool kLod>
+template <bool kTab, bool kLod>
 __global__ void k_trace_single(JobDev J, uint64_t total, unsigned long long *queue, uint32_t *status, int log_tile_w,
                                int chunk) {
     const int lane = threadIdx.x & 31;
@@ -257,9 +263,9 @@ __global__ void k_trace_single(JobDev J, uint64_t total, unsigned long long *que
             const float2 *r2 = reinterpret_cast<const float2 *>(J.rays) + 3 * (uint64_t)out_idx;
             float2 p0 = __ldg(r2), p1 = __ldg(r2 + 1), p2 = __ldg(r2 + 2);
             RayState st;
-            ray_init(st, J.oct, p0.x, p0.y, p1.x, p1.y, p2.x, p2.y);
+            ray_init_any<kTab>(st, J.oct, J.tab, p0.x, p0.y, p1.x, p1.y, p2.x, p2.y);
             RayResult res;
-            while (!ray_step<false, kLod>(st, stk, J.oct, J.n_words, J.ray_scale, res)) {
+            while (!ray_step_any<kTab, kLod>(st, stk, J.oct, J.tab, J.n_words, J.ray_scale, res)) {
             }
             write_result(a, 0, out_idx, res, p1.y, p2.x, p2.y);
         }
@@ -306,8 +312,10 @@ int launch_trace_image(const svo_octree *oct, const float *d_rays, uint32_t widt
     J.word = out.word;
     J.rgb = out.rgb;
     uint64_t total = (uint64_t)J.tiles_x * ((height + (32 / tile_w) - 1) / (32 / tile_w)) * 32;
+    J.tab = octree_table(oct, st);
     void (*kern)(JobDev, uint64_t, unsigned long long *, uint32_t *, int, int) =
-        ray_scale != 0.0f ? k_trace_single<true> : k_trace_single<false>;
+        J.tab ? (ray_scale != 0.0f ? k_trace_single<true, true> : k_trace_single<true, false>)
+              : (ray_scale != 0.0f ? k_trace_single<false, true> : k_trace_single<false, false>);
     int dev = 0, sms = 0, resident = 0;
     SVO_CUDA_TRY(cudaGetDevice(&dev));
     SVO_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -331,6 +339,7 @@ struct svo_batch {
     uint32_t *status_d = nullptr;
     uint64_t total = 0;
     bool any_lod = false;
+    bool all_tab = false;  // every view's octree has a descriptor table
     int device = 0, num_sms = 0;
     cudaStream_t cap_stream = nullptr;
     cudaGraph_t graph = nullptr;
@@ -352,6 +361,7 @@ int prepare_jobs(svo_batch *b, int tile_w) {
         JobDev &J = jobs[i];
         std::memset(&J, 0, sizeof(J));
         J.oct = v.octree->d_words;
+        J.tab = b->all_tab ? v.octree->d_tab : nullptr;
         J.n_words = (uint32_t)v.octree->n_words;
         J.width = v.width;
         J.height = v.height;
@@ -394,10 +404,17 @@ int enqueue_trace(svo_batch *b, const svo_trace_config &c, cudaStream_t st) {
     // A persistent grid larger than what is resident only adds CTAs that
     // start after the queue is drained: clamp to the occupancy limit.
     void (*kern)(BatchArgs);
-    if (c.refill_idle == 0)
-        kern = b->any_lod ? k_trace_tiles<true> : k_trace_tiles<false>;
-    else
-        kern = b->any_lod ? k_trace_persistent<true> : k_trace_persistent<false>;
+    if (b->all_tab) {
+        if (c.refill_idle == 0)
+            kern = b->any_lod ? k_trace_tiles<true, true> : k_trace_tiles<true, false>;
+        else
+            kern = b->any_lod ? k_trace_persistent<true, true> : k_trace_persistent<true, false>;
+    } else {
+        if (c.refill_idle == 0)
+            kern = b->any_lod ? k_trace_tiles<false, true> : k_trace_tiles<false, false>;
+        else
+            kern = b->any_lod ? k_trace_persistent<false, true> : k_trace_persistent<false, false>;
+    }
     int resident = 0;
     SVO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, kern, c.block_threads, smem));
     int per_sm = std::max(1, std::min(c.blocks_per_sm, resident));
@@ -520,6 +537,11 @@ int svo_batch_create(const svo_view *views, int n_views, svo_batch **out) {
         SVO_CUDA_TRY(cudaMalloc((void **)&b->queue_d, sizeof(unsigned long long)));
         SVO_CUDA_TRY(cudaMalloc((void **)&b->status_d, sizeof(uint32_t)));
         SVO_CUDA_TRY(cudaMemset(b->status_d, 0, sizeof(uint32_t)));
+        // Tables are built here, outside any capture; one view without a
+        // table puts the whole batch on the word traversal.
+        b->all_tab = true;
+        for (const auto &v : b->views)
+            if (!octree_table(v.octree, nullptr)) b->all_tab = false;
         return prepare_jobs(b.get(), 8);
     };
     int rc = setup();

@@ -28,6 +28,7 @@ namespace {
 
 struct DiffArgs {
     const uint32_t *oct;
+    const uint4 *tab;  // descriptor table (kernels instantiated with kTab)
     uint32_t n_words;
     const float *rays;
     uint32_t width, height, n_views;  // image = width x (height * n_views), view v = rows [v*height, (v+1)*height)
@@ -76,7 +77,7 @@ __device__ __forceinline__ Shading shade_terms(const float *p_n, uint32_t leaf, 
     return sh;
 }
 
-template <bool kRecord>
+template <bool kTab, bool kRecord>
 __global__ void k_diff_forward(DiffArgs a) {
     const int lane = threadIdx.x & 31;
     RayStack stk;
@@ -90,9 +91,9 @@ __global__ void k_diff_forward(DiffArgs a) {
         const float2 *r2 = reinterpret_cast<const float2 *>(a.rays) + 3 * (uint64_t)idx;
         float2 p0 = __ldg(r2), p1 = __ldg(r2 + 1), p2 = __ldg(r2 + 2);
         RayState st;
-        ray_init(st, a.oct, p0.x, p0.y, p1.x, p1.y, p2.x, p2.y);
+        ray_init_any<kTab>(st, a.oct, a.tab, p0.x, p0.y, p1.x, p1.y, p2.x, p2.y);
         RayResult res;
-        while (!ray_step<false, false>(st, stk, a.oct, a.n_words, 0.0f, res)) {
+        while (!ray_step_any<kTab, false>(st, stk, a.oct, a.tab, a.n_words, 0.0f, res)) {
         }
         if (res.status == kFault) atomicOr(a.status, 1u);
         bool hit = res.status == kLeafHit;
@@ -129,7 +130,7 @@ __device__ __forceinline__ float group_sum(unsigned peers, unsigned rank, unsign
 }
 
 // kRetrace: recompute the hit leaf by traversal instead of reading hit_leaf.
-template <bool kRetrace>
+template <bool kTab, bool kRetrace>
 __global__ void k_diff_backward(DiffArgs a) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
@@ -153,9 +154,9 @@ __global__ void k_diff_backward(DiffArgs a) {
             if (kRetrace) {
                 float2 p0 = __ldg(r2);
                 RayState st;
-                ray_init(st, a.oct, p0.x, p0.y, p1.x, dx, dy, dz);
+                ray_init_any<kTab>(st, a.oct, a.tab, p0.x, p0.y, p1.x, dx, dy, dz);
                 RayResult res;
-                while (!ray_step<false, false>(st, stk, a.oct, a.n_words, 0.0f, res)) {
+                while (!ray_step_any<kTab, false>(st, stk, a.oct, a.tab, a.n_words, 0.0f, res)) {
                 }
                 if (res.status == kFault) atomicOr(a.status, 1u);
                 if (res.status == kLeafHit) leaf = res.leaf;
@@ -259,8 +260,13 @@ int svo_diff_forward(const svo_octree *oct, const float *rays, uint32_t width, u
     if (!rgb) return set_error(SVO_ERR_INVALID, "rgb output required");
     a.hit_leaf = hit_leaf;
     a.rgb = rgb;
-    return hit_leaf ? launch_persistent(k_diff_forward<true>, a, (cudaStream_t)stream)
-                    : launch_persistent(k_diff_forward<false>, a, (cudaStream_t)stream);
+    cudaStream_t st = (cudaStream_t)stream;
+    a.tab = octree_table(oct, st);
+    if (a.tab)
+        return hit_leaf ? launch_persistent(k_diff_forward<true, true>, a, st)
+                        : launch_persistent(k_diff_forward<true, false>, a, st);
+    return hit_leaf ? launch_persistent(k_diff_forward<false, true>, a, st)
+                    : launch_persistent(k_diff_forward<false, false>, a, st);
 }
 
 int svo_diff_backward(const svo_octree *oct, const float *rays, uint32_t width, uint32_t height, uint32_t n_views,
@@ -274,8 +280,11 @@ int svo_diff_backward(const svo_octree *oct, const float *rays, uint32_t width, 
     a.d_rgb = d_rgb;
     a.g_rgb = grad_rgb;
     a.g_n = grad_normal;
-    return hit_leaf ? launch_persistent(k_diff_backward<false>, a, (cudaStream_t)stream)
-                    : launch_persistent(k_diff_backward<true>, a, (cudaStream_t)stream);
+    cudaStream_t st = (cudaStream_t)stream;
+    a.tab = hit_leaf ? nullptr : octree_table(oct, st);  // the table only serves the retrace
+    if (a.tab) return launch_persistent(k_diff_backward<true, true>, a, st);
+    return hit_leaf ? launch_persistent(k_diff_backward<false, false>, a, st)
+                    : launch_persistent(k_diff_backward<false, true>, a, st);
 }
 
 }  // extern "C"

@@ -287,6 +287,7 @@ int svo_octree_from_words(const uint32_t *words, uint64_t n_words, const float c
 int svo_octree_destroy(svo_octree *oct) {
     if (!oct) return SVO_OK;
     if (oct->d_words) cudaFree(oct->d_words);
+    if (oct->d_tab) cudaFree(oct->d_tab);
     if (oct->d_status) cudaFree(oct->d_status);
     if (oct->d_queue) cudaFree(oct->d_queue);
     if (oct->stage_dev) cudaFree(oct->stage_dev);
@@ -316,6 +317,22 @@ int svo_octree_set_index_width(svo_octree *oct, int bits) {
         return set_error(SVO_ERR_LIMIT, "an octree of %llu words needs 64-bit word indices",
                          (unsigned long long)oct->n_words);
     oct->index_bits = bits;
+    return SVO_OK;
+}
+
+int svo_octree_set_table(svo_octree *oct, int enable) {
+    if (!oct) return set_error(SVO_ERR_INVALID, "null argument");
+    oct->use_table = enable != 0;
+    return SVO_OK;
+}
+
+int svo_octree_table_size(svo_octree *oct, uint64_t *entries) {
+    if (!oct || !entries) return set_error(SVO_ERR_INVALID, "null argument");
+    const bool was = oct->use_table;
+    oct->use_table = true;
+    const uint4 *t = octree_table(oct, nullptr);
+    oct->use_table = was;
+    *entries = t ? oct->n_tab : 0;
     return SVO_OK;
 }
 

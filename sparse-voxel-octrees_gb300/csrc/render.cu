@@ -31,6 +31,7 @@ constexpr float kTreeMiss = 1e10f;
 
 struct FrameArgs {
     const uint32_t *oct;
+    const uint4 *tab;  // descriptor table (kernels instantiated with kTab)
     uint32_t n_words;
     float a[9];
     float pos[3];
@@ -85,6 +86,7 @@ __global__ void k_frame_setup(FrameArgs f) {
     }
 }
 
+template <bool kTab>
 __global__ void k_corners(FrameArgs f) {
     const int tx = blockIdx.x * blockDim.x + threadIdx.x;
     const int ty = blockIdx.y, s = blockIdx.z;
@@ -95,11 +97,12 @@ __global__ void k_corners(FrameArgs f) {
     if (ty >= tiles_y) return;
     float x, y, z;
     view_dir(f, f.dx_corner[tx], f.dy_corner[s * f.tiles_y_max + ty], x, y, z);
-    RayResult r = raymarch<false>(f.oct, f.n_words, f.pos[0], f.pos[1], f.pos[2], x, y, z, f.coarse, nullptr);
+    RayResult r = trace_ray<kTab>(f.oct, f.tab, f.n_words, f.pos[0], f.pos[1], f.pos[2], x, y, z, f.coarse);
     if (r.status == kFault) atomicOr(f.status, 1u);
     f.depth[((size_t)s * f.tiles_y_max + ty) * f.tiles_x + tx] = (r.status == kLeafHit || r.status == kLodHit) ? r.t : kTreeMiss;
 }
 
+template <bool kTab>
 __global__ void k_tiles(FrameArgs f, int total_tiles) {
     const int lane = threadIdx.x & 31;
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -128,8 +131,8 @@ __global__ void k_tiles(FrameArgs f, int total_tiles) {
         float x, y, z;
         view_dir(f, dx, dy, x, y, z);
         const float t0 = smax(minT - 0.03f, 0.0f);
-        RayResult res = raymarch<false>(f.oct, f.n_words, f.pos[0] + x * t0, f.pos[1] + y * t0, f.pos[2] + z * t0, x, y,
-                                        z, 0.0f, nullptr);
+        RayResult res = trace_ray<kTab>(f.oct, f.tab, f.n_words, f.pos[0] + x * t0, f.pos[1] + y * t0,
+                                        f.pos[2] + z * t0, x, y, z, 0.0f);
         if (res.status == kFault) atomicOr(f.status, 1u);
         float col = 0.0f;
         if (res.status == kLeafHit) col = shade_grey(res.word, x, y, z, f.light[0], f.light[1], f.light[2]);
@@ -157,6 +160,7 @@ extern "C" int svo_render_frame(const svo_octree *oct, const float rot[9], const
     cudaStream_t st = (cudaStream_t)stream;
     FrameArgs f;
     f.oct = oct->d_words;
+    f.tab = octree_table(oct, (cudaStream_t)stream);
     f.n_words = (uint32_t)oct->n_words;
     for (int i = 0; i < 9; ++i) f.a[i] = rot[i];
     for (int i = 0; i < 3; ++i) f.pos[i] = pos[i];
@@ -203,12 +207,18 @@ extern "C" int svo_render_frame(const svo_octree *oct, const float rot[9], const
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) {
         dim3 g1((unsigned)((f.tiles_x + 127) / 128), (unsigned)f.tiles_y_max, (unsigned)S);
-        k_corners<<<g1, 128, 0, st>>>(f);
+        if (f.tab)
+            k_corners<true><<<g1, 128, 0, st>>>(f);
+        else
+            k_corners<false><<<g1, 128, 0, st>>>(f);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess && total_tiles > 0) {
         uint64_t threads = (uint64_t)total_tiles * 64;
-        k_tiles<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(f, total_tiles);
+        if (f.tab)
+            k_tiles<true><<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(f, total_tiles);
+        else
+            k_tiles<false><<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(f, total_tiles);
         e = cudaGetLastError();
     }
     cudaFreeAsync(scratch, st);

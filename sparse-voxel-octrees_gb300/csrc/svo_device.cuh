@@ -135,19 +135,20 @@ template <typename Idx>
 struct RayStateT {
     float dTx, dTy, dTz, bTx, bTy, bTz;
     float minT, maxT, posX, posY, posZ, scaleExp2;
-    Idx parent;
+    Idx parent;  // the table traversal keeps the first internal child's table ordinal here
     uint32_t current, pushes, nload;
+    uint32_t lbase;  // table traversal: word index of the current node's child block
     int idx, scale, octantMask;
 };
 using RayState = RayStateT<uint32_t>;
 
 constexpr uint32_t kPushCap = 1u << 20;
 
-// Initialises the state for ray (o, d) and fetches the root descriptor
-// (n_words >= 1 for every octree handle).
+// Initialises the ray's geometry for (o, d) (VoxelOctree.cpp:213-250);
+// ray_init adds the root node.
 template <typename Idx>
-__device__ __forceinline__ void ray_init(RayStateT<Idx> &s, const uint32_t *__restrict__ oct, float ox, float oy,
-                                         float oz, float dx, float dy, float dz) {
+__device__ __forceinline__ void ray_setup(RayStateT<Idx> &s, float ox, float oy, float oz, float dx, float dy,
+                                          float dz) {
     if (fabsf(dx) < 1e-4f) dx = 1e-4f;
     if (fabsf(dy) < 1e-4f) dy = 1e-4f;
     if (fabsf(dz) < 1e-4f) dz = 1e-4f;
@@ -164,8 +165,6 @@ __device__ __forceinline__ void ray_init(RayStateT<Idx> &s, const uint32_t *__re
     s.minT = smax(2.0f * s.dTx - s.bTx, smax(2.0f * s.dTy - s.bTy, 2.0f * s.dTz - s.bTz));
     s.maxT = smin(s.dTx - s.bTx, smin(s.dTy - s.bTy, s.dTz - s.bTz));
     s.minT = smax(s.minT, 0.0f);
-    s.parent = 0;
-    s.current = __ldg(oct);
     s.idx = 0;
     s.posX = 1.0f;
     s.posY = 1.0f;
@@ -194,6 +193,26 @@ __device__ __forceinline__ void ray_init(RayStateT<Idx> &s, const uint32_t *__re
         s.minT = 1.0f;
         s.maxT = 0.0f;
     }
+}
+
+// Initialises the state for ray (o, d) and fetches the root descriptor
+// (n_words >= 1 for every octree handle).
+template <typename Idx>
+__device__ __forceinline__ void ray_init(RayStateT<Idx> &s, const uint32_t *__restrict__ oct, float ox, float oy,
+                                         float oz, float dx, float dy, float dz) {
+    ray_setup(s, ox, oy, oz, dx, dy, dz);
+    s.parent = 0;
+    s.current = __ldg(oct);
+}
+
+// The same for the table traversal: the root's table entry (ordinal 0).
+__device__ __forceinline__ void ray_init(RayState &s, const uint4 *__restrict__ tab, float ox, float oy, float oz,
+                                         float dx, float dy, float dz) {
+    ray_setup(s, ox, oy, oz, dx, dy, dz);
+    uint4 r = __ldg(tab);
+    s.current = r.x;
+    s.parent = r.y;
+    s.lbase = r.z;
 }
 
 // One pass of the loop body.  Returns false while the ray continues; true
@@ -322,6 +341,144 @@ __device__ __forceinline__ bool ray_step(RayStateT<Idx> &s, RayStack &stk, const
         s.idx = (int)((shX & 1u) | ((shY & 1u) << 1) | ((shZ & 1u) << 2));
     }
     return false;
+}
+
+// The loop body over a descriptor table (an octree handle builds one after
+// checking the whole tree): entry k = {descriptor word, table ordinal of its
+// first internal child, word index of its child block, 0}, the internal
+// children of a node holding consecutive ordinals in block order.  A PUSH is
+// then one 16-byte load, child = ordinal + (internal siblings before it), and
+// needs neither the offset and far-word decoding of :276-280 nor bounds
+// checks (the table exists only when every reachable offset, far word, child
+// slot and leaf slot is in range and no node is deeper than 22 levels).  The
+// geometry, the visiting order and every result are those of ray_step.
+template <bool kLod>
+__device__ __forceinline__ bool ray_step_tab(RayState &s, RayStack &stk, const uint32_t *__restrict__ words,
+                                             const uint4 *__restrict__ tab, float rayScale, RayResult &res) {
+    float cornerTX = s.posX * s.dTx - s.bTx;
+    float cornerTY = s.posY * s.dTy - s.bTy;
+    float cornerTZ = s.posZ * s.dTz - s.bTz;
+    float maxTC = fminf(cornerTX, fminf(cornerTY, cornerTZ));
+
+    int childShift = s.idx ^ s.octantMask;
+    uint32_t childMasks = s.current << childShift;
+
+    if ((childMasks & 0x8000u) && s.minT <= s.maxT) {
+        if (kLod && maxTC * rayScale >= s.scaleExp2) {
+            res.status = kLodHit;
+            res.t = maxTC;
+            return true;
+        }
+        float maxTV = fminf(s.maxT, maxTC);
+        float half = s.scaleExp2 * 0.5f;
+        float centerTX = half * s.dTx + cornerTX;
+        float centerTY = half * s.dTy + cornerTY;
+        float centerTZ = half * s.dTz + cornerTZ;
+
+        if (s.minT <= maxTV) {
+            if (!(childMasks & 0x80u)) {
+                uint32_t li = s.lbase + __popc(((childMasks >> (8 + childShift)) << childShift) & 127u);
+                res.word = __ldg(words + li);
+                res.leaf = li;
+                res.status = kLeafHit;
+                res.t = s.minT;
+                return true;
+            }
+            stk.e[s.scale] = make_uint4(s.parent, __float_as_uint(s.maxT), s.current, s.lbase);
+            uint4 c = __ldg(tab + s.parent + __popc(childMasks & 127u));
+            s.current = c.x;
+            s.parent = c.y;
+            s.lbase = c.z;
+
+            s.idx = 0;
+            s.scale--;
+            s.scaleExp2 = half;
+            if (centerTX > s.minT) { s.idx ^= 1; s.posX += s.scaleExp2; }
+            if (centerTY > s.minT) { s.idx ^= 2; s.posY += s.scaleExp2; }
+            if (centerTZ > s.minT) { s.idx ^= 4; s.posZ += s.scaleExp2; }
+            s.maxT = maxTV;
+            return false;
+        }
+    }
+
+    int stepMask = 0;
+    if (cornerTX <= maxTC) { stepMask ^= 1; s.posX -= s.scaleExp2; }
+    if (cornerTY <= maxTC) { stepMask ^= 2; s.posY -= s.scaleExp2; }
+    if (cornerTZ <= maxTC) { stepMask ^= 4; s.posZ -= s.scaleExp2; }
+
+    s.minT = maxTC;
+    s.idx ^= stepMask;
+
+    if ((s.idx & stepMask) != 0) {
+        uint32_t differing = 0;
+        if (stepMask & 1) differing |= __float_as_uint(s.posX) ^ __float_as_uint(s.posX + s.scaleExp2);
+        if (stepMask & 2) differing |= __float_as_uint(s.posY) ^ __float_as_uint(s.posY + s.scaleExp2);
+        if (stepMask & 4) differing |= __float_as_uint(s.posZ) ^ __float_as_uint(s.posZ + s.scaleExp2);
+        s.scale = 31 - __clz((int)differing);
+        if (s.scale >= kMaxScale || s.scale < 0) {
+            res.status = kMiss;
+            return true;
+        }
+        s.scaleExp2 = __uint_as_float((uint32_t)(s.scale - kMaxScale + 127) << 23);
+        uint4 e = stk.e[s.scale];
+        s.parent = e.x;
+        s.maxT = __uint_as_float(e.y);
+        s.current = e.z;
+        s.lbase = e.w;
+        uint32_t shX = __float_as_uint(s.posX) >> s.scale;
+        uint32_t shY = __float_as_uint(s.posY) >> s.scale;
+        uint32_t shZ = __float_as_uint(s.posZ) >> s.scale;
+        s.posX = __uint_as_float(shX << s.scale);
+        s.posY = __uint_as_float(shY << s.scale);
+        s.posZ = __uint_as_float(shZ << s.scale);
+        s.idx = (int)((shX & 1u) | ((shY & 1u) << 1) | ((shZ & 1u) << 2));
+    }
+    return false;
+}
+
+// Where an octree has a table (tab != nullptr on the host side, selected at
+// compile time here), the table step, else the checked word step.
+template <bool kTab, bool kLod>
+__device__ __forceinline__ bool ray_step_any(RayState &s, RayStack &stk, const uint32_t *__restrict__ words,
+                                             const uint4 *__restrict__ tab, uint32_t n_words, float rayScale,
+                                             RayResult &res) {
+    if constexpr (kTab)
+        return ray_step_tab<kLod>(s, stk, words, tab, rayScale, res);
+    else
+        return ray_step<false, kLod, uint32_t>(s, stk, words, n_words, rayScale, res);
+}
+
+template <bool kTab>
+__device__ __forceinline__ void ray_init_any(RayState &s, const uint32_t *__restrict__ words,
+                                             const uint4 *__restrict__ tab, float ox, float oy, float oz, float dx,
+                                             float dy, float dz) {
+    if constexpr (kTab)
+        ray_init(s, tab, ox, oy, oz, dx, dy, dz);
+    else
+        ray_init(s, words, ox, oy, oz, dx, dy, dz);
+}
+
+// A whole ray, checked or over a table.
+template <bool kTab>
+__device__ __forceinline__ RayResult trace_ray(const uint32_t *__restrict__ words, const uint4 *__restrict__ tab,
+                                               uint32_t n_words, float ox, float oy, float oz, float dx, float dy,
+                                               float dz, float rayScale) {
+    RayStack stk;
+    RayState s;
+    RayResult res;
+    res.status = kMiss;
+    res.t = __int_as_float(0x7f800000);
+    res.leaf = 0xFFFFFFFFu;
+    res.word = 0;
+    ray_init_any<kTab>(s, words, tab, ox, oy, oz, dx, dy, dz);
+    if (rayScale != 0.0f) {
+        while (!ray_step_any<kTab, true>(s, stk, words, tab, n_words, rayScale, res)) {
+        }
+    } else {
+        while (!ray_step_any<kTab, false>(s, stk, words, tab, n_words, rayScale, res)) {
+        }
+    }
+    return res;
 }
 
 template <bool kCountLoads, typename Idx = uint32_t>

@@ -1,6 +1,7 @@
 // svo_internal.h — host-side internals shared by the library's translation units.
 #pragma once
 
+#include <atomic>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdint>
@@ -24,6 +25,14 @@ struct svo_octree {
     unsigned long long *d_queue = nullptr;  // work counters: [0] svo_trace_image and the differentiable
                                             // launches, [1] and [2] svo_trace_image_host's two trace streams
     int index_bits = 32;  // 64: svo_trace uses 64-bit word indices even when n_words fits 32 bits
+
+    // Descriptor table of the table traversal (octree_table.cu), built by the
+    // first trace call that can use it; a cache of the immutable words.
+    mutable uint4 *d_tab = nullptr;
+    mutable uint64_t n_tab = 0;
+    mutable std::atomic<int> tab_state{0};  // 0 not built yet, 1 built, -1 the octree does not qualify
+    bool use_table = true;
+    mutable std::mutex tab_mtx;
 
     // Staging for svo_trace_host: one device arena and one pinned host arena,
     // split into two halves that alternate between two streams.
@@ -98,5 +107,11 @@ int launch_count_loads(const svo_octree *oct, const float *d_rays, uint64_t n, f
 
 // Creates a handle around device words (takes ownership).
 int make_handle(uint32_t *d_words, uint64_t n_words, const float center[3], svo_octree **out);
+
+// The handle's descriptor table (octree_table.cu), built on first use; null
+// when the octree does not qualify (over 2^32-1 words, or a reachable node
+// that fails the checks), when the table is switched off, or while `caller`
+// is being captured into a graph.  Synchronous the first time.
+const uint4 *octree_table(const svo_octree *oct, cudaStream_t caller);
 
 }  // namespace svo

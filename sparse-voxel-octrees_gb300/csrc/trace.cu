@@ -5,7 +5,9 @@
 // (Main.cpp:81-90).  Rays are 24-byte records (o, d) read as three float2;
 // outputs are structure-of-arrays so every store is coalesced.  It is
 // instantiated for 32-bit word indices (octrees of up to 2^32-1 words) and
-// 64-bit ones (larger octrees, whose far offsets exceed 32 bits).
+// 64-bit ones (larger octrees, whose far offsets exceed 32 bits);
+// k_trace_plain_tab walks the handle's descriptor table instead, where it
+// has one.
 #include "svo_device.cuh"
 #include "svo_internal.h"
 
@@ -14,6 +16,7 @@ namespace {
 
 struct TraceArgs {
     const uint32_t *oct;
+    const uint4 *tab;  // descriptor table (the table kernel only)
     uint64_t n_words;
     const float *rays;
     uint64_t n;
@@ -63,6 +66,16 @@ __global__ void __launch_bounds__(256) k_trace_plain(TraceArgs a) {
     store_result<Idx>(a, i, r, dx, dy, dz);
 }
 
+// The same over the handle's descriptor table.
+__global__ void __launch_bounds__(256) k_trace_plain_tab(TraceArgs a) {
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    float ox, oy, oz, dx, dy, dz;
+    load_ray(a.rays, i, ox, oy, oz, dx, dy, dz);
+    RayResult r = trace_ray<true>(a.oct, a.tab, 0u, ox, oy, oz, dx, dy, dz, a.ray_scale);
+    store_result<uint32_t>(a, i, r, dx, dy, dz);
+}
+
 __global__ void __launch_bounds__(256) k_count_loads(const uint32_t *oct, uint32_t n_words, const float *rays,
                                                     uint64_t n, float ray_scale, uint32_t *loads,
                                                     uint32_t *status) {
@@ -99,10 +112,14 @@ int launch_trace(const svo_octree *oct, const float *d_rays, uint64_t n, float r
     a.word = out.word;
     a.rgb = out.rgb;
     a.status = oct->d_status;
+    a.tab = nullptr;
+    const unsigned grid = (unsigned)((n + 255) / 256);
     if (wide_octree(oct) || oct->index_bits == 64)
-        k_trace_plain<uint64_t><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(a);
+        k_trace_plain<uint64_t><<<grid, 256, 0, st>>>(a);
+    else if ((a.tab = octree_table(oct, st)) != nullptr)
+        k_trace_plain_tab<<<grid, 256, 0, st>>>(a);
     else
-        k_trace_plain<uint32_t><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(a);
+        k_trace_plain<uint32_t><<<grid, 256, 0, st>>>(a);
     SVO_CUDA_TRY(cudaGetLastError());
     return SVO_OK;
 }

@@ -224,3 +224,32 @@ def test_nan_and_infinite_rays(cuda, svo, golden, oracle):
     torch.cuda.synchronize()
     assert not frame.any()
     assert tree.device_status() == 0
+
+
+def test_table_and_word_traversal_agree(cuda, svo, golden, oracle, scenes):
+    """The descriptor-table traversal (the default) and the word traversal
+    give identical outputs; the table has one entry per reachable node."""
+    g = golden["dragon"]
+    trees = [(g["words"], g["center"])]
+    trees.append(oracle.build_dense(scenes.random_grid((64, 64, 64), 0.5, 3)))
+    trees.append(oracle.build_dense(scenes.sphere_scene(256, 40, 2)))
+    rays = np.concatenate([scenes.random_rays(300_000, 17), g["rays"]])
+    for words, center in trees:
+        tree = svo.VoxelOctree.from_words(words, center)
+        nd, _ = tree.validate()
+        assert tree.table_size() == nd
+        ref = oracle.raymarch(words, rays, threads=8)
+        tab = _device_trace(cuda, svo, tree, rays)
+        tree.set_table(False)
+        plain = _device_trace(cuda, svo, tree, rays)
+        _assert_same(tab, ref)
+        _assert_same(plain, ref)
+        tree.close()
+
+
+def test_table_refused_for_corrupt_trees(cuda, svo):
+    for words in ([(0x3FFF << 18) | (0xFF << 8) | 0xFF], [(0xFF << 8) | 0xFF] + [0] * 8,
+                  [(1 << 18) | (0x01 << 8) | 0x02, 0]):
+        tree = svo.VoxelOctree.from_words(np.array(words, np.uint32), (0.5, 0.5, 0.5))
+        assert tree.table_size() == 0
+        tree.close()

@@ -1,13 +1,15 @@
 """The library's traversal step (csrc/svo_device.cuh), compiled for the host
 by tests/host_traversal.cpp, against the oracle: both word-index widths, the
-level-of-detail exit, rays with NaN or infinite components, and an octree of
-more than 2^32 words (its untouched pages stay unmapped).  No GPU needed."""
+table traversal over the breadth-first descriptor table (csrc/octree_table.cuh),
+the level-of-detail exit, rays with NaN or infinite components, and an octree
+of more than 2^32 words (its untouched pages stay unmapped).  No GPU needed."""
 import ctypes
 import os
 import subprocess
 
 import numpy as np
 import pytest
+from conftest import golden_builds
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
@@ -36,6 +38,32 @@ def host(tmp_path_factory):
         assert (out["hit"] != 3).all(), "a ray ended at a bounds check"
         return out
 
+    L.host_build_table.restype = ctypes.c_uint64
+    L.host_build_table.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint64]
+    L.host_traverse_tab.restype = None
+    L.host_traverse_tab.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
+                                    ctypes.c_float, ctypes.c_uint64] + [ctypes.c_void_p] * 5
+
+    def table(words):
+        words = np.ascontiguousarray(words, dtype=np.uint32)
+        tab = np.zeros((words.size, 4), np.uint32)
+        n = L.host_build_table(words.ctypes.data, words.size, tab.ctypes.data, words.size)
+        return tab[:n] if n else None
+
+    def traverse_tab(words, tab, rays, ray_scale=0.0, max_steps=1 << 24):
+        rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 6)
+        n = rays.shape[0]
+        out = {"hit": np.zeros(n, np.uint8), "t": np.zeros(n, np.float32), "leaf": np.zeros(n, np.uint64),
+               "word": np.zeros(n, np.uint32), "steps": np.zeros(n, np.uint64)}
+        tab = np.ascontiguousarray(tab)
+        L.host_traverse_tab(words.ctypes.data, tab.ctypes.data, rays.ctypes.data, n, float(ray_scale), max_steps,
+                            out["hit"].ctypes.data, out["t"].ctypes.data, out["leaf"].ctypes.data,
+                            out["word"].ctypes.data, out["steps"].ctypes.data)
+        assert (out["hit"] != 255).all(), "a ray did not finish"
+        return out
+
+    traverse.table = table
+    traverse.tab = traverse_tab
     return traverse
 
 
@@ -126,3 +154,56 @@ def test_octree_above_2e32_words(host, oracle, scenes, gap):
     assert (res["leaf"][h] > 0xFFFFFFFF).any()
     # the oracle (64-bit offsets, as the reference) reads the shifted words the same way
     _assert_same(oracle.raymarch(big, rays, threads=4), ref, leaf=False)
+
+
+def _table_cases(golden, oracle, scenes):
+    g = golden["dragon"]
+    yield g["words"]
+    yield oracle.build_dense(scenes.random_grid((64, 64, 64), 0.5, 3))[0]  # far words
+    yield oracle.build_dense(scenes.sphere_scene(128, 24, 0))[0]
+    for grid, mem, words, center in golden_builds(golden):
+        yield words
+
+
+def test_table_traversal_matches_oracle(host, oracle, golden, scenes):
+    rays = np.concatenate([scenes.random_rays(30_000, 9), _nan_rays(), golden["dragon"]["rays"][:2000]])
+    for words in _table_cases(golden, oracle, scenes):
+        tab = host.table(words)
+        assert tab is not None
+        order = _bfs_order(words)
+        assert tab.shape[0] == order.size
+        assert np.array_equal(tab[:, 0], words[order])
+        _assert_same(host.tab(words, tab, rays), oracle.raymarch(words, rays, threads=4))
+        lod = host.tab(words, tab, rays, ray_scale=0.02)
+        _assert_same(lod, oracle.raymarch(words, rays, ray_scale=0.02, threads=4), leaf=False)
+
+
+def _bfs_order(words):
+    """Word indices of the nodes reachable from the root, breadth first."""
+    out, level = [], [0]
+    while level:
+        out.extend(level)
+        nxt = []
+        for d in level:
+            w = int(words[d])
+            valid, nonleaf = (w >> 8) & 0xFF, w & 0xFF
+            if not valid:
+                continue
+            off = w >> 18
+            if w & 0x20000:
+                off = (off << 32) | int(words[d + 1])
+            stride = 2 if w & 0x10000 else 1
+            nxt.extend(d + off + j * stride for j in range(bin(nonleaf).count("1")))
+        level = nxt
+    return np.array(out, np.int64)
+
+
+def test_table_refused_for_unsafe_trees(host):
+    # child block past the end, a zero offset, a non-leaf bit outside the
+    # valid mask, and internal children below level 21 each leave no table
+    assert host.table(np.array([(0x3FFF << 18) | (0xFF << 8) | 0xFF], np.uint32)) is None
+    assert host.table(np.array([(0xFF << 8) | 0xFF] + [0] * 8, np.uint32)) is None
+    assert host.table(np.array([(1 << 18) | (0x01 << 8) | 0x02, 0], np.uint32)) is None
+    chain = [(1 << 18) | (0x80 << 8) | 0x80] * 23 + [0]  # 23 nested single internal children
+    assert host.table(np.array(chain, np.uint32)) is None
+    assert host.table(np.array(chain[1:], np.uint32)) is not None  # 22 nested is fine
