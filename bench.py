@@ -178,6 +178,10 @@ def setup_scene(args, rank, torch, svo, scenes):
     n_vox = int((grid != 0).sum().item())
     del grid
     torch.cuda.empty_cache()
+    # the traversal's descriptor table (built by the first trace call anyway)
+    t0 = time.perf_counter()
+    n_tab = tree.table_size()
+    t_table = time.perf_counter() - t0
     center = tree.center()
     cams = scenes.orbit_cameras(args.cams, 1000 + rank, center, radius=1.25, radius_hi=2.0, pitch=45.0)
     npix = args.width * args.height
@@ -213,7 +217,8 @@ def setup_scene(args, rank, torch, svo, scenes):
     shadow_slices = [(int(starts[i]), int(starts[i + 1])) for i in range(len(cams))]
     cam_slices = [(i * npix, (i + 1) * npix) for i in range(len(cams))]
     del t, hit, idx, o, d, p, so
-    info = {"gen_s": t_gen, "build_s": t_build, "voxels": n_vox, "words": tree.num_words()}
+    info = {"gen_s": t_gen, "build_s": t_build, "voxels": n_vox, "words": tree.num_words(), "table_s": t_table,
+            "table_entries": n_tab}
     return tree, prim, shadow, cam_slices, shadow_slices, info
 
 
@@ -462,7 +467,10 @@ def run_ours(args):
             "viewer_frames": frames,
             "voxel_file_build": extra_vf,
             "build": {"build_s": round(info["build_s"], 3), "scene_gen_s": round(info["gen_s"], 3),
-                      "voxels_per_s": round(info["voxels"] / info["build_s"], 1)},
+                      "voxels_per_s": round(info["voxels"] / info["build_s"], 1),
+                      "descriptor_table_s": round(info["table_s"], 4),
+                      "descriptor_table_entries": info["table_entries"],
+                      "descriptor_table_bytes": info["table_entries"] * 16},
             "kernel_ms": {"primary": round(t_prim_avg, 3), "shadow": round(sum(t_shadow) / len(t_shadow), 3)},
         }
         print(json.dumps(line))
