@@ -378,10 +378,15 @@ def run_ours(args):
             tree.trace_host(hs_pin, out=os_)
         if world > 1:
             torch.distributed.barrier()
+        t_calls = [0.0, 0.0]
         t0 = time.perf_counter()
         for _ in range(args.steps):
+            ta = time.perf_counter()
             tree.trace_image_host(hp_pin, W, H, light=LIGHT, out=op)
+            tb = time.perf_counter()
             tree.trace_host(hs_pin, out=os_)
+            t_calls[0] += tb - ta
+            t_calls[1] += time.perf_counter() - tb
         e2e_s = time.perf_counter() - t0
         if world > 1:
             tt = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
@@ -392,7 +397,9 @@ def run_ours(args):
         e2e = {"value": round(total_rays / e2e_s / 1e6, 2), "unit": "Mrays/s",
                "h2d_bytes_per_step": (Rp + Rs) * 24, "d2h_bytes_per_step": Rp * 20 + Rs * 1,
                "api": "svo_trace_image_host (primary) + svo_trace_host (shadow): pinned host rays in, "
-                      "t/leaf/rgb and shadow hit out", "exact": bool(exact_e2e)}
+                      "t/leaf/rgb and shadow hit out", "exact": bool(exact_e2e),
+               "call_ms": {"primary": round(t_calls[0] / args.steps * 1e3, 3),
+                           "shadow": round(t_calls[1] / args.steps * 1e3, 3)}}
         del hp_pin, hs_pin, op, os_
 
     peaks, peak_kind = load_peaks()

@@ -31,6 +31,7 @@ constexpr int kMaxSmemJobs = 2048;  // views whose slot offsets are staged in sh
 struct JobDev {
     const uint32_t *oct;
     const uint4 *tab;  // the octree's descriptor table (kernels instantiated with kTab)
+    uint32_t n_tab;
     uint32_t n_words;
     uint32_t width, height, tiles_x;
     const float *rays;
@@ -235,12 +236,22 @@ __global__ void k_trace_persistent(BatchArgs a) {
     }
 }
 
+// Table entries (the top levels) each CTA of the image kernel copies into
+// shared memory.
+constexpr int kImageStage = 0;
+
 // One image view, passed by value (svo_trace_image): the tile kernel's loop
 // without a job table.
-template <bool kTab, bool kLod>
+template <bool kTab, bool kLod, int kStage>
 __global__ void k_trace_single(JobDev J, uint64_t total, unsigned long long *queue, uint32_t *status, int log_tile_w,
                                int chunk) {
     const int lane = threadIdx.x & 31;
+    __shared__ uint4 s_tab[kStage > 0 ? kStage : 1];
+    if (kTab && kStage > 0) {
+        const uint32_t m = min((uint32_t)kStage, J.n_tab);
+        for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) s_tab[i] = __ldg(J.tab + i);
+        __syncthreads();
+    }
     RayStack stk;
     BatchArgs a;  // only the fields write_result reads
     a.jobs = &J;
@@ -265,7 +276,12 @@ __global__ void k_trace_single(JobDev J, uint64_t total, unsigned long long *que
             RayState st;
             ray_init_any<kTab>(st, J.oct, J.tab, p0.x, p0.y, p1.x, p1.y, p2.x, p2.y);
             RayResult res;
-            while (!ray_step_any<kTab, kLod>(st, stk, J.oct, J.tab, J.n_words, J.ray_scale, res)) {
+            if constexpr (kTab && kStage > 0) {
+                while (!ray_step_tab<kLod, kStage>(st, stk, J.oct, J.tab, J.ray_scale, res, s_tab)) {
+                }
+            } else {
+                while (!ray_step_any<kTab, kLod>(st, stk, J.oct, J.tab, J.n_words, J.ray_scale, res)) {
+                }
             }
             write_result(a, 0, out_idx, res, p1.y, p2.x, p2.y);
         }
@@ -313,9 +329,11 @@ int launch_trace_image(const svo_octree *oct, const float *d_rays, uint32_t widt
     J.rgb = out.rgb;
     uint64_t total = (uint64_t)J.tiles_x * ((height + (32 / tile_w) - 1) / (32 / tile_w)) * 32;
     J.tab = octree_table(oct, st);
+    J.n_tab = J.tab ? (uint32_t)oct->n_tab : 0u;
+    constexpr int S = kImageStage;
     void (*kern)(JobDev, uint64_t, unsigned long long *, uint32_t *, int, int) =
-        J.tab ? (ray_scale != 0.0f ? k_trace_single<true, true> : k_trace_single<true, false>)
-              : (ray_scale != 0.0f ? k_trace_single<false, true> : k_trace_single<false, false>);
+        J.tab ? (ray_scale != 0.0f ? k_trace_single<true, true, S> : k_trace_single<true, false, S>)
+              : (ray_scale != 0.0f ? k_trace_single<false, true, 0> : k_trace_single<false, false, 0>);
     int dev = 0, sms = 0, resident = 0;
     SVO_CUDA_TRY(cudaGetDevice(&dev));
     SVO_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -362,6 +380,7 @@ int prepare_jobs(svo_batch *b, int tile_w) {
         std::memset(&J, 0, sizeof(J));
         J.oct = v.octree->d_words;
         J.tab = b->all_tab ? v.octree->d_tab : nullptr;
+        J.n_tab = b->all_tab ? (uint32_t)v.octree->n_tab : 0u;
         J.n_words = (uint32_t)v.octree->n_words;
         J.width = v.width;
         J.height = v.height;

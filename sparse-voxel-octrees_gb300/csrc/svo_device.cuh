@@ -352,9 +352,12 @@ __device__ __forceinline__ bool ray_step(RayStateT<Idx> &s, RayStack &stk, const
 // checks (the table exists only when every reachable offset, far word, child
 // slot and leaf slot is in range and no node is deeper than 22 levels).  The
 // geometry, the visiting order and every result are those of ray_step.
-template <bool kLod>
+// kStage > 0: the first kStage table entries (the top levels, stored first)
+// are also in shared memory at stab, and PUSHes into them read it there.
+template <bool kLod, int kStage = 0>
 __device__ __forceinline__ bool ray_step_tab(RayState &s, RayStack &stk, const uint32_t *__restrict__ words,
-                                             const uint4 *__restrict__ tab, float rayScale, RayResult &res) {
+                                             const uint4 *__restrict__ tab, float rayScale, RayResult &res,
+                                             const uint4 *stab = nullptr) {
     float cornerTX = s.posX * s.dTx - s.bTx;
     float cornerTY = s.posY * s.dTy - s.bTy;
     float cornerTZ = s.posZ * s.dTz - s.bTz;
@@ -385,7 +388,12 @@ __device__ __forceinline__ bool ray_step_tab(RayState &s, RayStack &stk, const u
                 return true;
             }
             stk.e[s.scale] = make_uint4(s.parent, __float_as_uint(s.maxT), s.current, s.lbase);
-            uint4 c = __ldg(tab + s.parent + __popc(childMasks & 127u));
+            const uint32_t k = s.parent + __popc(childMasks & 127u);
+            uint4 c;
+            if (kStage > 0 && k < (uint32_t)kStage)
+                c = stab[k];
+            else
+                c = __ldg(tab + k);
             s.current = c.x;
             s.parent = c.y;
             s.lbase = c.z;
