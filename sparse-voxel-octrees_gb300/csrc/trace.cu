@@ -8,6 +8,8 @@
 // 64-bit ones (larger octrees, whose far offsets exceed 32 bits);
 // k_trace_plain_tab walks the handle's descriptor table instead, where it
 // has one.
+#include <algorithm>
+
 #include "svo_device.cuh"
 #include "svo_internal.h"
 
@@ -76,6 +78,28 @@ __global__ void __launch_bounds__(256) k_trace_plain_tab(TraceArgs a) {
     store_result<uint32_t>(a, i, r, dx, dy, dz);
 }
 
+// The table kernel as a persistent grid: each warp takes the next 32 rays
+// from a per-launch counter, so a warp that finishes early starts new rays
+// instead of leaving its slot idle until the slowest warp of its CTA is done.
+__global__ void __launch_bounds__(256) k_trace_queue_tab(TraceArgs a, unsigned long long *queue) {
+    const int lane = threadIdx.x & 31;
+    while (true) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(queue, 32ull);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= a.n) break;
+        const uint64_t i = base + lane;
+        if (i >= a.n) continue;
+        float ox, oy, oz, dx, dy, dz;
+        load_ray(a.rays, i, ox, oy, oz, dx, dy, dz);
+        RayResult r = trace_ray<true>(a.oct, a.tab, 0u, ox, oy, oz, dx, dy, dz, a.ray_scale);
+        store_result<uint32_t>(a, i, r, dx, dy, dz);
+    }
+}
+
+// svo_trace's table kernel: the persistent queue form, or one thread per ray.
+constexpr bool kPlainQueue = true;
+
 __global__ void __launch_bounds__(256) k_count_loads(const uint32_t *oct, uint32_t n_words, const float *rays,
                                                     uint64_t n, float ray_scale, uint32_t *loads,
                                                     uint32_t *status) {
@@ -116,9 +140,27 @@ int launch_trace(const svo_octree *oct, const float *d_rays, uint64_t n, float r
     const unsigned grid = (unsigned)((n + 255) / 256);
     if (wide_octree(oct) || oct->index_bits == 64)
         k_trace_plain<uint64_t><<<grid, 256, 0, st>>>(a);
-    else if ((a.tab = octree_table(oct, st)) != nullptr)
+    else if ((a.tab = octree_table(oct, st)) != nullptr) {
+        if (kPlainQueue) {
+            int dev = 0, sms = 0, resident = 0;
+            SVO_CUDA_TRY(cudaGetDevice(&dev));
+            SVO_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+            SVO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k_trace_queue_tab, 256, 0));
+            void *q = nullptr;
+            SVO_CUDA_TRY(scratch_alloc(&q, sizeof(unsigned long long), st));
+            cudaError_t e = cudaMemsetAsync(q, 0, sizeof(unsigned long long), st);
+            const uint64_t warps = (n + 31) / 32;
+            const uint64_t ctas = std::min<uint64_t>((uint64_t)sms * std::max(1, resident), (warps + 7) / 8);
+            if (e == cudaSuccess) {
+                k_trace_queue_tab<<<(unsigned)ctas, 256, 0, st>>>(a, (unsigned long long *)q);
+                e = cudaGetLastError();
+            }
+            cudaFreeAsync(q, st);
+            if (e != cudaSuccess) return cuda_fail(e, "svo_trace");
+            return SVO_OK;
+        }
         k_trace_plain_tab<<<grid, 256, 0, st>>>(a);
-    else
+    } else
         k_trace_plain<uint32_t><<<grid, 256, 0, st>>>(a);
     SVO_CUDA_TRY(cudaGetLastError());
     return SVO_OK;
