@@ -144,7 +144,7 @@ __global__ void k_trace_tiles(BatchArgs a) {
     __syncthreads();
     const uint64_t *beg = staged ? s_begin : a.begin;
     const int lane = threadIdx.x & 31;
-    RayStack stk;
+    RayStackFor<kTab> stk;
     while (true) {
         unsigned long long base = 0;
         if (lane == 0) base = atomicAdd(a.queue, (unsigned long long)a.chunk);
@@ -182,7 +182,7 @@ __global__ void k_trace_persistent(BatchArgs a) {
     const int lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;
     RayState st;
-    RayStack stk;
+    RayStackFor<kTab> stk;
     bool active = false;
     int job = 0;
     uint32_t out_idx = 0, nw = 0;
@@ -252,7 +252,7 @@ __global__ void k_trace_single(JobDev J, uint64_t total, unsigned long long *que
         for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) s_tab[i] = __ldg(J.tab + i);
         __syncthreads();
     }
-    RayStack stk;
+    RayStackFor<kTab> stk;
     BatchArgs a;  // only the fields write_result reads
     a.jobs = &J;
     a.status = status;

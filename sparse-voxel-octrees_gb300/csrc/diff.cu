@@ -80,7 +80,7 @@ __device__ __forceinline__ Shading shade_terms(const float *p_n, uint32_t leaf, 
 template <bool kTab, bool kRecord>
 __global__ void k_diff_forward(DiffArgs a) {
     const int lane = threadIdx.x & 31;
-    RayStack stk;
+    RayStackFor<kTab> stk;
     while (true) {
         unsigned long long base = 0;
         if (lane == 0) base = atomicAdd(a.queue, 32ull);
@@ -135,7 +135,7 @@ __global__ void k_diff_backward(DiffArgs a) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
-    RayStack stk;
+    RayStackFor<kTab> stk;
     while (true) {
         unsigned long long base = 0;
         if (lane == 0) base = atomicAdd(a.queue, 32ull);

@@ -8,6 +8,7 @@
 #pragma once
 
 #include <cstdint>
+#include <type_traits>
 
 namespace svo {
 
@@ -131,6 +132,17 @@ struct RayStack {
     uint4 e[kMaxScale];  // {parent low word, maxT bits, descriptor, parent high word} per scale
 };
 
+// The table traversal's stack: {table ordinal of the node, maxT bits} per
+// scale.  A POP reloads the node's entry (descriptor, children, block) from
+// the table, as the reference reloads the descriptor (:253-254, `current =
+// 0` at :338), so a PUSH stores 8 bytes instead of 16.
+struct TabStack {
+    uint2 e[kMaxScale];
+};
+
+template <bool kTab>
+using RayStackFor = std::conditional_t<kTab, TabStack, RayStack>;
+
 template <typename Idx>
 struct RayStateT {
     float dTx, dTy, dTz, bTx, bTy, bTz;
@@ -138,6 +150,7 @@ struct RayStateT {
     Idx parent;  // the table traversal keeps the first internal child's table ordinal here
     uint32_t current, pushes, nload;
     uint32_t lbase;  // table traversal: word index of the current node's child block
+    uint32_t self;   // table traversal: the current node's table ordinal
     int idx, scale, octantMask;
 };
 using RayState = RayStateT<uint32_t>;
@@ -213,6 +226,7 @@ __device__ __forceinline__ void ray_init(RayState &s, const uint4 *__restrict__ 
     s.current = r.x;
     s.parent = r.y;
     s.lbase = r.z;
+    s.self = 0;
 }
 
 // One pass of the loop body.  Returns false while the ray continues; true
@@ -351,11 +365,14 @@ __device__ __forceinline__ bool ray_step(RayStateT<Idx> &s, RayStack &stk, const
 // needs neither the offset and far-word decoding of :276-280 nor bounds
 // checks (the table exists only when every reachable offset, far word, child
 // slot and leaf slot is in range and no node is deeper than 22 levels).  The
-// geometry, the visiting order and every result are those of ray_step.
+// stack keeps 8 bytes per scale (the node's ordinal and maxT) and a POP
+// reloads the node's entry: local-memory stores are written through to L2,
+// and halving them was worth 9% on the config-1 step.  The geometry, the
+// visiting order and every result are those of ray_step.
 // kStage > 0: the first kStage table entries (the top levels, stored first)
 // are also in shared memory at stab, and PUSHes into them read it there.
 template <bool kLod, int kStage = 0>
-__device__ __forceinline__ bool ray_step_tab(RayState &s, RayStack &stk, const uint32_t *__restrict__ words,
+__device__ __forceinline__ bool ray_step_tab(RayState &s, TabStack &stk, const uint32_t *__restrict__ words,
                                              const uint4 *__restrict__ tab, float rayScale, RayResult &res,
                                              const uint4 *stab = nullptr) {
     float cornerTX = s.posX * s.dTx - s.bTx;
@@ -387,13 +404,14 @@ __device__ __forceinline__ bool ray_step_tab(RayState &s, RayStack &stk, const u
                 res.t = s.minT;
                 return true;
             }
-            stk.e[s.scale] = make_uint4(s.parent, __float_as_uint(s.maxT), s.current, s.lbase);
+            stk.e[s.scale] = make_uint2(s.self, __float_as_uint(s.maxT));
             const uint32_t k = s.parent + __popc(childMasks & 127u);
             uint4 c;
             if (kStage > 0 && k < (uint32_t)kStage)
                 c = stab[k];
             else
                 c = __ldg(tab + k);
+            s.self = k;
             s.current = c.x;
             s.parent = c.y;
             s.lbase = c.z;
@@ -428,11 +446,13 @@ __device__ __forceinline__ bool ray_step_tab(RayState &s, RayStack &stk, const u
             return true;
         }
         s.scaleExp2 = __uint_as_float((uint32_t)(s.scale - kMaxScale + 127) << 23);
-        uint4 e = stk.e[s.scale];
-        s.parent = e.x;
+        const uint2 e = stk.e[s.scale];
+        s.self = e.x;
         s.maxT = __uint_as_float(e.y);
-        s.current = e.z;
-        s.lbase = e.w;
+        const uint4 c = __ldg(tab + s.self);
+        s.current = c.x;
+        s.parent = c.y;
+        s.lbase = c.z;
         uint32_t shX = __float_as_uint(s.posX) >> s.scale;
         uint32_t shY = __float_as_uint(s.posY) >> s.scale;
         uint32_t shZ = __float_as_uint(s.posZ) >> s.scale;
@@ -447,7 +467,7 @@ __device__ __forceinline__ bool ray_step_tab(RayState &s, RayStack &stk, const u
 // Where an octree has a table (tab != nullptr on the host side, selected at
 // compile time here), the table step, else the checked word step.
 template <bool kTab, bool kLod>
-__device__ __forceinline__ bool ray_step_any(RayState &s, RayStack &stk, const uint32_t *__restrict__ words,
+__device__ __forceinline__ bool ray_step_any(RayState &s, RayStackFor<kTab> &stk, const uint32_t *__restrict__ words,
                                              const uint4 *__restrict__ tab, uint32_t n_words, float rayScale,
                                              RayResult &res) {
     if constexpr (kTab)
@@ -471,7 +491,7 @@ template <bool kTab>
 __device__ __forceinline__ RayResult trace_ray(const uint32_t *__restrict__ words, const uint4 *__restrict__ tab,
                                                uint32_t n_words, float ox, float oy, float oz, float dx, float dy,
                                                float dz, float rayScale) {
-    RayStack stk;
+    RayStackFor<kTab> stk;
     RayState s;
     RayResult res;
     res.status = kMiss;

@@ -21,6 +21,10 @@ struct uint4 {
     uint32_t x, y, z, w;
 };
 static inline uint4 make_uint4(uint32_t x, uint32_t y, uint32_t z, uint32_t w) { return uint4{x, y, z, w}; }
+struct uint2 {
+    uint32_t x, y;
+};
+static inline uint2 make_uint2(uint32_t x, uint32_t y) { return uint2{x, y}; }
 static inline uint32_t __ldg(const uint32_t *p) { return *p; }
 static inline uint4 __ldg(const uint4 *p) { return *p; }
 static inline int __popc(uint32_t v) { return __builtin_popcount(v); }
@@ -121,7 +125,7 @@ extern "C" void host_traverse_tab(const uint32_t *words, const uint32_t *tab, co
     const uint4 *tb = reinterpret_cast<const uint4 *>(tab);
     for (uint64_t i = 0; i < n; ++i) {
         const float *r = rays + 6 * i;
-        RayStack stk;
+        TabStack stk;
         RayState s;
         RayResult res;
         res.status = kMiss;
