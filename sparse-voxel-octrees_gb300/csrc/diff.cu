@@ -77,17 +77,28 @@ __device__ __forceinline__ Shading shade_terms(const float *p_n, uint32_t leaf, 
     return sh;
 }
 
+// Slots a warp takes from the queue at once (multiples of 32): a forward
+// warp traces one 8x4 tile at a time; the adjoint, without traversal, is
+// short per slot, so it takes several tiles per queue access.
+constexpr int kFwdChunk = 64;
+constexpr int kBwdChunk = 128;
+
 template <bool kTab, bool kRecord>
 __global__ void k_diff_forward(DiffArgs a) {
     const int lane = threadIdx.x & 31;
     RayStackFor<kTab> stk;
+    unsigned long long base = 0, end = 0;
     while (true) {
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(a.queue, 32ull);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= a.total) break;
+        if (base >= end) {
+            if (lane == 0) base = atomicAdd(a.queue, (unsigned long long)kFwdChunk);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base >= a.total) break;
+            end = min(base + (unsigned long long)kFwdChunk, (unsigned long long)a.total);
+        }
+        const unsigned long long slot = base + lane;
+        base += 32;
         uint32_t idx, view;
-        if (!tile_pixel(a, base + lane, idx, view)) continue;
+        if (!tile_pixel(a, slot, idx, view)) continue;
         const float2 *r2 = reinterpret_cast<const float2 *>(a.rays) + 3 * (uint64_t)idx;
         float2 p0 = __ldg(r2), p1 = __ldg(r2 + 1), p2 = __ldg(r2 + 2);
         RayState st;
@@ -136,13 +147,18 @@ __global__ void k_diff_backward(DiffArgs a) {
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     RayStackFor<kTab> stk;
+    unsigned long long base = 0, end = 0;
     while (true) {
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(a.queue, 32ull);
-        base = __shfl_sync(FULL, base, 0);
-        if (base >= a.total) break;
+        if (base >= end) {
+            if (lane == 0) base = atomicAdd(a.queue, (unsigned long long)kBwdChunk);
+            base = __shfl_sync(FULL, base, 0);
+            if (base >= a.total) break;
+            end = min(base + (unsigned long long)kBwdChunk, (unsigned long long)a.total);
+        }
+        const unsigned long long slot = base + lane;
+        base += 32;
         uint32_t idx = 0, view = 0;
-        bool live = tile_pixel(a, base + lane, idx, view);
+        bool live = tile_pixel(a, slot, idx, view);
         uint32_t leaf = 0xFFFFFFFFu;
         float dx = 0.f, dy = 0.f, dz = 0.f;
         if (live) {

@@ -78,18 +78,25 @@ __global__ void __launch_bounds__(256) k_trace_plain_tab(TraceArgs a) {
     store_result<uint32_t>(a, i, r, dx, dy, dz);
 }
 
-// The table kernel as a persistent grid: each warp takes the next 32 rays
-// from a per-launch counter, so a warp that finishes early starts new rays
-// instead of leaving its slot idle until the slowest warp of its CTA is done.
+// The table kernel as a persistent grid: each warp takes the next
+// kQueueChunk rays from a per-launch counter (32 at a time), so a warp that
+// finishes early starts new rays instead of leaving its slot idle until the
+// slowest warp of its CTA is done.
+constexpr int kQueueChunk = 32;
+
 __global__ void __launch_bounds__(256) k_trace_queue_tab(TraceArgs a, unsigned long long *queue) {
     const int lane = threadIdx.x & 31;
+    unsigned long long base = 0, end = 0;
     while (true) {
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(queue, 32ull);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= a.n) break;
+        if (base >= end) {
+            if (lane == 0) base = atomicAdd(queue, (unsigned long long)kQueueChunk);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base >= a.n) break;
+            end = min(base + (unsigned long long)kQueueChunk, (unsigned long long)a.n);
+        }
         const uint64_t i = base + lane;
-        if (i >= a.n) continue;
+        base += 32;
+        if (i >= end) continue;
         float ox, oy, oz, dx, dy, dz;
         load_ray(a.rays, i, ox, oy, oz, dx, dy, dz);
         RayResult r = trace_ray<true>(a.oct, a.tab, 0u, ox, oy, oz, dx, dy, dz, a.ray_scale);
