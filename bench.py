@@ -462,7 +462,7 @@ def run_ours(args):
                        "parallelism": "replicas x%d" % world},
             "e2e": e2e, "gpu_launches": 2 * args.steps, "roofline": roofline, "cpu_baseline": cpu,
             "clocks": clk.summary(),
-            "plain": {"api": "svo_trace for primary and shadow rays (one thread per ray)",
+            "plain": {"api": "svo_trace for primary (row order) and shadow rays",
                       "ms_per_step": round(ms_plain, 3), "mrays_s": round(rays_per_step / ms_plain / 1e3, 1),
                       "exact_vs_value_path": bool(exact_plain)},
             "batched": {"api": "svo_batch: 32 image views + shadow view, autotuned, CUDA graph",
