@@ -78,10 +78,11 @@ __device__ __forceinline__ bool setup_slot(const BatchArgs &a, const uint64_t *b
     uint64_t local = slot - beg[j];
     uint32_t px = 0, py = 0;
     if (J.width) {
-        uint64_t tile = local >> 5;
-        uint32_t r = (uint32_t)(local & 31);
-        px = (uint32_t)(tile % J.tiles_x) * (1u << a.log_tile_w) + (r & ((1u << a.log_tile_w) - 1u));
-        py = (uint32_t)(tile / J.tiles_x) * (32u >> a.log_tile_w) + (r >> a.log_tile_w);
+        // tile < 2^27 (a view has at most 2^32 pixels): 32-bit division
+        const uint32_t tile = (uint32_t)(local >> 5), r = (uint32_t)(local & 31);
+        const uint32_t ty = tile / J.tiles_x, tx = tile - ty * J.tiles_x;
+        px = tx * (1u << a.log_tile_w) + (r & ((1u << a.log_tile_w) - 1u));
+        py = ty * (32u >> a.log_tile_w) + (r >> a.log_tile_w);
         if (px >= J.width || py >= J.height) return false;
         out_idx = py * J.width + px;
     } else {
@@ -265,10 +266,10 @@ __global__ void k_trace_single(JobDev J, uint64_t total, unsigned long long *que
         for (unsigned long long s0 = base; s0 < end; s0 += 32) {
             uint64_t local = s0 + lane;
             if (local >= end) continue;
-            uint64_t tile = local >> 5;
-            uint32_t r = (uint32_t)(local & 31);
-            uint32_t px = (uint32_t)(tile % J.tiles_x) * (1u << log_tile_w) + (r & ((1u << log_tile_w) - 1u));
-            uint32_t py = (uint32_t)(tile / J.tiles_x) * (32u >> log_tile_w) + (r >> log_tile_w);
+            const uint32_t tile = (uint32_t)(local >> 5), r = (uint32_t)(local & 31);  // tile < 2^27
+            const uint32_t ty = tile / J.tiles_x, tx = tile - ty * J.tiles_x;
+            uint32_t px = tx * (1u << log_tile_w) + (r & ((1u << log_tile_w) - 1u));
+            uint32_t py = ty * (32u >> log_tile_w) + (r >> log_tile_w);
             if (px >= J.width || py >= J.height) continue;
             uint32_t out_idx = py * J.width + px;
             const float2 *r2 = reinterpret_cast<const float2 *>(J.rays) + 3 * (uint64_t)out_idx;

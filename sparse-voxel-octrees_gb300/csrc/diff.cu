@@ -45,10 +45,11 @@ struct DiffArgs {
 };
 
 __device__ __forceinline__ bool tile_pixel(const DiffArgs &a, uint64_t slot, uint32_t &idx, uint32_t &view) {
-    uint64_t tile = slot >> 5;
-    uint32_t r = (uint32_t)(slot & 31);
-    uint32_t px = (uint32_t)(tile % a.tiles_x) * 8u + (r & 7u);
-    uint32_t py = (uint32_t)(tile / a.tiles_x) * 4u + (r >> 3);
+    if (slot >= a.total) return false;
+    const uint32_t tile = (uint32_t)(slot >> 5), r = (uint32_t)(slot & 31);  // tile < 2^27: 32-bit division
+    const uint32_t ty = tile / a.tiles_x, tx = tile - ty * a.tiles_x;
+    uint32_t px = tx * 8u + (r & 7u);
+    uint32_t py = ty * 4u + (r >> 3);
     if (px >= a.width || py >= a.height * a.n_views) return false;
     idx = py * a.width + px;
     view = py / a.height;
