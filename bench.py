@@ -64,6 +64,8 @@ def parse():
                         "4: differentiable shading fwd+bwd")
     p.add_argument("--no-extra", action="store_true", help="skip the config-3 batched comparison in the default run")
     p.add_argument("--views", type=int, default=96)
+    p.add_argument("--max-side", type=int, default=0,
+                   help="config 3: clamp each octree's side to this (a smaller case for profiling)")
     p.add_argument("--train-steps", type=int, default=200, help="Adam steps of the config-4 leg")
     return p.parse_args()
 
@@ -509,6 +511,8 @@ def run_config3(args, torch, svo, scenes, tune_cache=None):
     trees = []
     total_rays = 0
     for (i, side, gen, W, H) in config3_views(args.views):
+        if args.max_side:
+            side = min(side, args.max_side)
         grid = scenes.gpu_sphere_scene(side, 48, i) if gen == "sphere" else scenes.gpu_terrain_scene(side, 200, i)
         tree = svo.VoxelOctree(svo.VoxelData(grid))
         del grid
@@ -556,14 +560,31 @@ def run_config3(args, torch, svo, scenes, tune_cache=None):
 
     ms_plain = timed(plain_step)
     ms_batched = timed(batched_step)
-    exact = all(torch.equal(v["out"][k], po[3][k]) for v, po in zip(views, plain_out) for k in ("t", "leaf", "rgb"))
-    return {"workload": "%d octrees (depth 7-11, sphere/terrain generators, seeds 1..%d), one view each, "
-                        "256x256..1920x1080 log-uniform pixels" % (len(views), len(views)),
+    same = lambda: all(torch.equal(v["out"][k], po[3][k]) for v, po in zip(views, plain_out)
+                       for k in ("t", "leaf", "rgb"))
+    exact = same()
+    # the chosen plain-tile shape (or the default tile shape, when lane refill
+    # won) at each per-warp table cache depth the autotuner tries
+    base = cfg.as_dict()
+    if base["refill_idle"] != 0:
+        base.update(refill_idle=0, steps_per_round=1, chunk=32)
+    cache_sweep = {}
+    for ce in (0, 64, 256):
+        if (base["block_threads"] // 32) * ce * 16 > 65536:
+            continue
+        c = svo.default_config(**dict(base, cache_entries=ce))
+        ms = timed(lambda: batch.trace(c, stream))
+        cache_sweep[str(ce)] = {"ms": round(ms, 3), "exact_hit_parity": bool(same())}
+    depth_hi = min(11, args.max_side.bit_length() - 1) if args.max_side else 11
+    return {"workload": "%d octrees (depth 7-%d, sphere/terrain generators, seeds 1..%d), one view each, "
+                        "256x256..1920x1080 log-uniform pixels" % (len(views), depth_hi, len(views)),
             "rays_per_step": total_rays, "octree_words": int(sum(t.num_words() for t in trees)),
             "plain_ms": round(ms_plain, 3), "batched_ms": round(ms_batched, 3),
             "plain_mrays_s": round(total_rays / ms_plain / 1e3, 1),
             "batched_mrays_s": round(total_rays / ms_batched / 1e3, 1),
             "speedup": round(ms_plain / ms_batched, 3), "exact_hit_parity": bool(exact),
+            "table_cache_sweep": {"shape": {k: v for k, v in base.items() if k != "cache_entries"},
+                                  "ms_by_cache_entries": cache_sweep},
             "config": cfg.as_dict(), "autotune_s": round(tune_s, 1), "setup_s": round(setup_s, 1),
             "launches": {"plain": len(views), "batched": 1}}
 

@@ -11,6 +11,13 @@
 // them, so lanes keep doing traversal steps instead of waiting for the
 // slowest ray of a fixed 32-ray batch.  Nothing waits on another warp or CTA.
 //
+// Optionally (plain-tile schedule) each warp keeps the first `cache_entries`
+// descriptor-table entries (the top levels: the table is stored breadth
+// first) of one octree in its own slice of shared memory, reloaded when the
+// octree of the warp's next 32 slots changes; lanes tracing another octree
+// read the global table.  The cached entries are copies of the global ones,
+// so results do not depend on the cache.  The autotuner picks the depth.
+//
 // Each ray runs the same ray_init / ray_step as svo_trace (VoxelOctree.cpp:
 // 207-346), so results are bit-identical to the plain kernel's.
 #include <algorithm>
@@ -55,7 +62,35 @@ struct BatchArgs {
     int steps_per_round;
     int log_tile_w;
     int chunk;
+    int cache_entries;      // per-warp table cache (0 = none)
+    uint32_t cache_offset;  // byte offset of the warp caches in dynamic shared memory
 };
+
+constexpr int kMaxCacheEntries = 512;
+constexpr int kMaxCacheBytes = 64 * 1024;  // per CTA
+
+// Fills a warp's table cache with the first entries of job j's table and
+// returns how many it holds.  Called by all 32 lanes with no lane still
+// reading the cache.
+__device__ __forceinline__ uint32_t load_warp_cache(const JobDev *jobs, int j, uint4 *wc, int cap, int lane) {
+    const uint4 *tab = jobs[j].tab;
+    const uint32_t n = min((uint32_t)cap, jobs[j].n_tab);
+    __syncwarp();
+    for (uint32_t i = lane; i < n; i += 32) wc[i] = __ldg(tab + i);
+    __syncwarp();
+    return n;
+}
+
+// The table step, reading the warp's cache for rays of the cached octree.
+template <bool kTab, bool kLod, bool kCache>
+__device__ __forceinline__ bool batch_step(RayState &s, RayStackFor<kTab> &stk, const uint32_t *__restrict__ words,
+                                           const uint4 *__restrict__ tab, uint32_t n_words, float rayScale,
+                                           RayResult &res, const uint4 *wc, uint32_t wc_n) {
+    if constexpr (kTab && kCache)
+        return ray_step_tab<kLod, true>(s, stk, words, tab, rayScale, res, wc, wc_n);
+    else
+        return ray_step_any<kTab, kLod>(s, stk, words, tab, n_words, rayScale, res);
+}
 
 __device__ __forceinline__ int find_job(const uint64_t *beg, int n_jobs, uint64_t slot) {
     int lo = 0, hi = n_jobs;  // beg[lo] <= slot < beg[hi]
@@ -136,15 +171,19 @@ __device__ __forceinline__ void write_result(const BatchArgs &a, int job, uint32
 
 // refill_idle == 0: a warp takes `chunk` slots at once and runs them 32 at a
 // time, each lane to completion, before it takes the next chunk.
-template <bool kTab, bool kLod>
-__global__ void k_trace_tiles(BatchArgs a) {
-    extern __shared__ uint64_t s_begin[];
+template <bool kTab, bool kLod, bool kCache>
+__device__ __forceinline__ void trace_tiles(const BatchArgs &a, unsigned char *s_dyn) {
+    uint64_t *s_begin = reinterpret_cast<uint64_t *>(s_dyn);
     const bool staged = a.n_jobs + 1 <= kMaxSmemJobs;
     if (staged)
         for (int i = threadIdx.x; i <= a.n_jobs; i += blockDim.x) s_begin[i] = a.begin[i];
     __syncthreads();
     const uint64_t *beg = staged ? s_begin : a.begin;
     const int lane = threadIdx.x & 31;
+    uint4 *wc = nullptr;
+    if (kCache) wc = reinterpret_cast<uint4 *>(s_dyn + a.cache_offset) + (threadIdx.x >> 5) * a.cache_entries;
+    int cjob = -1;
+    uint32_t cn = 0;
     RayStackFor<kTab> stk;
     while (true) {
         unsigned long long base = 0;
@@ -153,6 +192,16 @@ __global__ void k_trace_tiles(BatchArgs a) {
         if (base >= a.total) break;
         unsigned long long end = min(base + (unsigned long long)a.chunk, (unsigned long long)a.total);
         for (unsigned long long s0 = base; s0 < end; s0 += 32) {
+            if constexpr (kCache) {
+                // The octree of the group's first slot (a group spans two
+                // views only at the end of one), loaded before any ray state
+                // is live.  s0 is the same in every lane.
+                const int want = find_job(beg, a.n_jobs, s0);
+                if (want != cjob) {
+                    cn = load_warp_cache(a.jobs, want, wc, a.cache_entries, lane);
+                    cjob = want;
+                }
+            }
             uint64_t slot = s0 + lane;
             if (slot >= end) continue;
             RayState st;
@@ -162,8 +211,9 @@ __global__ void k_trace_tiles(BatchArgs a) {
             const uint4 *tab;
             float rs, rdx, rdy, rdz;
             if (!setup_slot<kTab>(a, beg, slot, st, job, out_idx, oct, tab, nw, rs, rdx, rdy, rdz)) continue;
+            const uint32_t my_n = (kCache && job == cjob) ? cn : 0u;
             RayResult res;
-            while (!ray_step_any<kTab, kLod>(st, stk, oct, tab, nw, rs, res)) {
+            while (!batch_step<kTab, kLod, kCache>(st, stk, oct, tab, nw, rs, res, wc, my_n)) {
             }
             write_result(a, job, out_idx, res, rdx, rdy, rdz);
         }
@@ -171,8 +221,23 @@ __global__ void k_trace_tiles(BatchArgs a) {
 }
 
 template <bool kTab, bool kLod>
+__global__ void k_trace_tiles(BatchArgs a) {
+    extern __shared__ __align__(16) unsigned char s_dyn[];
+    trace_tiles<kTab, kLod, false>(a, s_dyn);
+}
+
+// With the table cache: capped at 48 registers (5 CTAs of 256 threads per
+// SM, as the uncached kernel); uncapped it takes 60.
+template <bool kLod>
+__global__ void __maxnreg__(48) k_trace_tiles_cached(BatchArgs a) {
+    extern __shared__ __align__(16) unsigned char s_dyn[];
+    trace_tiles<true, kLod, true>(a, s_dyn);
+}
+
+template <bool kTab, bool kLod>
 __global__ void k_trace_persistent(BatchArgs a) {
-    extern __shared__ uint64_t s_begin[];
+    extern __shared__ __align__(16) unsigned char s_dyn[];
+    uint64_t *s_begin = reinterpret_cast<uint64_t *>(s_dyn);
     const bool staged = a.n_jobs + 1 <= kMaxSmemJobs;
     if (staged)
         for (int i = threadIdx.x; i <= a.n_jobs; i += blockDim.x) s_begin[i] = a.begin[i];
@@ -278,7 +343,8 @@ __global__ void k_trace_single(JobDev J, uint64_t total, unsigned long long *que
             ray_init_any<kTab>(st, J.oct, J.tab, p0.x, p0.y, p1.x, p1.y, p2.x, p2.y);
             RayResult res;
             if constexpr (kTab && kStage > 0) {
-                while (!ray_step_tab<kLod, kStage>(st, stk, J.oct, J.tab, J.ray_scale, res, s_tab)) {
+                const uint32_t m = min((uint32_t)kStage, J.n_tab);
+                while (!ray_step_tab<kLod, true>(st, stk, J.oct, J.tab, J.ray_scale, res, s_tab, m)) {
                 }
             } else {
                 while (!ray_step_any<kTab, kLod>(st, stk, J.oct, J.tab, J.n_words, J.ray_scale, res)) {
@@ -299,7 +365,10 @@ bool config_ok(const svo_trace_config &c) {
     return c.block_threads >= 32 && c.block_threads <= 1024 && c.block_threads % 32 == 0 && c.blocks_per_sm >= 1 &&
            c.blocks_per_sm <= 32 && c.refill_idle >= 0 && c.refill_idle <= 32 && c.steps_per_round >= 1 &&
            c.steps_per_round <= 4096 && (c.tile_w == 4 || c.tile_w == 8 || c.tile_w == 16 || c.tile_w == 32) &&
-           c.chunk >= 32 && c.chunk <= 8192 && c.chunk % 32 == 0;
+           c.chunk >= 32 && c.chunk <= 8192 && c.chunk % 32 == 0 && c.cache_entries >= 0 &&
+           c.cache_entries <= kMaxCacheEntries && c.cache_entries % 32 == 0 &&
+           (c.cache_entries == 0 || c.refill_idle == 0) &&
+           (c.block_threads / 32) * c.cache_entries * (int)sizeof(uint4) <= kMaxCacheBytes;
 }
 
 }  // namespace
@@ -408,6 +477,35 @@ int prepare_jobs(svo_batch *b, int tile_w) {
     return SVO_OK;
 }
 
+using BatchKernel = void (*)(BatchArgs);
+
+// The kernel for a launch shape: plain tiles or lane refill, table or word
+// traversal, level-of-detail exit, per-warp table cache (table only).
+BatchKernel batch_kernel(bool tab, bool lod, bool refill, bool cache) {
+    if (refill) {
+        if (tab) return lod ? k_trace_persistent<true, true> : k_trace_persistent<true, false>;
+        return lod ? k_trace_persistent<false, true> : k_trace_persistent<false, false>;
+    }
+    if (tab) {
+        if (cache) return lod ? k_trace_tiles_cached<true> : k_trace_tiles_cached<false>;
+        return lod ? k_trace_tiles<true, true> : k_trace_tiles<true, false>;
+    }
+    return lod ? k_trace_tiles<false, true> : k_trace_tiles<false, false>;
+}
+
+// Dynamic shared memory above the default 48 KB needs an opt-in per kernel;
+// it is set outside any stream capture, when a batch is created.
+int allow_large_smem() {
+    const int bytes = (int)(((kMaxSmemJobs * sizeof(uint64_t)) + 15) / 16 * 16) + kMaxCacheBytes;
+    for (int tab = 0; tab < 2; ++tab)
+        for (int lod = 0; lod < 2; ++lod)
+            for (int refill = 0; refill < 2; ++refill)
+                for (int cache = 0; cache <= (tab && !refill); ++cache)
+                    SVO_CUDA_TRY(cudaFuncSetAttribute(batch_kernel(tab, lod, refill, cache),
+                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    return SVO_OK;
+}
+
 int enqueue_trace(svo_batch *b, const svo_trace_config &c, cudaStream_t st) {
     BatchArgs a;
     a.jobs = b->jobs_d;
@@ -420,21 +518,15 @@ int enqueue_trace(svo_batch *b, const svo_trace_config &c, cudaStream_t st) {
     a.steps_per_round = c.steps_per_round;
     a.log_tile_w = log2_of(c.tile_w);
     a.chunk = c.chunk;
+    // [slot offsets (when staged)][one table cache per warp]
     size_t smem = (a.n_jobs + 1 <= kMaxSmemJobs) ? (size_t)(a.n_jobs + 1) * sizeof(uint64_t) : 0;
+    const bool cache = b->all_tab && c.cache_entries > 0;
+    a.cache_entries = cache ? c.cache_entries : 0;
+    a.cache_offset = (uint32_t)((smem + 15) / 16 * 16);
+    if (cache) smem = a.cache_offset + (size_t)(c.block_threads / 32) * c.cache_entries * sizeof(uint4);
     // A persistent grid larger than what is resident only adds CTAs that
     // start after the queue is drained: clamp to the occupancy limit.
-    void (*kern)(BatchArgs);
-    if (b->all_tab) {
-        if (c.refill_idle == 0)
-            kern = b->any_lod ? k_trace_tiles<true, true> : k_trace_tiles<true, false>;
-        else
-            kern = b->any_lod ? k_trace_persistent<true, true> : k_trace_persistent<true, false>;
-    } else {
-        if (c.refill_idle == 0)
-            kern = b->any_lod ? k_trace_tiles<false, true> : k_trace_tiles<false, false>;
-        else
-            kern = b->any_lod ? k_trace_persistent<false, true> : k_trace_persistent<false, false>;
-    }
+    BatchKernel kern = batch_kernel(b->all_tab, b->any_lod, c.refill_idle != 0, cache);
     int resident = 0;
     SVO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, kern, c.block_threads, smem));
     int per_sm = std::max(1, std::min(c.blocks_per_sm, resident));
@@ -483,11 +575,13 @@ bool cache_lookup(const std::string &key, svo_trace_config *c) {
         if (s.find(tag) == std::string::npos) continue;
         svo_trace_config t;
         const char *q = strstr(line, "\"block_threads\":");
+        t.cache_entries = 0;
+        const char *ce = strstr(line, "\"cache_entries\":");
         if (q && sscanf(q, "\"block_threads\": %d, \"blocks_per_sm\": %d, \"refill_idle\": %d, \"steps_per_round\": %d, "
                            "\"tile_w\": %d, \"chunk\": %d",
                         &t.block_threads, &t.blocks_per_sm, &t.refill_idle, &t.steps_per_round, &t.tile_w,
                         &t.chunk) == 6 &&
-            config_ok(t)) {
+            (!ce || sscanf(ce, "\"cache_entries\": %d", &t.cache_entries) == 1) && config_ok(t)) {
             *c = t;
             found = true;  // the last matching line wins
         }
@@ -508,8 +602,9 @@ void cache_store(const std::string &key, const svo_trace_config &c, float ms) {
     if (!fp) return;
     fprintf(fp,
             "{\"key\": \"%s\", \"block_threads\": %d, \"blocks_per_sm\": %d, \"refill_idle\": %d, \"steps_per_round\": "
-            "%d, \"tile_w\": %d, \"chunk\": %d, \"ms\": %.4f}\n",
-            key.c_str(), c.block_threads, c.blocks_per_sm, c.refill_idle, c.steps_per_round, c.tile_w, c.chunk, ms);
+            "%d, \"tile_w\": %d, \"chunk\": %d, \"cache_entries\": %d, \"ms\": %.4f}\n",
+            key.c_str(), c.block_threads, c.blocks_per_sm, c.refill_idle, c.steps_per_round, c.tile_w, c.chunk,
+            c.cache_entries, ms);
     fclose(fp);
 }
 
@@ -530,6 +625,7 @@ int svo_batch_default_config(svo_trace_config *cfg) {
     cfg->steps_per_round = 8;
     cfg->tile_w = 8;
     cfg->chunk = 64;
+    cfg->cache_entries = 0;
     return SVO_OK;
 }
 
@@ -562,6 +658,8 @@ int svo_batch_create(const svo_view *views, int n_views, svo_batch **out) {
         b->all_tab = true;
         for (const auto &v : b->views)
             if (!octree_table(v.octree, nullptr)) b->all_tab = false;
+        int rc = allow_large_smem();
+        if (rc) return rc;
         return prepare_jobs(b.get(), 8);
     };
     int rc = setup();
@@ -637,7 +735,7 @@ int svo_batch_autotune(svo_batch *b, svo_trace_config *best, float *best_ms, svo
         return prepare_jobs(b, best->tile_w);
     }
     std::vector<svo_trace_config> cands;
-    auto add = [&](int bt, int refill, int steps, int tw, int chunk) {
+    auto add = [&](int bt, int refill, int steps, int tw, int chunk, int cache) {
         svo_trace_config c;
         c.block_threads = bt;
         c.blocks_per_sm = 2048 / bt;
@@ -645,15 +743,19 @@ int svo_batch_autotune(svo_batch *b, svo_trace_config *best, float *best_ms, svo
         c.steps_per_round = steps;
         c.tile_w = tw;
         c.chunk = chunk;
-        cands.push_back(c);
+        c.cache_entries = b->all_tab ? cache : 0;
+        if (cache == 0 || b->all_tab) cands.push_back(c);
     };
-    for (int bt : {128, 256, 512})
-        for (int tw : {4, 8, 16})
-            for (int chunk : {32, 128}) add(bt, 0, 1, tw, chunk);  // whole-warp tiles, no refill
+    // table cache depths: none; 64 entries (levels 0-1 hold at most 9 nodes,
+    // level 2 at most 64 more); 256 entries (levels 0-2 hold at most 73)
+    for (int cache : {0, 64, 256})
+        for (int bt : {128, 256, 512})
+            for (int tw : {4, 8, 16})
+                for (int chunk : {32, 128}) add(bt, 0, 1, tw, chunk, cache);  // whole-warp tiles, no refill
     for (int bt : {128, 256})
         for (int refill : {8, 16, 32})
             for (int steps : {16, 64})
-                for (int tw : {4, 8}) add(bt, refill, steps, tw, 64);
+                for (int tw : {4, 8}) add(bt, refill, steps, tw, 64, 0);
     cudaEvent_t e0, e1;
     SVO_CUDA_TRY(cudaEventCreate(&e0));
     SVO_CUDA_TRY(cudaEventCreate(&e1));

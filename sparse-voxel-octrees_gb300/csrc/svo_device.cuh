@@ -369,12 +369,13 @@ __device__ __forceinline__ bool ray_step(RayStateT<Idx> &s, RayStack &stk, const
 // reloads the node's entry: local-memory stores are written through to L2,
 // and halving them was worth 9% on the config-1 step.  The geometry, the
 // visiting order and every result are those of ray_step.
-// kStage > 0: the first kStage table entries (the top levels, stored first)
-// are also in shared memory at stab, and PUSHes into them read it there.
-template <bool kLod, int kStage = 0>
+// kStaged: the first stage_n table entries (the top levels, stored first)
+// are also in shared memory at stab, and PUSHes and POPs into them read them
+// there (the same values as the global table).
+template <bool kLod, bool kStaged = false>
 __device__ __forceinline__ bool ray_step_tab(RayState &s, TabStack &stk, const uint32_t *__restrict__ words,
                                              const uint4 *__restrict__ tab, float rayScale, RayResult &res,
-                                             const uint4 *stab = nullptr) {
+                                             const uint4 *stab = nullptr, uint32_t stage_n = 0) {
     float cornerTX = s.posX * s.dTx - s.bTx;
     float cornerTY = s.posY * s.dTy - s.bTy;
     float cornerTZ = s.posZ * s.dTz - s.bTz;
@@ -407,7 +408,7 @@ __device__ __forceinline__ bool ray_step_tab(RayState &s, TabStack &stk, const u
             stk.e[s.scale] = make_uint2(s.self, __float_as_uint(s.maxT));
             const uint32_t k = s.parent + __popc(childMasks & 127u);
             uint4 c;
-            if (kStage > 0 && k < (uint32_t)kStage)
+            if (kStaged && k < stage_n)
                 c = stab[k];
             else
                 c = __ldg(tab + k);
@@ -449,7 +450,11 @@ __device__ __forceinline__ bool ray_step_tab(RayState &s, TabStack &stk, const u
         const uint2 e = stk.e[s.scale];
         s.self = e.x;
         s.maxT = __uint_as_float(e.y);
-        const uint4 c = __ldg(tab + s.self);
+        uint4 c;
+        if (kStaged && s.self < stage_n)
+            c = stab[s.self];
+        else
+            c = __ldg(tab + s.self);
         s.current = c.x;
         s.parent = c.y;
         s.lbase = c.z;

@@ -100,7 +100,13 @@ def test_batch_default(cuda, svo, scene):
 @pytest.mark.parametrize("cfg", [dict(refill_idle=0), dict(refill_idle=0, chunk=96, tile_w=4),
                                  dict(tile_w=4), dict(tile_w=16), dict(tile_w=32), dict(refill_idle=1),
                                  dict(refill_idle=32, steps_per_round=1), dict(block_threads=128, chunk=32),
-                                 dict(steps_per_round=64, chunk=256)])
+                                 dict(steps_per_round=64, chunk=256),
+                                 # per-warp table caches: above and below the trees' table sizes, 16 to 64 KB
+                                 # of shared memory per CTA (above 48 KB needs the opt-in)
+                                 dict(refill_idle=0, cache_entries=64),
+                                 dict(refill_idle=0, cache_entries=512, block_threads=128, tile_w=4, chunk=128),
+                                 dict(refill_idle=0, cache_entries=32, block_threads=1024, chunk=32),
+                                 dict(refill_idle=0, cache_entries=256, block_threads=512, tile_w=16)])
 def test_batch_launch_shapes(cuda, svo, scene, cfg):
     torch = cuda
     views, refs = scene
@@ -119,6 +125,28 @@ def test_batch_graph_replay(cuda, svo, scene):
         _clear(torch, views)
         b.launch_graph(torch.cuda.current_stream())
         _check(torch, views, refs)
+
+
+def test_batch_graph_replay_cached(cuda, svo, scene):
+    torch = cuda
+    views, refs = scene
+    b = svo.Batch(views)
+    b.capture_graph(svo.default_config(refill_idle=0, cache_entries=128, tile_w=4))
+    for _ in range(2):
+        _clear(torch, views)
+        b.launch_graph(torch.cuda.current_stream())
+        _check(torch, views, refs)
+
+
+@pytest.mark.parametrize("cfg", [dict(refill_idle=16, cache_entries=64),  # the cache needs the tile schedule
+                                 dict(refill_idle=0, cache_entries=48),   # not a multiple of 32
+                                 dict(refill_idle=0, cache_entries=544),  # above 512
+                                 dict(refill_idle=0, cache_entries=512, block_threads=512)])  # 128 KB per CTA
+def test_batch_rejects_bad_cache(cuda, svo, scene, cfg):
+    views, _ = scene
+    b = svo.Batch(views)
+    with pytest.raises(svo.SvoError):
+        b.trace(svo.default_config(**cfg))
 
 
 def test_batch_autotune(cuda, svo, scene, tmp_path, monkeypatch):
