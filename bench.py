@@ -572,9 +572,18 @@ def run_config3(args, torch, svo, scenes, tune_cache=None):
     for ce in (0, 64, 256):
         if (base["block_threads"] // 32) * ce * 16 > 65536:
             continue
-        c = svo.default_config(**dict(base, cache_entries=ce))
+        c = svo.default_config(**dict(base, cache_entries=ce, reg_cap=0))
         ms = timed(lambda: batch.trace(c, stream))
         cache_sweep[str(ce)] = {"ms": round(ms, 3), "exact_hit_parity": bool(same())}
+    # the chosen lane-refill shape (or the default one) with each register budget
+    rbase = cfg.as_dict()
+    if rbase["refill_idle"] == 0:
+        rbase = svo.default_config().as_dict()
+    reg_sweep = {}
+    for cap in (0, 48):
+        c = svo.default_config(**dict(rbase, reg_cap=cap))
+        ms = timed(lambda: batch.trace(c, stream))
+        reg_sweep[str(cap)] = {"ms": round(ms, 3), "exact_hit_parity": bool(same())}
     depth_hi = min(11, args.max_side.bit_length() - 1) if args.max_side else 11
     return {"workload": "%d octrees (depth 7-%d, sphere/terrain generators, seeds 1..%d), one view each, "
                         "256x256..1920x1080 log-uniform pixels" % (len(views), depth_hi, len(views)),
@@ -583,8 +592,10 @@ def run_config3(args, torch, svo, scenes, tune_cache=None):
             "plain_mrays_s": round(total_rays / ms_plain / 1e3, 1),
             "batched_mrays_s": round(total_rays / ms_batched / 1e3, 1),
             "speedup": round(ms_plain / ms_batched, 3), "exact_hit_parity": bool(exact),
-            "table_cache_sweep": {"shape": {k: v for k, v in base.items() if k != "cache_entries"},
+            "table_cache_sweep": {"shape": {k: v for k, v in base.items() if k not in ("cache_entries", "reg_cap")},
                                   "ms_by_cache_entries": cache_sweep},
+            "register_budget_sweep": {"shape": {k: v for k, v in rbase.items() if k != "reg_cap"},
+                                      "ms_by_reg_cap": reg_sweep},
             "config": cfg.as_dict(), "autotune_s": round(tune_s, 1), "setup_s": round(setup_s, 1),
             "launches": {"plain": len(views), "batched": 1}}
 

@@ -386,7 +386,9 @@ typedef struct svo_trace_config {
     int chunk;           /* ray slots a warp takes from the work queue at once (multiple of 32) */
     int cache_entries;   /* descriptor-table entries (the top levels) of its current octree each warp
                             keeps in shared memory: 0 = none, else a multiple of 32 up to 512, at most
-                            64 KB per CTA; used when every view's octree has a table */
+                            64 KB per CTA; plain-tile schedule (refill_idle 0) over tables only */
+    int reg_cap;         /* lane-refill kernel build: 0 = default (64 registers per thread, 4 CTAs of 256
+                            per SM), 48 = at most 48 registers (5 CTAs, a few spilled values) */
 } svo_trace_config;
 
 typedef struct svo_batch svo_batch;
@@ -405,7 +407,8 @@ int svo_batch_trace(svo_batch *b, const svo_trace_config *cfg, svo_stream stream
 int svo_batch_capture_graph(svo_batch *b, const svo_trace_config *cfg);
 int svo_batch_launch_graph(svo_batch *b, svo_stream stream);
 /* Times candidate launch shapes (block size, refill threshold, steps per
- * round, tile width, rays per queue access, table cache depth) on this batch and returns the fastest; results are
+ * round, tile width, rays per queue access, table cache depth, register
+ * budget) on this batch and returns the fastest; results are
  * cached per device and workload in a JSON-lines file ($SVO_AUTOTUNE_CACHE,
  * default ~/.cache/svo_gb300_autotune.jsonl; SVO_AUTOTUNE_FORCE=1 re-times).
  * *best_ms is -1 when the cache answered.  Synchronises `stream`. */

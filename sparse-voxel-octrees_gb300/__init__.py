@@ -59,7 +59,7 @@ class View(ctypes.Structure):
 class TraceConfig(ctypes.Structure):
     _fields_ = [("block_threads", ctypes.c_int), ("blocks_per_sm", ctypes.c_int), ("refill_idle", ctypes.c_int),
                 ("steps_per_round", ctypes.c_int), ("tile_w", ctypes.c_int), ("chunk", ctypes.c_int),
-                ("cache_entries", ctypes.c_int)]
+                ("cache_entries", ctypes.c_int), ("reg_cap", ctypes.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -235,8 +235,7 @@ __global__ void __maxnreg__(48) k_trace_tiles_cached(BatchArgs a) {
 }
 
 template <bool kTab, bool kLod>
-__global__ void k_trace_persistent(BatchArgs a) {
-    extern __shared__ __align__(16) unsigned char s_dyn[];
+__device__ __forceinline__ void trace_refill(const BatchArgs &a, unsigned char *s_dyn) {
     uint64_t *s_begin = reinterpret_cast<uint64_t *>(s_dyn);
     const bool staged = a.n_jobs + 1 <= kMaxSmemJobs;
     if (staged)
@@ -300,6 +299,21 @@ __global__ void k_trace_persistent(BatchArgs a) {
             }
         }
     }
+}
+
+template <bool kTab, bool kLod>
+__global__ void k_trace_persistent(BatchArgs a) {
+    extern __shared__ __align__(16) unsigned char s_dyn[];
+    trace_refill<kTab, kLod>(a, s_dyn);
+}
+
+// The same kernel built with at most 48 registers per thread (reg_cap 48):
+// 5 resident CTAs of 256 threads per SM instead of 4, for a few spilled
+// registers.
+template <bool kTab, bool kLod>
+__global__ void __maxnreg__(48) k_trace_persistent_r48(BatchArgs a) {
+    extern __shared__ __align__(16) unsigned char s_dyn[];
+    trace_refill<kTab, kLod>(a, s_dyn);
 }
 
 // Table entries (the top levels) each CTA of the image kernel copies into
@@ -367,7 +381,7 @@ bool config_ok(const svo_trace_config &c) {
            c.steps_per_round <= 4096 && (c.tile_w == 4 || c.tile_w == 8 || c.tile_w == 16 || c.tile_w == 32) &&
            c.chunk >= 32 && c.chunk <= 8192 && c.chunk % 32 == 0 && c.cache_entries >= 0 &&
            c.cache_entries <= kMaxCacheEntries && c.cache_entries % 32 == 0 &&
-           (c.cache_entries == 0 || c.refill_idle == 0) &&
+           (c.cache_entries == 0 || c.refill_idle == 0) && (c.reg_cap == 0 || c.reg_cap == 48) &&
            (c.block_threads / 32) * c.cache_entries * (int)sizeof(uint4) <= kMaxCacheBytes;
 }
 
@@ -479,9 +493,14 @@ int prepare_jobs(svo_batch *b, int tile_w) {
 
 using BatchKernel = void (*)(BatchArgs);
 
-// The kernel for a launch shape: plain tiles or lane refill, table or word
-// traversal, level-of-detail exit, per-warp table cache (table only).
-BatchKernel batch_kernel(bool tab, bool lod, bool refill, bool cache) {
+// The kernel for a launch shape: plain tiles or lane refill (default or
+// 48-register build), table or word traversal, level-of-detail exit,
+// per-warp table cache (tiles over tables only).
+BatchKernel batch_kernel(bool tab, bool lod, bool refill, bool cache, bool r48 = false) {
+    if (refill && r48) {
+        if (tab) return lod ? k_trace_persistent_r48<true, true> : k_trace_persistent_r48<true, false>;
+        return lod ? k_trace_persistent_r48<false, true> : k_trace_persistent_r48<false, false>;
+    }
     if (refill) {
         if (tab) return lod ? k_trace_persistent<true, true> : k_trace_persistent<true, false>;
         return lod ? k_trace_persistent<false, true> : k_trace_persistent<false, false>;
@@ -501,8 +520,9 @@ int allow_large_smem() {
         for (int lod = 0; lod < 2; ++lod)
             for (int refill = 0; refill < 2; ++refill)
                 for (int cache = 0; cache <= (tab && !refill); ++cache)
-                    SVO_CUDA_TRY(cudaFuncSetAttribute(batch_kernel(tab, lod, refill, cache),
-                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+                    for (int r48 = 0; r48 <= refill; ++r48)
+                        SVO_CUDA_TRY(cudaFuncSetAttribute(batch_kernel(tab, lod, refill, cache, r48),
+                                                          cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
     return SVO_OK;
 }
 
@@ -526,7 +546,7 @@ int enqueue_trace(svo_batch *b, const svo_trace_config &c, cudaStream_t st) {
     if (cache) smem = a.cache_offset + (size_t)(c.block_threads / 32) * c.cache_entries * sizeof(uint4);
     // A persistent grid larger than what is resident only adds CTAs that
     // start after the queue is drained: clamp to the occupancy limit.
-    BatchKernel kern = batch_kernel(b->all_tab, b->any_lod, c.refill_idle != 0, cache);
+    BatchKernel kern = batch_kernel(b->all_tab, b->any_lod, c.refill_idle != 0, cache, c.reg_cap == 48);
     int resident = 0;
     SVO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, kern, c.block_threads, smem));
     int per_sm = std::max(1, std::min(c.blocks_per_sm, resident));
@@ -576,12 +596,15 @@ bool cache_lookup(const std::string &key, svo_trace_config *c) {
         svo_trace_config t;
         const char *q = strstr(line, "\"block_threads\":");
         t.cache_entries = 0;
+        t.reg_cap = 0;
         const char *ce = strstr(line, "\"cache_entries\":");
+        const char *rc = strstr(line, "\"reg_cap\":");
         if (q && sscanf(q, "\"block_threads\": %d, \"blocks_per_sm\": %d, \"refill_idle\": %d, \"steps_per_round\": %d, "
                            "\"tile_w\": %d, \"chunk\": %d",
                         &t.block_threads, &t.blocks_per_sm, &t.refill_idle, &t.steps_per_round, &t.tile_w,
                         &t.chunk) == 6 &&
-            (!ce || sscanf(ce, "\"cache_entries\": %d", &t.cache_entries) == 1) && config_ok(t)) {
+            (!ce || sscanf(ce, "\"cache_entries\": %d", &t.cache_entries) == 1) &&
+            (!rc || sscanf(rc, "\"reg_cap\": %d", &t.reg_cap) == 1) && config_ok(t)) {
             *c = t;
             found = true;  // the last matching line wins
         }
@@ -602,9 +625,9 @@ void cache_store(const std::string &key, const svo_trace_config &c, float ms) {
     if (!fp) return;
     fprintf(fp,
             "{\"key\": \"%s\", \"block_threads\": %d, \"blocks_per_sm\": %d, \"refill_idle\": %d, \"steps_per_round\": "
-            "%d, \"tile_w\": %d, \"chunk\": %d, \"cache_entries\": %d, \"ms\": %.4f}\n",
+            "%d, \"tile_w\": %d, \"chunk\": %d, \"cache_entries\": %d, \"reg_cap\": %d, \"ms\": %.4f}\n",
             key.c_str(), c.block_threads, c.blocks_per_sm, c.refill_idle, c.steps_per_round, c.tile_w, c.chunk,
-            c.cache_entries, ms);
+            c.cache_entries, c.reg_cap, ms);
     fclose(fp);
 }
 
@@ -626,6 +649,7 @@ int svo_batch_default_config(svo_trace_config *cfg) {
     cfg->tile_w = 8;
     cfg->chunk = 64;
     cfg->cache_entries = 0;
+    cfg->reg_cap = 0;
     return SVO_OK;
 }
 
@@ -735,7 +759,7 @@ int svo_batch_autotune(svo_batch *b, svo_trace_config *best, float *best_ms, svo
         return prepare_jobs(b, best->tile_w);
     }
     std::vector<svo_trace_config> cands;
-    auto add = [&](int bt, int refill, int steps, int tw, int chunk, int cache) {
+    auto add = [&](int bt, int refill, int steps, int tw, int chunk, int cache, int cap = 0) {
         svo_trace_config c;
         c.block_threads = bt;
         c.blocks_per_sm = 2048 / bt;
@@ -744,6 +768,7 @@ int svo_batch_autotune(svo_batch *b, svo_trace_config *best, float *best_ms, svo
         c.tile_w = tw;
         c.chunk = chunk;
         c.cache_entries = b->all_tab ? cache : 0;
+        c.reg_cap = cap;
         if (cache == 0 || b->all_tab) cands.push_back(c);
     };
     // table cache depths: none; 64 entries (levels 0-1 hold at most 9 nodes,
@@ -752,10 +777,12 @@ int svo_batch_autotune(svo_batch *b, svo_trace_config *best, float *best_ms, svo
         for (int bt : {128, 256, 512})
             for (int tw : {4, 8, 16})
                 for (int chunk : {32, 128}) add(bt, 0, 1, tw, chunk, cache);  // whole-warp tiles, no refill
-    for (int bt : {128, 256})
-        for (int refill : {8, 16, 32})
-            for (int steps : {16, 64})
-                for (int tw : {4, 8}) add(bt, refill, steps, tw, 64, 0);
+    // lane refill, default build (64 registers) or 48-register build
+    for (int cap : {0, 48})
+        for (int bt : {128, 256})
+            for (int refill : {8, 16, 32})
+                for (int steps : {16, 64})
+                    for (int tw : {4, 8}) add(bt, refill, steps, tw, 64, 0, cap);
     cudaEvent_t e0, e1;
     SVO_CUDA_TRY(cudaEventCreate(&e0));
     SVO_CUDA_TRY(cudaEventCreate(&e1));

@@ -51,6 +51,28 @@ struct GridGeom {
     uint8_t *topflag;   // per M-block "has any voxel" (Morton-indexed), or null
 };
 
+// A 16^3 brick wholly inside the grid, whose rows start on 16-byte
+// boundaries, is read as 1024 uint4 (4 per thread of a 256-thread CTA).
+// uint4 q of the brick covers x = 4*(q & 3) .. +3, y = (q >> 2) & 15,
+// z = q >> 6, i.e. cells 4q .. 4q+3 of the brick's row-major order.
+__device__ __forceinline__ bool brick_vec4(const GridGeom &g, int gx0, int gy0, int gz0) {
+    return g.log_brick == 4 && kBrickThreads == 256 && gx0 + 16 <= g.w && gy0 + 16 <= g.h && gz0 + 16 <= g.d &&
+           (g.w & 3) == 0 && (reinterpret_cast<uintptr_t>(g.grid) & 15) == 0;
+}
+
+// Loads the brick's 4 uint4 of this thread, all issued before any is used:
+// a scan of the whole grid is bound by the loads in flight, not by the
+// instructions that test them.
+__device__ __forceinline__ void brick_load4(const GridGeom &g, int gx0, int gy0, int gz0, uint4 (&v)[4]) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int q = threadIdx.x + k * 256;
+        const int gx = gx0 + ((q & 3) << 2), gy = gy0 + ((q >> 2) & 15), gz = gz0 + (q >> 6);
+        v[k] = __ldg(reinterpret_cast<const uint4 *>(g.grid + (uint64_t)gx +
+                                                     (uint64_t)g.w * ((uint64_t)gy + (uint64_t)g.h * gz)));
+    }
+}
+
 // Phase 1a: per brick, count voxels that survive (V') and flag M-blocks that
 // hold any voxel (V).  One CTA per brick; consecutive threads read
 // consecutive x so each warp load covers whole 32-byte sectors of a row.
@@ -62,7 +84,26 @@ __global__ void __launch_bounds__(kBrickThreads) k_brick_count(GridGeom g, uint6
         uint32_t bx = compact3(b), by = compact3(b >> 1), bz = compact3(b >> 2);
         int gx0 = (int)(bx << lb), gy0 = (int)(by << lb), gz0 = (int)(bz << lb);
         uint32_t cnt = 0, any = 0;
-        if (gx0 < g.w && gy0 < g.h && gz0 < g.d) {
+        if (brick_vec4(g, gx0, gy0, gz0)) {
+            uint4 v[4];
+            brick_load4(g, gx0, gy0, gz0, v);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int q = threadIdx.x + k * 256;
+                const int gx = gx0 + ((q & 3) << 2), gy = gy0 + ((q >> 2) & 15), gz = gz0 + (q >> 6);
+                const uint32_t e[4] = {v[k].x, v[k].y, v[k].z, v[k].w};
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    if (e[j]) {
+                        any = 1;
+                        if (!(g.drop_last_z && gz == g.d - 1)) ++cnt;
+                        if (g.topflag && g.log_block < lb)
+                            g.topflag[morton3((uint32_t)(gx + j) >> g.log_block, (uint32_t)gy >> g.log_block,
+                                              (uint32_t)gz >> g.log_block)] = 1;
+                    }
+                }
+            }
+        } else if (gx0 < g.w && gy0 < g.h && gz0 < g.d) {
             for (int c = threadIdx.x; c < cells; c += kBrickThreads) {
                 int gx = gx0 + (c & (E - 1)), gy = gy0 + ((c >> lb) & (E - 1)), gz = gz0 + (c >> (2 * lb));
                 if (gx < g.w && gy < g.h && gz < g.d) {
@@ -94,7 +135,7 @@ __global__ void __launch_bounds__(kBrickThreads) k_brick_count(GridGeom g, uint6
 __global__ void __launch_bounds__(kBrickThreads) k_brick_emit(GridGeom g, uint64_t n_bricks, const uint32_t *__restrict__ counts,
                                                             const uint64_t *__restrict__ offsets,
                                                             uint64_t *__restrict__ keys, uint32_t *__restrict__ payload) {
-    __shared__ uint32_t tile[16 * 16 * 16];
+    __shared__ __align__(16) uint32_t tile[16 * 16 * 16];
     const int E = 1 << g.log_brick;
     const int cells = E * E * E;
     const int per = (cells + kBrickThreads - 1) / kBrickThreads;
@@ -102,12 +143,24 @@ __global__ void __launch_bounds__(kBrickThreads) k_brick_emit(GridGeom g, uint64
         if (counts[b] == 0) continue;  // uniform across the CTA
         uint32_t bx = compact3(b), by = compact3(b >> 1), bz = compact3(b >> 2);
         int gx0 = (int)(bx << g.log_brick), gy0 = (int)(by << g.log_brick), gz0 = (int)(bz << g.log_brick);
-        for (int c = threadIdx.x; c < cells; c += kBrickThreads) {
-            int gx = gx0 + (c & (E - 1)), gy = gy0 + ((c >> g.log_brick) & (E - 1)), gz = gz0 + (c >> (2 * g.log_brick));
-            uint32_t v = 0;
-            if (gx < g.w && gy < g.h && gz < g.d && !(g.drop_last_z && gz == g.d - 1))
-                v = __ldg(g.grid + (uint64_t)gx + (uint64_t)g.w * ((uint64_t)gy + (uint64_t)g.h * gz));
-            tile[c] = v;
+        if (brick_vec4(g, gx0, gy0, gz0)) {
+            uint4 v[4];
+            brick_load4(g, gx0, gy0, gz0, v);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int q = threadIdx.x + k * 256;
+                if (g.drop_last_z && gz0 + (q >> 6) == g.d - 1) v[k] = make_uint4(0u, 0u, 0u, 0u);
+                reinterpret_cast<uint4 *>(tile)[q] = v[k];  // cells 4q .. 4q+3
+            }
+        } else {
+            for (int c = threadIdx.x; c < cells; c += kBrickThreads) {
+                int gx = gx0 + (c & (E - 1)), gy = gy0 + ((c >> g.log_brick) & (E - 1)),
+                    gz = gz0 + (c >> (2 * g.log_brick));
+                uint32_t v = 0;
+                if (gx < g.w && gy < g.h && gz < g.d && !(g.drop_last_z && gz == g.d - 1))
+                    v = __ldg(g.grid + (uint64_t)gx + (uint64_t)g.w * ((uint64_t)gy + (uint64_t)g.h * gz));
+                tile[c] = v;
+            }
         }
         __syncthreads();
         uint32_t cnt = 0;

@@ -106,7 +106,10 @@ def test_batch_default(cuda, svo, scene):
                                  dict(refill_idle=0, cache_entries=64),
                                  dict(refill_idle=0, cache_entries=512, block_threads=128, tile_w=4, chunk=128),
                                  dict(refill_idle=0, cache_entries=32, block_threads=1024, chunk=32),
-                                 dict(refill_idle=0, cache_entries=256, block_threads=512, tile_w=16)])
+                                 dict(refill_idle=0, cache_entries=256, block_threads=512, tile_w=16),
+                                 # the 48-register build of the lane-refill kernel
+                                 dict(reg_cap=48), dict(reg_cap=48, refill_idle=1, block_threads=128),
+                                 dict(reg_cap=48, refill_idle=32, steps_per_round=64, tile_w=4)])
 def test_batch_launch_shapes(cuda, svo, scene, cfg):
     torch = cuda
     views, refs = scene
@@ -141,8 +144,9 @@ def test_batch_graph_replay_cached(cuda, svo, scene):
 @pytest.mark.parametrize("cfg", [dict(refill_idle=16, cache_entries=64),  # the cache needs the tile schedule
                                  dict(refill_idle=0, cache_entries=48),   # not a multiple of 32
                                  dict(refill_idle=0, cache_entries=544),  # above 512
-                                 dict(refill_idle=0, cache_entries=512, block_threads=512)])  # 128 KB per CTA
-def test_batch_rejects_bad_cache(cuda, svo, scene, cfg):
+                                 dict(refill_idle=0, cache_entries=512, block_threads=512),  # 128 KB per CTA
+                                 dict(reg_cap=32)])                                          # no such build
+def test_batch_rejects_bad_config(cuda, svo, scene, cfg):
     views, _ = scene
     b = svo.Batch(views)
     with pytest.raises(svo.SvoError):

@@ -161,3 +161,24 @@ def test_streamed_terrain_scene(svo, oracle, scenes, tmp_path):
     ow, oc = oracle.build_dense(grid, 1 << 20)
     ws, c = _streamed(svo, path, 1 << 20, 64, 256 * 256)
     assert np.array_equal(ws, ow) and np.array_equal(c, oc)
+
+
+def test_grid_alignment_paths(cuda, svo, oracle, scenes):
+    """Bricks wholly inside a grid whose rows start on 16-byte boundaries are
+    read as uint4; the same grid at a 4-byte offset, or with a width that is
+    not a multiple of 4, is read word by word.  Both give the oracle's words,
+    with cache blocks larger and smaller than a brick (the budget 3000 gives
+    8^3 blocks, whose flags the count kernel sets voxel by voxel)."""
+    torch = cuda
+    for shape in ((48, 40, 64), (33, 50, 36), (32, 32, 30)):
+        g = scenes.random_grid(shape, 0.3, 11)
+        n = g.size
+        flat = torch.from_numpy(g.reshape(-1).view(np.int32)).cuda()
+        buf = torch.zeros(n + 8, dtype=torch.int32, device="cuda")
+        for mem in (1 << 30, 3000):
+            ow, oc = oracle.build_dense(g, mem)
+            for off in (0, 1, 4):  # 16-byte aligned, 4-byte aligned, 16-byte aligned
+                buf[off:off + n] = flat
+                tree = svo.VoxelOctree(svo.VoxelData(buf[off:off + n].view(shape), mem))
+                assert np.array_equal(tree.words(), ow), (shape, mem, off)
+                assert np.array_equal(tree.center(), oc)
