@@ -130,12 +130,16 @@ __global__ void __launch_bounds__(kBrickThreads) k_brick_count(GridGeom g, uint6
 }
 
 // Phase 1b: emit (key, payload) for V' in Morton order.  The brick is staged
-// in shared memory with coalesced row reads, then each thread walks a run of
-// consecutive local Morton codes.
+// in shared memory with coalesced row reads; each thread counts a run of
+// consecutive local Morton codes, a block scan places the runs, the occupied
+// codes are compacted into shared memory in Morton order, and the CTA writes
+// the brick's keys and payloads with consecutive threads on consecutive
+// elements.
 __global__ void __launch_bounds__(kBrickThreads) k_brick_emit(GridGeom g, uint64_t n_bricks, const uint32_t *__restrict__ counts,
                                                             const uint64_t *__restrict__ offsets,
                                                             uint64_t *__restrict__ keys, uint32_t *__restrict__ payload) {
     __shared__ __align__(16) uint32_t tile[16 * 16 * 16];
+    __shared__ uint16_t order[16 * 16 * 16];  // the brick's occupied local Morton codes, ascending
     const int E = 1 << g.log_brick;
     const int cells = E * E * E;
     const int per = (cells + kBrickThreads - 1) / kBrickThreads;
@@ -173,20 +177,22 @@ __global__ void __launch_bounds__(kBrickThreads) k_brick_emit(GridGeom g, uint64
             }
         }
         uint32_t total;
-        uint32_t pre = block_excl_scan<uint32_t>(cnt, &total);
-        uint64_t out = offsets[b] + pre;
-        uint64_t kbase = b << (3 * g.log_brick);
+        uint32_t o = block_excl_scan<uint32_t>(cnt, &total);
         for (int k = 0; k < per; ++k) {
             int m = m0 + k;
             if (m < cells) {
                 uint32_t lx = compact3((uint64_t)m), ly = compact3((uint64_t)m >> 1), lz = compact3((uint64_t)m >> 2);
-                uint32_t v = tile[lx + E * (ly + E * lz)];
-                if (v) {
-                    keys[out] = kbase | (uint64_t)m;
-                    payload[out] = v;
-                    ++out;
-                }
+                if (tile[lx + E * (ly + E * lz)]) order[o++] = (uint16_t)m;
             }
+        }
+        __syncthreads();
+        const uint64_t out0 = offsets[b];
+        const uint64_t kbase = b << (3 * g.log_brick);
+        for (uint32_t i = threadIdx.x; i < total; i += kBrickThreads) {
+            const uint32_t m = order[i];
+            const uint32_t lx = compact3((uint64_t)m), ly = compact3((uint64_t)m >> 1), lz = compact3((uint64_t)m >> 2);
+            keys[out0 + i] = kbase | (uint64_t)m;
+            payload[out0 + i] = tile[lx + E * (ly + E * lz)];
         }
         __syncthreads();
     }

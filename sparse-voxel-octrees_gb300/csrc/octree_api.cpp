@@ -12,6 +12,7 @@
 #include <cstring>
 #include <memory>
 #include <thread>
+#include <vector>
 
 #include "svo_internal.h"
 
@@ -120,8 +121,6 @@ static int ensure_staging(svo_octree *oct, size_t dev_bytes) {
     oct->stage_dev_bytes = 0;
     SVO_CUDA_TRY(cudaMalloc(&oct->stage_dev, dev_bytes));
     oct->stage_dev_bytes = dev_bytes;
-    for (auto &s : oct->stage_streams)
-        if (!s) SVO_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     return SVO_OK;
 }
 
@@ -134,6 +133,86 @@ static int check_device_status(const svo_octree *oct) {
                                          "(corrupt octree?)");
     }
     return SVO_OK;
+}
+
+// Chunk plan (in units of rays or rows) for the host pipelines: chunks of
+// `target` rounded down to a multiple of `align`, the remainder last.  Both
+// directions of the host link are busy in the steady state, so the copies,
+// not the traces, bound a call; shorter chunks at the ends (to shorten the
+// unoverlapped first copy-in and last copy-out) measured slower on GB300.
+// Results do not depend on the plan: every ray is traced on its own.
+static std::vector<uint64_t> plan_chunks(uint64_t total, uint64_t target, uint64_t align) {
+    const uint64_t t = std::max(align, target / align * align);
+    std::vector<uint64_t> plan;
+    for (uint64_t s = 0; s < total; s += t) plan.push_back(std::min(t, total - s));
+    return plan;
+}
+
+// The host-buffer pipeline of svo_trace_host and svo_trace_image_host.  Chunk
+// k's rays go in on a copy-in stream, are traced on trace stream k % 2 (the
+// two have separate work counters, so one chunk's persistent launch fills the
+// tail of the previous one) and come out on a copy-out stream.  Trace stream
+// h owns half h of the staging arena; the half's rays are overwritten only
+// after its previous trace, and its results only after their copy-out.
+// launch(d_rays, rays, outputs, stream, half) enqueues one chunk's trace.
+template <typename Launch>
+static int host_pipeline(svo_octree *oct, const float *rays, const std::vector<uint64_t> &plan, uint64_t max_chunk,
+                         const svo_trace_out &out, Launch launch) {
+    const uint64_t C = max_chunk;
+    // Per half: rays 24 B, hit 1, t 4, leaf 4, word 4, rgb 12 (256-byte aligned arrays).
+    auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+    const size_t half = al(C * 24) + al(C) + al(C * 4) * 3 + al(C * 12);
+    int rc = ensure_staging(oct, 2 * half);
+    if (rc) return rc;
+    if (!oct->img_streams[0]) {
+        for (auto &st : oct->img_streams) SVO_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        for (int k = 0; k < 2; ++k) {
+            SVO_CUDA_TRY(cudaEventCreateWithFlags(&oct->img_in[k], cudaEventDisableTiming));
+            SVO_CUDA_TRY(cudaEventCreateWithFlags(&oct->img_traced[k], cudaEventDisableTiming));
+            SVO_CUDA_TRY(cudaEventCreateWithFlags(&oct->img_out[k], cudaEventDisableTiming));
+        }
+    }
+    cudaStream_t si = oct->img_streams[0], so = oct->img_streams[3];
+    cudaStream_t skh[2] = {oct->img_streams[1], oct->img_streams[2]};
+    uint64_t c0 = 0;
+    for (size_t j = 0; j < plan.size(); c0 += plan[j], ++j) {
+        const int h = (int)(j & 1);
+        const uint64_t m = plan[j];
+        cudaStream_t sk = skh[h];
+        uint8_t *base = (uint8_t *)oct->stage_dev + h * half;
+        float *d_rays = (float *)base;
+        uint8_t *d_hit = base + al(C * 24);
+        float *d_t = (float *)(d_hit + al(C));
+        uint32_t *d_leaf = (uint32_t *)((uint8_t *)d_t + al(C * 4));
+        uint32_t *d_word = (uint32_t *)((uint8_t *)d_leaf + al(C * 4));
+        float *d_rgb = (float *)((uint8_t *)d_word + al(C * 4));
+        if (j >= 2) SVO_CUDA_TRY(cudaStreamWaitEvent(si, oct->img_traced[h], 0));
+        SVO_CUDA_TRY(cudaMemcpyAsync(d_rays, rays + 6 * c0, m * 24, cudaMemcpyHostToDevice, si));
+        SVO_CUDA_TRY(cudaEventRecord(oct->img_in[h], si));
+        SVO_CUDA_TRY(cudaStreamWaitEvent(sk, oct->img_in[h], 0));
+        if (j >= 2) SVO_CUDA_TRY(cudaStreamWaitEvent(sk, oct->img_out[h], 0));
+        svo_trace_out o;
+        o.hit = out.hit ? d_hit : nullptr;
+        o.t = out.t ? d_t : nullptr;
+        o.leaf = out.leaf ? d_leaf : nullptr;
+        o.word = out.word ? d_word : nullptr;
+        o.rgb = out.rgb ? d_rgb : nullptr;
+        rc = launch(d_rays, m, o, sk, h);
+        if (rc) return rc;
+        SVO_CUDA_TRY(cudaEventRecord(oct->img_traced[h], sk));
+        SVO_CUDA_TRY(cudaStreamWaitEvent(so, oct->img_traced[h], 0));
+        if (out.hit) SVO_CUDA_TRY(cudaMemcpyAsync(out.hit + c0, d_hit, m, cudaMemcpyDeviceToHost, so));
+        if (out.t) SVO_CUDA_TRY(cudaMemcpyAsync(out.t + c0, d_t, m * 4, cudaMemcpyDeviceToHost, so));
+        if (out.leaf) SVO_CUDA_TRY(cudaMemcpyAsync(out.leaf + c0, d_leaf, m * 4, cudaMemcpyDeviceToHost, so));
+        if (out.word) SVO_CUDA_TRY(cudaMemcpyAsync(out.word + c0, d_word, m * 4, cudaMemcpyDeviceToHost, so));
+        if (out.rgb) SVO_CUDA_TRY(cudaMemcpyAsync(out.rgb + 3 * c0, d_rgb, m * 12, cudaMemcpyDeviceToHost, so));
+        SVO_CUDA_TRY(cudaEventRecord(oct->img_out[h], so));
+    }
+    SVO_CUDA_TRY(cudaStreamSynchronize(si));
+    SVO_CUDA_TRY(cudaStreamSynchronize(skh[0]));
+    SVO_CUDA_TRY(cudaStreamSynchronize(skh[1]));
+    SVO_CUDA_TRY(cudaStreamSynchronize(so));
+    return check_device_status(oct);
 }
 
 }  // namespace svo
@@ -291,8 +370,6 @@ int svo_octree_destroy(svo_octree *oct) {
     if (oct->d_status) cudaFree(oct->d_status);
     if (oct->d_queue) cudaFree(oct->d_queue);
     if (oct->stage_dev) cudaFree(oct->stage_dev);
-    for (auto &s : oct->stage_streams)
-        if (s) cudaStreamDestroy(s);
     for (auto &s : oct->img_streams)
         if (s) cudaStreamDestroy(s);
     for (int k = 0; k < 2; ++k) {
@@ -531,41 +608,14 @@ int svo_trace_host(svo_octree *oct, const float *rays, uint64_t n, float ray_sca
                    const svo_trace_out *out) {
     if (!oct || (!rays && n) || !out) return set_error(SVO_ERR_INVALID, "null argument");
     if (n > 0xFFFFFFFFull) return set_error(SVO_ERR_LIMIT, "more than 2^32-1 rays");
+    if (n == 0) return SVO_OK;
     std::lock_guard<std::mutex> lock(oct->staging_mtx);
-    const uint64_t C = kStageRays;
-    // Per half: rays 24 B, hit 1, t 4, leaf 4, word 4, rgb 12 (padded to 64 B alignment per array).
-    auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
-    const size_t half = al(C * 24) + al(C) + al(C * 4) * 3 + al(C * 12);
-    int rc = ensure_staging(oct, 2 * half);
-    if (rc) return rc;
-    for (uint64_t c0 = 0, j = 0; c0 < n; c0 += C, ++j) {
-        uint64_t m = std::min(C, n - c0);
-        cudaStream_t st = oct->stage_streams[j & 1];
-        uint8_t *base = (uint8_t *)oct->stage_dev + (j & 1) * half;
-        float *d_rays = (float *)base;
-        uint8_t *d_hit = base + al(C * 24);
-        float *d_t = (float *)(d_hit + al(C));
-        uint32_t *d_leaf = (uint32_t *)((uint8_t *)d_t + al(C * 4));
-        uint32_t *d_word = (uint32_t *)((uint8_t *)d_leaf + al(C * 4));
-        float *d_rgb = (float *)((uint8_t *)d_word + al(C * 4));
-        SVO_CUDA_TRY(cudaMemcpyAsync(d_rays, rays + 6 * c0, m * 24, cudaMemcpyHostToDevice, st));
-        svo_trace_out o;
-        o.hit = out->hit ? d_hit : nullptr;
-        o.t = out->t ? d_t : nullptr;
-        o.leaf = out->leaf ? d_leaf : nullptr;
-        o.word = out->word ? d_word : nullptr;
-        o.rgb = out->rgb ? d_rgb : nullptr;
-        rc = launch_trace(oct, d_rays, m, ray_scale, light, o, st);
-        if (rc) return rc;
-        if (out->hit) SVO_CUDA_TRY(cudaMemcpyAsync(out->hit + c0, d_hit, m, cudaMemcpyDeviceToHost, st));
-        if (out->t) SVO_CUDA_TRY(cudaMemcpyAsync(out->t + c0, d_t, m * 4, cudaMemcpyDeviceToHost, st));
-        if (out->leaf) SVO_CUDA_TRY(cudaMemcpyAsync(out->leaf + c0, d_leaf, m * 4, cudaMemcpyDeviceToHost, st));
-        if (out->word) SVO_CUDA_TRY(cudaMemcpyAsync(out->word + c0, d_word, m * 4, cudaMemcpyDeviceToHost, st));
-        if (out->rgb) SVO_CUDA_TRY(cudaMemcpyAsync(out->rgb + 3 * c0, d_rgb, m * 12, cudaMemcpyDeviceToHost, st));
-    }
-    SVO_CUDA_TRY(cudaStreamSynchronize(oct->stage_streams[0]));
-    SVO_CUDA_TRY(cudaStreamSynchronize(oct->stage_streams[1]));
-    return check_device_status(oct);
+    // warp-aligned chunks
+    const std::vector<uint64_t> plan = plan_chunks(n, kStageRays, 32);
+    return host_pipeline(oct, rays, plan, kStageRays, *out,
+                         [&](const float *d_rays, uint64_t m, const svo_trace_out &o, cudaStream_t st, int) {
+                             return launch_trace(oct, d_rays, m, ray_scale, light, o, st);
+                         });
 }
 
 int svo_trace_image_host(svo_octree *oct, const float *rays, uint32_t width, uint32_t height, float ray_scale,
@@ -574,70 +624,17 @@ int svo_trace_image_host(svo_octree *oct, const float *rays, uint32_t width, uin
     if ((uint64_t)width * height > 0xFFFFFFFFull) return set_error(SVO_ERR_LIMIT, "more than 2^32-1 pixels");
     if (width == 0 || height == 0) return SVO_OK;
     std::lock_guard<std::mutex> lock(oct->staging_mtx);
-    // Chunks of whole rows (a multiple of the 4-row tile height), about
-    // kStageRays rays each, alternating between two streams.
-    uint64_t rows = std::max<uint64_t>(4, (kStageRays / width) & ~uint64_t(3));
-    const uint64_t C = rows * width;
-    auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
-    const size_t half = al(C * 24) + al(C) + al(C * 4) * 3 + al(C * 12);
-    int rc = ensure_staging(oct, 2 * half);
-    if (rc) return rc;
-    // Chunks alternate between two trace streams with their own work
-    // counters, so one chunk's launch fills the tail of the previous one,
-    // while the next chunk's rays come in and the previous chunk's results go
-    // out on two copy streams.
-    if (!oct->img_streams[0]) {
-        for (auto &st : oct->img_streams) SVO_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-        for (int k = 0; k < 2; ++k) {
-            SVO_CUDA_TRY(cudaEventCreateWithFlags(&oct->img_in[k], cudaEventDisableTiming));
-            SVO_CUDA_TRY(cudaEventCreateWithFlags(&oct->img_traced[k], cudaEventDisableTiming));
-            SVO_CUDA_TRY(cudaEventCreateWithFlags(&oct->img_out[k], cudaEventDisableTiming));
-        }
-    }
-    cudaStream_t si = oct->img_streams[0], so = oct->img_streams[3];
-    cudaStream_t skh[2] = {oct->img_streams[1], oct->img_streams[2]};
-    uint64_t j = 0;
-    for (uint64_t y0 = 0; y0 < height; y0 += rows, ++j) {
-        const int h = (int)(j & 1);
-        cudaStream_t sk = skh[h];
-        uint64_t nr = std::min<uint64_t>(rows, height - y0);
-        uint64_t m = nr * width, c0 = y0 * width;
-        uint8_t *base = (uint8_t *)oct->stage_dev + h * half;
-        float *d_rays = (float *)base;
-        uint8_t *d_hit = base + al(C * 24);
-        float *d_t = (float *)(d_hit + al(C));
-        uint32_t *d_leaf = (uint32_t *)((uint8_t *)d_t + al(C * 4));
-        uint32_t *d_word = (uint32_t *)((uint8_t *)d_leaf + al(C * 4));
-        float *d_rgb = (float *)((uint8_t *)d_word + al(C * 4));
-        // rays of this half are free once the trace two chunks back is done
-        if (j >= 2) SVO_CUDA_TRY(cudaStreamWaitEvent(si, oct->img_traced[h], 0));
-        SVO_CUDA_TRY(cudaMemcpyAsync(d_rays, rays + 6 * c0, m * 24, cudaMemcpyHostToDevice, si));
-        SVO_CUDA_TRY(cudaEventRecord(oct->img_in[h], si));
-        // outputs of this half are free once their copy two chunks back is done
-        SVO_CUDA_TRY(cudaStreamWaitEvent(sk, oct->img_in[h], 0));
-        if (j >= 2) SVO_CUDA_TRY(cudaStreamWaitEvent(sk, oct->img_out[h], 0));
-        svo_trace_out o;
-        o.hit = out->hit ? d_hit : nullptr;
-        o.t = out->t ? d_t : nullptr;
-        o.leaf = out->leaf ? d_leaf : nullptr;
-        o.word = out->word ? d_word : nullptr;
-        o.rgb = out->rgb ? d_rgb : nullptr;
-        rc = launch_trace_image(oct, d_rays, width, (uint32_t)nr, ray_scale, light, o, sk, 1 + h);
-        if (rc) return rc;
-        SVO_CUDA_TRY(cudaEventRecord(oct->img_traced[h], sk));
-        SVO_CUDA_TRY(cudaStreamWaitEvent(so, oct->img_traced[h], 0));
-        if (out->hit) SVO_CUDA_TRY(cudaMemcpyAsync(out->hit + c0, d_hit, m, cudaMemcpyDeviceToHost, so));
-        if (out->t) SVO_CUDA_TRY(cudaMemcpyAsync(out->t + c0, d_t, m * 4, cudaMemcpyDeviceToHost, so));
-        if (out->leaf) SVO_CUDA_TRY(cudaMemcpyAsync(out->leaf + c0, d_leaf, m * 4, cudaMemcpyDeviceToHost, so));
-        if (out->word) SVO_CUDA_TRY(cudaMemcpyAsync(out->word + c0, d_word, m * 4, cudaMemcpyDeviceToHost, so));
-        if (out->rgb) SVO_CUDA_TRY(cudaMemcpyAsync(out->rgb + 3 * c0, d_rgb, m * 12, cudaMemcpyDeviceToHost, so));
-        SVO_CUDA_TRY(cudaEventRecord(oct->img_out[h], so));
-    }
-    SVO_CUDA_TRY(cudaStreamSynchronize(si));
-    SVO_CUDA_TRY(cudaStreamSynchronize(skh[0]));
-    SVO_CUDA_TRY(cudaStreamSynchronize(skh[1]));
-    SVO_CUDA_TRY(cudaStreamSynchronize(so));
-    return check_device_status(oct);
+    // Chunks of whole rows, a multiple of the 4-row tile height (all but the
+    // last), about kStageRays rays at full size; each chunk is traced as an
+    // image of its own.
+    const uint64_t rows = std::max<uint64_t>(4, (kStageRays / width) & ~uint64_t(3));
+    std::vector<uint64_t> plan = plan_chunks(height, rows, 4);
+    for (auto &c : plan) c *= width;
+    return host_pipeline(oct, rays, plan, rows * width, *out,
+                         [&](const float *d_rays, uint64_t m, const svo_trace_out &o, cudaStream_t st, int half) {
+                             return launch_trace_image(oct, d_rays, width, (uint32_t)(m / width), ray_scale, light,
+                                                       o, st, 1 + half);
+                         });
 }
 
 }  // extern "C"

@@ -34,16 +34,12 @@ struct svo_octree {
     bool use_table = true;
     mutable std::mutex tab_mtx;
 
-    // Staging for svo_trace_host: one device arena and one pinned host arena,
-    // split into two halves that alternate between two streams.
+    // Host-buffer pipeline of svo_trace_host and svo_trace_image_host: one
+    // device staging arena split into two halves, copy-in, trace and copy-out
+    // streams, and per-half events (inputs landed, trace done, outputs copied).
     std::mutex staging_mtx;
     void *stage_dev = nullptr;
     size_t stage_dev_bytes = 0;
-    void *stage_host = nullptr;
-    size_t stage_host_bytes = 0;
-    cudaStream_t stage_streams[2] = {nullptr, nullptr};
-    // svo_trace_image_host pipeline: copy-in, trace and copy-out streams and
-    // per-half events (inputs landed, trace done, outputs copied).
     cudaStream_t img_streams[4] = {nullptr, nullptr, nullptr, nullptr};  // copy in, trace x2, copy out
     cudaEvent_t img_in[2] = {nullptr, nullptr}, img_traced[2] = {nullptr, nullptr}, img_out[2] = {nullptr, nullptr};
 };

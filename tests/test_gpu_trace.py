@@ -172,6 +172,36 @@ def test_trace_image_host_matches_oracle(svo, oracle, scenes):
     _assert_same(host, oracle.raymarch(words, rays, light=(0.0, 1.0, 0.0), threads=8))
 
 
+def test_host_pipelines_long_calls(cuda, svo, oracle, scenes):
+    """Host calls of several staged chunks (full 4 M-ray chunks and a
+    remainder, alternating between the two trace streams and staging halves)
+    give the device-resident entry points' results on the same rays."""
+    torch = cuda
+    grid = scenes.sphere_scene(128, 24, 5)
+    words, center = oracle.build_dense(grid)
+    tree = svo.VoxelOctree.from_words(words, center)
+    cam = scenes.orbit_cameras(1, 9, center)[0]
+    W, H = 1024, 10_611  # 10.9 M rays: image chunks of 4096 rows, linear chunks of 4 M rays
+    rays = scenes.camera_rays(cam, W, H)
+    light = (0.0, 1.0, 0.0)
+    ref = _device_trace(cuda, svo, tree, rays, light=light)
+    _assert_same(tree.trace_host(rays, light=light), ref | {"grey": ref["rgb"][:, 0].copy()})
+    d_rays = torch.from_numpy(rays).cuda()
+    out = {"hit": torch.empty(W * H, dtype=torch.uint8, device="cuda"),
+           "t": torch.empty(W * H, dtype=torch.float32, device="cuda"),
+           "leaf": torch.empty(W * H, dtype=torch.int32, device="cuda"),
+           "word": torch.empty(W * H, dtype=torch.int32, device="cuda"),
+           "rgb": torch.empty((W * H, 3), dtype=torch.float32, device="cuda")}
+    tree.trace_image(d_rays, W, H, light=light, out=out)
+    torch.cuda.synchronize()
+    img = {k: v.cpu().numpy() for k, v in out.items()}
+    img["leaf"] = img["leaf"].view(np.uint32)
+    img["word"] = img["word"].view(np.uint32)
+    _assert_same(img, ref | {"grey": ref["rgb"][:, 0].copy()})
+    _assert_same(tree.trace_image_host(rays, W, H, light=light), ref | {"grey": ref["rgb"][:, 0].copy()})
+    assert tree.device_status() == 0
+
+
 def test_nan_and_infinite_rays(cuda, svo, golden, oracle):
     """Rays with NaN corner distances (NaN components, or an infinite origin
     along an infinite direction) end as misses after one pass, in every
