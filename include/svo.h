@@ -246,20 +246,25 @@ int svo_octree_build_ply(const char *path, int side, int threads, uint64_t mem, 
 /* ------------------------------------------------------------------- trace */
 
 /* Per-ray outputs; any pointer may be NULL to skip that output.
- *   hit:  0 miss, 1 leaf hit, 2 level-of-detail exit (ray_scale > 0,
- *         VoxelOctree.cpp:265-268)
- *   t:    raymarch's t on a hit, +inf on a miss
- *   leaf: index into the word array of the hit leaf's payload word
- *         (VoxelOctree.cpp:282), 0xFFFFFFFF when no leaf was hit
- *   word: the leaf payload (raymarch's `normal` out-parameter), 0 when none
- *   rgb:  3 floats per ray, the viewer's shade() (Main.cpp:81-90) of the leaf
- *         word for the ray direction and `light`; 0 when no leaf was hit */
+ *   hit:   0 miss, 1 leaf hit, 2 level-of-detail exit (ray_scale > 0,
+ *          VoxelOctree.cpp:265-268)
+ *   t:     raymarch's t on a hit, +inf on a miss
+ *   leaf:  index into the word array of the hit leaf's payload word
+ *          (VoxelOctree.cpp:282), 0xFFFFFFFF when no leaf was hit
+ *   word:  the leaf payload (raymarch's `normal` out-parameter), 0 when none
+ *   rgb:   3 floats per ray, the viewer's shade() (Main.cpp:81-90) of the leaf
+ *          word for the ray direction and `light`; 0 when no leaf was hit
+ *   rgba8: the same colour as the viewer stores a traced pixel (renderTile,
+ *          Main.cpp:126-131): c = uint32(min(shade, 1) * 255.0) with the
+ *          product in double, packed c | c << 8 | c << 16 | 0xFF000000;
+ *          0xFF000000 when no leaf was hit */
 typedef struct svo_trace_out {
     uint8_t *hit;
     float *t;
     uint32_t *leaf;
     uint32_t *word;
     float *rgb;
+    uint32_t *rgba8;
 } svo_trace_out;
 
 /* Replaces a loop of VoxelOctree::raymarch(o, d, rayScale, normal, t)

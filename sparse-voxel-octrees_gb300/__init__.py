@@ -47,7 +47,12 @@ class SvoError(RuntimeError):
 
 
 class TraceOut(ctypes.Structure):
-    _fields_ = [("hit", _vp), ("t", _vp), ("leaf", _vp), ("word", _vp), ("rgb", _vp)]
+    _fields_ = [("hit", _vp), ("t", _vp), ("leaf", _vp), ("word", _vp), ("rgb", _vp), ("rgba8", _vp)]
+
+
+# Per-ray outputs of the trace entry points (svo_trace_out): rgba8 is the
+# viewer's packed 8-bit colour of a traced pixel (renderTile, Main.cpp:126-131).
+TRACE_OUTPUTS = ("hit", "t", "leaf", "word", "rgb", "rgba8")
 
 
 class View(ctypes.Structure):
@@ -421,11 +426,11 @@ class VoxelOctree:
     # -- batched tracing
     def trace(self, rays, n=None, ray_scale=0.0, light=(0.0, 0.0, 1.0), out=None, stream=None):
         """Device form: rays is a CUDA tensor (R, 6) float32; out maps any of
-        hit/t/leaf/word/rgb to preallocated CUDA tensors."""
+        hit/t/leaf/word/rgb/rgba8 to preallocated CUDA tensors."""
         if n is None:
             n = rays.shape[0]
         o = TraceOut()
-        for k in ("hit", "t", "leaf", "word", "rgb"):
+        for k in TRACE_OUTPUTS:
             v = (out or {}).get(k)
             setattr(o, k, _dev_ptr(v).value if v is not None else None)
         lt = np.ascontiguousarray(light, dtype=np.float32)
@@ -439,10 +444,10 @@ class VoxelOctree:
         rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 6)
         R = rays.shape[0]
         shapes = {"hit": ((R,), np.uint8), "t": ((R,), np.float32), "leaf": ((R,), np.uint32),
-                  "word": ((R,), np.uint32), "rgb": ((R, 3), np.float32)}
+                  "word": ((R,), np.uint32), "rgb": ((R, 3), np.float32), "rgba8": ((R,), np.uint32)}
         res = out if out is not None else {k: np.empty(*shapes[k]) for k in outputs}
         o = TraceOut()
-        for k in ("hit", "t", "leaf", "word", "rgb"):
+        for k in TRACE_OUTPUTS:
             v = res.get(k)
             setattr(o, k, v.ctypes.data if v is not None else None)
         lt = np.ascontiguousarray(light, dtype=np.float32)
@@ -453,7 +458,7 @@ class VoxelOctree:
     def trace_image(self, rays, width, height, ray_scale=0.0, light=(0.0, 0.0, 1.0), out=None, stream=None):
         """Device form for row-major image rays (R = width*height)."""
         o = TraceOut()
-        for k in ("hit", "t", "leaf", "word", "rgb"):
+        for k in TRACE_OUTPUTS:
             v = (out or {}).get(k)
             setattr(o, k, _dev_ptr(v).value if v is not None else None)
         lt = np.ascontiguousarray(light, dtype=np.float32)
@@ -466,10 +471,10 @@ class VoxelOctree:
         R = rays.shape[0]
         assert R == width * height
         shapes = {"hit": ((R,), np.uint8), "t": ((R,), np.float32), "leaf": ((R,), np.uint32),
-                  "word": ((R,), np.uint32), "rgb": ((R, 3), np.float32)}
+                  "word": ((R,), np.uint32), "rgb": ((R, 3), np.float32), "rgba8": ((R,), np.uint32)}
         res = out if out is not None else {k: np.empty(*shapes[k]) for k in outputs}
         o = TraceOut()
-        for k in ("hit", "t", "leaf", "word", "rgb"):
+        for k in TRACE_OUTPUTS:
             v = res.get(k)
             setattr(o, k, v.ctypes.data if v is not None else None)
         lt = np.ascontiguousarray(light, dtype=np.float32)
@@ -570,7 +575,7 @@ class Batch:
             for k in range(3):
                 cv.light[k] = float(lt[k])
             out = v.get("out", {})
-            for k in ("hit", "t", "leaf", "word", "rgb"):
+            for k in TRACE_OUTPUTS:
                 t = out.get(k)
                 setattr(cv.out, k, _dev_ptr(t).value if t is not None else None)
         self._h = _vp()

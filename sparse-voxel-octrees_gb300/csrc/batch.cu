@@ -49,6 +49,7 @@ struct JobDev {
     uint32_t *leaf;
     uint32_t *word;
     float *rgb;
+    uint32_t *rgba8;
 };
 
 struct BatchArgs {
@@ -161,11 +162,14 @@ __device__ __forceinline__ void write_result(const BatchArgs &a, int job, uint32
     if (J.t) J.t[out_idx] = hs == 0 ? __int_as_float(0x7f800000) : res.t;
     if (J.leaf) J.leaf[out_idx] = leaf ? res.leaf : 0xFFFFFFFFu;
     if (J.word) J.word[out_idx] = leaf ? res.word : 0u;
-    if (J.rgb) {
+    if (J.rgb || J.rgba8) {
         float g = leaf ? shade_grey(res.word, rdx, rdy, rdz, J.lx, J.ly, J.lz) : 0.0f;
-        J.rgb[3 * (uint64_t)out_idx + 0] = g;
-        J.rgb[3 * (uint64_t)out_idx + 1] = g;
-        J.rgb[3 * (uint64_t)out_idx + 2] = g;
+        if (J.rgb) {
+            J.rgb[3 * (uint64_t)out_idx + 0] = g;
+            J.rgb[3 * (uint64_t)out_idx + 1] = g;
+            J.rgb[3 * (uint64_t)out_idx + 2] = g;
+        }
+        if (J.rgba8) J.rgba8[out_idx] = pack_rgba8(g);
     }
 }
 
@@ -411,6 +415,7 @@ int launch_trace_image(const svo_octree *oct, const float *d_rays, uint32_t widt
     J.leaf = out.leaf;
     J.word = out.word;
     J.rgb = out.rgb;
+    J.rgba8 = out.rgba8;
     uint64_t total = (uint64_t)J.tiles_x * ((height + (32 / tile_w) - 1) / (32 / tile_w)) * 32;
     J.tab = octree_table(oct, st);
     J.n_tab = J.tab ? (uint32_t)oct->n_tab : 0u;
@@ -480,6 +485,7 @@ int prepare_jobs(svo_batch *b, int tile_w) {
         J.leaf = v.out.leaf;
         J.word = v.out.word;
         J.rgb = v.out.rgb;
+        J.rgba8 = v.out.rgba8;
         uint64_t slots = v.width ? (uint64_t)J.tiles_x * ((v.height + th - 1) / th) * 32 : v.n_rays;
         beg[i + 1] = beg[i] + slots;
     }

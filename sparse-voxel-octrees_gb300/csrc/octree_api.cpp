@@ -159,9 +159,9 @@ template <typename Launch>
 static int host_pipeline(svo_octree *oct, const float *rays, const std::vector<uint64_t> &plan, uint64_t max_chunk,
                          const svo_trace_out &out, Launch launch) {
     const uint64_t C = max_chunk;
-    // Per half: rays 24 B, hit 1, t 4, leaf 4, word 4, rgb 12 (256-byte aligned arrays).
+    // Per half: rays 24 B, hit 1, t 4, leaf 4, word 4, rgb 12, rgba8 4 (256-byte aligned arrays).
     auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
-    const size_t half = al(C * 24) + al(C) + al(C * 4) * 3 + al(C * 12);
+    const size_t half = al(C * 24) + al(C) + al(C * 4) * 4 + al(C * 12);
     int rc = ensure_staging(oct, 2 * half);
     if (rc) return rc;
     if (!oct->img_streams[0]) {
@@ -186,6 +186,7 @@ static int host_pipeline(svo_octree *oct, const float *rays, const std::vector<u
         uint32_t *d_leaf = (uint32_t *)((uint8_t *)d_t + al(C * 4));
         uint32_t *d_word = (uint32_t *)((uint8_t *)d_leaf + al(C * 4));
         float *d_rgb = (float *)((uint8_t *)d_word + al(C * 4));
+        uint32_t *d_rgba8 = (uint32_t *)((uint8_t *)d_rgb + al(C * 12));
         if (j >= 2) SVO_CUDA_TRY(cudaStreamWaitEvent(si, oct->img_traced[h], 0));
         SVO_CUDA_TRY(cudaMemcpyAsync(d_rays, rays + 6 * c0, m * 24, cudaMemcpyHostToDevice, si));
         SVO_CUDA_TRY(cudaEventRecord(oct->img_in[h], si));
@@ -197,6 +198,7 @@ static int host_pipeline(svo_octree *oct, const float *rays, const std::vector<u
         o.leaf = out.leaf ? d_leaf : nullptr;
         o.word = out.word ? d_word : nullptr;
         o.rgb = out.rgb ? d_rgb : nullptr;
+        o.rgba8 = out.rgba8 ? d_rgba8 : nullptr;
         rc = launch(d_rays, m, o, sk, h);
         if (rc) return rc;
         SVO_CUDA_TRY(cudaEventRecord(oct->img_traced[h], sk));
@@ -206,6 +208,8 @@ static int host_pipeline(svo_octree *oct, const float *rays, const std::vector<u
         if (out.leaf) SVO_CUDA_TRY(cudaMemcpyAsync(out.leaf + c0, d_leaf, m * 4, cudaMemcpyDeviceToHost, so));
         if (out.word) SVO_CUDA_TRY(cudaMemcpyAsync(out.word + c0, d_word, m * 4, cudaMemcpyDeviceToHost, so));
         if (out.rgb) SVO_CUDA_TRY(cudaMemcpyAsync(out.rgb + 3 * c0, d_rgb, m * 12, cudaMemcpyDeviceToHost, so));
+        if (out.rgba8)
+            SVO_CUDA_TRY(cudaMemcpyAsync(out.rgba8 + c0, d_rgba8, m * 4, cudaMemcpyDeviceToHost, so));
         SVO_CUDA_TRY(cudaEventRecord(oct->img_out[h], so));
     }
     SVO_CUDA_TRY(cudaStreamSynchronize(si));

@@ -90,6 +90,14 @@ __device__ __forceinline__ float shade_grey(uint32_t word, float dx, float dy, f
     return c * 0.9f * fabsf(lx * nx + ly * ny + lz * nz) + specular * 0.2f;
 }
 
+// The viewer's 8-bit colour of a traced pixel (renderTile, Main.cpp:126-131,
+// the non-Apple byte order): c = uint32(std::min(shade, 1.0f) * 255.0), the
+// product in double, in the three colour bytes, alpha 0xFF.
+__device__ __forceinline__ uint32_t pack_rgba8(float grey) {
+    const uint32_t c = (uint32_t)((double)smin(grey, 1.0f) * 255.0);
+    return c | (c << 8) | (c << 16) | 0xFF000000u;
+}
+
 enum : int { kMiss = 0, kLeafHit = 1, kLodHit = 2, kFault = 3 };
 
 // Per-ray traversal state of VoxelOctree::raymarch (VoxelOctree.cpp:207-346),

@@ -29,6 +29,7 @@ struct TraceArgs {
     uint32_t *leaf;
     uint32_t *word;
     float *rgb;
+    uint32_t *rgba8;
     uint32_t *status;
 };
 
@@ -50,11 +51,14 @@ __device__ __forceinline__ void store_result(const TraceArgs &a, uint64_t i, con
     bool leaf = r.status == kLeafHit;
     if (a.leaf) a.leaf[i] = leaf ? (uint32_t)r.leaf : 0xFFFFFFFFu;  // the host admits it only below 2^32
     if (a.word) a.word[i] = leaf ? r.word : 0u;
-    if (a.rgb) {
+    if (a.rgb || a.rgba8) {
         float g = leaf ? shade_grey(r.word, dx, dy, dz, a.lx, a.ly, a.lz) : 0.0f;
-        a.rgb[3 * i + 0] = g;
-        a.rgb[3 * i + 1] = g;
-        a.rgb[3 * i + 2] = g;
+        if (a.rgb) {
+            a.rgb[3 * i + 0] = g;
+            a.rgb[3 * i + 1] = g;
+            a.rgb[3 * i + 2] = g;
+        }
+        if (a.rgba8) a.rgba8[i] = pack_rgba8(g);
     }
 }
 
@@ -142,6 +146,7 @@ int launch_trace(const svo_octree *oct, const float *d_rays, uint64_t n, float r
     a.leaf = out.leaf;
     a.word = out.word;
     a.rgb = out.rgb;
+    a.rgba8 = out.rgba8;
     a.status = oct->d_status;
     a.tab = nullptr;
     const unsigned grid = (unsigned)((n + 255) / 256);

@@ -5,6 +5,8 @@ graph and with the autotuned configuration."""
 import numpy as np
 import pytest
 
+from test_gpu_trace import pack_rgba8
+
 pytestmark = pytest.mark.gpu
 
 
@@ -13,13 +15,14 @@ def _outputs(torch, n):
             "t": torch.empty(n, dtype=torch.float32, device="cuda"),
             "leaf": torch.empty(n, dtype=torch.int32, device="cuda"),
             "word": torch.empty(n, dtype=torch.int32, device="cuda"),
-            "rgb": torch.empty((n, 3), dtype=torch.float32, device="cuda")}
+            "rgb": torch.empty((n, 3), dtype=torch.float32, device="cuda"),
+            "rgba8": torch.empty(n, dtype=torch.int32, device="cuda")}
 
 
 def _host(out):
     r = {k: v.cpu().numpy() for k, v in out.items()}
-    r["leaf"] = r["leaf"].view(np.uint32)
-    r["word"] = r["word"].view(np.uint32)
+    for k in ("leaf", "word", "rgba8"):
+        r[k] = r[k].view(np.uint32)
     return r
 
 
@@ -30,6 +33,7 @@ def _same(res, ref, grey=True):
     assert np.array_equal(res["word"], ref["word"])
     if grey:
         assert np.array_equal(res["rgb"][:, 0].view(np.uint32), ref["grey"].view(np.uint32))
+        assert np.array_equal(res["rgba8"], pack_rgba8(ref["grey"], ref["hit"]))
 
 
 @pytest.fixture(scope="module")

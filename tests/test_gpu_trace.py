@@ -17,14 +17,25 @@ def _device_trace(cuda, svo, tree, rays, ray_scale=0.0, light=(0.0, 0.0, 1.0)):
         "leaf": torch.empty(R, dtype=torch.int32, device="cuda"),
         "word": torch.empty(R, dtype=torch.int32, device="cuda"),
         "rgb": torch.empty((R, 3), dtype=torch.float32, device="cuda"),
+        "rgba8": torch.empty(R, dtype=torch.int32, device="cuda"),
     }
     tree.trace(d_rays, ray_scale=ray_scale, light=light, out=out)
     torch.cuda.synchronize()
     res = {k: v.cpu().numpy() for k, v in out.items()}
-    res["leaf"] = res["leaf"].view(np.uint32)
-    res["word"] = res["word"].view(np.uint32)
+    for k in ("leaf", "word", "rgba8"):
+        res[k] = res[k].view(np.uint32)
     assert tree.device_status() == 0
     return res
+
+
+def pack_rgba8(grey, hit):
+    """The viewer's packed colour of a traced pixel (renderTile,
+    Main.cpp:126-131): uint32(std::min(shade, 1.0f) * 255.0) with the product
+    in double, in the three colour bytes, alpha 0xFF; shade 0 without a leaf."""
+    g = np.where(hit == 1, grey, np.float32(0.0)).astype(np.float32)
+    g = np.where(np.float32(1.0) < g, np.float32(1.0), g)
+    c = (g.astype(np.float64) * 255.0).astype(np.uint32)
+    return c | (c << 8) | (c << 16) | np.uint32(0xFF000000)
 
 
 def _assert_same(res, ref, grey=True):
@@ -37,6 +48,8 @@ def _assert_same(res, ref, grey=True):
         assert np.array_equal(res["rgb"][:, 0].view(np.uint32), g.view(np.uint32))
         assert np.array_equal(res["rgb"][:, 1], res["rgb"][:, 0])
         assert np.array_equal(res["rgb"][:, 2], res["rgb"][:, 0])
+        if "rgba8" in res:
+            assert np.array_equal(res["rgba8"], pack_rgba8(g, ref["hit"]))
 
 
 def test_dragon_golden_rays(cuda, svo, golden, oracle):
@@ -185,20 +198,22 @@ def test_host_pipelines_long_calls(cuda, svo, oracle, scenes):
     rays = scenes.camera_rays(cam, W, H)
     light = (0.0, 1.0, 0.0)
     ref = _device_trace(cuda, svo, tree, rays, light=light)
-    _assert_same(tree.trace_host(rays, light=light), ref | {"grey": ref["rgb"][:, 0].copy()})
+    ref["grey"] = ref["rgb"][:, 0].copy()
+    _assert_same(tree.trace_host(rays, light=light, outputs=svo.TRACE_OUTPUTS), ref)
     d_rays = torch.from_numpy(rays).cuda()
     out = {"hit": torch.empty(W * H, dtype=torch.uint8, device="cuda"),
            "t": torch.empty(W * H, dtype=torch.float32, device="cuda"),
            "leaf": torch.empty(W * H, dtype=torch.int32, device="cuda"),
            "word": torch.empty(W * H, dtype=torch.int32, device="cuda"),
-           "rgb": torch.empty((W * H, 3), dtype=torch.float32, device="cuda")}
+           "rgb": torch.empty((W * H, 3), dtype=torch.float32, device="cuda"),
+           "rgba8": torch.empty(W * H, dtype=torch.int32, device="cuda")}
     tree.trace_image(d_rays, W, H, light=light, out=out)
     torch.cuda.synchronize()
     img = {k: v.cpu().numpy() for k, v in out.items()}
-    img["leaf"] = img["leaf"].view(np.uint32)
-    img["word"] = img["word"].view(np.uint32)
-    _assert_same(img, ref | {"grey": ref["rgb"][:, 0].copy()})
-    _assert_same(tree.trace_image_host(rays, W, H, light=light), ref | {"grey": ref["rgb"][:, 0].copy()})
+    for k in ("leaf", "word", "rgba8"):
+        img[k] = img[k].view(np.uint32)
+    _assert_same(img, ref)
+    _assert_same(tree.trace_image_host(rays, W, H, light=light, outputs=svo.TRACE_OUTPUTS), ref)
     assert tree.device_status() == 0
 
 
