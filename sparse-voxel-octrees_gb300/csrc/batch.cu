@@ -20,7 +20,10 @@
 //
 // Each ray runs the same ray_init / ray_step as svo_trace (VoxelOctree.cpp:
 // 207-346), so results are bit-identical to the plain kernel's.
+#include <sys/stat.h>
+
 #include <algorithm>
+#include <cerrno>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -619,14 +622,20 @@ bool cache_lookup(const std::string &key, svo_trace_config *c) {
     return found;
 }
 
+// Creates every missing directory of `dir` (mkdir -p, without a shell).
+bool make_dirs(const std::string &dir) {
+    for (size_t i = 1; i <= dir.size(); ++i) {
+        if (i < dir.size() && dir[i] != '/') continue;
+        const std::string part = dir.substr(0, i);
+        if (mkdir(part.c_str(), 0755) != 0 && errno != EEXIST) return false;
+    }
+    return true;
+}
+
 void cache_store(const std::string &key, const svo_trace_config &c, float ms) {
     std::string path = cache_path();
     size_t slash = path.rfind('/');
-    if (slash != std::string::npos) {
-        std::string dir = path.substr(0, slash);
-        std::string cmd = "mkdir -p '" + dir + "' 2>/dev/null";
-        if (system(cmd.c_str()) != 0) return;
-    }
+    if (slash != std::string::npos && slash > 0 && !make_dirs(path.substr(0, slash))) return;
     FILE *fp = fopen(path.c_str(), "a");
     if (!fp) return;
     fprintf(fp,
