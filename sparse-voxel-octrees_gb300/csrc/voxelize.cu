@@ -426,6 +426,7 @@ struct FoldArgs {
     float half;
     uint32_t *data;
     uint8_t *counts;
+    uint32_t *next;  // work counter of this launch (zero at launch): bricks taken so far
 };
 
 // PlyLoader::writeTriangleCell on a register copy of one buffer cell.
@@ -528,8 +529,15 @@ __global__ void __launch_bounds__(kFoldWarps * 32, 8) k_fold_bricks(FoldArgs a) 
     const float hv[3] = {a.half, a.half, a.half};
     const int end0 = a.org[0] + a.buf[0], end1 = a.org[1] + a.buf[1], end2 = a.org[2] + a.buf[2];
     const uint32_t lt = (1u << lane) - 1u;
-    const uint32_t nwarps = gridDim.x * kFoldWarps;
-    for (uint32_t j = a.b_first + blockIdx.x * kFoldWarps + wid; j < a.b_last; j += nwarps) {
+    // Warps take bricks from a counter: a brick's cost grows with its
+    // triangles, and a fixed stride left most warps idle behind the few that
+    // drew the heaviest bricks.  Bricks own disjoint buffer cells, so the
+    // order they are folded in does not change the result.
+    for (;;) {
+        uint32_t jt = 0;
+        if (lane == 0) jt = atomicAdd(a.next, 1u);
+        const uint32_t j = a.b_first + __shfl_sync(0xffffffffu, jt, 0);
+        if (j >= a.b_last) break;
         const uint32_t key = a.bkey[j];
         const int ox = (int)(compact3(key) << le), oy = (int)(compact3((uint64_t)key >> 1) << le),
                   oz = (int)(compact3((uint64_t)key >> 2) << le);
@@ -1088,6 +1096,9 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
     std::vector<std::pair<uint64_t, uint64_t>> ghosts;  // flat ranges of the dropped slices so far
     uint64_t ghost_len = 0;
     const unsigned fold_grid = (unsigned)sms * 8, warp_grid = (unsigned)sms * 16;
+    Dev<uint32_t> fold_next;  // one work counter per block's fold launch
+    SVO_ALLOC(fold_next, jobs.size());
+    SVO_CUDA_TRY(cudaMemsetAsync(fold_next.p, 0, jobs.size() * sizeof(uint32_t), st));
     for (const BlockJob &j : jobs) {
         FoldArgs fa;
         fa.org[0] = (int)(compact3(j.morton) << lb);
@@ -1116,6 +1127,7 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
             fa.half = 0.5f * hx;
             fa.data = data.p;
             fa.counts = counts.p;
+            fa.next = fold_next.p + (&j - jobs.data());
             unsigned grid = (unsigned)std::min<uint64_t>((j.last - j.first + kFoldWarps - 1) / kFoldWarps, fold_grid);
             k_fold_bricks<<<grid, kFoldWarps * 32, 0, st>>>(fa);
             SVO_LAUNCH_OK("k_fold_bricks");
