@@ -150,6 +150,26 @@ def dist_setup(args):
     return rank, world, local
 
 
+def rank_cameras(scenes, n, rank, center):
+    """The n orbit cameras rank `rank` traces: every rank draws its own views
+    (seed 1000 + rank) over its replica of the octree, so no rays are shared
+    and nothing is exchanged on the data path."""
+    return scenes.orbit_cameras(n, 1000 + rank, center, radius=1.25, radius_hi=2.0, pitch=45.0)
+
+
+def reduce_over_ranks(torch, units, seconds, device):
+    """The job's units (summed over ranks; ranks trace different views, so
+    their shadow-ray counts differ) and its time (the slowest rank's)."""
+    dist = torch.distributed
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return units, seconds
+    u = torch.tensor([float(units)], dtype=torch.float64, device=device)
+    t = torch.tensor([float(seconds)], dtype=torch.float64, device=device)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return int(u.item()), float(t.item())
+
+
 def cpu_threads():
     try:
         return len(os.sched_getaffinity(0))
@@ -196,7 +216,7 @@ def setup_scene(args, rank, torch, svo, scenes):
     n_tab = tree.table_size()
     t_table = time.perf_counter() - t0
     center = tree.center()
-    cams = scenes.orbit_cameras(args.cams, 1000 + rank, center, radius=1.25, radius_hi=2.0, pitch=45.0)
+    cams = rank_cameras(scenes, args.cams, rank, center)
     npix = args.width * args.height
     prim = torch.empty((len(cams) * npix, 6), dtype=torch.float32, device="cuda")
     for i, cam in enumerate(cams):
@@ -345,12 +365,7 @@ def run_ours(args):
         raise RuntimeError("traversal error flag raised")
     ref_p = {k: v.clone() for k, v in out_p.items()}
     ref_s = out_s["hit"].clone()
-    ms_max = ms
-    if world > 1:
-        tt = torch.tensor([ms], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        ms_max = float(tt.item())
-    total_rays = rays_per_step * args.steps * world
+    total_rays, ms_max = reduce_over_ranks(torch, rays_per_step * args.steps, ms, "cuda")
     value = total_rays / (ms_max / 1e3) / 1e6
 
     # 2. the plain per-ray kernel on the same rays (svo_trace for both sets)
@@ -430,11 +445,7 @@ def run_ours(args):
             tree.trace_host(hs_pin, out=os_)
             t_calls[0] += tb - ta
             t_calls[1] += time.perf_counter() - tb
-        e2e_s = time.perf_counter() - t0
-        if world > 1:
-            tt = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
-            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-            e2e_s = float(tt.item())
+        _, e2e_s = reduce_over_ranks(torch, 0, time.perf_counter() - t0, "cuda")
         exact_e2e = all(np.array_equal(op[k].view(np.uint32), ref_p[k].cpu().numpy().view(np.uint32))
                         for k in op) and np.array_equal(os_["hit"], ref_s.cpu().numpy())
         e2e = {"value": round(total_rays / e2e_s / 1e6, 2), "unit": "Mrays/s",
@@ -470,7 +481,7 @@ def run_ours(args):
                          "VoxelOctree::raymarch, %d threads)" % (ncam, len(cam_slices), n, secs, thr)}
     if not args.no_extra and world == 1:
         center = tree.center()
-        cams = scenes.orbit_cameras(args.cams, 1000 + rank, center, radius=1.25, radius_hi=2.0, pitch=45.0)
+        cams = rank_cameras(scenes, args.cams, rank, center)
         frames = {"scene": run_frames(args, torch, svo, tree, cams, oracle, words),
                   "dragon": run_dragon_frames(args, torch, svo, scenes, oracle)}
     del words
@@ -1008,7 +1019,7 @@ def run_reference(args):
     n_vox = keys.size
     del keys, pay
     center = np.array([0.5, 0.5, 0.5], np.float32)
-    cams = scenes.orbit_cameras(args.cams, 1000 + rank, center, radius=1.25, radius_hi=2.0, pitch=45.0)
+    cams = rank_cameras(scenes, args.cams, rank, center)
     prims = [scenes.camera_rays(c, args.width, args.height) for c in cams]
     shadows = []
     for r in prims:  # primary pass once to derive the shadow rays, as in our arm
