@@ -177,21 +177,38 @@ def cpu_threads():
         return os.cpu_count() or 1
 
 
-def cpu_trace_sample(oracle, words, prim_rays, shadow_rays, cam_slices, shadow_slices, budget_s=12.0):
+def pack_rgba8(grey, hit):
+    """The viewer's packed colour of a traced pixel (renderTile,
+    Main.cpp:126-131), from the oracle's shade and hit flag."""
+    g = np.where(hit == 1, grey, np.float32(0.0)).astype(np.float32)
+    g = np.where(np.float32(1.0) < g, np.float32(1.0), g)
+    c = (g.astype(np.float64) * 255.0).astype(np.uint32)
+    return c | (c << 8) | (c << 16) | np.uint32(0xFF000000)
+
+
+def cpu_trace_sample(oracle, words, prim_rays, shadow_rays, cam_slices, shadow_slices, gpu=None, budget_s=12.0):
     """Time the oracle's raymarch over whole cameras (primary + their shadow
-    rays) on all host threads until about `budget_s` seconds have elapsed."""
+    rays) on all host threads until about `budget_s` seconds have elapsed.
+    With `gpu` (the GPU's t, word and rgba8 of the primary rays and hit of
+    the shadow rays, as numpy arrays) every sampled camera is also compared
+    with it bit for bit, outside the timed calls."""
     threads = cpu_threads()
-    rays_done, elapsed, cams = 0, 0.0, 0
+    rays_done, elapsed, cams, exact = 0, 0.0, 0, True
     for (a, b), (sa, sb) in zip(cam_slices, shadow_slices):
         t0 = time.perf_counter()
-        oracle.raymarch(words, prim_rays[a:b], light=LIGHT, threads=threads)
-        oracle.raymarch(words, shadow_rays[sa:sb], threads=threads)
+        rp = oracle.raymarch(words, prim_rays[a:b], light=LIGHT, threads=threads)
+        rs = oracle.raymarch(words, shadow_rays[sa:sb], threads=threads)
         elapsed += time.perf_counter() - t0
+        if gpu is not None:
+            exact = exact and np.array_equal(gpu["t"][a:b].view(np.uint32), rp["t"].view(np.uint32)) and \
+                np.array_equal(gpu["word"][a:b].view(np.uint32), rp["word"]) and \
+                np.array_equal(gpu["rgba8"][a:b].view(np.uint32), pack_rgba8(rp["grey"], rp["hit"])) and \
+                np.array_equal(gpu["hit"][sa:sb], rs["hit"])
         rays_done += (b - a) + (sb - sa)
         cams += 1
         if elapsed >= budget_s:
             break
-    return rays_done, elapsed, cams, threads
+    return rays_done, elapsed, cams, threads, (exact if gpu is not None else None)
 
 
 def setup_scene(args, rank, torch, svo, scenes):
@@ -466,6 +483,7 @@ def run_ours(args):
                 "bytes_per_ray": round(bytes_prim / Rp, 2), "launch_ms": round(t_prim_avg, 3)}
 
     cpu = None
+    oracle_parity = None
     frames = None
     oracle = words = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -474,11 +492,17 @@ def run_ours(args):
         pyoracle.build_oracle(with_reference=False)
         oracle = pyoracle.Oracle()
         words = tree.words()
-        n, secs, ncam, thr = cpu_trace_sample(oracle, words, prim.cpu().numpy(), shadow.cpu().numpy(),
-                                              cam_slices, shadow_slices)
+        gpu = {k: v.cpu().numpy() for k, v in ref_p.items()}
+        gpu["hit"] = ref_s.cpu().numpy()
+        n, secs, ncam, thr, exact_cpu = cpu_trace_sample(oracle, words, prim.cpu().numpy(), shadow.cpu().numpy(),
+                                                         cam_slices, shadow_slices, gpu=gpu)
+        del gpu
         cpu = {"value": round(n / secs / 1e6, 3), "unit": "Mrays/s", "cores": thr, "kind": "port",
                "sample": "%d of %d cameras: %d primary+shadow rays in %.1f s (oracle C restatement of "
                          "VoxelOctree::raymarch, %d threads)" % (ncam, len(cam_slices), n, secs, thr)}
+        oracle_parity = {"cameras": ncam, "rays": n, "exact": bool(exact_cpu),
+                         "what": "the timed step's primary t, leaf word and RGBA8 and shadow hit flags against "
+                                 "the oracle's raymarch + shade on the same words and rays, bit for bit"}
     if not args.no_extra and world == 1:
         center = tree.center()
         cams = rank_cameras(scenes, args.cams, rank, center)
@@ -517,6 +541,7 @@ def run_ours(args):
                                                                                       rays_per_step * 24 / 1e9),
                        "parallelism": "replicas x%d" % world},
             "e2e": e2e, "gpu_launches": 2 * args.steps, "roofline": roofline, "cpu_baseline": cpu,
+            "oracle_parity": oracle_parity,
             "clocks": clk.summary(),
             "plain": {"api": "svo_trace for primary (row order) and shadow rays",
                       "ms_per_step": round(ms_plain, 3), "mrays_s": round(rays_per_step / ms_plain / 1e3, 1),

@@ -1,6 +1,8 @@
 """GPU traversal parity: svo_trace / svo_trace_host against the oracle's
 restatement of VoxelOctree::raymarch and the viewer's shade() — bit-exact
 hit flags, t bits, leaf indices, leaf words and shaded colours."""
+import os
+
 import numpy as np
 import pytest
 
@@ -214,6 +216,37 @@ def test_host_pipelines_long_calls(cuda, svo, oracle, scenes):
         img[k] = img[k].view(np.uint32)
     _assert_same(img, ref)
     _assert_same(tree.trace_image_host(rays, W, H, light=light, outputs=svo.TRACE_OUTPUTS), ref)
+    assert tree.device_status() == 0
+
+
+def test_config0_views_match_oracle(cuda, svo, oracle, scenes):
+    """The small plain-path configuration in full: the 256^3 union of 48
+    spheres (seed 0), built on the GPU, and 12 orbit views (radius 2, seeded
+    yaw and pitch) at 1024x768 with headlights, traced by the image entry
+    point; every output of all 9.4 M rays bit-exact against the oracle."""
+    torch = cuda
+    grid = scenes.sphere_scene(256, 48, 0)
+    words, center = oracle.build_dense(grid)
+    tree = svo.VoxelOctree(svo.VoxelData(grid))
+    assert np.array_equal(tree.words(), words)
+    W, H = 1024, 768
+    hits = 0
+    for cam in scenes.orbit_cameras(12, 0, center, radius=2.0):
+        d_rays = scenes.gpu_camera_rays(cam, W, H)
+        light = scenes.headlight(cam)
+        out = {k: torch.empty(W * H, dtype=dt, device="cuda")
+               for k, dt in (("hit", torch.uint8), ("t", torch.float32), ("leaf", torch.int32),
+                             ("word", torch.int32), ("rgba8", torch.int32))}
+        out["rgb"] = torch.empty((W * H, 3), dtype=torch.float32, device="cuda")
+        tree.trace_image(d_rays, W, H, light=light, out=out)
+        torch.cuda.synchronize()
+        res = {k: v.cpu().numpy() for k, v in out.items()}
+        for k in ("leaf", "word", "rgba8"):
+            res[k] = res[k].view(np.uint32)
+        ref = oracle.raymarch(words, d_rays.cpu().numpy(), light=light, threads=os.cpu_count() or 4)
+        _assert_same(res, ref)
+        hits += int((ref["hit"] == 1).sum())
+    assert hits > 1_000_000
     assert tree.device_status() == 0
 
 
