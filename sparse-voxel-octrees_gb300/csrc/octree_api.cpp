@@ -174,48 +174,57 @@ static int host_pipeline(svo_octree *oct, const float *rays, const std::vector<u
     }
     cudaStream_t si = oct->img_streams[0], so = oct->img_streams[3];
     cudaStream_t skh[2] = {oct->img_streams[1], oct->img_streams[2]};
-    uint64_t c0 = 0;
-    for (size_t j = 0; j < plan.size(); c0 += plan[j], ++j) {
-        const int h = (int)(j & 1);
-        const uint64_t m = plan[j];
-        cudaStream_t sk = skh[h];
-        uint8_t *base = (uint8_t *)oct->stage_dev + h * half;
-        float *d_rays = (float *)base;
-        uint8_t *d_hit = base + al(C * 24);
-        float *d_t = (float *)(d_hit + al(C));
-        uint32_t *d_leaf = (uint32_t *)((uint8_t *)d_t + al(C * 4));
-        uint32_t *d_word = (uint32_t *)((uint8_t *)d_leaf + al(C * 4));
-        float *d_rgb = (float *)((uint8_t *)d_word + al(C * 4));
-        uint32_t *d_rgba8 = (uint32_t *)((uint8_t *)d_rgb + al(C * 12));
-        if (j >= 2) SVO_CUDA_TRY(cudaStreamWaitEvent(si, oct->img_traced[h], 0));
-        SVO_CUDA_TRY(cudaMemcpyAsync(d_rays, rays + 6 * c0, m * 24, cudaMemcpyHostToDevice, si));
-        SVO_CUDA_TRY(cudaEventRecord(oct->img_in[h], si));
-        SVO_CUDA_TRY(cudaStreamWaitEvent(sk, oct->img_in[h], 0));
-        if (j >= 2) SVO_CUDA_TRY(cudaStreamWaitEvent(sk, oct->img_out[h], 0));
-        svo_trace_out o;
-        o.hit = out.hit ? d_hit : nullptr;
-        o.t = out.t ? d_t : nullptr;
-        o.leaf = out.leaf ? d_leaf : nullptr;
-        o.word = out.word ? d_word : nullptr;
-        o.rgb = out.rgb ? d_rgb : nullptr;
-        o.rgba8 = out.rgba8 ? d_rgba8 : nullptr;
-        rc = launch(d_rays, m, o, sk, h);
-        if (rc) return rc;
-        SVO_CUDA_TRY(cudaEventRecord(oct->img_traced[h], sk));
-        SVO_CUDA_TRY(cudaStreamWaitEvent(so, oct->img_traced[h], 0));
-        if (out.hit) SVO_CUDA_TRY(cudaMemcpyAsync(out.hit + c0, d_hit, m, cudaMemcpyDeviceToHost, so));
-        if (out.t) SVO_CUDA_TRY(cudaMemcpyAsync(out.t + c0, d_t, m * 4, cudaMemcpyDeviceToHost, so));
-        if (out.leaf) SVO_CUDA_TRY(cudaMemcpyAsync(out.leaf + c0, d_leaf, m * 4, cudaMemcpyDeviceToHost, so));
-        if (out.word) SVO_CUDA_TRY(cudaMemcpyAsync(out.word + c0, d_word, m * 4, cudaMemcpyDeviceToHost, so));
-        if (out.rgb) SVO_CUDA_TRY(cudaMemcpyAsync(out.rgb + 3 * c0, d_rgb, m * 12, cudaMemcpyDeviceToHost, so));
-        if (out.rgba8)
-            SVO_CUDA_TRY(cudaMemcpyAsync(out.rgba8 + c0, d_rgba8, m * 4, cudaMemcpyDeviceToHost, so));
-        SVO_CUDA_TRY(cudaEventRecord(oct->img_out[h], so));
+    auto enqueue = [&]() -> int {
+        uint64_t c0 = 0;
+        for (size_t j = 0; j < plan.size(); c0 += plan[j], ++j) {
+            const int h = (int)(j & 1);
+            const uint64_t m = plan[j];
+            cudaStream_t sk = skh[h];
+            uint8_t *base = (uint8_t *)oct->stage_dev + h * half;
+            float *d_rays = (float *)base;
+            uint8_t *d_hit = base + al(C * 24);
+            float *d_t = (float *)(d_hit + al(C));
+            uint32_t *d_leaf = (uint32_t *)((uint8_t *)d_t + al(C * 4));
+            uint32_t *d_word = (uint32_t *)((uint8_t *)d_leaf + al(C * 4));
+            float *d_rgb = (float *)((uint8_t *)d_word + al(C * 4));
+            uint32_t *d_rgba8 = (uint32_t *)((uint8_t *)d_rgb + al(C * 12));
+            if (j >= 2) SVO_CUDA_TRY(cudaStreamWaitEvent(si, oct->img_traced[h], 0));
+            SVO_CUDA_TRY(cudaMemcpyAsync(d_rays, rays + 6 * c0, m * 24, cudaMemcpyHostToDevice, si));
+            SVO_CUDA_TRY(cudaEventRecord(oct->img_in[h], si));
+            SVO_CUDA_TRY(cudaStreamWaitEvent(sk, oct->img_in[h], 0));
+            if (j >= 2) SVO_CUDA_TRY(cudaStreamWaitEvent(sk, oct->img_out[h], 0));
+            svo_trace_out o;
+            o.hit = out.hit ? d_hit : nullptr;
+            o.t = out.t ? d_t : nullptr;
+            o.leaf = out.leaf ? d_leaf : nullptr;
+            o.word = out.word ? d_word : nullptr;
+            o.rgb = out.rgb ? d_rgb : nullptr;
+            o.rgba8 = out.rgba8 ? d_rgba8 : nullptr;
+            rc = launch(d_rays, m, o, sk, h);
+            if (rc) return rc;
+            SVO_CUDA_TRY(cudaEventRecord(oct->img_traced[h], sk));
+            SVO_CUDA_TRY(cudaStreamWaitEvent(so, oct->img_traced[h], 0));
+            if (out.hit) SVO_CUDA_TRY(cudaMemcpyAsync(out.hit + c0, d_hit, m, cudaMemcpyDeviceToHost, so));
+            if (out.t) SVO_CUDA_TRY(cudaMemcpyAsync(out.t + c0, d_t, m * 4, cudaMemcpyDeviceToHost, so));
+            if (out.leaf) SVO_CUDA_TRY(cudaMemcpyAsync(out.leaf + c0, d_leaf, m * 4, cudaMemcpyDeviceToHost, so));
+            if (out.word) SVO_CUDA_TRY(cudaMemcpyAsync(out.word + c0, d_word, m * 4, cudaMemcpyDeviceToHost, so));
+            if (out.rgb) SVO_CUDA_TRY(cudaMemcpyAsync(out.rgb + 3 * c0, d_rgb, m * 12, cudaMemcpyDeviceToHost, so));
+            if (out.rgba8)
+                SVO_CUDA_TRY(cudaMemcpyAsync(out.rgba8 + c0, d_rgba8, m * 4, cudaMemcpyDeviceToHost, so));
+            SVO_CUDA_TRY(cudaEventRecord(oct->img_out[h], so));
+        }
+        return SVO_OK;
+    };
+    rc = enqueue();
+    // All four streams are drained even when a chunk failed to enqueue: the
+    // staging halves must be idle before the next call reuses them.
+    cudaError_t e = cudaSuccess;
+    for (cudaStream_t q : {si, skh[0], skh[1], so}) {
+        const cudaError_t eq = cudaStreamSynchronize(q);
+        if (e == cudaSuccess) e = eq;
     }
-    SVO_CUDA_TRY(cudaStreamSynchronize(si));
-    SVO_CUDA_TRY(cudaStreamSynchronize(skh[0]));
-    SVO_CUDA_TRY(cudaStreamSynchronize(skh[1]));
-    SVO_CUDA_TRY(cudaStreamSynchronize(so));
+    if (rc) return rc;
+    if (e != cudaSuccess) return cuda_fail(e, "host trace pipeline");
     return check_device_status(oct);
 }
 
