@@ -140,3 +140,26 @@ def test_oct_read_corrupt(svo, golden, tmp_path):
     open(p, "wb").write(bytes(data))
     with pytest.raises(svo.SvoError):
         svo.oct_read(p)
+
+
+def test_struct_layouts_match_header(svo, tmp_path):
+    """The ctypes mirrors of svo_trace_out, svo_view and svo_trace_config have
+    the C header's size and field offsets (compiled here with the system C
+    compiler, which follows the same ABI as the library's host code)."""
+    mirrors = {"svo_trace_out": svo.TraceOut, "svo_view": svo.View, "svo_trace_config": svo.TraceConfig}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "svo.h"', "int main(void) {"]
+    for cname, py in mirrors.items():
+        lines.append('printf("%s size %%zu\\n", sizeof(%s));' % (cname, cname))
+        for field, _ in py._fields_:
+            lines.append('printf("%s %s %%zu\\n", offsetof(%s, %s));' % (cname, field, cname, field))
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {(ln.split()[0], ln.split()[1]): int(ln.split()[2]) for ln in out if ln.strip()}
+    for cname, py in mirrors.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for field, _ in py._fields_:
+            assert got[(cname, field)] == getattr(py, field).offset, (cname, field)
