@@ -981,14 +981,15 @@ def run_config4(args, torch, svo, scenes, n_steps=200):
 
 
 def profiled_traffic(rays):
-    """DRAM bytes per launch from the committed ncu summary (scaled per ray), or None."""
-    path = os.path.join(ROOT, "profiles", "trace_image_config1.txt")
-    try:
-        for line in open(path):
-            if line.startswith("dram_bytes_per_ray:"):
-                return int(float(line.split(":")[1]) * rays)
-    except OSError:
-        pass
+    """DRAM bytes per launch from the committed ncu summaries (per ray, times
+    the launch's rays): the full-size one-pass capture, else the small case."""
+    for name in ("dram_config1_fullsize.txt", "trace_image_config1.txt"):
+        try:
+            for line in open(os.path.join(ROOT, "profiles", name)):
+                if line.startswith("dram_bytes_per_ray:"):
+                    return int(float(line.split(":")[1]) * rays)
+        except OSError:
+            pass
     return None
 
 
