@@ -296,7 +296,6 @@ def run_ours(args):
     ge.build()
     svo = ge._package()
     import svo_gb300.scenes as scenes
-    os.environ.setdefault("SVO_AUTOTUNE_CACHE", os.path.join(ROOT, "gpurun_out", "autotune.jsonl"))
 
     if args.config == 4:
         r4 = run_config4(args, torch, svo, scenes, n_steps=args.train_steps)
