@@ -64,13 +64,15 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--config", type=int, default=1, choices=[1, 2, 3, 4],
-                   help="1: plain traversal (headline); 3: batched vs plain over 96 octrees and views; "
-                        "4: differentiable shading fwd+bwd")
-    p.add_argument("--no-extra", action="store_true", help="skip the config-3 batched comparison in the default run")
+                   help="workload of the main line: 1 plain traversal of the 2048^3 terrain (default); 2 the "
+                        "327,680-triangle mesh build at 1024^3; 3 batched vs plain over 96 octrees and views; "
+                        "4 differentiable leaf shading fwd+bwd on the 512^3 sphere union")
+    p.add_argument("--no-extra", action="store_true",
+                   help="skip the other workloads' legs (batched, shading, mesh build, frames) in the default run")
     p.add_argument("--views", type=int, default=96)
     p.add_argument("--max-side", type=int, default=0,
-                   help="config 3: clamp each octree's side to this (a smaller case for profiling)")
-    p.add_argument("--train-steps", type=int, default=200, help="Adam steps of the config-4 leg")
+                   help="batched workload: clamp each octree's side to this (a smaller case for profiling)")
+    p.add_argument("--train-steps", type=int, default=200, help="Adam steps of the leaf-shading leg")
     return p.parse_args()
 
 
@@ -298,7 +300,7 @@ def run_ours(args):
     import svo_gb300.scenes as scenes
 
     if args.config == 4:
-        r4 = run_config4(args, torch, svo, scenes, n_steps=args.train_steps)
+        r4 = run_leaf_shading(args, torch, svo, scenes, n_steps=args.train_steps)
         if rank == 0:
             print(json.dumps({"metric": "fwd+bwd Mrays/s", "value": r4["fwd_bwd_mrays_s"], "unit": "Mrays/s",
                               "n_gpus": world, "steps": r4["steps"], "warmup": 0,
@@ -309,7 +311,7 @@ def run_ours(args):
         return
 
     if args.config == 2:
-        r2 = run_config2(args, torch, svo, scenes, check=not args.no_cpu)
+        r2 = run_mesh_build(args, torch, svo, scenes, check=not args.no_cpu)
         if rank == 0:
             print(json.dumps({"metric": "voxels/s", "value": r2["voxels_per_s"], "unit": "voxels/s",
                               "n_gpus": world, "steps": r2["steps"], "warmup": r2["warmup"],
@@ -323,7 +325,7 @@ def run_ours(args):
         return
 
     if args.config == 3:
-        r3 = run_config3(args, torch, svo, scenes)
+        r3 = run_batched(args, torch, svo, scenes)
         if rank == 0:
             print(json.dumps({"metric": "Mrays/s", "value": r3["batched_mrays_s"], "unit": "Mrays/s",
                               "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -513,11 +515,11 @@ def run_ours(args):
     if not args.no_extra and world == 1:
         del prim, shadow, out_p, out_s, ref_p, ref_s, tree
         torch.cuda.empty_cache()
-        extra = run_config3(args, torch, svo, scenes)
+        extra = run_batched(args, torch, svo, scenes)
         torch.cuda.empty_cache()
-        extra4 = run_config4(args, torch, svo, scenes)
+        extra4 = run_leaf_shading(args, torch, svo, scenes)
         torch.cuda.empty_cache()
-        extra2 = run_config2(args, torch, svo, scenes, steps=3, warmup=1, check=not args.no_cpu)
+        extra2 = run_mesh_build(args, torch, svo, scenes, steps=3, warmup=1, check=not args.no_cpu)
         torch.cuda.empty_cache()
         extra_vf = run_voxel_file(args, torch, svo, scenes)
 
@@ -566,7 +568,7 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
-def config3_views(n_views, seed=3):
+def batched_views(n_views, seed=3):
     """96 (octree, view) pairs: depth U{7..11}, even index -> sphere-union
     generator (48 spheres), odd -> terrain generator (200 spheres), scene seed
     = index; one orbit camera each, pixel count log-uniform in
@@ -582,14 +584,14 @@ def config3_views(n_views, seed=3):
     return specs
 
 
-def run_config3(args, torch, svo, scenes, tune_cache=None):
+def run_batched(args, torch, svo, scenes, tune_cache=None):
     """Batched persistent launch (graph-captured, autotuned) against the plain
-    per-view kernel over the config-3 views; checks exact parity."""
+    per-view kernel over the 96 views of batched_views; checks exact parity."""
     t0 = time.perf_counter()
     views, plain_out, rays_list = [], [], []
     trees = []
     total_rays = 0
-    for (i, side, gen, W, H) in config3_views(args.views):
+    for (i, side, gen, W, H) in batched_views(args.views):
         if args.max_side:
             side = min(side, args.max_side)
         grid = scenes.gpu_sphere_scene(side, 48, i) if gen == "sphere" else scenes.gpu_terrain_scene(side, 200, i)
@@ -776,7 +778,7 @@ def profile_kernels(torch, fn):
         return None, {"unavailable": repr(e)[:120]}
 
 
-def run_config2(args, torch, svo, scenes, steps=None, warmup=None, check=True):
+def run_mesh_build(args, torch, svo, scenes, steps=None, warmup=None, check=True):
     """Mesh build: a level-7 icosphere (327,680 triangles) radially displaced
     by 4-octave seeded noise (15% of the radius), per-vertex RGB ~U[0,255],
     written as a binary little-endian PLY (float xyz, uchar rgb); voxelized at
@@ -892,7 +894,7 @@ def run_voxel_file(args, torch, svo, scenes, side=512, slab_mib=64):
                     "the occupied voxels on the device instead of the whole grid"}
 
 
-def run_config4(args, torch, svo, scenes, n_steps=200):
+def run_leaf_shading(args, torch, svo, scenes, n_steps=200):
     """Differentiable leaf shading: 512^3 sphere union (160 spheres, seed 7),
     per-leaf FP32 rgb and normal parameters ~U[0,1], 24 views 512x512 against
     targets from a seeded 3-octave noise colour field; L2 loss, forward +

@@ -195,13 +195,13 @@ def payload_from_occupancy(occ):
 # ---------------------------------------------------------------- scenes
 
 def sphere_scene_params(side, n_spheres, seed):
-    """Config-0 family: centres U[side/8, 7 side/8]^3, radii U[6, 32] * side/256."""
+    """The sphere-union scene: centres U[side/8, 7 side/8]^3, radii U[6, 32] * side/256."""
     s = side / 256.0
     return sphere_params(n_spheres, seed, 32 * s, 224 * s, 6 * s, 32 * s)
 
 
 def terrain_scene_params(side, n_spheres, seed):
-    """Config-1 family: 5-octave terrain (amplitude 0.3*side, 2-voxel shell)
+    """The terrain scene: 5-octave terrain (amplitude 0.3*side, 2-voxel shell)
     plus spheres with radii U[10, 120] * side/2048 and centres U[0.1, 0.9]*side."""
     heights = terrain_heights(side, seed)
     s = side / 2048.0

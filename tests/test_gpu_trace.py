@@ -219,8 +219,8 @@ def test_host_pipelines_long_calls(cuda, svo, oracle, scenes):
     assert tree.device_status() == 0
 
 
-def test_config0_views_match_oracle(cuda, svo, oracle, scenes):
-    """The small plain-path configuration in full: the 256^3 union of 48
+def test_sphere_union_256_views_match_oracle(cuda, svo, oracle, scenes):
+    """The small plain-traversal workload in full: the 256^3 union of 48
     spheres (seed 0), built on the GPU, and 12 orbit views (radius 2, seeded
     yaw and pitch) at 1024x768 with headlights, traced by the image entry
     point; every output of all 9.4 M rays bit-exact against the oracle."""
