@@ -85,18 +85,20 @@ int make_handle(uint32_t *d_words, uint64_t n_words, const float center[3], svo_
     h->n_words = n_words;
     std::memcpy(h->center, center, sizeof(h->center));
     cudaGetDevice(&h->device);
-    cudaError_t e = cudaMalloc((void **)&h->d_status, sizeof(uint32_t));
+    // One 32-byte control block: the three work counters, then the error word.
+    void *ctrl = nullptr;
+    cudaError_t e = cudaMalloc(&ctrl, 32);
     if (e != cudaSuccess) {
         cudaFree(d_words);
         h->d_words = nullptr;
-        return cuda_fail(e, "cudaMalloc(status)");
+        return cuda_fail(e, "cudaMalloc(control block)");
     }
-    e = cudaMemset(h->d_status, 0, sizeof(uint32_t));
-    if (e != cudaSuccess) return cuda_fail(e, "cudaMemset(status)");
-    e = cudaMalloc((void **)&h->d_queue, 3 * sizeof(unsigned long long));
+    h->d_queue = static_cast<unsigned long long *>(ctrl);
+    h->d_status = reinterpret_cast<uint32_t *>(static_cast<char *>(ctrl) + 3 * sizeof(unsigned long long));
+    e = cudaMemset(ctrl, 0, 32);
     if (e != cudaSuccess) {
         svo_octree_destroy(h.release());
-        return cuda_fail(e, "cudaMalloc(queue)");
+        return cuda_fail(e, "cudaMemset(control block)");
     }
     *out = h.release();
     return SVO_OK;
@@ -380,8 +382,7 @@ int svo_octree_destroy(svo_octree *oct) {
     if (!oct) return SVO_OK;
     if (oct->d_words) cudaFree(oct->d_words);
     if (oct->d_tab) cudaFree(oct->d_tab);
-    if (oct->d_status) cudaFree(oct->d_status);
-    if (oct->d_queue) cudaFree(oct->d_queue);
+    if (oct->d_queue) cudaFree(oct->d_queue);  // the control block (d_status lies inside it)
     if (oct->stage_dev) cudaFree(oct->stage_dev);
     for (auto &s : oct->img_streams)
         if (s) cudaStreamDestroy(s);

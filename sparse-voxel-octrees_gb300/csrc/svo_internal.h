@@ -21,6 +21,7 @@ struct svo_octree {
     uint64_t n_words = 0;
     float center[3] = {0.0f, 0.0f, 0.0f};
     int device = 0;
+    // One 32-byte device control block: d_queue at its start, d_status at byte 24.
     uint32_t *d_status = nullptr;  // device error word: bit 0 = a ray ended with kFault
     unsigned long long *d_queue = nullptr;  // work counters: [0] svo_trace_image and the differentiable
                                             // launches, [1] and [2] svo_trace_image_host's two trace streams
