@@ -374,20 +374,65 @@ inline unsigned blocks_for(uint64_t n, int t = 256) {
         if (_e != cudaSuccess) return ::svo::cuda_fail(_e, "launch of " name); \
     } while (0)
 
-// Stream-ordered temporary buffer.
+// Bump allocator over a few pool chunks for the level build's many
+// short-lived arrays.  One stream-ordered allocation and free per array cost
+// about 240 driver calls per build, most of them right after a host
+// synchronisation, when the GPU waits on the host.  The chunks return to the
+// pool (stream-ordered) when the arena is destroyed, after every launch that
+// uses them has been enqueued.
+class BuildArena {
+public:
+    explicit BuildArena(cudaStream_t s) : st_(s) {}
+    BuildArena(const BuildArena &) = delete;
+    BuildArena &operator=(const BuildArena &) = delete;
+    ~BuildArena() {
+        for (void *c : chunks_) cudaFreeAsync(c, st_);
+    }
+    cudaError_t alloc(void **p, size_t bytes) {
+        bytes = (bytes + 255) & ~size_t(255);
+        if (bytes > left_) {
+            const size_t cb = std::max(bytes, kChunk);
+            void *c = nullptr;
+            cudaError_t e = scratch_alloc(&c, cb, st_);
+            if (e != cudaSuccess) return e;
+            chunks_.push_back(c);
+            cur_ = static_cast<char *>(c);
+            left_ = cb;
+        }
+        *p = cur_;
+        cur_ += bytes;
+        left_ -= bytes;
+        return cudaSuccess;
+    }
+
+private:
+    static constexpr size_t kChunk = size_t(64) << 20;
+    cudaStream_t st_;
+    std::vector<void *> chunks_;
+    char *cur_ = nullptr;
+    size_t left_ = 0;
+};
+
+// Stream-ordered temporary buffer, from the pool or from a BuildArena.
 template <typename T>
 struct DevBuf {
     T *p = nullptr;
     cudaStream_t st = nullptr;
+    bool owned = false;  // false: memory of a BuildArena (freed with the arena)
     DevBuf() = default;
     DevBuf(const DevBuf &) = delete;
     DevBuf &operator=(const DevBuf &) = delete;
     cudaError_t alloc(uint64_t n, cudaStream_t s) {
         st = s;
+        owned = true;
         return scratch_alloc((void **)&p, (size_t)(n ? n : 1) * sizeof(T), s);
     }
+    cudaError_t alloc(uint64_t n, BuildArena &a) {
+        owned = false;
+        return a.alloc((void **)&p, (size_t)(n ? n : 1) * sizeof(T));
+    }
     void release() {
-        if (p) cudaFreeAsync(p, st);
+        if (p && owned) cudaFreeAsync(p, st);
         p = nullptr;
     }
     ~DevBuf() { release(); }
@@ -408,10 +453,15 @@ struct LevelArrays {
     } while (0)
 
 template <typename TO>
-int scan_to(const uint32_t *in, TO *out, uint64_t n, TO *total_host, cudaStream_t st) {
+int scan_to(const uint32_t *in, TO *out, uint64_t n, TO *total_host, cudaStream_t st, BuildArena *arena = nullptr) {
     DevBuf<TO> scratch, tot;
-    SVO_TRY_ALLOC(scratch.alloc(scan_scratch_elems(n), st));
-    SVO_TRY_ALLOC(tot.alloc(1, st));
+    if (arena) {
+        SVO_TRY_ALLOC(scratch.alloc(scan_scratch_elems(n), *arena));
+        SVO_TRY_ALLOC(tot.alloc(1, *arena));
+    } else {
+        SVO_TRY_ALLOC(scratch.alloc(scan_scratch_elems(n), st));
+        SVO_TRY_ALLOC(tot.alloc(1, st));
+    }
     SVO_CUDA_TRY((exclusive_scan<uint32_t, TO>(in, out, n, tot.p, scratch.p, st)));
     SVO_CUDA_TRY(cudaMemcpyAsync(total_host, tot.p, sizeof(TO), cudaMemcpyDeviceToHost, st));
     SVO_CUDA_TRY(cudaStreamSynchronize(st));
@@ -429,6 +479,7 @@ int build_from_sorted_device(const uint64_t *d_keys, const uint32_t *d_payload, 
     if (multi_block && !d_topflag) return set_error(SVO_ERR_INVALID, "build: missing cache-block flags");
     if (N >= 0xFFFFFFFFull) return set_error(SVO_ERR_LIMIT, "%llu occupied voxels exceed 2^32-1", (unsigned long long)N);
     int rc = SVO_OK;
+    BuildArena arena(st);  // declared first: released after every array below
 
     // Phase 2: levels e = 1..D (node edge 2^e); level 0 is the leaves.
     std::vector<LevelArrays> lv(D + 1);
@@ -438,8 +489,8 @@ int build_from_sorted_device(const uint64_t *d_keys, const uint32_t *d_payload, 
     for (int e = 1; e <= D; ++e) {
         LevelArrays &L = lv[e];
         DevBuf<uint32_t> head, pidx;
-        SVO_TRY_ALLOC(head.alloc(nc, st));
-        SVO_TRY_ALLOC(pidx.alloc(nc, st));
+        SVO_TRY_ALLOC(head.alloc(nc, arena));
+        SVO_TRY_ALLOC(pidx.alloc(nc, arena));
         if (nc) {
             k_heads<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, head.p);
             SVO_LAUNCH_CHECK("k_heads");
@@ -448,30 +499,30 @@ int build_from_sorted_device(const uint64_t *d_keys, const uint32_t *d_payload, 
             // Dense grouping over cache blocks, adding blocks that only the top
             // lookup table marks (descriptors without children).
             DevBuf<uint32_t> first, present, bidx;
-            SVO_TRY_ALLOC(first.alloc(n_blocks, st));
-            SVO_TRY_ALLOC(present.alloc(n_blocks, st));
-            SVO_TRY_ALLOC(bidx.alloc(n_blocks, st));
+            SVO_TRY_ALLOC(first.alloc(n_blocks, arena));
+            SVO_TRY_ALLOC(present.alloc(n_blocks, arena));
+            SVO_TRY_ALLOC(bidx.alloc(n_blocks, arena));
             SVO_CUDA_TRY(cudaMemsetAsync(first.p, 0xFF, n_blocks * sizeof(uint32_t), st));
             if (nc) k_block_first<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, head.p, first.p);
             k_block_present<<<blocks_for(n_blocks), 256, 0, st>>>(first.p, d_topflag, n_blocks, present.p);
             SVO_LAUNCH_CHECK("k_block_present");
             uint32_t np = 0;
-            rc = scan_to<uint32_t>(present.p, bidx.p, n_blocks, &np, st);
+            rc = scan_to<uint32_t>(present.p, bidx.p, n_blocks, &np, st, &arena);
             if (rc) return rc;
             L.n = np;
-            SVO_TRY_ALLOC(L.key.alloc(np, st));
-            SVO_TRY_ALLOC(L.start.alloc(np, st));
+            SVO_TRY_ALLOC(L.key.alloc(np, arena));
+            SVO_TRY_ALLOC(L.start.alloc(np, arena));
             k_block_parents<<<blocks_for(n_blocks), 256, 0, st>>>(first.p, present.p, bidx.p, n_blocks, nc, L.key.p,
                                                                   L.start.p);
             if (nc) k_child_pidx_from_blocks<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, bidx.p, pidx.p);
             SVO_LAUNCH_CHECK("k_child_pidx_from_blocks");
         } else {
             uint32_t np = 0;
-            rc = scan_to<uint32_t>(head.p, pidx.p, nc, &np, st);
+            rc = scan_to<uint32_t>(head.p, pidx.p, nc, &np, st, &arena);
             if (rc) return rc;
             L.n = np;
-            SVO_TRY_ALLOC(L.key.alloc(np, st));
-            SVO_TRY_ALLOC(L.start.alloc(np, st));
+            SVO_TRY_ALLOC(L.key.alloc(np, arena));
+            SVO_TRY_ALLOC(L.start.alloc(np, arena));
             if (nc) {
                 k_parents_from_heads<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, head.p, pidx.p, L.key.p, L.start.p);
                 k_child_pidx_from_heads<<<blocks_for(nc), 256, 0, st>>>(head.p, nc, pidx.p);
@@ -481,13 +532,13 @@ int build_from_sorted_device(const uint64_t *d_keys, const uint32_t *d_payload, 
         // The root always exists, even over an empty grid.
         if (e == D && L.n == 0) {
             L.n = 1;
-            SVO_TRY_ALLOC(L.key.alloc(1, st));
-            SVO_TRY_ALLOC(L.start.alloc(1, st));
+            SVO_TRY_ALLOC(L.key.alloc(1, arena));
+            SVO_TRY_ALLOC(L.start.alloc(1, arena));
             SVO_CUDA_TRY(cudaMemsetAsync(L.key.p, 0, sizeof(uint64_t), st));
             SVO_CUDA_TRY(cudaMemsetAsync(L.start.p, 0, sizeof(uint32_t), st));
         }
-        SVO_TRY_ALLOC(L.mask.alloc(L.n, st));
-        SVO_TRY_ALLOC(L.count.alloc(L.n, st));
+        SVO_TRY_ALLOC(L.mask.alloc(L.n, arena));
+        SVO_TRY_ALLOC(L.count.alloc(L.n, arena));
         k_parent_masks<<<blocks_for(L.n), 256, 0, st>>>(L.key.p, L.start.p, L.n, ckey, nc, L.mask.p, L.count.p);
         SVO_LAUNCH_CHECK("k_parent_masks");
         if (e == 1) {
@@ -502,8 +553,8 @@ int build_from_sorted_device(const uint64_t *d_keys, const uint32_t *d_payload, 
     // Subtree sizes, bottom-up.
     for (int e = 1; e <= D; ++e) {
         LevelArrays &L = lv[e];
-        SVO_TRY_ALLOC(L.S.alloc(L.n, st));
-        SVO_TRY_ALLOC(L.large.alloc(L.n, st));
+        SVO_TRY_ALLOC(L.S.alloc(L.n, arena));
+        SVO_TRY_ALLOC(L.large.alloc(L.n, arena));
         k_subtree<<<blocks_for(L.n), 256, 0, st>>>(L.n, L.count.p, L.start.p, e > 1 ? lv[e - 1].S.p : nullptr,
                                                   e == 1, L.S.p, L.large.p);
         SVO_LAUNCH_CHECK("k_subtree");
@@ -516,17 +567,17 @@ int build_from_sorted_device(const uint64_t *d_keys, const uint32_t *d_payload, 
     uint32_t *words = nullptr;
     SVO_CUDA_TRY(cudaMallocAsync((void **)&words, (size_t)W * sizeof(uint32_t), st));
     DevBuf<uint32_t> err;
-    SVO_TRY_ALLOC(err.alloc(1, st));
+    SVO_TRY_ALLOC(err.alloc(1, arena));
     SVO_CUDA_TRY(cudaMemsetAsync(err.p, 0, sizeof(uint32_t), st));
 
     // Placement, top-down.
-    SVO_TRY_ALLOC(lv[D].B.alloc(1, st));
+    SVO_TRY_ALLOC(lv[D].B.alloc(1, arena));
     k_set_u64<<<1, 1, 0, st>>>(lv[D].B.p, 1);
     k_root_word<<<1, 1, 0, st>>>(lv[D].mask.p, lv[D].large.p, D == 1, words);
     for (int e = D; e >= 2; --e) {
         LevelArrays &P = lv[e];
         LevelArrays &C = lv[e - 1];
-        SVO_TRY_ALLOC(C.B.alloc(C.n, st));
+        SVO_TRY_ALLOC(C.B.alloc(C.n, arena));
         k_place<<<blocks_for(P.n), 256, 0, st>>>(P.n, P.count.p, P.start.p, P.large.p, P.B.p, C.S.p, C.mask.p,
                                                 C.large.p, e - 1 == 1, C.B.p, words, W, err.p);
         SVO_LAUNCH_CHECK("k_place");
