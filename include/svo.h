@@ -238,6 +238,26 @@ void svo_mesh_destroy(svo_mesh *mesh);
 int svo_octree_build_mesh(const svo_mesh *mesh, int side, int threads, uint64_t mem, svo_stream stream,
                           svo_octree **out);
 
+/* Replaces PlyLoader::convertToVolume(path, maxSize, memoryBudget)
+ * (PlyLoader.cpp:506-534), the builder's --mode 1 (Main.cpp:312-324): the
+ * mesh voxelized at suggestedDimensions(side) = w x h x d with a `threads`
+ * thread pool's sub-block partition, written as a .voxel file (int32 w, h,
+ * d, then w*h*d words, x fastest, 0 = empty) that svo_octree_build_voxel_file
+ * and the reference's VoxelData(path, mem) read.  The reference processes
+ * z-slabs of mem / (w*h) slices into one buffer it never clears between
+ * slabs; these calls take the case where `mem` holds the whole volume as one
+ * slab (mem >= w*h*d) and return SVO_ERR_LIMIT otherwise, SVO_ERR_MEMORY when
+ * mem holds no slice (the reference's ASSERT).  The reference's own
+ * conversion stops with SIGFPE on x86-64: its progress line divides by a
+ * block count only isBlockEmpty raises, which this path never calls.
+ * svo_mesh_to_volume leaves the words in d_volume (device memory for the
+ * w*h*d words of svo_mesh_dimensions); it works on `stream` and synchronises
+ * it before returning, to read the conversion's error flags. */
+int svo_mesh_to_volume(const svo_mesh *mesh, int side, int threads, uint64_t mem, uint32_t *d_volume,
+                       svo_stream stream);
+int svo_mesh_write_voxel_file(const svo_mesh *mesh, const char *path, int side, int threads, uint64_t mem,
+                              svo_stream stream);
+
 /* svo_mesh_load_ply + svo_octree_build_mesh + svo_mesh_destroy: the
  * builder's in-memory mode (Main.cpp -builder with a .ply input). */
 int svo_octree_build_ply(const char *path, int side, int threads, uint64_t mem, svo_stream stream,

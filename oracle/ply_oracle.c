@@ -202,12 +202,13 @@ static void best_partition(int *w, int *h, int *d, int threads) {
     }
 }
 
-/* PlyLoader::setupBlockProcessing + buildBlockLists, PlyLoader.cpp:407-437, 272-294 */
-static int setup_blocks(mesh *m, int side, int block, int vw, int vh, int vd, int threads) {
+/* PlyLoader::setupBlockProcessing + buildBlockLists, PlyLoader.cpp:407-437,
+ * 272-294, for a bw x bh x bd block over a vw x vh x vd volume */
+static int setup_blocks3(mesh *m, int side, int bw, int bh, int bd, int vw, int vh, int vd, int threads) {
     m->sideLength = side - 2;
-    m->blockW = m->subW = block;
-    m->blockH = m->subH = block;
-    m->blockD = m->subD = block;
+    m->blockW = m->subW = bw;
+    m->blockH = m->subH = bh;
+    m->blockD = m->subD = bd;
     best_partition(&m->subW, &m->subH, &m->subD, threads);
     m->partW = m->blockW / m->subW;
     m->partH = m->blockH / m->subH;
@@ -229,6 +230,11 @@ static int setup_blocks(mesh *m, int side, int block, int vw, int vh, int vd, in
     for (uint64_t i = ncell; i >= 1; --i) m->offsets[i] = m->offsets[i - 1];
     m->offsets[0] = 0;
     return 0;
+}
+
+/* VoxelData's cache blocks are cubes */
+static int setup_blocks(mesh *m, int side, int block, int vw, int vh, int vd, int threads) {
+    return setup_blocks3(m, side, block, block, block, vw, vh, vd, threads);
 }
 
 /* PlyLoader::isBlockEmpty, PlyLoader.cpp:476-493 */
@@ -413,6 +419,41 @@ int svo_oracle_mesh_setup(void *mp, int side, int block, const int dims[3], int 
     m->counts = (uint8_t *)calloc((size_t)block * block * block, 1);
     if (!m->counts) return -3;
     return setup_blocks(m, side, block, dims[0], dims[1], dims[2], threads);
+}
+
+/* PlyLoader::convertToVolume, PlyLoader.cpp:506-534, into out (w*h*d words
+ * of suggestedDimensions(side)): the slab height is the budget over w*h
+ * bytes (blockMemRequirement counts one byte per cell), the slab is the
+ * block of setupBlockProcessing, and processBlock runs slab after slab into
+ * one buffer that is never cleared between slabs (the reference reuses
+ * `data`), each slab's first min(slab, d - z) slices written out.  Returns -1
+ * when the budget holds no slice (the reference's ASSERT), -3 on allocation
+ * failure. */
+int svo_oracle_mesh_to_volume(void *mp, int side, uint64_t mem, int threads, uint32_t *out) {
+    mesh *m = (mesh *)mp;
+    int dims[3];
+    svo_oracle_mesh_dims(mp, side, dims);
+    const int w = dims[0], h = dims[1], d = dims[2];
+    const uint64_t slice_cost = (uint64_t)w * (uint64_t)h;
+    int slice = (int)(mem / slice_cost);
+    if (slice > d) slice = d;
+    if (slice == 0) return -1;
+    const size_t cells = (size_t)w * h * slice;
+    uint32_t *data = (uint32_t *)calloc(cells, 4);
+    free(m->counts);
+    m->counts = (uint8_t *)calloc(cells, 1);
+    free(m->offsets); m->offsets = NULL;
+    free(m->lists); m->lists = NULL;
+    if (!data || !m->counts) { free(data); return -3; }
+    int rc = setup_blocks3(m, side, w, h, slice, w, h, d, threads);
+    if (rc) { free(data); return rc; }
+    for (int z = 0; z < d; z += slice) {
+        svo_oracle_mesh_process_block(mp, data, 0, 0, z, w, h, slice);
+        const int nz = slice < d - z ? slice : d - z;
+        memcpy(out + (size_t)w * h * z, data, (size_t)w * h * nz * 4);
+    }
+    free(data);
+    return 0;
 }
 
 int svo_oracle_mesh_num_tris(void *mp) { return ((mesh *)mp)->ntris; }

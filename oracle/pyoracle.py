@@ -84,6 +84,8 @@ class Oracle:
         L.svo_oracle_build_mesh.restype = ctypes.c_int
         L.svo_oracle_build_mesh.argtypes = [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(_u32p),
                                             _u64p, _f32p]
+        L.svo_oracle_mesh_to_volume.restype = ctypes.c_int
+        L.svo_oracle_mesh_to_volume.argtypes = [_vp, ctypes.c_int, ctypes.c_uint64, ctypes.c_int, _u32p]
         L.svo_oracle_render_frame.restype = ctypes.c_int
         L.svo_oracle_render_frame.argtypes = [_u32p, ctypes.c_uint64, _f32p, _f32p, ctypes.c_float, ctypes.c_int,
                                               ctypes.c_int, ctypes.c_int, ctypes.c_int, _u32p, ctypes.c_int]
@@ -213,6 +215,29 @@ class Oracle:
             words = np.ctypeslib.as_array(p, shape=(n.value,)).copy()
             self.L.svo_oracle_free(ctypes.cast(p, _vp))
             return words, c
+        finally:
+            self.L.svo_oracle_mesh_destroy(m)
+
+    def mesh_to_volume(self, pos, faces, side, threads, mem=1 << 30, normals=None, colors=None):
+        """PlyLoader::convertToVolume (the builder's --mode 1) for a parsed
+        mesh: the (d, h, w) uint32 volume it writes after its header."""
+        pos = np.ascontiguousarray(pos, dtype=np.float32).reshape(-1, 3)
+        nrm = None if normals is None else np.ascontiguousarray(normals, dtype=np.float32).reshape(-1, 3)
+        col = None if colors is None else np.ascontiguousarray(colors, dtype=np.float32).reshape(-1, 3)
+        flat = flatten_faces(faces)
+        m = self.L.svo_oracle_mesh_create(_ptr(pos, _f32p), _ptr(nrm, _f32p), _ptr(col, _f32p), pos.shape[0],
+                                          flat.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), len(faces))
+        if not m:
+            raise MemoryError("svo_oracle_mesh_create")
+        try:
+            dims = (ctypes.c_int * 3)()
+            self.L.svo_oracle_mesh_dims(m, int(side), dims)
+            w, h, d = dims
+            out = np.zeros((d, h, w), np.uint32)
+            rc = self.L.svo_oracle_mesh_to_volume(m, int(side), int(mem), int(threads), _ptr(out, _u32p))
+            if rc != 0:
+                raise RuntimeError("svo_oracle_mesh_to_volume failed: %d" % rc)
+            return out
         finally:
             self.L.svo_oracle_mesh_destroy(m)
 
@@ -359,6 +384,9 @@ class Reference:
         L.ref_build_ply.restype = _vp
         L.ref_build_ply.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_uint64]
         L.ref_ply_to_voxel_file.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_uint64]
+        L.ref_ply_volume.restype = ctypes.c_int
+        L.ref_ply_volume.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(ctypes.c_int),
+                                     _u32p]
         L.ref_load.restype = _vp
         L.ref_load.argtypes = [ctypes.c_char_p]
         L.ref_save.argtypes = [_vp, ctypes.c_char_p]
@@ -442,6 +470,20 @@ class Reference:
         if self._isolated:
             return self._worker_for(threads).call("ply_to_voxel_file", ply_path, voxel_path, side, mem, timeout=60.0)
         return self.L.ref_ply_to_voxel_file(ply_path.encode(), voxel_path.encode(), int(side), int(mem))
+
+    def ply_volume(self, ply_path, side, mem=1 << 30, threads=4):
+        """The reference's convertToVolume steps (ref_shim.cpp ref_ply_volume)
+        with a `threads`-thread pool: the (d, h, w) uint32 volume."""
+        if self._isolated:
+            return self._worker_for(threads).call("ply_volume", ply_path, side, mem, timeout=60.0)
+        dims = (ctypes.c_int * 3)()
+        self.L.ref_ply_volume(ply_path.encode(), int(side), int(mem), dims, None)
+        w, h, d = dims
+        out = np.zeros((d, h, w), np.uint32)
+        rc = self.L.ref_ply_volume(ply_path.encode(), int(side), int(mem), dims, _ptr(out, _u32p))
+        if rc != 0:
+            raise RuntimeError("ref_ply_volume failed: %d" % rc)
+        return out
 
     def tree_from_words(self, words, center):
         """An in-process reference tree holding `words` (written to a

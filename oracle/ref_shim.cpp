@@ -13,6 +13,7 @@
  *   - VoxelOctree(VoxelData *)                VoxelOctree.cpp:125-137
  *   - VoxelData(const char *path, size_t mem) VoxelData.cpp:37-48
  *   - VoxelData(PlyLoader *, int, size_t)     VoxelData.cpp:50-56
+ *   - PlyLoader::convertToVolume              PlyLoader.cpp:506-534 (without its file)
  *   - VoxelOctree::raymarch                   VoxelOctree.cpp:207-346
  *   - compressMaterial / decompressMaterial   Util.hpp:64-100
  *   - triBoxOverlap                           third-party/tribox3.c:132-206
@@ -21,6 +22,7 @@
  * through member pointers formed by explicit template instantiation, where
  * access checking does not apply (C++11 [temp.explicit]/12).
  */
+#include <algorithm>
 #include <cstdint>
 #include <cstring>
 #include <thread>
@@ -72,6 +74,42 @@ void *ref_build_ply(const char *ply_path, int side, uint64_t mem) {
 int ref_ply_to_voxel_file(const char *ply_path, const char *voxel_path, int side, uint64_t mem) {
     std::unique_ptr<PlyLoader> loader(new PlyLoader(ply_path));
     loader->convertToVolume(voxel_path, side, size_t(mem));
+    return 0;
+}
+
+// PlyLoader::convertToVolume (PlyLoader.cpp:506-534) into `out` instead of
+// a file: the same suggestedDimensions, slab height (budget / w*h bytes),
+// setupBlockProcessing with the slab as the block, and processBlock slab
+// after slab into one buffer that is reused without clearing, as the
+// reference reuses `data`.  convertToVolume never calls isBlockEmpty, so
+// processBlock's progress line divides by a zero block count (SIGFPE on
+// x86-64; AArch64 integer division gives 0 and the conversion completes).
+// One isBlockEmpty call on the first slab that holds triangles makes that
+// count nonzero; it only feeds the progress line.  The reference's buffer
+// comes from new[] uninitialised (fresh zero pages for large volumes); here
+// it starts zeroed.  dims gets w, h, d; with out == NULL nothing else runs.
+// Returns -1 when the budget holds no slice (the reference's ASSERT).
+int ref_ply_volume(const char *ply_path, int side, uint64_t mem, int *dims, uint32_t *out) {
+    std::unique_ptr<PlyLoader> loader(new PlyLoader(ply_path));
+    int w, h, d;
+    loader->suggestedDimensions(side, w, h, d);
+    dims[0] = w;
+    dims[1] = h;
+    dims[2] = d;
+    if (!out) return 0;
+    size_t sliceCost = loader->blockMemRequirement(w, h, 1);
+    int sliceZ = std::min((int)(size_t(mem) / sliceCost), d);
+    if (sliceZ == 0) return -1;
+    std::vector<uint32> data(size_t(w) * size_t(h) * size_t(sliceZ), 0u);
+    loader->setupBlockProcessing(side, w, h, sliceZ, w, h, d);
+    bool any = false;
+    for (int z = 0; z < d && !any; z += sliceZ) any = !loader->isBlockEmpty(0, 0, z);
+    for (int z = 0; z < d; z += sliceZ) {
+        if (any) loader->processBlock(data.data(), 0, 0, z, w, h, sliceZ);
+        size_t n = size_t(w) * size_t(h) * size_t(std::min(sliceZ, d - z));
+        std::memcpy(out + size_t(w) * size_t(h) * size_t(z), data.data(), n * sizeof(uint32));
+    }
+    loader->teardownBlockProcessing();
     return 0;
 }
 

@@ -96,6 +96,10 @@ int svo_oracle_mesh_num_tris(void *mesh);
 void svo_oracle_mesh_destroy(void *mesh);
 int svo_oracle_build_mesh(void *mesh, int side, int threads, uint64_t mem, uint32_t **words, uint64_t *nwords,
                           float center[3]);
+/* PlyLoader::convertToVolume (the builder's --mode 1) into out: w*h*d words
+ * of svo_oracle_mesh_dims(side), x fastest.  Returns 0, -1 (mem holds no
+ * slice), -3 (allocation), -5 (as above). */
+int svo_oracle_mesh_to_volume(void *mesh, int side, uint64_t mem, int threads, uint32_t *out);
 /* render_oracle.c: the viewer's frame (Main.cpp:92-202, n_strips strips as
  * its threads cut it, pixel_stride 1 or the half-size 3), RGBA8 into out
  * (W*H words, row-major).  rot = tform a11..a33, pos = the camera position

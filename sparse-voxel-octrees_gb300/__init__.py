@@ -108,6 +108,9 @@ def _load():
                                          ctypes.POINTER(_f32p), _u64p, ctypes.POINTER(ctypes.POINTER(ctypes.c_int32)),
                                          _u64p, _f32p, _f32p]),
         "svo_mesh_dimensions": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
+        "svo_mesh_to_volume": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_uint64, _vp, _vp]),
+        "svo_mesh_write_voxel_file": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_int, ctypes.c_int,
+                                                     ctypes.c_uint64, _vp]),
         "svo_mesh_destroy": (None, [_vp]),
         "svo_octree_build_mesh": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_uint64, _vp,
                                                  ctypes.POINTER(_vp)]),
@@ -258,6 +261,23 @@ class PlyLoader:
         dims = (ctypes.c_int * 3)()
         check(lib.svo_mesh_dimensions(self._h, int(side), dims))
         return tuple(dims)
+
+    def convertToVolume(self, path, maxSize, memoryBudget=DEFAULT_MEM, threads=None):
+        """PlyLoader::convertToVolume (PlyLoader.cpp:506-534): the .voxel file
+        of this mesh at suggestedDimensions(maxSize), voxelized with a
+        `threads`-thread pool's sub-block partition (svo_mesh_write_voxel_file;
+        the budget must hold the whole volume, w*h*d bytes)."""
+        threads = int(threads if threads is not None else (os.cpu_count() or 1))
+        check(lib.svo_mesh_write_voxel_file(self._h, os.fsencode(path), int(maxSize), threads, int(memoryBudget),
+                                            None))
+
+    def to_volume(self, side, threads, mem=DEFAULT_MEM, stream=None):
+        """The same volume as a (d, h, w) int32 CUDA tensor (svo_mesh_to_volume)."""
+        import torch
+        w, h, d = self.suggested_dimensions(side)
+        out = torch.empty((d, h, w), dtype=torch.int32, device="cuda")
+        check(lib.svo_mesh_to_volume(self._h, int(side), int(threads), int(mem), _dev_ptr(out), _stream_ptr(stream)))
+        return out
 
     def close(self):
         if self._h:

@@ -35,6 +35,7 @@
 //  5. The octree from the Morton-ordered voxels and the block flags
 //     (build_from_sorted_device).
 #include <algorithm>
+#include <memory>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -876,19 +877,44 @@ int mesh_upload(const MeshHost &h, svo_mesh **out) {
     return SVO_OK;
 }
 
+// The mesh build.  With d_volume == nullptr: VoxelData(PlyLoader*, side,
+// mem) + VoxelOctree, words out.  With d_volume: PlyLoader::convertToVolume
+// (PlyLoader.cpp:506-534, the builder's --mode 1) for a budget that holds
+// the whole volume as one slab, the w*h*d voxel words (x fastest) out in
+// d_volume.  That conversion is one block covering the volume, partitioned
+// from (w, h, d) instead of a cubic cache block, and its buffer is the
+// output: no extraction, no octree.
 int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cudaStream_t st, uint32_t **d_words,
-                      uint64_t *n_words, float center[3]) {
+                      uint64_t *n_words, float center[3], uint32_t *d_volume) {
     if (side < 5 || side > (1 << 20)) return set_error(SVO_ERR_INVALID, "side %d outside [5, 2^20]", side);
     if (threads < 1) return set_error(SVO_ERR_INVALID, "threads must be >= 1");
+    const bool volume = d_volume != nullptr;
     int dims[3];
     mesh_dims(m, side, dims);
-    // VoxelData::init (VoxelData.cpp:211-262) with the loader's cell cost 4 + 1
-    const int lb = cache_block_log2(dims[0], dims[1], dims[2], mem, 5);
-    if (lb < 1)
-        return set_error(SVO_ERR_MEMORY, "memory budget %llu too small for a %dx%dx%d volume",
-                         (unsigned long long)mem, dims[0], dims[1], dims[2]);
     const uint64_t V = round_pow2((uint64_t)std::max(dims[0], std::max(dims[1], dims[2])));
     const int D = log2_floor(V);
+    int lb;
+    if (volume) {
+        // convertToVolume's slab height: the budget over one byte per cell of a w x h slice
+        const uint64_t slice_cost = (uint64_t)dims[0] * (uint64_t)dims[1];
+        const uint64_t slice = std::min<uint64_t>(mem / slice_cost, (uint64_t)dims[2]);
+        if (slice == 0)
+            return set_error(SVO_ERR_MEMORY, "memory budget %llu holds no %dx%d slice", (unsigned long long)mem,
+                             dims[0], dims[1]);
+        if (slice < (uint64_t)dims[2])
+            return set_error(SVO_ERR_LIMIT,
+                             "memory budget %llu gives slabs of %llu slices for depth %d; the GPU conversion takes "
+                             "the whole volume as one slab (mem >= w*h*d = %llu)",
+                             (unsigned long long)mem, (unsigned long long)slice, dims[2],
+                             (unsigned long long)slice_cost * (uint64_t)dims[2]);
+        lb = D;  // one block covers the volume
+    } else {
+        // VoxelData::init (VoxelData.cpp:211-262) with the loader's cell cost 4 + 1
+        lb = cache_block_log2(dims[0], dims[1], dims[2], mem, 5);
+        if (lb < 1)
+            return set_error(SVO_ERR_MEMORY, "memory budget %llu too small for a %dx%dx%d volume",
+                             (unsigned long long)mem, dims[0], dims[1], dims[2]);
+    }
     const int B = 1 << lb;
     // VoxelData::getCenter (VoxelData.cpp:297-303)
     for (int k = 0; k < 3; ++k) center[k] = (float)dims[k] * 0.5f / (float)V;
@@ -896,10 +922,12 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
     // PlyLoader::setupBlockProcessing (PlyLoader.cpp:407-437)
     ListGeom g;
     int sub[3] = {B, B, B};
+    if (volume)  // setupBlockProcessing(maxSize, w, h, d, w, h, d): the block is the volume
+        for (int k = 0; k < 3; ++k) sub[k] = dims[k];
     best_partition(sub[0], sub[1], sub[2], threads);
     for (int k = 0; k < 3; ++k) {
         g.sub[k] = sub[k];
-        g.part[k] = B / sub[k];
+        g.part[k] = (volume ? dims[k] : B) / sub[k];
         g.grid[k] = g.part[k] * (dims[k] + B - 1) / B;
         g.dims[k] = dims[k];
         g.cell_h[k] = (float)sub[k] / (float)(side - 4);
@@ -1050,10 +1078,11 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
     Dev<uint32_t> data;
     Dev<uint8_t> counts;
     Dev<float> acc;
-    SVO_ALLOC(data, buf_cells);
+    if (!volume) SVO_ALLOC(data, buf_cells);
+    uint32_t *const data_p = volume ? d_volume : data.p;  // the conversion's buffer is its output
     SVO_ALLOC(counts, buf_cells);
     SVO_ALLOC(acc, (uint64_t)n_l * K);
-    SVO_CUDA_TRY(cudaMemsetAsync(data.p, 0, buf_cells * sizeof(uint32_t), st));
+    SVO_CUDA_TRY(cudaMemsetAsync(data_p, 0, buf_cells * sizeof(uint32_t), st));
     SVO_CUDA_TRY(cudaMemsetAsync(counts.p, 0, buf_cells, st));
     const float hx = 1.0f / (float)(side - 4);
     k_center_table<<<grid_for(n_l), 256, 0, st>>>(n_l, K, hx, acc.p);
@@ -1083,8 +1112,9 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
     SVO_CUDA_TRY(cudaMemsetAsync(dN.p, 0, sizeof(uint64_t), st));
     // Every emitted voxel lies in a brick folded by its block or is a word an
     // earlier block's dropped slice left behind (each emitted once).
-    uint64_t cap = (uint64_t)nb << (3 * g.log_e);
+    uint64_t cap = volume ? 0 : (uint64_t)nb << (3 * g.log_e);
     for (const BlockJob &j : jobs) {
+        if (volume) break;
         int oz = (int)(compact3((uint64_t)j.morton >> 2) << lb);
         int bd = std::min(B, dims[2] - oz);
         if (bd > 0 && (bd & 1) && lb >= 2) cap += (uint64_t)B * B;
@@ -1125,13 +1155,14 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
             fa.acc = acc.p;
             fa.K = K;
             fa.half = 0.5f * hx;
-            fa.data = data.p;
+            fa.data = data_p;
             fa.counts = counts.p;
             fa.next = fold_next.p + (&j - jobs.data());
             unsigned grid = (unsigned)std::min<uint64_t>((j.last - j.first + kFoldWarps - 1) / kFoldWarps, fold_grid);
             k_fold_bricks<<<grid, kFoldWarps * 32, 0, st>>>(fa);
             SVO_LAUNCH_OK("k_fold_bricks");
         }
+        if (volume) continue;  // the folded buffer is the output
         // candidate bricks: folded here, or under an earlier block's dropped
         // slice (all bricks, when those slices are large)
         const uint64_t vol = (uint64_t)fa.buf[0] * fa.buf[1] * fa.buf[2];
@@ -1177,6 +1208,13 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
             ghosts.emplace_back(plane * (uint64_t)(fa.buf[2] - 1), plane * (uint64_t)fa.buf[2]);
             ghost_len += plane;
         }
+    }
+    if (volume) {
+        uint32_t e_v = 0;
+        SVO_CUDA_TRY(cudaMemcpyAsync(&e_v, err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        SVO_CUDA_TRY(cudaStreamSynchronize(st));
+        if (e_v) return set_error(SVO_ERR_DEVICE, "mesh conversion check failed (flags %u)", e_v);
+        return SVO_OK;
     }
     uint64_t N = 0;
     uint32_t e_h = 0;
@@ -1298,9 +1336,54 @@ extern "C" int svo_octree_build_mesh(const svo_mesh *m, int side, int threads, u
     uint32_t *dw = nullptr;
     uint64_t nw = 0;
     float center[3];
-    int rc = build_mesh_device(m, side, threads, mem, (cudaStream_t)stream, &dw, &nw, center);
+    int rc = build_mesh_device(m, side, threads, mem, (cudaStream_t)stream, &dw, &nw, center, nullptr);
     if (rc) return rc;
     return make_handle(dw, nw, center, out);
+}
+
+extern "C" int svo_mesh_to_volume(const svo_mesh *m, int side, int threads, uint64_t mem, uint32_t *d_volume,
+                                  svo_stream stream) {
+    clear_error();
+    if (!m || !d_volume) return set_error(SVO_ERR_INVALID, "null argument");
+    int cur = 0;
+    SVO_CUDA_TRY(cudaGetDevice(&cur));
+    if (cur != m->device) return set_error(SVO_ERR_INVALID, "mesh lives on device %d, current device is %d", m->device, cur);
+    uint32_t *dw = nullptr;
+    uint64_t nw = 0;
+    float center[3];
+    return build_mesh_device(m, side, threads, mem, (cudaStream_t)stream, &dw, &nw, center, d_volume);
+}
+
+extern "C" int svo_mesh_write_voxel_file(const svo_mesh *m, const char *path, int side, int threads, uint64_t mem,
+                                         svo_stream stream) {
+    clear_error();
+    if (!m || !path) return set_error(SVO_ERR_INVALID, "null argument");
+    int dims[3];
+    int rc = svo_mesh_dimensions(m, side, dims);
+    if (rc) return rc;
+    const uint64_t cells = (uint64_t)dims[0] * dims[1] * dims[2];
+    cudaStream_t st = (cudaStream_t)stream;
+    uint32_t *dv = nullptr;
+    SVO_CUDA_TRY(cudaMalloc((void **)&dv, cells * sizeof(uint32_t)));
+    std::unique_ptr<uint32_t, cudaError_t (*)(void *)> dguard(dv, cudaFree);
+    rc = svo_mesh_to_volume(m, side, threads, mem, dv, stream);
+    if (rc) return rc;
+    FILE *fp = fopen(path, "wb");
+    if (!fp) return set_error(SVO_ERR_IO, "cannot open %s", path);
+    std::unique_ptr<FILE, int (*)(FILE *)> fguard(fp, fclose);
+    // the .voxel layout VoxelData reads (VoxelData.cpp:37-48): int32 w, h, d, then the words, x fastest
+    if (fwrite(dims, 4, 3, fp) != 3) return set_error(SVO_ERR_IO, "%s: write failed", path);
+    const uint64_t chunk = 16ull << 20;  // words per staged copy (64 MB)
+    uint32_t *pin = nullptr;
+    SVO_CUDA_TRY(cudaMallocHost((void **)&pin, std::min(chunk, cells) * sizeof(uint32_t)));
+    std::unique_ptr<uint32_t, cudaError_t (*)(void *)> pguard(pin, cudaFreeHost);
+    for (uint64_t c0 = 0; c0 < cells; c0 += chunk) {
+        const uint64_t n = std::min(chunk, cells - c0);
+        SVO_CUDA_TRY(cudaMemcpyAsync(pin, dv + c0, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        SVO_CUDA_TRY(cudaStreamSynchronize(st));
+        if (fwrite(pin, sizeof(uint32_t), n, fp) != n) return set_error(SVO_ERR_IO, "%s: write failed", path);
+    }
+    return SVO_OK;
 }
 
 extern "C" int svo_octree_build_ply(const char *path, int side, int threads, uint64_t mem, svo_stream stream,

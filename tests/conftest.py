@@ -77,6 +77,7 @@ def golden():
         "builds": np.load(os.path.join(GOLDEN, "builds.npz")),
         "codec": np.load(os.path.join(GOLDEN, "codec.npz")),
         "ply": np.load(os.path.join(GOLDEN, "ply.npz")),
+        "volumes": np.load(os.path.join(GOLDEN, "volumes.npz")),
     }
 
 
@@ -111,3 +112,13 @@ def golden_ply(golden):
         mesh = {"pos": g["pos"], "faces": faces, "colors": g["colors"].astype(np.float32),
                 "colors_u8": g["colors"], "normals": g["normals"] if with_n else None, "binary": bool(binary)}
         yield mesh, int(side), int(threads), int(mem), g["words"][wo[k]:wo[k + 1]], g["centers"][k]
+
+
+def golden_volumes(golden):
+    """Yields (mesh, side, threads, mem, volume (d, h, w)) for volumes.npz,
+    whose mesh is ply.npz's (colours as written to its PLY)."""
+    mesh = next(golden_ply(golden))[0]
+    g = golden["volumes"]
+    off = g["offsets"]
+    for k, (side, threads, mem, w, h, d) in enumerate(g["meta"].tolist()):
+        yield mesh, int(side), int(threads), int(mem), g["words"][off[k]:off[k + 1]].reshape(int(d), int(h), int(w))

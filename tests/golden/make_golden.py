@@ -16,6 +16,12 @@ Outputs (all produced by the reference's own code through oracle/_ref):
                for a seeded edge-case mesh (displaced icosphere plus
                degenerate triangles and polygons; the mesh arrays are stored
                too) over thread counts, sides and memory budgets
+  volumes.npz  PlyLoader::convertToVolume's volumes (the builder's --mode 1)
+               for the same mesh, in one slab and in several, produced by the
+               reference's own setupBlockProcessing / processBlock steps
+               (oracle/ref_shim.cpp ref_ply_volume)
+
+  python tests/golden/make_golden.py volumes   writes volumes.npz only
 """
 import hashlib
 import importlib.util
@@ -70,9 +76,37 @@ def golden_grid(shape, density, seed):
     return np.where(occ, vals, 0).astype(np.uint32)
 
 
+# (side, threads, mem) of volumes.npz: one slab, one slab, four slabs of 20 slices
+VOLUME_CASES = [(48, 8, 1 << 30), (57, 16, 1 << 30), (64, 6, 62 * 62 * 20)]
+
+
+def make_volumes(R):
+    g = np.load(os.path.join(OUT, "ply.npz"))
+    flat = g["faces"].tolist()
+    faces, i = [], 0
+    while i < len(flat):
+        faces.append(flat[i + 1:i + 1 + flat[i]])
+        i += 1 + flat[i]
+    vols, meta = [], []
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "m.ply")
+        scenes.write_ply(path, g["pos"], faces, colors=g["colors"])
+        for (side, threads, mem) in VOLUME_CASES:
+            v = R.ply_volume(path, side, mem, threads=threads)
+            vols.append(v.ravel())
+            meta.append((side, threads, mem) + tuple(reversed(v.shape)))
+    np.savez_compressed(os.path.join(OUT, "volumes.npz"), meta=np.array(meta, np.uint64),
+                        offsets=np.cumsum([0] + [v.size for v in vols]).astype(np.uint64),
+                        words=np.concatenate(vols))
+    print("volumes.npz", os.path.getsize(os.path.join(OUT, "volumes.npz")))
+
+
 def main():
     R = Reference()
     R.start_threads(4)
+    if len(sys.argv) > 1 and sys.argv[1] == "volumes":
+        make_volumes(R)
+        return
     # ---- dragon
     path = os.path.join(REF_SRC, "models", "XYZRGB-Dragon.oct")
     raw = open(path, "rb").read()
@@ -143,6 +177,7 @@ def main():
                         words=np.concatenate(wlist), centers=np.array(centers, np.float32))
     for f in ("dragon.npz", "builds.npz", "codec.npz", "ply.npz"):
         print(f, os.path.getsize(os.path.join(OUT, f)))
+    make_volumes(R)
 
 
 if __name__ == "__main__":

@@ -5,7 +5,7 @@ streams and centres."""
 import numpy as np
 import pytest
 
-from conftest import golden_ply
+from conftest import golden_ply, golden_volumes
 
 pytestmark = pytest.mark.gpu
 
@@ -121,3 +121,70 @@ def test_budget_too_small(cuda, svo, scenes):
     with pytest.raises(svo.SvoError) as e:
         svo.VoxelOctree(svo.VoxelData(loader, 64, 10, 4))
     assert e.value.code == svo.SVO_ERR_MEMORY
+
+
+# ---- PlyLoader::convertToVolume (the builder's --mode 1): svo_mesh_to_volume /
+# svo_mesh_write_voxel_file
+
+def test_golden_volumes(cuda, svo, scenes, golden, tmp_path):
+    """The reference's volumes in the committed fixture: the one-slab cases
+    bit for bit; a budget that gives several slabs is refused."""
+    n = 0
+    for mesh, side, threads, mem, vol in golden_volumes(golden):
+        path = str(tmp_path / "g.ply")
+        scenes.write_ply(path, mesh["pos"], mesh["faces"], colors=mesh["colors_u8"])
+        loader = svo.PlyLoader(path)
+        w, h, d = loader.suggested_dimensions(side)
+        if mem >= w * h * d:
+            got = loader.to_volume(side, threads, mem).cpu().numpy().view(np.uint32)
+            assert np.array_equal(got, vol), (side, threads, mem)
+            n += 1
+        else:
+            with pytest.raises(svo.SvoError) as e:
+                loader.to_volume(side, threads, mem)
+            assert e.value.code == svo.SVO_ERR_LIMIT
+    assert n == 2
+
+
+@pytest.mark.parametrize("level,side,threads", [(3, 64, 4), (4, 100, 16), (4, 77, 3), (3, 9, 2), (5, 256, 8)])
+def test_volume_matches_oracle(cuda, svo, oracle, scenes, level, side, threads):
+    pos, faces, col = scenes.edge_case_mesh(level, side + threads)
+    loader = svo.PlyLoader.from_arrays(pos, faces, colors=col.astype(np.float32))
+    got = loader.to_volume(side, threads, 1 << 30).cpu().numpy().view(np.uint32)
+    ref = oracle.mesh_to_volume(pos, faces, side, threads, 1 << 30, colors=col.astype(np.float32))
+    assert np.array_equal(got, ref)
+    assert np.count_nonzero(ref) > 0
+
+
+def test_voxel_file_written_and_read_back(cuda, svo, oracle, scenes, tmp_path):
+    """convertToVolume's file is VoxelData's .voxel layout: the header and
+    words of the device volume, and the .voxel build of it is the oracle's
+    build of the same grid."""
+    pos, faces, col = scenes.edge_case_mesh(4, 12)
+    loader = svo.PlyLoader.from_arrays(pos, faces, colors=col.astype(np.float32))
+    path = str(tmp_path / "m.voxel")
+    loader.convertToVolume(path, 96, 1 << 30, threads=8)
+    vol = loader.to_volume(96, 8, 1 << 30).cpu().numpy().view(np.uint32)
+    raw = np.fromfile(path, dtype=np.uint32)
+    d, h, w = vol.shape
+    assert raw[:3].view(np.int32).tolist() == [w, h, d]
+    assert np.array_equal(raw[3:].reshape(d, h, w), vol)
+    tree = svo.VoxelOctree(svo.VoxelData(path, 1 << 30))
+    ow, oc = oracle.build_dense(vol, 1 << 30)
+    assert np.array_equal(tree.words(), ow) and np.array_equal(tree.center(), oc)
+    with pytest.raises(svo.SvoError) as e:  # the budget holds no slice (the reference's ASSERT)
+        loader.to_volume(96, 8, 10)
+    assert e.value.code == svo.SVO_ERR_MEMORY
+
+
+def test_workload_mesh_volume_matches_oracle(cuda, svo, oracle, scenes):
+    """The bench's mesh (327,680 triangles) converted at side 1024 with 16
+    threads: one slab of about 1.06 G voxels within the builder's 1 GiB."""
+    pos, f, col = scenes.displaced_icosphere(7, 3)
+    loader = svo.PlyLoader.from_arrays(pos, f, colors=col.astype(np.float32))
+    w, h, d = loader.suggested_dimensions(1024)
+    assert w * h * d <= 1 << 30
+    got = loader.to_volume(1024, 16, 1 << 30).cpu().numpy().view(np.uint32)
+    ref = oracle.mesh_to_volume(pos, f, 1024, 16, 1 << 30, colors=col.astype(np.float32))
+    assert np.array_equal(got, ref)
+    assert np.count_nonzero(ref) > 1_000_000

@@ -6,7 +6,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import golden_ply
+from conftest import golden_ply, golden_volumes
 
 
 def _be_floats(v):
@@ -94,3 +94,31 @@ def test_icosphere_counts(scenes):
     e = np.sort(np.concatenate([f[:, [0, 1]], f[:, [1, 2]], f[:, [2, 0]]]), axis=1)
     _, cnt = np.unique(e[:, 0] * 10000 + e[:, 1], return_counts=True)
     assert (cnt == 2).all()
+
+
+@pytest.mark.parametrize("side,threads,mem", [(48, 1, 1 << 30), (48, 8, 1 << 30), (57, 16, 1 << 30),
+                                              (64, 6, 62 * 62 * 20),   # slabs of 20 slices, never cleared between
+                                              (41, 4, 39 * 39 * 7 + 5)])  # 7 slabs of 6 slices over an odd depth
+def test_mesh_to_volume_matches_reference(oracle, reference, scenes, tmp_path, side, threads, mem):
+    """PlyLoader::convertToVolume (the builder's --mode 1): the oracle's
+    restatement against the reference's own setupBlockProcessing and
+    processBlock steps, in one slab and in several."""
+    pos, faces, col = scenes.edge_case_mesh(3, side)
+    path = str(tmp_path / "m.ply")
+    scenes.write_ply(path, pos, faces, colors=col)
+    rv = reference.ply_volume(path, side, mem, threads=threads)
+    ov = oracle.mesh_to_volume(pos, faces, side, threads, mem, colors=col.astype(np.float32))
+    assert rv.shape == ov.shape == tuple(reversed(oracle.mesh_dims(pos, faces, side)))
+    assert np.count_nonzero(rv) > 100
+    assert np.array_equal(rv, ov)
+
+
+def test_golden_volumes(oracle, golden):
+    """The oracle's convertToVolume against the reference's volumes in the
+    committed fixture (one slab twice, four slabs once)."""
+    n = 0
+    for mesh, side, threads, mem, vol in golden_volumes(golden):
+        ov = oracle.mesh_to_volume(mesh["pos"], mesh["faces"], side, threads, mem, colors=mesh["colors"])
+        assert np.array_equal(ov, vol), (side, threads, mem)
+        n += 1
+    assert n == 3
