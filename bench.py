@@ -834,6 +834,23 @@ def run_mesh_build(args, torch, svo, scenes, steps=None, warmup=None, check=True
            "e2e_voxels_per_s": round(n_leaves / e2e_s, 1), "ply_load_ms": round(load_s * 1e3, 3),
            "ply_bytes": ply_bytes, "launches_per_build": launches, "kernels": kernels, "cpu_baseline": None,
            "exact_vs_oracle": None}
+    # the same mesh written out as a volume (PlyLoader::convertToVolume, the
+    # builder's --mode 1): device time of svo_mesh_to_volume into one buffer
+    w3, h3, d3 = loader.suggested_dimensions(MESH_SIDE)
+    vol = torch.empty((d3, h3, w3), dtype=torch.int32, device="cuda")
+    vol_ms = []
+    for k in range(warmup + steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        loader.to_volume(MESH_SIDE, MESH_THREADS, MESH_MEM, out=vol)
+        torch.cuda.synchronize()
+        if k >= warmup:
+            vol_ms.append((time.perf_counter() - t0) * 1e3)
+    vol_nz = int(torch.count_nonzero(vol).item())
+    out["to_volume"] = {"cells": w3 * h3 * d3, "dims": [w3, h3, d3], "voxels": vol_nz,
+                        "ms": round(sorted(vol_ms)[len(vol_ms) // 2], 3),
+                        "cells_per_s": round(w3 * h3 * d3 / (sorted(vol_ms)[len(vol_ms) // 2] / 1e3), 1),
+                        "exact_vs_oracle": None, "cpu_baseline": None}
     if check:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import pyoracle
@@ -847,6 +864,15 @@ def run_mesh_build(args, torch, svo, scenes, steps=None, warmup=None, check=True
                                "sample": "the full build (oracle/ply_oracle.c, single-threaded restatement of "
                                          "PlyLoader + VoxelData + VoxelOctree) on the same mesh",
                                "build_s": round(cpu_s, 3)}
+        t0 = time.perf_counter()
+        ov = oracle.mesh_to_volume(pos, faces, MESH_SIDE, MESH_THREADS, MESH_MEM, colors=col.astype(np.float32))
+        cpu_v = time.perf_counter() - t0
+        out["to_volume"]["exact_vs_oracle"] = bool(np.array_equal(ov, vol.cpu().numpy().view(np.uint32)))
+        out["to_volume"]["cpu_baseline"] = {"s": round(cpu_v, 3), "cores": 1, "kind": "port",
+                                            "sample": "oracle/ply_oracle.c's convertToVolume restatement, "
+                                                      "single-threaded, same mesh and parameters"}
+        del ov
+    del vol
     os.unlink(path)
     os.rmdir(tmp)
     return out

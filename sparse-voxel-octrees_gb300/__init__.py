@@ -271,11 +271,14 @@ class PlyLoader:
         check(lib.svo_mesh_write_voxel_file(self._h, os.fsencode(path), int(maxSize), threads, int(memoryBudget),
                                             None))
 
-    def to_volume(self, side, threads, mem=DEFAULT_MEM, stream=None):
-        """The same volume as a (d, h, w) int32 CUDA tensor (svo_mesh_to_volume)."""
+    def to_volume(self, side, threads, mem=DEFAULT_MEM, stream=None, out=None):
+        """The same volume as a (d, h, w) int32 CUDA tensor (svo_mesh_to_volume),
+        written into `out` when given."""
         import torch
         w, h, d = self.suggested_dimensions(side)
-        out = torch.empty((d, h, w), dtype=torch.int32, device="cuda")
+        if out is None:
+            out = torch.empty((d, h, w), dtype=torch.int32, device="cuda")
+        assert tuple(out.shape) == (d, h, w) and out.is_contiguous() and str(out.dtype) == "torch.int32"
         check(lib.svo_mesh_to_volume(self._h, int(side), int(threads), int(mem), _dev_ptr(out), _stream_ptr(stream)))
         return out
 
