@@ -179,7 +179,7 @@ def test_voxel_file_written_and_read_back(cuda, svo, oracle, scenes, tmp_path):
 
 def test_workload_mesh_volume_matches_oracle(cuda, svo, oracle, scenes):
     """The bench's mesh (327,680 triangles) converted at side 1024 with 16
-    threads: one slab of about 1.06 G voxels within the builder's 1 GiB."""
+    threads: one slab of about 1.01 G cells within the builder's 1 GiB."""
     pos, f, col = scenes.displaced_icosphere(7, 3)
     loader = svo.PlyLoader.from_arrays(pos, f, colors=col.astype(np.float32))
     w, h, d = loader.suggested_dimensions(1024)
