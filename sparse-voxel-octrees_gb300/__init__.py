@@ -278,7 +278,8 @@ class PlyLoader:
         w, h, d = self.suggested_dimensions(side)
         if out is None:
             out = torch.empty((d, h, w), dtype=torch.int32, device="cuda")
-        assert tuple(out.shape) == (d, h, w) and out.is_contiguous() and str(out.dtype) == "torch.int32"
+        if tuple(out.shape) != (d, h, w) or not out.is_contiguous() or str(out.dtype) != "torch.int32":
+            raise ValueError("out must be a contiguous int32 CUDA tensor of shape %s" % ((d, h, w),))
         check(lib.svo_mesh_to_volume(self._h, int(side), int(threads), int(mem), _dev_ptr(out), _stream_ptr(stream)))
         return out
 
@@ -350,7 +351,8 @@ class VoxelOctree:
                 g = source.grid
                 d, h, w = g.shape
                 if source.on_device:
-                    assert str(g.dtype) in ("torch.int32", "torch.uint32") and g.is_contiguous()
+                    if str(g.dtype) not in ("torch.int32", "torch.uint32") or not g.is_contiguous():
+                        raise ValueError("a device grid must be a contiguous int32 or uint32 tensor")
                     check(lib.svo_octree_build_dense(_dev_ptr(g), w, h, d, source.mem, 1, _stream_ptr(stream),
                                                      ctypes.byref(self._h)))
                 else:
@@ -492,7 +494,8 @@ class VoxelOctree:
                          outputs=("hit", "t", "leaf", "word", "rgb"), out=None):
         rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 6)
         R = rays.shape[0]
-        assert R == width * height
+        if R != width * height:
+            raise ValueError("%d rays for a %dx%d image" % (R, width, height))
         shapes = {"hit": ((R,), np.uint8), "t": ((R,), np.float32), "leaf": ((R,), np.uint32),
                   "word": ((R,), np.uint32), "rgb": ((R, 3), np.float32), "rgba8": ((R,), np.uint32)}
         res = out if out is not None else {k: np.empty(*shapes[k]) for k in outputs}
@@ -527,7 +530,8 @@ class VoxelOctree:
         p = np.ascontiguousarray(pos, dtype=np.float32).reshape(3)
         if out is None:
             out = torch.empty((height, width), dtype=torch.int32, device="cuda")
-        assert out.is_cuda and out.is_contiguous() and out.numel() == width * height
+        if not (out.is_cuda and out.is_contiguous() and out.numel() == width * height):
+            raise ValueError("out must be a contiguous CUDA tensor of width*height words")
         check(lib.svo_render_frame(self._h, r.ctypes.data_as(_f32p), p.ctypes.data_as(_f32p), width, height, n_strips,
                                    pixel_stride, _dev_ptr(out), _stream_ptr(stream)))
         return out
@@ -555,7 +559,8 @@ class LeafAdam:
         self.t += 1
         for p, (m, v) in zip(self.params, self.state):
             g = p.grad
-            assert p.is_contiguous() and g is not None and g.is_contiguous()
+            if g is None or not (p.is_contiguous() and g.is_contiguous()):
+                raise ValueError("LeafAdam needs contiguous parameters with gradients")
             check(lib.svo_adam_step(_dev_ptr(p), _dev_ptr(g), _dev_ptr(m), _dev_ptr(v), p.numel(), self.lr,
                                     float(self.betas[0]), float(self.betas[1]), self.eps, self.t,
                                     1 if self.zero_grad else 0, _stream_ptr(stream)))
