@@ -243,11 +243,13 @@ int svo_octree_build_mesh(const svo_mesh *mesh, int side, int threads, uint64_t 
  * mesh voxelized at suggestedDimensions(side) = w x h x d with a `threads`
  * thread pool's sub-block partition, written as a .voxel file (int32 w, h,
  * d, then w*h*d words, x fastest, 0 = empty) that svo_octree_build_voxel_file
- * and the reference's VoxelData(path, mem) read.  The reference processes
- * z-slabs of mem / (w*h) slices into one buffer it never clears between
- * slabs; these calls take the case where `mem` holds the whole volume as one
- * slab (mem >= w*h*d) and return SVO_ERR_LIMIT otherwise, SVO_ERR_MEMORY when
- * mem holds no slice (the reference's ASSERT).  The reference's own
+ * and the reference's VoxelData(path, mem) read.  As the reference does,
+ * the volume is processed in z-slabs of S = mem / (w*h) slices through one
+ * w*h*S buffer (words and per-cell counts) that is never cleared between
+ * slabs, so a cell blends with what the slab before left at the same place
+ * and a slab with no triangles repeats the previous slab's words; each slab
+ * contributes its first min(S, d - z) slices.  SVO_ERR_MEMORY when mem holds
+ * no slice (the reference's ASSERT).  The reference's own
  * conversion stops with SIGFPE on x86-64: its progress line divides by a
  * block count only isBlockEmpty raises, which this path never calls.
  * svo_mesh_to_volume leaves the words in d_volume (device memory for the

@@ -265,8 +265,9 @@ class PlyLoader:
     def convertToVolume(self, path, maxSize, memoryBudget=DEFAULT_MEM, threads=None):
         """PlyLoader::convertToVolume (PlyLoader.cpp:506-534): the .voxel file
         of this mesh at suggestedDimensions(maxSize), voxelized with a
-        `threads`-thread pool's sub-block partition (svo_mesh_write_voxel_file;
-        the budget must hold the whole volume, w*h*d bytes)."""
+        `threads`-thread pool's sub-block partition, in z-slabs of
+        memoryBudget // (w*h) slices through one buffer that is never cleared
+        between slabs (svo_mesh_write_voxel_file)."""
         threads = int(threads if threads is not None else (os.cpu_count() or 1))
         check(lib.svo_mesh_write_voxel_file(self._h, os.fsencode(path), int(maxSize), threads, int(memoryBudget),
                                             None))

@@ -245,7 +245,10 @@ struct ListGeom {
     int dims[3];             // volume W/H/D
     int log_e;               // brick edge 2^log_e
     int log_block;           // cache-block edge 2^log_block
-    uint64_t n_blocks;       // Morton-indexed block flags
+    uint64_t n_blocks;       // Morton-indexed block flags (z-slabs in slab mode)
+    int slab_mode;           // 1: blocks are z-slabs of part[2] cell layers (convertToVolume), block
+                             // index = gz / part[2], and pair keys carry it above brick_bits
+    int brick_bits;          // bits of a brick's Morton key
 };
 
 __device__ __forceinline__ int point_to_grid(float p, float s) { return (int)(p * s + 1.0f); }
@@ -292,8 +295,11 @@ __global__ void k_tri_pairs(uint64_t n_tris, const float *__restrict__ tris, Lis
             atomicOr(err, 1u);  // the reference would index past its block offsets
             return;
         }
+        const uint32_t slab = g.slab_mode ? (uint32_t)(gz / g.part[2]) : 0u;
         if (kMode == 0) {
-            uint64_t blk = morton3((uint32_t)(gx / g.part[0]), (uint32_t)(gy / g.part[1]), (uint32_t)(gz / g.part[2]));
+            uint64_t blk = g.slab_mode ? (uint64_t)slab
+                                       : morton3((uint32_t)(gx / g.part[0]), (uint32_t)(gy / g.part[1]),
+                                                 (uint32_t)(gz / g.part[2]));
             if (blk < g.n_blocks) block_flag[blk] = 1;
             else atomicOr(err, 2u);
         }
@@ -309,7 +315,7 @@ __global__ void k_tri_pairs(uint64_t n_tris, const float *__restrict__ tris, Lis
             for (int by = a[1] >> g.log_e; by <= (b[1] >> g.log_e); ++by)
                 for (int bx = a[0] >> g.log_e; bx <= (b[0] >> g.log_e); ++bx) {
                     if (kMode == 1) {
-                        pair_key[o + n] = (uint32_t)morton3((uint32_t)bx, (uint32_t)by, (uint32_t)bz);
+                        pair_key[o + n] = (slab << g.brick_bits) | (uint32_t)morton3((uint32_t)bx, (uint32_t)by, (uint32_t)bz);
                         pair_tri[o + n] = (uint32_t)t;
                         pair_cell[o + n] = (uint32_t)gx + (uint32_t)g.grid[0] * ((uint32_t)gy + (uint32_t)g.grid[1] * (uint32_t)gz);
                     }
@@ -428,6 +434,7 @@ struct FoldArgs {
     uint32_t *data;
     uint8_t *counts;
     uint32_t *next;  // work counter of this launch (zero at launch): bricks taken so far
+    uint32_t brick_mask;  // the brick's Morton key within a pair key (slab mode keys carry the slab above it)
 };
 
 // PlyLoader::writeTriangleCell on a register copy of one buffer cell.
@@ -539,14 +546,15 @@ __global__ void __launch_bounds__(kFoldWarps * 32, 8) k_fold_bricks(FoldArgs a) 
         if (lane == 0) jt = atomicAdd(a.next, 1u);
         const uint32_t j = a.b_first + __shfl_sync(0xffffffffu, jt, 0);
         if (j >= a.b_last) break;
-        const uint32_t key = a.bkey[j];
+        const uint32_t key = a.bkey[j] & a.brick_mask;
         const int ox = (int)(compact3(key) << le), oy = (int)(compact3((uint64_t)key >> 1) << le),
                   oz = (int)(compact3((uint64_t)key >> 2) << le);
         __syncwarp();
         for (int i = lane; i < E3; i += 32) {
             int x = ox + (i & (E - 1)), y = oy + ((i >> le) & (E - 1)), z = oz + (i >> (2 * le));
             uint32_t wv = 0, cv = 0;
-            if (x < end0 && y < end1 && z < end2) {
+            // a slab's bricks may start below its first slice (z-slabs need not be brick-aligned)
+            if (x >= a.org[0] && y >= a.org[1] && z >= a.org[2] && x < end0 && y < end1 && z < end2) {
                 uint64_t bi = (uint64_t)(x - a.org[0]) +
                               (uint64_t)a.buf[0] * ((uint64_t)(y - a.org[1]) + (uint64_t)a.buf[1] * (uint64_t)(z - a.org[2]));
                 wv = a.data[bi];
@@ -654,6 +662,7 @@ __global__ void __launch_bounds__(kFoldWarps * 32, 8) k_fold_bricks(FoldArgs a) 
         for (int i = lane; i < E3; i += 32) {
             if (!((sm.touched[i >> 5] >> (i & 31)) & 1u)) continue;
             int x = ox + (i & (E - 1)), y = oy + ((i >> le) & (E - 1)), z = oz + (i >> (2 * le));
+            if (x < a.org[0] || y < a.org[1] || z < a.org[2] || x >= end0 || y >= end1 || z >= end2) continue;
             uint64_t bi = (uint64_t)(x - a.org[0]) +
                           (uint64_t)a.buf[0] * ((uint64_t)(y - a.org[1]) + (uint64_t)a.buf[1] * (uint64_t)(z - a.org[2]));
             a.data[bi] = sm.w[i];
@@ -879,11 +888,11 @@ int mesh_upload(const MeshHost &h, svo_mesh **out) {
 
 // The mesh build.  With d_volume == nullptr: VoxelData(PlyLoader*, side,
 // mem) + VoxelOctree, words out.  With d_volume: PlyLoader::convertToVolume
-// (PlyLoader.cpp:506-534, the builder's --mode 1) for a budget that holds
-// the whole volume as one slab, the w*h*d voxel words (x fastest) out in
-// d_volume.  That conversion is one block covering the volume, partitioned
-// from (w, h, d) instead of a cubic cache block, and its buffer is the
-// output: no extraction, no octree.
+// (PlyLoader.cpp:506-534, the builder's --mode 1), the w*h*d voxel words (x
+// fastest) out in d_volume.  Its blocks are z-slabs of S = mem / (w*h)
+// slices, partitioned from (w, h, S), folded one after another into one
+// w*h*S buffer that is never cleared (the reference reuses `data`), each
+// slab's first min(S, d - z) slices copied out; no extraction, no octree.
 int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cudaStream_t st, uint32_t **d_words,
                       uint64_t *n_words, float center[3], uint32_t *d_volume) {
     if (side < 5 || side > (1 << 20)) return set_error(SVO_ERR_INVALID, "side %d outside [5, 2^20]", side);
@@ -894,6 +903,7 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
     const uint64_t V = round_pow2((uint64_t)std::max(dims[0], std::max(dims[1], dims[2])));
     const int D = log2_floor(V);
     int lb;
+    int slab = 0, n_slabs = 0;  // volume mode: slices per slab, slabs
     if (volume) {
         // convertToVolume's slab height: the budget over one byte per cell of a w x h slice
         const uint64_t slice_cost = (uint64_t)dims[0] * (uint64_t)dims[1];
@@ -901,13 +911,9 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
         if (slice == 0)
             return set_error(SVO_ERR_MEMORY, "memory budget %llu holds no %dx%d slice", (unsigned long long)mem,
                              dims[0], dims[1]);
-        if (slice < (uint64_t)dims[2])
-            return set_error(SVO_ERR_LIMIT,
-                             "memory budget %llu gives slabs of %llu slices for depth %d; the GPU conversion takes "
-                             "the whole volume as one slab (mem >= w*h*d = %llu)",
-                             (unsigned long long)mem, (unsigned long long)slice, dims[2],
-                             (unsigned long long)slice_cost * (uint64_t)dims[2]);
-        lb = D;  // one block covers the volume
+        slab = (int)slice;
+        n_slabs = (dims[2] + slab - 1) / slab;
+        lb = D;  // bricks are keyed over the whole power-of-two volume
     } else {
         // VoxelData::init (VoxelData.cpp:211-262) with the loader's cell cost 4 + 1
         lb = cache_block_log2(dims[0], dims[1], dims[2], mem, 5);
@@ -921,26 +927,29 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
 
     // PlyLoader::setupBlockProcessing (PlyLoader.cpp:407-437)
     ListGeom g;
-    int sub[3] = {B, B, B};
-    if (volume)  // setupBlockProcessing(maxSize, w, h, d, w, h, d): the block is the volume
-        for (int k = 0; k < 3; ++k) sub[k] = dims[k];
+    // block edges: the cubic cache block, or convertToVolume's w x h x S slab
+    // (setupBlockProcessing(maxSize, w, h, S, w, h, d))
+    const int blk[3] = {volume ? dims[0] : B, volume ? dims[1] : B, volume ? slab : B};
+    int sub[3] = {blk[0], blk[1], blk[2]};
     best_partition(sub[0], sub[1], sub[2], threads);
     for (int k = 0; k < 3; ++k) {
         g.sub[k] = sub[k];
-        g.part[k] = (volume ? dims[k] : B) / sub[k];
-        g.grid[k] = g.part[k] * (dims[k] + B - 1) / B;
+        g.part[k] = blk[k] / sub[k];
+        g.grid[k] = g.part[k] * (dims[k] + blk[k] - 1) / blk[k];  // the reference's order: multiply, then divide
         g.dims[k] = dims[k];
         g.cell_h[k] = (float)sub[k] / (float)(side - 4);
     }
     g.grid_scale = (float)(side - 4);
     g.log_e = std::min(3, lb);  // 8^3 bricks (the block edge when smaller); pairs carry their sub-block
     g.log_block = lb;
+    g.slab_mode = volume ? 1 : 0;
+    g.brick_bits = 3 * (D - g.log_e);
     const int lbv = D - lb;  // log2 of blocks per axis
-    g.n_blocks = 1ull << (3 * lbv);
+    g.n_blocks = volume ? (uint64_t)n_slabs : 1ull << (3 * lbv);
     if (g.n_blocks > (1ull << 27))
         return set_error(SVO_ERR_LIMIT, "memory budget gives %llu cache blocks; the GPU build supports at most 2^27",
                          (unsigned long long)g.n_blocks);
-    const int key_bits = 3 * (D - g.log_e);
+    const int key_bits = g.brick_bits + (volume ? log2_floor(round_pow2((uint64_t)n_slabs)) : 0);
     if (key_bits > 32) return set_error(SVO_ERR_LIMIT, "side %d with %d^3 bricks needs more than 32-bit brick keys",
                                         side, 1 << g.log_e);
     const int K = std::max(sub[0], std::max(sub[1], sub[2]));
@@ -1066,9 +1075,11 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
     rlast.release();
 
     // the persistent block buffer (VoxelData::_bufferedData, zeroed) and the
-    // loader's per-cell counts, sized for the largest block volume
-    uint64_t buf_cells = 1;
+    // loader's per-cell counts, sized for the largest block volume (a whole
+    // w x h x S slab in the conversion)
+    uint64_t buf_cells = volume ? (uint64_t)dims[0] * (uint64_t)dims[1] * (uint64_t)slab : 1;
     for (const BlockJob &j : jobs) {
+        if (volume) break;
         int o[3] = {(int)(compact3(j.morton) << lb), (int)(compact3((uint64_t)j.morton >> 1) << lb),
                     (int)(compact3((uint64_t)j.morton >> 2) << lb)};
         uint64_t v = 1;
@@ -1078,8 +1089,9 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
     Dev<uint32_t> data;
     Dev<uint8_t> counts;
     Dev<float> acc;
-    if (!volume) SVO_ALLOC(data, buf_cells);
-    uint32_t *const data_p = volume ? d_volume : data.p;  // the conversion's buffer is its output
+    const bool direct = volume && n_slabs == 1;  // a one-slab conversion folds straight into its output
+    if (!direct) SVO_ALLOC(data, buf_cells);
+    uint32_t *const data_p = direct ? d_volume : data.p;
     SVO_ALLOC(counts, buf_cells);
     SVO_ALLOC(acc, (uint64_t)n_l * K);
     SVO_CUDA_TRY(cudaMemsetAsync(data_p, 0, buf_cells * sizeof(uint32_t), st));
@@ -1091,6 +1103,72 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
     int dev = 0, sms = 0;
     SVO_CUDA_TRY(cudaGetDevice(&dev));
     SVO_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const unsigned fold_grid = (unsigned)sms * 8, warp_grid = (unsigned)sms * 16;
+    Dev<uint32_t> fold_next;  // one work counter per block's fold launch
+    SVO_ALLOC(fold_next, jobs.size());
+    SVO_CUDA_TRY(cudaMemsetAsync(fold_next.p, 0, jobs.size() * sizeof(uint32_t), st));
+    const uint32_t brick_mask = g.slab_mode ? (uint32_t)((1ull << g.brick_bits) - 1) : 0xFFFFFFFFu;
+    // PlyLoader::processBlock (PlyLoader.cpp:439-458) of job ji, whose buffer
+    // starts at org with edges buf: its bricks' pairs folded into data_p
+    auto fold_block = [&](size_t ji, const int org[3], const int buf[3]) -> int {
+        const BlockJob &j = jobs[ji];
+        if (j.last <= j.first) return SVO_OK;
+        FoldArgs fa;
+        for (int k = 0; k < 3; ++k) {
+            fa.org[k] = org[k];
+            fa.buf[k] = buf[k];
+            fa.sub[k] = sub[k];
+            fa.grid[k] = g.grid[k];
+        }
+        fa.tris = m->d_tris;
+        fa.box = box.p;
+        fa.pair_tri = stri;
+        fa.pair_cell = scell;
+        fa.bkey = bkey.p;
+        fa.bstart = bstart.p;
+        fa.b_first = j.first;
+        fa.b_last = j.last;
+        fa.log_e = g.log_e;
+        fa.acc = acc.p;
+        fa.K = K;
+        fa.half = 0.5f * hx;
+        fa.data = data_p;
+        fa.counts = counts.p;
+        fa.next = fold_next.p + ji;
+        fa.brick_mask = brick_mask;
+        unsigned grid = (unsigned)std::min<uint64_t>((j.last - j.first + kFoldWarps - 1) / kFoldWarps, fold_grid);
+        k_fold_bricks<<<grid, kFoldWarps * 32, 0, st>>>(fa);
+        SVO_LAUNCH_OK("k_fold_bricks");
+        return SVO_OK;
+    };
+
+    if (volume) {
+        // convertToVolume (PlyLoader.cpp:506-534): every slab in order, the
+        // buffer (words and counts) carried over uncleared from the slab
+        // before, its first min(S, d - z) slices copied out -- a slab with no
+        // triangles copies out what the previous one left.
+        const uint64_t plane = (uint64_t)dims[0] * (uint64_t)dims[1];
+        size_t ji = 0;
+        for (int s = 0; s < n_slabs; ++s) {
+            const int org[3] = {0, 0, s * slab}, buf[3] = {dims[0], dims[1], slab};
+            if (ji < jobs.size() && jobs[ji].morton == (uint32_t)s) {
+                int rc = fold_block(ji, org, buf);
+                if (rc) return rc;
+                ++ji;
+            }
+            if (!direct) {
+                const uint64_t nz = (uint64_t)std::min(slab, dims[2] - s * slab);
+                SVO_CUDA_TRY(cudaMemcpyAsync(d_volume + plane * (uint64_t)(s * slab), data_p,
+                                             plane * nz * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
+            }
+        }
+        uint32_t e_v = 0;
+        SVO_CUDA_TRY(cudaMemcpyAsync(&e_v, err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        SVO_CUDA_TRY(cudaStreamSynchronize(st));
+        if (e_v) return set_error(SVO_ERR_DEVICE, "mesh conversion check failed (flags %u)", e_v);
+        if (ji != jobs.size()) return set_error(SVO_ERR_DEVICE, "mesh conversion: slab jobs out of order");
+        return SVO_OK;
+    }
 
     // 4. blocks in order: fold, then extract (and clear) the block's voxels.
     // Counts stay on the device, so the loop queues its work without waiting.
@@ -1112,9 +1190,8 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
     SVO_CUDA_TRY(cudaMemsetAsync(dN.p, 0, sizeof(uint64_t), st));
     // Every emitted voxel lies in a brick folded by its block or is a word an
     // earlier block's dropped slice left behind (each emitted once).
-    uint64_t cap = volume ? 0 : (uint64_t)nb << (3 * g.log_e);
+    uint64_t cap = (uint64_t)nb << (3 * g.log_e);
     for (const BlockJob &j : jobs) {
-        if (volume) break;
         int oz = (int)(compact3((uint64_t)j.morton >> 2) << lb);
         int bd = std::min(B, dims[2] - oz);
         if (bd > 0 && (bd & 1) && lb >= 2) cap += (uint64_t)B * B;
@@ -1125,10 +1202,6 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
     SVO_ALLOC(pay, cap);
     std::vector<std::pair<uint64_t, uint64_t>> ghosts;  // flat ranges of the dropped slices so far
     uint64_t ghost_len = 0;
-    const unsigned fold_grid = (unsigned)sms * 8, warp_grid = (unsigned)sms * 16;
-    Dev<uint32_t> fold_next;  // one work counter per block's fold launch
-    SVO_ALLOC(fold_next, jobs.size());
-    SVO_CUDA_TRY(cudaMemsetAsync(fold_next.p, 0, jobs.size() * sizeof(uint32_t), st));
     for (const BlockJob &j : jobs) {
         FoldArgs fa;
         fa.org[0] = (int)(compact3(j.morton) << lb);
@@ -1137,32 +1210,11 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
         bool inside = true;
         for (int k = 0; k < 3; ++k) {
             fa.buf[k] = std::min(B, dims[k] - fa.org[k]);
-            fa.sub[k] = sub[k];
             if (fa.buf[k] <= 0) inside = false;
         }
         if (!inside) continue;  // VoxelData::prepareDataAccess returns early
-        if (j.last > j.first) {
-            fa.tris = m->d_tris;
-            fa.box = box.p;
-            fa.pair_tri = stri;
-            fa.pair_cell = scell;
-            for (int k = 0; k < 3; ++k) fa.grid[k] = g.grid[k];
-            fa.bkey = bkey.p;
-            fa.bstart = bstart.p;
-            fa.b_first = j.first;
-            fa.b_last = j.last;
-            fa.log_e = g.log_e;
-            fa.acc = acc.p;
-            fa.K = K;
-            fa.half = 0.5f * hx;
-            fa.data = data_p;
-            fa.counts = counts.p;
-            fa.next = fold_next.p + (&j - jobs.data());
-            unsigned grid = (unsigned)std::min<uint64_t>((j.last - j.first + kFoldWarps - 1) / kFoldWarps, fold_grid);
-            k_fold_bricks<<<grid, kFoldWarps * 32, 0, st>>>(fa);
-            SVO_LAUNCH_OK("k_fold_bricks");
-        }
-        if (volume) continue;  // the folded buffer is the output
+        int rc = fold_block((size_t)(&j - jobs.data()), fa.org, fa.buf);
+        if (rc) return rc;
         // candidate bricks: folded here, or under an earlier block's dropped
         // slice (all bricks, when those slices are large)
         const uint64_t vol = (uint64_t)fa.buf[0] * fa.buf[1] * fa.buf[2];
@@ -1208,13 +1260,6 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
             ghosts.emplace_back(plane * (uint64_t)(fa.buf[2] - 1), plane * (uint64_t)fa.buf[2]);
             ghost_len += plane;
         }
-    }
-    if (volume) {
-        uint32_t e_v = 0;
-        SVO_CUDA_TRY(cudaMemcpyAsync(&e_v, err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-        SVO_CUDA_TRY(cudaStreamSynchronize(st));
-        if (e_v) return set_error(SVO_ERR_DEVICE, "mesh conversion check failed (flags %u)", e_v);
-        return SVO_OK;
     }
     uint64_t N = 0;
     uint32_t e_h = 0;

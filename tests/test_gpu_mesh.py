@@ -127,23 +127,20 @@ def test_budget_too_small(cuda, svo, scenes):
 # svo_mesh_write_voxel_file
 
 def test_golden_volumes(cuda, svo, scenes, golden, tmp_path):
-    """The reference's volumes in the committed fixture: the one-slab cases
-    bit for bit; a budget that gives several slabs is refused."""
-    n = 0
+    """The reference's volumes in the committed fixture bit for bit: two
+    budgets that hold the volume as one slab, one that gives four slabs of
+    20 slices."""
+    n = multi = 0
     for mesh, side, threads, mem, vol in golden_volumes(golden):
         path = str(tmp_path / "g.ply")
         scenes.write_ply(path, mesh["pos"], mesh["faces"], colors=mesh["colors_u8"])
         loader = svo.PlyLoader(path)
         w, h, d = loader.suggested_dimensions(side)
-        if mem >= w * h * d:
-            got = loader.to_volume(side, threads, mem).cpu().numpy().view(np.uint32)
-            assert np.array_equal(got, vol), (side, threads, mem)
-            n += 1
-        else:
-            with pytest.raises(svo.SvoError) as e:
-                loader.to_volume(side, threads, mem)
-            assert e.value.code == svo.SVO_ERR_LIMIT
-    assert n == 2
+        got = loader.to_volume(side, threads, mem).cpu().numpy().view(np.uint32)
+        assert np.array_equal(got, vol), (side, threads, mem)
+        n += 1
+        multi += mem < w * h * d
+    assert n == 3 and multi == 1
 
 
 @pytest.mark.parametrize("level,side,threads", [(3, 64, 4), (4, 100, 16), (4, 77, 3), (3, 9, 2), (5, 256, 8)])
@@ -154,6 +151,48 @@ def test_volume_matches_oracle(cuda, svo, oracle, scenes, level, side, threads):
     ref = oracle.mesh_to_volume(pos, faces, side, threads, 1 << 30, colors=col.astype(np.float32))
     assert np.array_equal(got, ref)
     assert np.count_nonzero(ref) > 0
+
+
+@pytest.mark.parametrize("level,side,threads,slices", [(4, 41, 4, 6), (3, 64, 8, 1), (4, 77, 3, 13), (3, 50, 16, 7),
+                                                      (4, 100, 6, 16)])
+def test_volume_slabs_match_oracle(cuda, svo, oracle, scenes, level, side, threads, slices):
+    """Budgets of `slices` w x h slices: the volume is converted slab by slab
+    (slabs not aligned to the 8^3 bricks, the last one partial) through a
+    buffer that keeps the previous slab's words and counts."""
+    pos, faces, col = scenes.edge_case_mesh(level, side + slices)
+    loader = svo.PlyLoader.from_arrays(pos, faces, colors=col.astype(np.float32))
+    w, h, d = loader.suggested_dimensions(side)
+    mem = w * h * slices + w * h // 2
+    assert slices < d
+    got = loader.to_volume(side, threads, mem).cpu().numpy().view(np.uint32)
+    ref = oracle.mesh_to_volume(pos, faces, side, threads, mem, colors=col.astype(np.float32))
+    assert np.array_equal(got, ref), (side, threads, slices)
+    assert np.count_nonzero(ref) > 0
+
+
+def test_volume_empty_slabs_repeat_the_buffer(cuda, svo, oracle, scenes):
+    """Two blobs far apart in z: the slabs between them hold no triangles, so
+    the reference copies out the buffer the last folded slab left, and so
+    does the device conversion."""
+    pos, faces, col = scenes.edge_case_mesh(3, 5)
+    lo, hi = pos.min(axis=0), pos.max(axis=0)
+    small = (pos - lo) / float((hi - lo).max()) * np.float32(0.25)
+    pos2 = np.concatenate([small, small + np.array([0.1, 0.0, 1.0], np.float32)]).astype(np.float32)
+    n = pos.shape[0]
+    faces2 = list(faces) + [[v + n for v in fc] for fc in faces]
+    col2 = np.concatenate([col, col]).astype(np.float32)
+    loader = svo.PlyLoader.from_arrays(pos2, faces2, colors=col2)
+    side, threads = 80, 4
+    w, h, d = loader.suggested_dimensions(side)
+    mem = w * h * 9
+    got = loader.to_volume(side, threads, mem).cpu().numpy().view(np.uint32)
+    ref = oracle.mesh_to_volume(pos2, faces2, side, threads, mem, colors=col2)
+    assert np.array_equal(got, ref)
+    # a slab in the gap repeats the slab before it
+    S = 9
+    assert d > 3 * S
+    assert any(ref[s * S:(s + 1) * S].any() and np.array_equal(ref[s * S:(s + 1) * S], ref[(s - 1) * S:s * S])
+               for s in range(1, d // S))
 
 
 def test_voxel_file_written_and_read_back(cuda, svo, oracle, scenes, tmp_path):
