@@ -736,6 +736,7 @@ def run_dragon_frames(args, torch, svo, scenes, oracle=None):
 
 
 MESH_LEVEL, MESH_SEED, MESH_SIDE, MESH_THREADS, MESH_MEM = 7, 3, 1024, 16, 1 << 30
+MESH_SLAB_MEM = 1 << 28  # 270 of the volume's 1023 slices per slab: four slabs
 
 
 def profiled_launches_per_build():
@@ -838,19 +839,28 @@ def run_mesh_build(args, torch, svo, scenes, steps=None, warmup=None, check=True
     # builder's --mode 1): device time of svo_mesh_to_volume into one buffer
     w3, h3, d3 = loader.suggested_dimensions(MESH_SIDE)
     vol = torch.empty((d3, h3, w3), dtype=torch.int32, device="cuda")
-    vol_ms = []
-    for k in range(warmup + steps):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        loader.to_volume(MESH_SIDE, MESH_THREADS, MESH_MEM, out=vol)
-        torch.cuda.synchronize()
-        if k >= warmup:
-            vol_ms.append((time.perf_counter() - t0) * 1e3)
-    vol_nz = int(torch.count_nonzero(vol).item())
-    out["to_volume"] = {"cells": w3 * h3 * d3, "dims": [w3, h3, d3], "voxels": vol_nz,
-                        "ms": round(sorted(vol_ms)[len(vol_ms) // 2], 3),
-                        "cells_per_s": round(w3 * h3 * d3 / (sorted(vol_ms)[len(vol_ms) // 2] / 1e3), 1),
-                        "exact_vs_oracle": None, "cpu_baseline": None}
+
+    def time_volume(mem):
+        vol_ms = []
+        for k in range(warmup + steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            loader.to_volume(MESH_SIDE, MESH_THREADS, mem, out=vol)
+            torch.cuda.synchronize()
+            if k >= warmup:
+                vol_ms.append((time.perf_counter() - t0) * 1e3)
+        med = sorted(vol_ms)[len(vol_ms) // 2]
+        slab = min(mem // (w3 * h3), d3)
+        return {"cells": w3 * h3 * d3, "dims": [w3, h3, d3], "mem": mem, "slabs": -(-d3 // slab),
+                "voxels": int(torch.count_nonzero(vol).item()), "ms": round(med, 3),
+                "cells_per_s": round(w3 * h3 * d3 / (med / 1e3), 1), "exact_vs_oracle": None}
+
+    # z-slabs of a budget below the volume: the reference's slab loop through
+    # one buffer it never clears
+    out["to_volume_slabs"] = time_volume(MESH_SLAB_MEM)
+    slab_vol = vol.cpu().numpy().view(np.uint32).copy() if check else None
+    out["to_volume"] = time_volume(MESH_MEM)
+    out["to_volume"]["cpu_baseline"] = None
     if check:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import pyoracle
@@ -872,6 +882,9 @@ def run_mesh_build(args, torch, svo, scenes, steps=None, warmup=None, check=True
                                             "sample": "oracle/ply_oracle.c's convertToVolume restatement, "
                                                       "single-threaded, same mesh and parameters"}
         del ov
+        ov = oracle.mesh_to_volume(pos, faces, MESH_SIDE, MESH_THREADS, MESH_SLAB_MEM, colors=col.astype(np.float32))
+        out["to_volume_slabs"]["exact_vs_oracle"] = bool(np.array_equal(ov, slab_vol))
+        del ov, slab_vol
     del vol
     os.unlink(path)
     os.rmdir(tmp)
