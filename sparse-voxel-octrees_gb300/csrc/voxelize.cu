@@ -950,8 +950,9 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
         return set_error(SVO_ERR_LIMIT, "memory budget gives %llu cache blocks; the GPU build supports at most 2^27",
                          (unsigned long long)g.n_blocks);
     const int key_bits = g.brick_bits + (volume ? log2_floor(round_pow2((uint64_t)n_slabs)) : 0);
-    if (key_bits > 32) return set_error(SVO_ERR_LIMIT, "side %d with %d^3 bricks needs more than 32-bit brick keys",
-                                        side, 1 << g.log_e);
+    if (key_bits > 32)
+        return set_error(SVO_ERR_LIMIT, "side %d with %d^3 bricks%s needs more than 32-bit brick keys", side,
+                         1 << g.log_e, volume && n_slabs > 1 ? " and this many slabs" : "");
     const int K = std::max(sub[0], std::max(sub[1], sub[2]));
     const int n_l = std::max(dims[0], std::max(dims[1], dims[2])) + 1;
     if ((uint64_t)n_l * (uint64_t)K > (1ull << 28))
