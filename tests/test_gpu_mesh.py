@@ -211,6 +211,14 @@ def test_voxel_file_written_and_read_back(cuda, svo, oracle, scenes, tmp_path):
     tree = svo.VoxelOctree(svo.VoxelData(path, 1 << 30))
     ow, oc = oracle.build_dense(vol, 1 << 30)
     assert np.array_equal(tree.words(), ow) and np.array_equal(tree.center(), oc)
+    # a budget of 11 slices: the file holds the slab-by-slab volume, the oracle's
+    mem = w * h * 11
+    loader.convertToVolume(path, 96, mem, threads=8)
+    raw = np.fromfile(path, dtype=np.uint32)
+    ref = oracle.mesh_to_volume(pos, faces, 96, 8, mem, colors=col.astype(np.float32))
+    assert raw[:3].view(np.int32).tolist() == [w, h, d]
+    assert np.array_equal(raw[3:].reshape(d, h, w), ref)
+    assert not np.array_equal(ref, vol)
     with pytest.raises(svo.SvoError) as e:  # the budget holds no slice (the reference's ASSERT)
         loader.to_volume(96, 8, 10)
     assert e.value.code == svo.SVO_ERR_MEMORY
