@@ -1090,9 +1090,9 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
     Dev<uint32_t> data;
     Dev<uint8_t> counts;
     Dev<float> acc;
-    const bool direct = volume && n_slabs == 1;  // a one-slab conversion folds straight into its output
-    if (!direct) SVO_ALLOC(data, buf_cells);
-    uint32_t *const data_p = direct ? d_volume : data.p;
+    // the conversion folds every slab in place in its output (region 0 zeroed here)
+    if (!volume) SVO_ALLOC(data, buf_cells);
+    uint32_t *const data_p = volume ? d_volume : data.p;
     SVO_ALLOC(counts, buf_cells);
     SVO_ALLOC(acc, (uint64_t)n_l * K);
     SVO_CUDA_TRY(cudaMemsetAsync(data_p, 0, buf_cells * sizeof(uint32_t), st));
@@ -1110,8 +1110,8 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
     SVO_CUDA_TRY(cudaMemsetAsync(fold_next.p, 0, jobs.size() * sizeof(uint32_t), st));
     const uint32_t brick_mask = g.slab_mode ? (uint32_t)((1ull << g.brick_bits) - 1) : 0xFFFFFFFFu;
     // PlyLoader::processBlock (PlyLoader.cpp:439-458) of job ji, whose buffer
-    // starts at org with edges buf: its bricks' pairs folded into data_p
-    auto fold_block = [&](size_t ji, const int org[3], const int buf[3]) -> int {
+    // `data` starts at org with edges buf: its bricks' pairs folded into it
+    auto fold_block = [&](size_t ji, const int org[3], const int buf[3], uint32_t *data) -> int {
         const BlockJob &j = jobs[ji];
         if (j.last <= j.first) return SVO_OK;
         FoldArgs fa;
@@ -1133,7 +1133,7 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
         fa.acc = acc.p;
         fa.K = K;
         fa.half = 0.5f * hx;
-        fa.data = data_p;
+        fa.data = data;
         fa.counts = counts.p;
         fa.next = fold_next.p + ji;
         fa.brick_mask = brick_mask;
@@ -1144,23 +1144,27 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
     };
 
     if (volume) {
-        // convertToVolume (PlyLoader.cpp:506-534): every slab in order, the
-        // buffer (words and counts) carried over uncleared from the slab
-        // before, its first min(S, d - z) slices copied out -- a slab with no
-        // triangles copies out what the previous one left.
+        // convertToVolume (PlyLoader.cpp:506-534): every slab in order through
+        // a buffer (words and counts) the reference never clears, so slab s
+        // starts from what slab s - 1 left and a slab with no triangles
+        // repeats it.  Here slab s is folded in place in its own output
+        // region, which first receives a copy of region s - 1 (the buffer
+        // after slab s - 1).  The last slab's region holds only its d - z
+        // slices; no triangle reaches a cell at z >= d (their voxel boxes end
+        // at d - 1), so the shorter buffer changes no output cell.
         const uint64_t plane = (uint64_t)dims[0] * (uint64_t)dims[1];
         size_t ji = 0;
         for (int s = 0; s < n_slabs; ++s) {
-            const int org[3] = {0, 0, s * slab}, buf[3] = {dims[0], dims[1], slab};
+            const int nz = std::min(slab, dims[2] - s * slab);
+            uint32_t *region = d_volume + plane * (uint64_t)(s * slab);
+            if (s > 0)
+                SVO_CUDA_TRY(cudaMemcpyAsync(region, region - plane * (uint64_t)slab, plane * (uint64_t)nz * sizeof(uint32_t),
+                                             cudaMemcpyDeviceToDevice, st));
+            const int org[3] = {0, 0, s * slab}, buf[3] = {dims[0], dims[1], nz};
             if (ji < jobs.size() && jobs[ji].morton == (uint32_t)s) {
-                int rc = fold_block(ji, org, buf);
+                int rc = fold_block(ji, org, buf, region);
                 if (rc) return rc;
                 ++ji;
-            }
-            if (!direct) {
-                const uint64_t nz = (uint64_t)std::min(slab, dims[2] - s * slab);
-                SVO_CUDA_TRY(cudaMemcpyAsync(d_volume + plane * (uint64_t)(s * slab), data_p,
-                                             plane * nz * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
             }
         }
         uint32_t e_v = 0;
@@ -1214,7 +1218,7 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
             if (fa.buf[k] <= 0) inside = false;
         }
         if (!inside) continue;  // VoxelData::prepareDataAccess returns early
-        int rc = fold_block((size_t)(&j - jobs.data()), fa.org, fa.buf);
+        int rc = fold_block((size_t)(&j - jobs.data()), fa.org, fa.buf, data_p);
         if (rc) return rc;
         // candidate bricks: folded here, or under an earlier block's dropped
         // slice (all bricks, when those slices are large)
