@@ -890,9 +890,10 @@ int mesh_upload(const MeshHost &h, svo_mesh **out) {
 // mem) + VoxelOctree, words out.  With d_volume: PlyLoader::convertToVolume
 // (PlyLoader.cpp:506-534, the builder's --mode 1), the w*h*d voxel words (x
 // fastest) out in d_volume.  Its blocks are z-slabs of S = mem / (w*h)
-// slices, partitioned from (w, h, S), folded one after another into one
-// w*h*S buffer that is never cleared (the reference reuses `data`), each
-// slab's first min(S, d - z) slices copied out; no extraction, no octree.
+// slices, partitioned from (w, h, S) and folded one after another with the
+// reference's never-cleared buffer (it reuses `data` and the counts), the
+// words folded in place in each slab's output region; no extraction, no
+// octree.
 int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cudaStream_t st, uint32_t **d_words,
                       uint64_t *n_words, float center[3], uint32_t *d_volume) {
     if (side < 5 || side > (1 << 20)) return set_error(SVO_ERR_INVALID, "side %d outside [5, 2^20]", side);
