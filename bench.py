@@ -63,10 +63,13 @@ def parse():
     p.add_argument("--height", type=int, default=H_PIX)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--config", type=int, default=1, choices=[1, 2, 3, 4],
-                   help="workload of the main line: 1 plain traversal of the 2048^3 terrain (default); 2 the "
-                        "327,680-triangle mesh build at 1024^3; 3 batched vs plain over 96 octrees and views; "
-                        "4 differentiable leaf shading fwd+bwd on the 512^3 sphere union")
+    p.add_argument("--config", type=int, default=1, choices=[0, 1, 2, 3, 4],
+                   help="workload of the main line: 0 the 256^3 sphere union, 12 views at 1024x768; 1 plain "
+                        "traversal of the 2048^3 terrain (default); 2 the 327,680-triangle mesh build at 1024^3; "
+                        "3 batched vs plain over 96 octrees and views; 4 differentiable leaf shading fwd+bwd on "
+                        "the 512^3 sphere union")
+    p.add_argument("--sweeps", action="store_true",
+                   help="batched workload: also time the table-cache depths and register budgets")
     p.add_argument("--no-extra", action="store_true",
                    help="skip the other workloads' legs (batched, shading, mesh build, frames) in the default run")
     p.add_argument("--views", type=int, default=96)
@@ -143,6 +146,12 @@ class ClockSampler:
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
                 "samples": len(sm), "interval_ms": 20}
+
+
+def smi_index(local):
+    """nvidia-smi's index of this process's GPU."""
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+    return vis.split(",")[local] if vis else local
 
 
 def dist_setup(args):
@@ -283,6 +292,18 @@ def setup_scene(args, rank, torch, svo, scenes):
     return tree, prim, shadow, cam_slices, shadow_slices, info
 
 
+def workload_config(args, n_words, n_vox, Rp, Rs, world):
+    """The plain-traversal workload's `config`, identical in both arms."""
+    return {"workload": "plain traversal: %d^3 octree (terrain + %d spheres), %d cams %dx%d primary rays "
+                        "+ 1 shadow ray per hit" % (args.side, N_SPHERES, args.cams, args.width, args.height),
+            "outputs": {"primary": "t, leaf word (raymarch's normal), RGBA8 colour (renderTile's packing of "
+                                   "shade()): 12 B/ray", "shadow": "hit flag: 1 B/ray"},
+            "octree_words": int(n_words), "voxels": int(n_vox), "primary_rays": int(Rp), "shadow_rays": int(Rs),
+            "rays_per_step": int(Rp + Rs),
+            "l2": "no flush: octree %.2f GB and rays %.2f GB exceed L2" % (n_words * 4 / 1e9, (Rp + Rs) * 24 / 1e9),
+            "parallelism": "replicas x%d" % world}
+
+
 def _timed(torch, fn, steps, warmup, stream, events=None):
     for _ in range(warmup):
         fn(None)
@@ -333,6 +354,18 @@ def run_ours(args):
                               "gpu_launches": r2["launches_per_build"] * r2["steps"]}))
         return
 
+    if args.config == 0:
+        r0 = run_sphere_views(args, torch, svo, scenes)
+        if rank == 0:
+            print(json.dumps({"metric": "Mrays/s", "value": r0["mrays_s"], "unit": "Mrays/s", "n_gpus": world,
+                              "steps": args.steps, "warmup": args.warmup, "ms_per_step": r0["ms_per_step"],
+                              "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                              "data": "synthetic (seeded sphere union, seeded orbit cameras)",
+                              "config": {"workload": r0["workload"], "l2": r0["l2"]}, "e2e": r0["e2e"],
+                              "roofline": r0["roofline"], "cpu_baseline": r0["cpu_baseline"],
+                              "sphere_views": r0, "gpu_launches": r0["launches_per_step"] * args.steps}))
+        return
+
     if args.config == 3:
         r3 = run_batched(args, torch, svo, scenes)
         if rank == 0:
@@ -380,9 +413,7 @@ def run_ours(args):
     evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
     if world > 1:
         torch.distributed.barrier()
-    vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
-    smi_index = vis.split(",")[local] if vis else local
-    with ClockSampler(smi_index) as clk:
+    with ClockSampler(smi_index(local)) as clk:
         ms = _timed(torch, image_step, args.steps, args.warmup, stream, evs)
     if world > 1:
         torch.distributed.barrier()
@@ -486,11 +517,12 @@ def run_ours(args):
     peaks, peak_kind = load_peaks()
     t_prim_avg = sum(t_prim) / len(t_prim)
     achieved = bytes_prim / (t_prim_avg / 1e3) / 1e9
+    traffic, traffic_source = profiled_traffic(Rp)
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": profiled_traffic(Rp),
+                "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": traffic, "traffic_source": traffic_source,
                 "kernel": "k_trace_single (svo_trace_image, primary rays)", "peak_kind": peak_kind,
-                "algorithmic_bytes_per_launch": bytes_prim, "issue_bound": profiled_issue(),
-                "bytes_per_ray": round(bytes_prim / Rp, 2), "launch_ms": round(t_prim_avg, 3)}
+                "algorithmic_bytes_per_launch": bytes_prim, "bytes_per_ray": round(bytes_prim / Rp, 2),
+                "launch_ms": round(t_prim_avg, 3), "issue_bound": profiled_issue()}
 
     cpu = None
     oracle_parity = None
@@ -510,9 +542,21 @@ def run_ours(args):
         cpu = {"value": round(n / secs / 1e6, 3), "unit": "Mrays/s", "cores": thr, "kind": "port",
                "sample": "%d of %d cameras: %d primary+shadow rays in %.1f s (oracle C restatement of "
                          "VoxelOctree::raymarch, %d threads)" % (ncam, len(cam_slices), n, secs, thr)}
-        oracle_parity = {"cameras": ncam, "rays": n, "exact": bool(exact_cpu),
+        # the octree's words against the oracle's build of the same scene
+        # (CPU scene generator + sorted-voxel build, oracle/scene_build.c)
+        t0 = time.perf_counter()
+        heights, centers, radii = scenes.terrain_scene_params(args.side, N_SPHERES, SCENE_SEED)
+        keys, pay = oracle.scene_voxels(args.side, heights, scenes.sphere_boxes((args.side,) * 3, centers, radii),
+                                        np.concatenate([centers, radii[:, None]], 1), threads=cpu_threads())
+        o_words = oracle.build_sorted(keys, pay, args.side.bit_length() - 1)
+        del keys, pay
+        words_exact = bool(o_words.size == words.size and np.array_equal(o_words, words))
+        del o_words
+        oracle_parity = {"cameras": ncam, "rays": n, "exact": bool(exact_cpu), "words_exact": words_exact,
+                         "words": int(words.size), "oracle_build_s": round(time.perf_counter() - t0, 1),
                          "what": "the timed step's primary t, leaf word and RGBA8 and shadow hit flags against "
-                                 "the oracle's raymarch + shade on the same words and rays, bit for bit"}
+                                 "the oracle's raymarch + shade on the same rays, bit for bit; words_exact: the GPU "
+                                 "build's octree words against the oracle's build of the same scene"}
     if not args.no_extra and world == 1:
         center = tree.center()
         cams = rank_cameras(scenes, args.cams, rank, center)
@@ -520,9 +564,11 @@ def run_ours(args):
                   "dragon": run_dragon_frames(args, torch, svo, scenes, oracle)}
     del words
 
-    extra = extra2 = extra4 = extra_vf = None
+    extra = extra0 = extra2 = extra4 = extra_vf = None
     if not args.no_extra and world == 1:
         del prim, shadow, out_p, out_s, ref_p, ref_s, tree
+        torch.cuda.empty_cache()
+        extra0 = run_sphere_views(args, torch, svo, scenes)
         torch.cuda.empty_cache()
         extra = run_batched(args, torch, svo, scenes)
         torch.cuda.empty_cache()
@@ -533,79 +579,179 @@ def run_ours(args):
         extra_vf = run_voxel_file(args, torch, svo, scenes)
 
     if rank == 0:
+        mr = lambda ms: round(rays_per_step / ms / 1e3, 1)
         line = {
             "metric": "Mrays/s", "value": round(value, 2), "unit": "Mrays/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded terrain + spheres, seeded orbit cameras)",
-            "config": {"workload": "plain traversal: %d^3 octree (terrain + %d spheres), %d cams %dx%d primary rays "
-                                   "+ 1 shadow ray per hit" % (args.side, N_SPHERES, args.cams, args.width,
-                                                               args.height),
-                       "shadow_ray_order": "per camera, by 8x4 pixel tile",
-                       "outputs": {"primary": "t, leaf word (raymarch's normal), RGBA8 colour (renderTile's "
-                                              "packing of shade()): 12 B/ray", "shadow": "hit flag: 1 B/ray"},
-                       "api": "svo_trace_image (primary, 8x4-pixel tiles, persistent) + svo_trace (shadow)",
-                       "octree_words": info["words"], "voxels": info["voxels"], "primary_rays": Rp,
-                       "shadow_rays": Rs, "rays_per_step": rays_per_step,
-                       "l2": "no flush: octree %.2f GB and rays %.2f GB exceed L2" % (info["words"] * 4 / 1e9,
-                                                                                      rays_per_step * 24 / 1e9),
-                       "parallelism": "replicas x%d" % world},
+            "config": workload_config(args, info["words"], info["voxels"], Rp, Rs, world),
+            "api": "svo_trace_image (primary, 8x4-pixel tiles, persistent) + svo_trace (shadow rays, ordered "
+                   "per camera by 8x4 pixel tile)",
             "e2e": e2e, "gpu_launches": 2 * args.steps, "roofline": roofline, "cpu_baseline": cpu,
             "oracle_parity": oracle_parity,
             "clocks": clk.summary(),
-            "plain": {"api": "svo_trace for primary (row order) and shadow rays",
-                      "ms_per_step": round(ms_plain, 3), "mrays_s": round(rays_per_step / ms_plain / 1e3, 1),
-                      "exact_vs_value_path": bool(exact_plain)},
+            "kernel_ms": {"primary": round(t_prim_avg, 3), "shadow": round(sum(t_shadow) / len(t_shadow), 3)},
+            "plain": {"api": "svo_trace for primary (row order) and shadow rays", "ms_per_step": round(ms_plain, 3),
+                      "mrays_s": mr(ms_plain), "exact_vs_value_path": bool(exact_plain)},
             "alt_outputs": alt_outputs,
             "batched": {"api": "svo_batch: 32 image views + shadow view, autotuned, CUDA graph",
-                        "ms_per_step": round(ms_batched, 3), "mrays_s": round(rays_per_step / ms_batched / 1e3, 1),
+                        "ms_per_step": round(ms_batched, 3), "mrays_s": mr(ms_batched),
                         "config": cfg.as_dict(), "exact_vs_value_path": bool(exact_batched)},
+            "build": {"build_s": round(info["build_s"], 3), "build_warm_s": round(info["build_warm_s"], 4),
+                      "voxels_per_s": round(info["voxels"] / info["build_s"], 1),
+                      "warm_voxels_per_s": round(info["voxels"] / info["build_warm_s"], 1),
+                      "warm_words_equal": info["warm_same"], "scene_gen_s": round(info["gen_s"], 3),
+                      "descriptor_table_s": round(info["table_s"], 4),
+                      "descriptor_table_entries": info["table_entries"]},
+            "sphere_views": extra0,
             "batched_vs_plain": extra,
             "fwd_bwd": extra4,
             "mesh_build": extra2,
             "viewer_frames": frames,
             "voxel_file_build": extra_vf,
-            "build": {"build_s": round(info["build_s"], 3), "scene_gen_s": round(info["gen_s"], 3),
-                      "voxels_per_s": round(info["voxels"] / info["build_s"], 1),
-                      "build_warm_s": round(info["build_warm_s"], 4),
-                      "warm_voxels_per_s": round(info["voxels"] / info["build_warm_s"], 1),
-                      "warm_words_equal": info["warm_same"],
-                      "build_note": "build_s is the process's first build (first-touch device allocations); "
-                                    "build_warm_s the same build again, scratch from the library's pool",
-                      "descriptor_table_s": round(info["table_s"], 4),
-                      "descriptor_table_entries": info["table_entries"],
-                      "descriptor_table_bytes": info["table_entries"] * 16},
-            "kernel_ms": {"primary": round(t_prim_avg, 3), "shadow": round(sum(t_shadow) / len(t_shadow), 3)},
         }
+        line["summary"] = summary_of(line)
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
 
 
-def batched_views(n_views, seed=3):
-    """96 (octree, view) pairs: depth U{7..11}, even index -> sphere-union
-    generator (48 spheres), odd -> terrain generator (200 spheres), scene seed
-    = index; one orbit camera each, pixel count log-uniform in
-    [256x256, 1920x1080] at 16:9 clipped to [256, 1920] x [256, 1080]."""
-    rng = np.random.default_rng(seed)
-    specs = []
-    for i in range(1, n_views + 1):
-        depth = int(rng.integers(7, 12))
-        pix = float(np.exp(rng.uniform(np.log(256 * 256), np.log(1920 * 1080))))
-        W = int(min(1920, max(256, round((pix * 16 / 9) ** 0.5))))
-        H = int(min(1080, max(256, round(pix / W))))
-        specs.append((i, 1 << depth, "sphere" if i % 2 == 0 else "terrain", W, H))
-    return specs
+def summary_of(line):
+    """The legs' headline figures, printed last on the line."""
+    g = lambda d, *ks: None if d is None else (g(d.get(ks[0]), *ks[1:]) if len(ks) > 1 else d.get(ks[0]))
+    s = {"plain_traversal_mrays_s": line["value"], "plain_traversal_e2e_mrays_s": g(line, "e2e", "value"),
+         "plain_traversal_exact": g(line, "oracle_parity", "exact"),
+         "plain_traversal_words_exact": g(line, "oracle_parity", "words_exact"),
+         "primary_roofline_frac": g(line, "roofline", "frac"),
+         "cpu_baseline_mrays_s": g(line, "cpu_baseline", "value"),
+         "sphere_views_mrays_s": g(line, "sphere_views", "mrays_s"),
+         "sphere_views_exact": g(line, "sphere_views", "exact_vs_oracle"),
+         "batched_mrays_s": g(line, "batched_vs_plain", "batched_mrays_s"),
+         "plain_image_mrays_s": g(line, "batched_vs_plain", "plain_image_mrays_s"),
+         "plain_queue_mrays_s": g(line, "batched_vs_plain", "plain_mrays_s"),
+         "batched_speedup_vs_best_plain": g(line, "batched_vs_plain", "speedup_vs_best_plain"),
+         "batched_exact_hit_parity": g(line, "batched_vs_plain", "exact_hit_parity"),
+         "fwd_bwd_mrays_s": g(line, "fwd_bwd", "fwd_bwd_mrays_s"),
+         "fwd_bwd_step_ms_with_adam": g(line, "fwd_bwd", "step_ms_with_adam"),
+         "fwd_bwd_hit_leaves_exact": g(line, "fwd_bwd", "check", "hit_leaves_exact"),
+         "fwd_bwd_fd_max_rel": g(line, "fwd_bwd", "check", "fd_max_rel"),
+         "fwd_bwd_fd_own_truncation_max_rel": g(line, "fwd_bwd", "check", "fp64_analytic_vs_fd_max_rel"),
+         "fwd_bwd_richardson_fd_max_rel": g(line, "fwd_bwd", "check", "richardson_fd_max_rel"),
+         "mesh_build_ms": g(line, "mesh_build", "build_ms"),
+         "mesh_build_exact": g(line, "mesh_build", "exact_vs_oracle")}
+    return s
+
+
+def run_sphere_views(args, torch, svo, scenes, n_views=12, W=1024, H=768):
+    """The 256^3 sphere union (48 solid spheres, seed 0), 12 orbit views
+    (radius 2, seeded yaw/pitch) at 1024x768, FP32 primary rays, each view
+    shaded with its own headlight.  A step traces the 12 views with
+    svo_trace_image, one launch per view, returning t, leaf word and RGBA8
+    (12 B/ray).  e2e: svo_trace_image_host per view from pinned host rays.
+    CPU baseline and parity: the oracle's raymarch + shade over all 12 views
+    on all host threads, compared bit for bit."""
+    side = 256
+    grid = scenes.gpu_sphere_scene(side, 48, 0)
+    tree = svo.VoxelOctree(svo.VoxelData(grid))
+    del grid
+    center = tree.center()
+    cams = scenes.orbit_cameras(n_views, 0, center, radius=2.0)
+    lights = [scenes.headlight(c) for c in cams]
+    npix = W * H
+    R = n_views * npix
+    rays = torch.empty((R, 6), dtype=torch.float32, device="cuda")
+    for i, c in enumerate(cams):
+        scenes.gpu_camera_rays(c, W, H, out=rays[i * npix:(i + 1) * npix])
+    out = {"t": torch.empty(R, dtype=torch.float32, device="cuda"),
+           "word": torch.empty(R, dtype=torch.int32, device="cuda"),
+           "rgba8": torch.empty(R, dtype=torch.int32, device="cuda")}
+    views = [(rays[i * npix:(i + 1) * npix], {k: v[i * npix:(i + 1) * npix] for k, v in out.items()}, lights[i])
+             for i in range(n_views)]
+    stream = torch.cuda.current_stream()
+    loads = torch.empty(R, dtype=torch.int32, device="cuda")
+    tree.count_loads(rays, loads=loads)
+    n_loads = int(loads.sum().item())
+    del loads
+    bytes_step = 4 * n_loads + R * (24 + 12)
+
+    def step(ev):
+        for r, o, l in views:
+            tree.trace_image(r, W, H, out=o, light=l, stream=stream)
+
+    with ClockSampler(smi_index(int(os.environ.get("LOCAL_RANK", "0")))) as clk:
+        ms = _timed(torch, step, args.steps, args.warmup, stream) / args.steps
+    assert tree.device_status() == 0
+    gpu = {k: v.cpu().numpy().view(np.uint32) for k, v in out.items()}
+    peaks, peak_kind = load_peaks()
+    achieved = bytes_step / (ms / 1e3) / 1e9
+    res = {"workload": "256^3 sphere union (48 spheres, seed 0), %d orbit views %dx%d, headlight shade" % (
+               n_views, W, H),
+           "api": "svo_trace_image, one launch per view", "rays_per_step": R, "octree_words": tree.num_words(),
+           "ms_per_step": round(ms, 4), "mrays_s": round(R / ms / 1e3, 1), "launches_per_step": n_views,
+           "l2": "no flush: rays %.0f MB + outputs %.0f MB per step exceed L2; the %.1f MB octree stays "
+                 "L2-resident, as it does for the reference's CPU caches" % (R * 24 / 1e6, R * 12 / 1e6,
+                                                                            tree.num_words() * 4 / 1e6),
+           "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                        "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": None,
+                        "traffic_source": "not captured for this workload",
+                        "kernel": "k_trace_single (svo_trace_image)", "peak_kind": peak_kind,
+                        "algorithmic_bytes_per_step": bytes_step, "bytes_per_ray": round(bytes_step / R, 2)},
+           "clocks": clk.summary(), "e2e": None, "cpu_baseline": None, "exact_vs_oracle": None}
+    if not args.no_e2e:
+        h_rays = rays.cpu().pin_memory().numpy()
+        h_out = {k: torch.empty(R, dtype=torch.int32 if k != "t" else torch.float32).pin_memory().numpy()
+                 for k in out}
+        hv = [(h_rays[i * npix:(i + 1) * npix], {k: v[i * npix:(i + 1) * npix] for k, v in h_out.items()},
+               lights[i]) for i in range(n_views)]
+
+        def host_step():
+            for r, o, l in hv:
+                tree.trace_image_host(r, W, H, light=l, out=o)
+
+        for _ in range(max(1, args.warmup)):
+            host_step()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            host_step()
+        e2e_s = (time.perf_counter() - t0) / args.steps
+        exact = all(np.array_equal(h_out[k].view(np.uint32), gpu[k]) for k in out)
+        res["e2e"] = {"value": round(R / e2e_s / 1e6, 1), "unit": "Mrays/s", "h2d_bytes_per_step": R * 24,
+                      "d2h_bytes_per_step": R * 12, "api": "svo_trace_image_host per view, pinned host buffers",
+                      "exact": bool(exact)}
+    if not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import pyoracle
+        pyoracle.build_oracle(with_reference=False)
+        oracle = pyoracle.Oracle()
+        words = tree.words()
+        h = rays.cpu().numpy()
+        threads = cpu_threads()
+        exact, secs = True, 0.0
+        for i in range(n_views):
+            sl = slice(i * npix, (i + 1) * npix)
+            t0 = time.perf_counter()
+            ref = oracle.raymarch(words, h[sl], light=lights[i], threads=threads)
+            secs += time.perf_counter() - t0
+            exact = exact and np.array_equal(gpu["t"][sl], ref["t"].view(np.uint32)) and \
+                np.array_equal(gpu["word"][sl], ref["word"]) and \
+                np.array_equal(gpu["rgba8"][sl], pack_rgba8(ref["grey"], ref["hit"]))
+        res["exact_vs_oracle"] = bool(exact)
+        res["cpu_baseline"] = {"value": round(R / secs / 1e6, 3), "unit": "Mrays/s", "cores": threads,
+                               "kind": "port", "sample": "all %d views (%d rays) once, oracle C restatement of "
+                                                         "VoxelOctree::raymarch + shade" % (n_views, R)}
+    tree.close()
+    return res
 
 
 def run_batched(args, torch, svo, scenes, tune_cache=None):
     """Batched persistent launch (graph-captured, autotuned) against the plain
-    per-view kernel over the 96 views of batched_views; checks exact parity."""
+    per-view kernel over the 96 views of scenes.batched_views; checks exact parity."""
     t0 = time.perf_counter()
     views, plain_out, rays_list = [], [], []
     trees = []
     total_rays = 0
-    for (i, side, gen, W, H) in batched_views(args.views):
+    for (i, side, gen, W, H) in scenes.batched_views(args.views):
         if args.max_side:
             side = min(side, args.max_side)
         grid = scenes.gpu_sphere_scene(side, 48, i) if gen == "sphere" else scenes.gpu_terrain_scene(side, 200, i)
@@ -619,9 +765,9 @@ def run_batched(args, torch, svo, scenes, tune_cache=None):
         mk = lambda: {"t": torch.empty(n, dtype=torch.float32, device="cuda"),
                       "leaf": torch.empty(n, dtype=torch.int32, device="cuda"),
                       "rgb": torch.empty((n, 3), dtype=torch.float32, device="cuda")}
-        out_b, out_p = mk(), mk()
+        out_b, out_p, out_i = mk(), mk(), mk()
         views.append({"octree": tree, "rays": rays, "width": W, "height": H, "light": light, "out": out_b})
-        plain_out.append((tree, rays, light, out_p))
+        plain_out.append((tree, rays, light, out_p, W, H, out_i))
         total_rays += n
     torch.cuda.empty_cache()
     setup_s = time.perf_counter() - t0
@@ -635,8 +781,12 @@ def run_batched(args, torch, svo, scenes, tune_cache=None):
     stream = torch.cuda.current_stream()
 
     def plain_step():
-        for tree, rays, light, out in plain_out:
+        for tree, rays, light, out, _, _, _ in plain_out:
             tree.trace(rays, out=out, light=light, stream=stream)
+
+    def image_step():
+        for tree, rays, light, _, W, H, out in plain_out:
+            tree.trace_image(rays, W, H, out=out, light=light, stream=stream)
 
     def batched_step():
         batch.launch_graph(stream)
@@ -654,10 +804,31 @@ def run_batched(args, torch, svo, scenes, tune_cache=None):
         return e0.elapsed_time(e1) / args.steps
 
     ms_plain = timed(plain_step)
+    ms_image = timed(image_step)
     ms_batched = timed(batched_step)
     same = lambda: all(torch.equal(v["out"][k], po[3][k]) for v, po in zip(views, plain_out)
                        for k in ("t", "leaf", "rgb"))
     exact = same()
+    exact_image = all(torch.equal(po[6][k], po[3][k]) for po in plain_out for k in ("t", "leaf", "rgb"))
+    ms_best_plain = min(ms_plain, ms_image)
+    res = {"workload": None, "rays_per_step": total_rays, "octree_words": int(sum(t.num_words() for t in trees)),
+           "plain_ms": round(ms_plain, 3), "plain_image_ms": round(ms_image, 3), "batched_ms": round(ms_batched, 3),
+           "plain_mrays_s": round(total_rays / ms_plain / 1e3, 1),
+           "plain_image_mrays_s": round(total_rays / ms_image / 1e3, 1),
+           "batched_mrays_s": round(total_rays / ms_batched / 1e3, 1),
+           "speedup": round(ms_plain / ms_batched, 3),
+           "speedup_vs_best_plain": round(ms_best_plain / ms_batched, 3),
+           "best_plain": "svo_trace_image" if ms_image <= ms_plain else "svo_trace",
+           "exact_hit_parity": bool(exact and exact_image),
+           "plain_apis": {"plain": "96 svo_trace launches (persistent, 32 rays per queue access, row order)",
+                          "plain_image": "96 svo_trace_image launches (persistent, 8x4-pixel tiles)"},
+           "config": cfg.as_dict(), "autotune_s": round(tune_s, 1), "setup_s": round(setup_s, 1),
+           "launches": {"plain": len(views), "plain_image": len(views), "batched": 1}}
+    depth_hi = min(11, args.max_side.bit_length() - 1) if args.max_side else 11
+    res["workload"] = ("%d octrees (depth 7-%d, sphere/terrain generators, seeds 1..%d), one view each, "
+                       "256x256..1920x1080 log-uniform pixels" % (len(views), depth_hi, len(views)))
+    if not getattr(args, "sweeps", False):
+        return res
     # the chosen plain-tile shape (or the default tile shape, when lane refill
     # won) at each per-warp table cache depth the autotuner tries
     base = cfg.as_dict()
@@ -679,20 +850,11 @@ def run_batched(args, torch, svo, scenes, tune_cache=None):
         c = svo.default_config(**dict(rbase, reg_cap=cap))
         ms = timed(lambda: batch.trace(c, stream))
         reg_sweep[str(cap)] = {"ms": round(ms, 3), "exact_hit_parity": bool(same())}
-    depth_hi = min(11, args.max_side.bit_length() - 1) if args.max_side else 11
-    return {"workload": "%d octrees (depth 7-%d, sphere/terrain generators, seeds 1..%d), one view each, "
-                        "256x256..1920x1080 log-uniform pixels" % (len(views), depth_hi, len(views)),
-            "rays_per_step": total_rays, "octree_words": int(sum(t.num_words() for t in trees)),
-            "plain_ms": round(ms_plain, 3), "batched_ms": round(ms_batched, 3),
-            "plain_mrays_s": round(total_rays / ms_plain / 1e3, 1),
-            "batched_mrays_s": round(total_rays / ms_batched / 1e3, 1),
-            "speedup": round(ms_plain / ms_batched, 3), "exact_hit_parity": bool(exact),
-            "table_cache_sweep": {"shape": {k: v for k, v in base.items() if k not in ("cache_entries", "reg_cap")},
-                                  "ms_by_cache_entries": cache_sweep},
-            "register_budget_sweep": {"shape": {k: v for k, v in rbase.items() if k != "reg_cap"},
-                                      "ms_by_reg_cap": reg_sweep},
-            "config": cfg.as_dict(), "autotune_s": round(tune_s, 1), "setup_s": round(setup_s, 1),
-            "launches": {"plain": len(views), "batched": 1}}
+    res["table_cache_sweep"] = {"shape": {k: v for k, v in base.items() if k not in ("cache_entries", "reg_cap")},
+                                "ms_by_cache_entries": cache_sweep}
+    res["register_budget_sweep"] = {"shape": {k: v for k, v in rbase.items() if k != "reg_cap"},
+                                    "ms_by_reg_cap": reg_sweep}
+    return res
 
 
 FRAME_W, FRAME_H, FRAME_STRIPS = 1280, 720, 16  # the viewer's GWidth, GHeight, NumThreads (Main.cpp:47-59)
@@ -997,6 +1159,21 @@ def run_leaf_shading(args, torch, svo, scenes, n_steps=200):
     scale = 2.0 / (3 * R)
     setup_s = time.perf_counter() - t0
     stream = torch.cuda.current_stream()
+    # one untimed forward + adjoint at the initial parameters, for the checks
+    # against the oracle after the timed loop
+    check = None
+    if not args.no_cpu:
+        tree.diff_forward(rays, W, H, V, lights, p_rgb.detach(), p_n.detach(), rgb, hit_leaf=leaf, stream=stream)
+        torch.sub(rgb, target, out=d_rgb)
+        d_rgb.mul_(scale)
+        tree.diff_backward(rays, W, H, V, lights, p_rgb.detach(), p_n.detach(), d_rgb, g_rgb, g_n, hit_leaf=leaf,
+                           stream=stream)
+        torch.cuda.synchronize()
+        check = {"leaf": leaf.cpu().numpy().view(np.uint32), "g_rgb": g_rgb.cpu().numpy(), "g_n": g_n.cpu().numpy(),
+                 "p_rgb": p_rgb.detach().cpu().numpy(), "p_n": p_n.detach().cpu().numpy(),
+                 "target": target.cpu().numpy()}
+        g_rgb.zero_()
+        g_n.zero_()
     ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(n_steps)]
     losses = []
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -1023,6 +1200,8 @@ def run_leaf_shading(args, torch, svo, scenes, n_steps=200):
     bwd = [e[2].elapsed_time(e[3]) for e in ev]  # the adjoint kernel
     step_ms = e0.elapsed_time(e1) / n_steps
     fb = (sum(fwd) + sum(bwd)) / n_steps
+    if check is not None:
+        check = shading_check(tree, rays.cpu().numpy(), lights.cpu().numpy(), W * H, check)
     return {"workload": "512^3 sphere union (160 spheres, seed 7), %d octree words; 24 views 512x512; per-leaf FP32 "
                         "rgb+normal params; L2 loss vs 3-octave noise colour field; Adam lr 1e-2" % nw,
             "rays_per_step": R, "steps": n_steps, "fwd_ms": round(sum(fwd) / n_steps, 3),
@@ -1031,20 +1210,80 @@ def run_leaf_shading(args, torch, svo, scenes, n_steps=200):
                             "the loss gradient and svo_adam_step (one pass per parameter tensor, gradient zeroed "
                             "in the same pass)",
             "step_ms_with_adam": round(step_ms, 3),
-            "loss": [[k, round(float(v.item()), 6)] for k, v in losses], "setup_s": round(setup_s, 1)}
+            "loss_first_last": [[k, round(float(v.item()), 6)] for k, v in (losses[0], losses[-1])],
+            "setup_s": round(setup_s, 1), "check": check}
+
+
+def shading_check(tree, rays, lights, per_view, c, n_leaves=256, h=1e-3):
+    """The leaf-shading leg's forward and adjoint at the initial parameters
+    against the oracle: every ray's hit leaf against the oracle's raymarch
+    (VoxelOctree::raymarch, leaf index at VoxelOctree.cpp:282), and the
+    adjoint's gradient against plain FP64 central differences (h = 1e-3) of
+    the same L2 loss on 256 random hit leaves (oracle/diff_oracle.py)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import diff_oracle
+    import pyoracle
+    pyoracle.build_oracle(with_reference=False)
+    oracle = pyoracle.Oracle()
+    t0 = time.perf_counter()
+    ref = oracle.raymarch(tree.words(), rays, threads=cpu_threads())
+    leaf = np.where(ref["hit"] == 1, ref["leaf"], np.uint32(0xFFFFFFFF)).astype(np.uint32)
+    hit_exact = bool(np.array_equal(leaf, c["leaf"]))
+    hit_leaves = np.unique(leaf[leaf != 0xFFFFFFFF])
+    pick = np.random.default_rng(5).choice(hit_leaves, size=min(n_leaves, hit_leaves.size), replace=False)
+    ray_light = np.repeat(lights, per_view, axis=0)
+    w = 1.0 / (3 * rays.shape[0])
+    fd_rgb, fd_n, kink = diff_oracle.finite_differences(leaf, rays[:, 3:], ray_light, c["p_rgb"], c["p_n"],
+                                                        c["target"], w, pick, h=h)
+    li = pick.astype(np.int64)
+    rel = lambda g, r: np.linalg.norm(g - r, axis=-1) / np.linalg.norm(r, axis=-1)
+    smooth = ~kink.any(axis=1)
+    e_rgb = rel(c["g_rgb"][li], fd_rgb)
+    e_n = rel(c["g_n"][li][smooth], fd_n[smooth])
+    fd_max = float(max(e_rgb.max(), e_n.max() if smooth.any() else 0.0))
+    # the same differences against the FP64 analytic gradient (how far plain
+    # central differences at this h are from the exact derivative: their
+    # O(h^2) term grows as 1/|p|^2 for short normal parameters), and the
+    # adjoint against Richardson-extrapolated differences (h, h/2)
+    a_rgb, a_n = diff_oracle.gradient(leaf, rays[:, 3:], ray_light, c["p_rgb"], c["p_n"], c["target"], w,
+                                      c["p_rgb"].shape[0], leaves=pick)
+    fd_floor = float(max(rel(a_rgb, fd_rgb).max(), rel(a_n[smooth], fd_n[smooth]).max() if smooth.any() else 0.0))
+    r_rgb, r_n, _ = diff_oracle.finite_differences(leaf, rays[:, 3:], ray_light, c["p_rgb"], c["p_n"], c["target"],
+                                                   w, pick, h=h, richardson=True)
+    rich = float(max(rel(c["g_rgb"][li], r_rgb).max(), rel(c["g_n"][li][smooth], r_n[smooth]).max()))
+    exact = float(max(rel(c["g_rgb"][li], a_rgb).max(), rel(c["g_n"][li], a_n).max()))
+    worst = int(np.argmax(rel(c["g_n"][li], fd_n)))
+    return {"hit_leaves_exact": hit_exact, "rays": int(rays.shape[0]), "hit_rays": int((leaf != 0xFFFFFFFF).sum()),
+            "fd_leaves": int(pick.size), "fd_h": h, "fd_max_rel": round(fd_max, 8),
+            "fd_rgb_max_rel": round(float(e_rgb.max()), 8),
+            "fd_normal_max_rel": round(float(e_n.max()), 8) if smooth.any() else None,
+            "fd_kink_leaves_left_out": int((~smooth).sum()),
+            "fp64_analytic_vs_fd_max_rel": round(fd_floor, 8),
+            "worst_leaf_normal_param_norm": round(float(np.linalg.norm(c["p_n"][li[worst]])), 4),
+            "richardson_fd_max_rel": round(rich, 8), "fp64_analytic_max_rel": round(exact, 8),
+            "check_s": round(time.perf_counter() - t0, 1),
+            "what": "initial parameters: hit leaf of every ray vs the oracle's raymarch; adjoint gradient vs plain "
+                    "FP64 central differences, vs Richardson-extrapolated ones and vs the FP64 analytic gradient "
+                    "(relative error of each leaf's 3-vector); fp64_analytic_vs_fd is the plain differences' own "
+                    "truncation error at this h"}
 
 
 def profiled_traffic(rays):
     """DRAM bytes per launch from the committed ncu summaries (per ray, times
-    the launch's rays): the full-size one-pass capture, else the small case."""
-    for name in ("dram_config1_fullsize.txt", "trace_image_config1.txt"):
+    the launch's rays), and where the figure comes from: it is read from a
+    committed capture, not measured in this run."""
+    for name, what in (("dram_config1_fullsize.txt", "one-pass ncu capture (dram__bytes_read.sum + "
+                                                      "dram__bytes_write.sum) of this kernel on this workload"),
+                       ("trace_image_config1.txt", "ncu capture of this kernel on the 1024^3 case")):
         try:
             for line in open(os.path.join(ROOT, "profiles", name)):
                 if line.startswith("dram_bytes_per_ray:"):
-                    return int(float(line.split(":")[1]) * rays)
+                    b = float(line.split(":")[1])
+                    return int(b * rays), "profiles/%s: %s, %.1f B/ray x this launch's rays; not measured in " \
+                                          "this run" % (name, what, b)
         except OSError:
             pass
-    return None
+    return None, None
 
 
 def profiled_issue():
@@ -1109,38 +1348,35 @@ def run_reference(args):
         so = p + shadow_offset(side)
         shadows.append(np.concatenate([so, np.broadcast_to(LIGHT, so.shape)], 1).astype(np.float32))
     setup_s = time.perf_counter() - t0
-    per_step = 4  # cameras per timed step (a bounded sample of the 32-camera step)
+    Rp = sum(p.shape[0] for p in prims)
+    Rs = sum(x.shape[0] for x in shadows)
 
-    def step(k):
-        n = 0
-        for j in range(per_step):
-            i = (k * per_step + j) % len(prims)
-            oracle.raymarch(words, prims[i], light=LIGHT, threads=threads)
-            oracle.raymarch(words, shadows[i], threads=threads)
-            n += prims[i].shape[0] + shadows[i].shape[0]
-        return n
+    def step():
+        # the whole workload: every camera's primary rays, then its shadow rays
+        for p, sh in zip(prims, shadows):
+            oracle.raymarch(words, p, light=LIGHT, threads=threads)
+            oracle.raymarch(words, sh, threads=threads)
+        return Rp + Rs
 
-    for k in range(args.warmup):
-        step(k)
+    for _ in range(args.warmup):
+        step()
     t0 = time.perf_counter()
     rays = 0
-    for k in range(args.steps):
-        rays += step(args.warmup + k)
+    for _ in range(args.steps):
+        rays += step()
     secs = time.perf_counter() - t0
     value = rays / secs / 1e6
-    rays_full = sum(p.shape[0] for p in prims) + sum(s.shape[0] for s in shadows)
-    sample = ("%d cameras (primary + shadow rays) per step of the %d-camera workload; %d rays in %.1f s on %d host "
-              "threads; oracle C restatement of VoxelOctree::raymarch (the reference's own build needs its sources, "
-              "absent on the GPU host)" % (per_step, len(prims), rays, secs, threads))
+    sample = ("the full step, all %d cameras (primary + shadow rays, %d rays) per step; %d rays in %.1f s on %d "
+              "host threads; oracle C restatement of VoxelOctree::raymarch + shade (the reference's own sources are "
+              "absent on the GPU host)" % (len(prims), Rp + Rs, rays, secs, threads))
     line = {
         "impl": "reference", "metric": "Mrays/s", "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(secs / args.steps * 1e3, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded terrain + spheres, seeded orbit cameras)",
-        "config": {"workload": "plain traversal: %d^3 octree (terrain + %d spheres), %d cams %dx%d primary rays "
-                               "+ 1 shadow ray per hit" % (side, N_SPHERES, args.cams, args.width, args.height),
-                   "octree_words": int(words.size), "voxels": int(n_vox), "rays_per_full_step": int(rays_full),
-                   "setup_s": round(setup_s, 1)},
+        "config": workload_config(args, words.size, n_vox, Rp, Rs, world),
+        "api": "oracle raymarch (VoxelOctree::raymarch restated in C) over all host threads, rows interleaved",
+        "setup_s": round(setup_s, 1),
         "cpu_baseline": {"value": round(value, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": round(value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},

@@ -179,11 +179,14 @@ int svo_octree_build_voxel_file_streamed(const char *path, uint64_t mem, uint64_
  *   Limits: virtual side <= 256 and at most 262,144 occupied voxels;
  *   larger inputs, or an output buffer smaller than the octree (*n_words is
  *   still set), return SVO_ERR_LIMIT.
- *   The first call on a device looks up the arena's device address; make
- *   that first call before any stream capture on that device.
+ *   The first call on a device looks up the arena's device address and
+ *   keeps it for the process; make that first call before any stream capture
+ *   on that device.  cudaDeviceReset between calls is not supported: the
+ *   kept address would no longer be valid.
  *   All calls share the one arena, so calls that overlap on the GPU (from
  *   several host threads or streams at once) race and must be serialised by
- *   the caller.  The call returns after its work on `stream` is complete. */
+ *   the caller.  The call returns after its work on `stream` is complete,
+ *   on success and on error alike. */
 int svo_octree_build_dense_noalloc(const uint32_t *d_grid, int w, int h, int d, uint64_t mem, uint32_t *d_words,
                                    uint64_t capacity, uint64_t *n_words, float center[3], svo_stream stream);
 

@@ -41,8 +41,20 @@ def loss(leaf, dirs, lights, p_rgb, p_n, target, w):
     return float((w * (c - target) ** 2).sum())
 
 
-def gradient(leaf, dirs, lights, p_rgb, p_n, target, w, n_words):
-    """Analytic dL/dp_rgb, dL/dp_n (float64, n_words x 3 each)."""
+def gradient(leaf, dirs, lights, p_rgb, p_n, target, w, n_words, leaves=None):
+    """Analytic dL/dp_rgb, dL/dp_n (float64, n_words x 3 each); with
+    `leaves`, only those leaves' rows (len(leaves) x 3 each, in that order)."""
+    if leaves is not None:
+        leaves = np.asarray(leaves, np.int64)
+        pos = {int(v): i for i, v in enumerate(leaves)}
+        sel = np.isin(leaf.astype(np.int64), leaves)
+        remap = np.full(leaf.shape, 0xFFFFFFFF, np.uint32)
+        remap[sel] = [pos[int(v)] for v in leaf[sel]]
+        sub_rgb = np.zeros((len(leaves), 3), np.float32)
+        sub_n = np.zeros((len(leaves), 3), np.float32)
+        sub_rgb[:] = p_rgb[leaves]
+        sub_n[:] = p_n[leaves]
+        return gradient(remap[sel], dirs[sel], lights[sel], sub_rgb, sub_n, target[sel], w, len(leaves))
     c = shade(leaf, dirs, lights, p_rgb, p_n)
     g = 2.0 * w * (c - target)
     hit = leaf != 0xFFFFFFFF

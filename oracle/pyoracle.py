@@ -116,25 +116,25 @@ class Oracle:
         return self.L.svo_oracle_shade(int(word), _ptr(d, _f32p), _ptr(light, _f32p))
 
     # -- raymarch
-    def raymarch(self, words, rays, ray_scale=0.0, light=(0.0, 0.0, 1.0), threads=1, loads=False):
-        """rays: (R, 6) float32.  Returns dict of hit (u8), t, leaf, word, grey[, loads]."""
+    RAY_OUTPUTS = ("hit", "t", "leaf", "word", "grey")
+
+    def raymarch(self, words, rays, ray_scale=0.0, light=(0.0, 0.0, 1.0), threads=1, loads=False,
+                 outputs=RAY_OUTPUTS):
+        """rays: (R, 6) float32.  Returns dict of the requested outputs among
+        hit (u8), t, leaf, word, grey[, loads]; outputs not asked for are not
+        computed (grey is the shade of a hit)."""
         words = np.ascontiguousarray(words, dtype=np.uint32)
         rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 6)
         light = np.ascontiguousarray(light, dtype=np.float32)
         R = rays.shape[0]
-        out = {
-            "hit": np.zeros(R, np.uint8),
-            "t": np.zeros(R, np.float32),
-            "leaf": np.zeros(R, np.uint32),
-            "word": np.zeros(R, np.uint32),
-            "grey": np.zeros(R, np.float32),
-        }
+        types = {"hit": np.uint8, "t": np.float32, "leaf": np.uint32, "word": np.uint32, "grey": np.float32}
+        out = {k: np.zeros(R, types[k]) for k in outputs}
         ld = np.zeros(R, np.uint32) if loads else None
         self.L.svo_oracle_raymarch_batch(_ptr(words, _u32p), words.size, _ptr(rays, _f32p), R,
                                          float(ray_scale), _ptr(light, _f32p),
-                                         _ptr(out["hit"], _u8p), _ptr(out["t"], _f32p),
-                                         _ptr(out["leaf"], _u32p), _ptr(out["word"], _u32p),
-                                         _ptr(out["grey"], _f32p), _ptr(ld, _u32p), int(threads))
+                                         _ptr(out.get("hit"), _u8p), _ptr(out.get("t"), _f32p),
+                                         _ptr(out.get("leaf"), _u32p), _ptr(out.get("word"), _u32p),
+                                         _ptr(out.get("grey"), _f32p), _ptr(ld, _u32p), int(threads))
         if loads:
             out["loads"] = ld
         return out

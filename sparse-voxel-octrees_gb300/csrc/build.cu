@@ -895,18 +895,25 @@ extern "C" int svo_octree_build_dense_noalloc(const uint32_t *d_grid, int w, int
     using namespace svo;
     if (!d_grid || !d_words || !n_words || !center || w <= 0 || h <= 0 || d <= 0)
         return set_error(SVO_ERR_INVALID, "bad arguments");
+    // checked before the doubling below, which would overflow past 2^30
+    if (w > kNoAllocMaxSide || h > kNoAllocMaxSide || d > kNoAllocMaxSide)
+        return set_error(SVO_ERR_LIMIT, "grid %d x %d x %d exceeds the allocation-free build's limit of side %d", w,
+                         h, d, kNoAllocMaxSide);
     int side = 1;
     while (side < w || side < h || side < d) side *= 2;
     if (side < 2) return set_error(SVO_ERR_INVALID, "virtual side %d below 2 (the reference recurses forever)", side);
-    if (side > kNoAllocMaxSide)
-        return set_error(SVO_ERR_LIMIT, "virtual side %d exceeds the allocation-free build's limit of %d", side,
-                         kNoAllocMaxSide);
     int lb = cache_block_log2(w, h, d, mem, 4);
     if (lb < 1) return set_error(SVO_ERR_MEMORY, "memory budget %llu admits no cache block", (unsigned long long)mem);
     int log_side = 0;
     while ((1 << log_side) < side) ++log_side;
     int rc = build_dense_noalloc(d_grid, w, h, d, log_side, lb, (cudaStream_t)stream, d_words, capacity, n_words);
-    if (rc) return rc;
+    if (rc) {
+        // an error can leave earlier launches queued; they still write to the
+        // shared arena, so wait for them before returning (the error already
+        // recorded stays the one reported)
+        cudaStreamSynchronize((cudaStream_t)stream);
+        return rc;
+    }
     center[0] = (float)w * 0.5f / (float)side;
     center[1] = (float)h * 0.5f / (float)side;
     center[2] = (float)d * 0.5f / (float)side;

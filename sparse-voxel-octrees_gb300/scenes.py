@@ -303,6 +303,31 @@ def orbit_cameras(n, seed, center, radius=2.0, radius_hi=None, pitch=60.0):
     return cams
 
 
+def batched_views(n_views, seed=3):
+    """The batched workload's (octree, view) pairs as (index, side, generator,
+    W, H): depth U{7..11}; even index -> sphere-union generator (48 spheres),
+    odd -> terrain generator (200 spheres), scene seed = index; one view each,
+    pixel count log-uniform in [256x256, 1920x1080] at 16:9, clipped to
+    [256, 1920] x [256, 1080]."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for i in range(1, n_views + 1):
+        depth = int(rng.integers(7, 12))
+        pix = float(np.exp(rng.uniform(np.log(256 * 256), np.log(1920 * 1080))))
+        W = int(min(1920, max(256, round((pix * 16 / 9) ** 0.5))))
+        H = int(min(1080, max(256, round(pix / W))))
+        specs.append((i, 1 << depth, "sphere" if i % 2 == 0 else "terrain", W, H))
+    return specs
+
+
+def scene_spec_params(side, generator, seed):
+    """(heights or None, centres, radii) of one batched-workload octree."""
+    if generator == "sphere":
+        centers, radii = sphere_scene_params(side, 48, seed)
+        return None, centers, radii
+    return terrain_scene_params(side, 200, seed)
+
+
 def random_rays(n, seed, lo=-1.0, hi=4.0):
     """Rays from U[lo, hi]^3 towards U[1, 2]^3 (unit directions), plus
     axis-aligned and grazing directions in the first rows."""

@@ -4,7 +4,8 @@ already handed to its own pool, or a frame loop that must avoid the
 device-wide synchronisation of cudaMalloc/cudaFree).  It works inside one
 fixed device arena of the library, so this test calls it twice in a row
 (and once more) and checks every result against the allocating entry point,
-svo_octree_build_dense.  Collected last so that a failure here never hides
+svo_octree_build_dense, and against the oracle's restatement of
+VoxelOctree(VoxelData*).  Collected last so that a failure here never hides
 the other tests' results."""
 import ctypes
 
@@ -33,7 +34,7 @@ def _reference_build(svo, grid, mem):
     return tree.words(), tree.center()
 
 
-def test_noalloc_build_matches_allocating_build(cuda, svo, scenes):
+def test_noalloc_build_matches_allocating_build(cuda, svo, scenes, oracle):
     torch = cuda
     svo.lib.svo_octree_build_dense_noalloc.restype = ctypes.c_int
     # a grid with several cache blocks and an odd depth (empty descriptors),
@@ -51,6 +52,10 @@ def test_noalloc_build_matches_allocating_build(cuda, svo, scenes):
         assert n == ref_words.size
         assert np.array_equal(words, ref_words)
         assert np.array_equal(center, ref_center)
+        # and the oracle's restatement of VoxelOctree(VoxelData*) itself
+        o_words, o_center = oracle.build_dense(grid, mem)
+        assert np.array_equal(words, o_words)
+        assert np.array_equal(center, o_center)
 
 
 def test_noalloc_build_rejects_sizes_beyond_its_limits(cuda, svo):
@@ -61,6 +66,15 @@ def test_noalloc_build_rejects_sizes_beyond_its_limits(cuda, svo):
     assert rc == svo.SVO_ERR_LIMIT and b"262144" in svo.lib.svo_last_error()
     big = np.zeros((1, 1, 300), np.uint32)  # virtual side 512 > 256
     rc, _, _, _ = _noalloc_build(svo, torch, big, 1 << 30)
+    assert rc == svo.SVO_ERR_LIMIT
+    # a side past 2^30 is refused before the grid is touched
+    n = ctypes.c_uint64()
+    c = np.zeros(3, np.float32)
+    dummy = torch.zeros(16, dtype=torch.int32, device="cuda")
+    rc = svo.lib.svo_octree_build_dense_noalloc(ctypes.c_void_p(dummy.data_ptr()), 1, 1, (1 << 30) + 1,
+                                                ctypes.c_uint64(1 << 30), ctypes.c_void_p(dummy.data_ptr()),
+                                                ctypes.c_uint64(16), ctypes.byref(n),
+                                                c.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), None)
     assert rc == svo.SVO_ERR_LIMIT
     small = np.ones((8, 8, 8), np.uint32)
     rc, _, _, n = _noalloc_build(svo, torch, small, 1 << 30, capacity=4)
