@@ -337,7 +337,7 @@ def run_ours(args):
                               "ms_per_step": r4["step_ms_with_adam"], "higher_is_better": True, "scaling": "weak",
                               "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                               "config": {"workload": "differentiable: " + r4["workload"]}, "fwd_bwd": r4,
-                              "gpu_launches": 2 * r4["steps"]}))
+                              "gpu_launches": 4 * r4["steps"]}))
         return
 
     if args.config == 2:
@@ -634,6 +634,7 @@ def summary_of(line):
          "batched_exact_hit_parity": g(line, "batched_vs_plain", "exact_hit_parity"),
          "fwd_bwd_mrays_s": g(line, "fwd_bwd", "fwd_bwd_mrays_s"),
          "fwd_bwd_step_ms_with_adam": g(line, "fwd_bwd", "step_ms_with_adam"),
+         "fwd_bwd_step_ms_dense_adam": g(line, "fwd_bwd", "dense_path", "step_ms_with_adam"),
          "fwd_bwd_hit_leaves_exact": g(line, "fwd_bwd", "check", "hit_leaves_exact"),
          "fwd_bwd_fd_max_rel": g(line, "fwd_bwd", "check", "fd_max_rel"),
          "fwd_bwd_fd_own_truncation_max_rel": g(line, "fwd_bwd", "check", "fp64_analytic_vs_fd_max_rel"),
@@ -1148,69 +1149,89 @@ def run_leaf_shading(args, torch, svo, scenes, n_steps=200):
     target[h] = gt * 0.9 * ln.abs()[:, None] + spec[:, None]
     del t, word, p, gt, n, d, l, ln, r, spec
     gen = torch.Generator(device="cuda").manual_seed(7)
-    p_rgb = torch.rand((nw, 3), generator=gen, device="cuda").requires_grad_()
-    p_n = torch.rand((nw, 3), generator=gen, device="cuda").requires_grad_()
-    opt = svo.LeafAdam([p_rgb, p_n], lr=1e-2)  # svo_adam_step: one pass per tensor, zeroes the gradient
+    p0_rgb = torch.rand((nw, 3), generator=gen, device="cuda")
+    p0_n = torch.rand((nw, 3), generator=gen, device="cuda")
     rgb = torch.empty((R, 3), dtype=torch.float32, device="cuda")
     leaf = torch.empty(R, dtype=torch.int32, device="cuda")
     d_rgb = torch.empty((R, 3), dtype=torch.float32, device="cuda")
-    g_rgb = torch.zeros_like(p_rgb)
-    g_n = torch.zeros_like(p_n)
-    scale = 2.0 / (3 * R)
+    scale = 2.0 / (3 * R)  # L = sum (rgb - target)^2 / (3R): dL/drgb = scale (rgb - target)
     setup_s = time.perf_counter() - t0
     stream = torch.cuda.current_stream()
     # one untimed forward + adjoint at the initial parameters, for the checks
-    # against the oracle after the timed loop
+    # against the oracle after the timed loops
     check = None
     if not args.no_cpu:
-        tree.diff_forward(rays, W, H, V, lights, p_rgb.detach(), p_n.detach(), rgb, hit_leaf=leaf, stream=stream)
+        g_rgb, g_n = torch.zeros_like(p0_rgb), torch.zeros_like(p0_n)
+        tree.diff_forward(rays, W, H, V, lights, p0_rgb, p0_n, rgb, hit_leaf=leaf, stream=stream)
         torch.sub(rgb, target, out=d_rgb)
         d_rgb.mul_(scale)
-        tree.diff_backward(rays, W, H, V, lights, p_rgb.detach(), p_n.detach(), d_rgb, g_rgb, g_n, hit_leaf=leaf,
-                           stream=stream)
+        tree.diff_backward(rays, W, H, V, lights, p0_rgb, p0_n, d_rgb, g_rgb, g_n, hit_leaf=leaf, stream=stream)
         torch.cuda.synchronize()
         check = {"leaf": leaf.cpu().numpy().view(np.uint32), "g_rgb": g_rgb.cpu().numpy(), "g_n": g_n.cpu().numpy(),
-                 "p_rgb": p_rgb.detach().cpu().numpy(), "p_n": p_n.detach().cpu().numpy(),
-                 "target": target.cpu().numpy()}
-        g_rgb.zero_()
-        g_n.zero_()
-    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(n_steps)]
-    losses = []
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for k in range(n_steps):
-        ev[k][0].record(stream)
-        tree.diff_forward(rays, W, H, V, lights, p_rgb.detach(), p_n.detach(), rgb, hit_leaf=leaf, stream=stream)
-        ev[k][1].record(stream)
-        torch.sub(rgb, target, out=d_rgb)
-        if k % 20 == 0 or k == n_steps - 1:
-            losses.append((k, d_rgb.square().sum() / (3 * R)))
-        d_rgb.mul_(scale)
-        ev[k][2].record(stream)
-        tree.diff_backward(rays, W, H, V, lights, p_rgb.detach(), p_n.detach(), d_rgb, g_rgb, g_n, hit_leaf=leaf,
-                           stream=stream)
-        ev[k][3].record(stream)
-        p_rgb.grad = g_rgb
-        p_n.grad = g_n
-        opt.step(stream)  # also zeroes g_rgb and g_n for the next adjoint
-    e1.record(stream)
-    torch.cuda.synchronize()
-    fwd = [e[0].elapsed_time(e[1]) for e in ev]
-    bwd = [e[2].elapsed_time(e[3]) for e in ev]  # the adjoint kernel
-    step_ms = e0.elapsed_time(e1) / n_steps
-    fb = (sum(fwd) + sum(bwd)) / n_steps
+                 "p_rgb": p0_rgb.cpu().numpy(), "p_n": p0_n.cpu().numpy(), "target": target.cpu().numpy()}
+        del g_rgb, g_n
+
+    def train(steps, fused):
+        """`steps` optimisation steps from the initial parameters.  fused:
+        svo_diff_backward_l2 (loss gradient and loss sum in the adjoint,
+        touched leaves recorded) + svo_adam_step_leaves; else the loss
+        gradient in torch + svo_diff_backward + dense svo_adam_step."""
+        p_rgb, p_n = p0_rgb.clone(), p0_n.clone()
+        g_rgb, g_n = torch.zeros_like(p_rgb), torch.zeros_like(p_n)
+        p_rgb.grad, p_n.grad = g_rgb, g_n
+        leaves = svo.LeafSet(nw) if fused else None
+        opt = svo.LeafAdam([p_rgb, p_n], lr=1e-2, leaves=leaves)  # zeroes the gradients it reads
+        loss_sum = torch.zeros(steps, dtype=torch.float64, device="cuda")
+        ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(steps)]
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for k in range(steps):
+            ev[k][0].record(stream)
+            tree.diff_forward(rays, W, H, V, lights, p_rgb, p_n, rgb, hit_leaf=leaf, stream=stream)
+            ev[k][1].record(stream)
+            if fused:
+                ev[k][2].record(stream)
+                tree.diff_backward_l2(rays, W, H, V, lights, p_rgb, p_n, rgb, target, scale, g_rgb, g_n,
+                                      hit_leaf=leaf, loss_sum=loss_sum[k:k + 1], leaves=leaves, stream=stream)
+            else:
+                torch.sub(rgb, target, out=d_rgb)
+                loss_sum[k:k + 1] = d_rgb.double().square().sum()
+                d_rgb.mul_(scale)
+                ev[k][2].record(stream)
+                tree.diff_backward(rays, W, H, V, lights, p_rgb, p_n, d_rgb, g_rgb, g_n, hit_leaf=leaf,
+                                   stream=stream)
+            ev[k][3].record(stream)
+            opt.step(stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        fwd = [e[0].elapsed_time(e[1]) for e in ev]
+        bwd = [e[2].elapsed_time(e[3]) for e in ev]
+        loss = (loss_sum / (3 * R)).cpu().numpy()
+        return {"step_ms": e0.elapsed_time(e1) / steps, "fwd_ms": sum(fwd) / steps, "bwd_ms": sum(bwd) / steps,
+                "loss": loss, "touched_leaves": leaves.size() if fused else None}
+
+    main = train(n_steps, fused=True)
+    dense = train(min(20, n_steps), fused=False)
+    fb = main["fwd_ms"] + main["bwd_ms"]
+    nd = len(dense["loss"])
     if check is not None:
         check = shading_check(tree, rays.cpu().numpy(), lights.cpu().numpy(), W * H, check)
     return {"workload": "512^3 sphere union (160 spheres, seed 7), %d octree words; 24 views 512x512; per-leaf FP32 "
                         "rgb+normal params; L2 loss vs 3-octave noise colour field; Adam lr 1e-2" % nw,
-            "rays_per_step": R, "steps": n_steps, "fwd_ms": round(sum(fwd) / n_steps, 3),
-            "bwd_ms": round(sum(bwd) / n_steps, 3), "fwd_bwd_mrays_s": round(R / fb / 1e3, 1),
-            "fwd_bwd_note": "svo_diff_forward + svo_diff_backward kernel time (CUDA events); step_ms_with_adam adds "
-                            "the loss gradient and svo_adam_step (one pass per parameter tensor, gradient zeroed "
-                            "in the same pass)",
-            "step_ms_with_adam": round(step_ms, 3),
-            "loss_first_last": [[k, round(float(v.item()), 6)] for k, v in (losses[0], losses[-1])],
+            "rays_per_step": R, "steps": n_steps, "fwd_ms": round(main["fwd_ms"], 3),
+            "bwd_ms": round(main["bwd_ms"], 3), "fwd_bwd_mrays_s": round(R / fb / 1e3, 1),
+            "fwd_bwd_note": "svo_diff_forward + svo_diff_backward_l2 kernel time (CUDA events); the adjoint forms the "
+                            "L2 loss gradient and the loss itself; step_ms_with_adam adds svo_adam_step_leaves over "
+                            "the leaves the adjoint has touched (identical to the dense Adam pass)",
+            "step_ms_with_adam": round(main["step_ms"], 3), "touched_leaves": main["touched_leaves"],
+            "loss_first_last": [[0, round(float(main["loss"][0]), 6)],
+                                [n_steps - 1, round(float(main["loss"][-1]), 6)]],
+            "dense_path": {"steps": nd, "step_ms_with_adam": round(dense["step_ms"], 3),
+                           "bwd_ms": round(dense["bwd_ms"], 3),
+                           "what": "loss gradient in torch, svo_diff_backward, dense svo_adam_step over every word",
+                           "loss_max_rel_diff_vs_fused": float(np.max(np.abs(dense["loss"] - main["loss"][:nd]) /
+                                                                      main["loss"][:nd]))},
             "setup_s": round(setup_s, 1), "check": check}
 
 

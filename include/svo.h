@@ -373,6 +373,26 @@ int svo_diff_backward(const svo_octree *oct, const float *rays, uint32_t width, 
                       const float *lights, const float *leaf_rgb, const float *leaf_normal, const uint32_t *hit_leaf,
                       const float *d_rgb, float *grad_rgb, float *grad_normal, svo_stream stream);
 
+/* No counterpart in the reference.  svo_diff_backward for the L2 loss
+ *   L = loss_scale / 2 * sum over rays and channels of (rgb - target)^2,
+ * with dL/drgb = loss_scale (rgb - target) formed inside the adjoint from the
+ * forward pass's rgb output (same parameters) and target (3 floats per ray,
+ * device) instead of a d_rgb array.  Optional:
+ *   loss_sum (device double): += sum of (rgb - target)^2 over all rays,
+ *     misses included (their rgb is 0);
+ *   touched / leaf_list / leaf_count (all or none): a record of the leaves
+ *     that have received a gradient.  touched holds one bit per octree word
+ *     ((n_words + 31) / 32 uint32, zeroed before the first call),
+ *     leaf_list leaf_capacity >= n_words entries, leaf_count one uint32
+ *     (zeroed with touched).  A leaf whose bit is clear gets its bit set and
+ *     is appended to leaf_list; the record grows over calls and is what
+ *     svo_adam_step_leaves updates. */
+int svo_diff_backward_l2(const svo_octree *oct, const float *rays, uint32_t width, uint32_t height,
+                         uint32_t n_views, const float *lights, const float *leaf_rgb, const float *leaf_normal,
+                         const uint32_t *hit_leaf, const float *rgb, const float *target, float loss_scale,
+                         float *grad_rgb, float *grad_normal, double *loss_sum, uint32_t *touched,
+                         uint32_t *leaf_list, uint32_t *leaf_count, uint64_t leaf_capacity, svo_stream stream);
+
 /* No counterpart in the reference.  One Adam step (no weight decay, no
  * amsgrad) over n parameters in one pass: exp_avg = beta1 exp_avg + (1 -
  * beta1) g, exp_avg_sq = beta2 exp_avg_sq + (1 - beta2) g^2, params -=
@@ -382,6 +402,18 @@ int svo_diff_backward(const svo_octree *oct, const float *rays, uint32_t width, 
  * asynchronous on `stream`.  step >= 1 counts this update. */
 int svo_adam_step(float *params, float *grads, float *exp_avg, float *exp_avg_sq, uint64_t n, float lr, float beta1,
                   float beta2, float eps, int step, int zero_grad, svo_stream stream);
+
+/* No counterpart in the reference.  svo_adam_step restricted to the leaves in
+ * leaf_list (the first *leaf_count entries, at most leaf_capacity; the count
+ * is read on the device): values [leaf*width, leaf*width + width) of each
+ * array, n_values in all.  When the list holds every leaf that has ever had
+ * a gradient (svo_diff_backward_l2's record) and the moments started at
+ * zero, the results are identical to svo_adam_step over all n_values: an
+ * unlisted value has g = m = v = 0, which the dense update leaves as it is. */
+int svo_adam_step_leaves(float *params, float *grads, float *exp_avg, float *exp_avg_sq, uint64_t n_values,
+                         uint32_t width, const uint32_t *leaf_list, const uint32_t *leaf_count,
+                         uint64_t leaf_capacity, float lr, float beta1, float beta2, float eps, int step,
+                         int zero_grad, svo_stream stream);
 
 /* ----------------------------------------------------------------- batched */
 

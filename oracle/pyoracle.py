@@ -405,6 +405,8 @@ class Reference:
         L.ref_inv_sqrt.argtypes = [ctypes.c_float]
         L.ref_tri_box_overlap.restype = ctypes.c_int
         L.ref_tri_box_overlap.argtypes = [_f32p, _f32p, _f32p]
+        L.ref_render_frame.restype = ctypes.c_int
+        L.ref_render_frame.argtypes = [_vp, _f32p, _f32p, ctypes.c_int, _u32p]
 
     def _worker_for(self, threads):
         """The spawned build worker whose reference thread pool has `threads`
@@ -524,6 +526,16 @@ class Reference:
         self.L.ref_raymarch(tree, _ptr(rays, _f32p), R, float(ray_scale), _ptr(hit, _u8p), _ptr(t, _f32p),
                             _ptr(w, _u32p), int(threads))
         return hit, t, w
+
+    def render_frame(self, tree, rot, trans, half_size=False):
+        """The viewer's 1280 x 720 frame by the reference's own renderBatch /
+        renderTile (ref_render.cpp), with inverse model-view [rot | trans]:
+        (720, 1280) uint32 RGBA8."""
+        out = np.zeros((720, 1280), np.uint32)
+        r = np.ascontiguousarray(rot, np.float32).reshape(9)
+        t = np.ascontiguousarray(trans, np.float32).reshape(3)
+        self.L.ref_render_frame(tree, _ptr(r, _f32p), _ptr(t, _f32p), 1 if half_size else 0, _ptr(out, _u32p))
+        return out
 
     def compress_material(self, n, shade):
         a = np.ascontiguousarray(n, dtype=np.float32)

@@ -9,9 +9,11 @@
  * rays every 8 pixels give a depth, each 8x8 tile whose four corners are not
  * all misses is traced from pos + dir * max(minT - 0.03, 0), shaded and
  * packed as RGBA8; pixels of skipped tiles stay 0.  The raymarch, invSqrt
- * and shade are this directory's restatements, pinned to the reference;
- * renderBatch itself lives in Main.cpp, which needs SDL, so this file is
- * pinned only through those parts.
+ * and shade are this directory's restatements, pinned to the reference.
+ * The whole frame is pinned to the reference's own renderBatch and
+ * renderTile, compiled from Main.cpp's text (ref_render.cpp), at the
+ * viewer's 1280 x 720 in 16 strips (tests/test_oracle_vs_reference.py and
+ * the committed frames in tests/golden/frames.npz).
  */
 #include <math.h>
 #include <pthread.h>

@@ -128,6 +128,12 @@ def _load():
                                             _vp, _vp, _vp]),
         "svo_diff_backward": (ctypes.c_int, [_vp, _vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _vp, _vp, _vp,
                                              _vp, _vp, _vp, _vp, _vp]),
+        "svo_diff_backward_l2": (ctypes.c_int, [_vp, _vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _vp, _vp,
+                                                _vp, _vp, _vp, _vp, ctypes.c_float, _vp, _vp, _vp, _vp, _vp, _vp,
+                                                ctypes.c_uint64, _vp]),
+        "svo_adam_step_leaves": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_uint64, ctypes.c_uint32, _vp, _vp,
+                                                ctypes.c_uint64, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                                ctypes.c_float, ctypes.c_int, ctypes.c_int, _vp]),
         "svo_render_frame": (ctypes.c_int, [_vp, _f32p, _f32p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                             ctypes.c_uint32, _vp, _vp]),
         "svo_adam_step": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_uint64, ctypes.c_float, ctypes.c_float,
@@ -523,6 +529,22 @@ class VoxelOctree:
                                     _dev_ptr(leaf_rgb), _dev_ptr(leaf_normal), _dev_ptr(hit_leaf), _dev_ptr(d_rgb),
                                     _dev_ptr(grad_rgb), _dev_ptr(grad_normal), _stream_ptr(stream)))
 
+    def diff_backward_l2(self, rays, width, height, n_views, lights, leaf_rgb, leaf_normal, rgb, target, loss_scale,
+                         grad_rgb, grad_normal, hit_leaf=None, loss_sum=None, leaves=None, stream=None):
+        """Adjoint of the L2 loss loss_scale/2 * sum (rgb - target)^2 with the
+        loss gradient formed in the kernel (svo_diff_backward_l2); loss_sum
+        (a float64 CUDA tensor) accumulates sum (rgb - target)^2, and
+        `leaves` (a LeafSet) records the leaves that received a gradient."""
+        tb = ll = lc = None
+        cap = 0
+        if leaves is not None:
+            tb, ll, lc, cap = leaves.touched, leaves.list, leaves.count, leaves.list.numel()
+        check(lib.svo_diff_backward_l2(self._h, _dev_ptr(rays), int(width), int(height), int(n_views),
+                                       _dev_ptr(lights), _dev_ptr(leaf_rgb), _dev_ptr(leaf_normal), _dev_ptr(hit_leaf),
+                                       _dev_ptr(rgb), _dev_ptr(target), float(loss_scale), _dev_ptr(grad_rgb),
+                                       _dev_ptr(grad_normal), _dev_ptr(loss_sum), _dev_ptr(tb), _dev_ptr(ll),
+                                       _dev_ptr(lc), int(cap), _stream_ptr(stream)))
+
     def render_frame(self, rot, pos, width=1280, height=720, n_strips=16, pixel_stride=1, out=None, stream=None):
         """The viewer's frame (svo_render_frame) into `out`, an int32 CUDA
         tensor of height*width RGBA8 words (allocated when None)."""
@@ -544,16 +566,35 @@ class VoxelOctree:
                                         _stream_ptr(stream)))
 
 
+class LeafSet:
+    """The leaves that have received a gradient (svo_diff_backward_l2's
+    record): a bit per octree word, the leaves in order of first touch, and
+    their count, all on the device and zeroed at creation."""
+
+    def __init__(self, n_words, device="cuda"):
+        import torch
+        self.touched = torch.zeros((n_words + 31) // 32, dtype=torch.int32, device=device)
+        self.list = torch.zeros(max(1, n_words), dtype=torch.int32, device=device)
+        self.count = torch.zeros(1, dtype=torch.int32, device=device)
+
+    def size(self):
+        return int(self.count.item())
+
+
 class LeafAdam:
     """Adam over per-leaf parameter tensors (CUDA float32, contiguous) with
     svo_adam_step: one fused pass per tensor that also zeroes the gradient
-    (pass zero_grad=False to keep it).  step() reads each tensor's .grad."""
+    (pass zero_grad=False to keep it).  step() reads each tensor's .grad.
+    With `leaves` (a LeafSet kept by diff_backward_l2) only the listed
+    leaves' `width` values per leaf are updated (svo_adam_step_leaves), with
+    results identical to the dense pass."""
 
-    def __init__(self, params, lr=1e-2, betas=(0.9, 0.999), eps=1e-8, zero_grad=True):
+    def __init__(self, params, lr=1e-2, betas=(0.9, 0.999), eps=1e-8, zero_grad=True, leaves=None, width=3):
         import torch
         self.params = list(params)
         self.lr, self.betas, self.eps, self.zero_grad = float(lr), betas, float(eps), zero_grad
         self.state = [(torch.zeros_like(p), torch.zeros_like(p)) for p in self.params]
+        self.leaves, self.width = leaves, int(width)
         self.t = 0
 
     def step(self, stream=None):
@@ -562,6 +603,13 @@ class LeafAdam:
             g = p.grad
             if g is None or not (p.is_contiguous() and g.is_contiguous()):
                 raise ValueError("LeafAdam needs contiguous parameters with gradients")
+            if self.leaves is not None:
+                L = self.leaves
+                check(lib.svo_adam_step_leaves(_dev_ptr(p), _dev_ptr(g), _dev_ptr(m), _dev_ptr(v), p.numel(),
+                                               self.width, _dev_ptr(L.list), _dev_ptr(L.count), L.list.numel(),
+                                               self.lr, float(self.betas[0]), float(self.betas[1]), self.eps, self.t,
+                                               1 if self.zero_grad else 0, _stream_ptr(stream)))
+                continue
             check(lib.svo_adam_step(_dev_ptr(p), _dev_ptr(g), _dev_ptr(m), _dev_ptr(v), p.numel(), self.lr,
                                     float(self.betas[0]), float(self.betas[1]), self.eps, self.t,
                                     1 if self.zero_grad else 0, _stream_ptr(stream)))

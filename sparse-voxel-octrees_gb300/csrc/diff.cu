@@ -42,6 +42,15 @@ struct DiffArgs {
     float *g_rgb, *g_n;
     unsigned long long *queue;
     uint32_t *status;
+    // fused L2 loss (svo_diff_backward_l2): dL/drgb = loss_scale (rgb - target)
+    const float *target;
+    float loss_scale;
+    double *loss_sum;  // optional: += sum over rays and channels of (rgb - target)^2
+    // optional record of the leaves that received a gradient
+    uint32_t *touched;     // one bit per octree word
+    uint32_t *leaf_list;   // leaves in order of first touch
+    uint32_t *leaf_count;  // entries in leaf_list
+    uint32_t leaf_cap;
 };
 
 __device__ __forceinline__ bool tile_pixel(const DiffArgs &a, uint64_t slot, uint32_t &idx, uint32_t &view) {
@@ -141,13 +150,26 @@ __device__ __forceinline__ float group_sum(unsigned peers, unsigned rank, unsign
     return v;
 }
 
+// Records `leaf` in the touched set the first time any warp adds a gradient
+// to it (called by the one lane that adds the leaf's gradient).
+__device__ __forceinline__ void mark_touched(const DiffArgs &a, uint32_t leaf) {
+    const uint32_t w = leaf >> 5, bit = 1u << (leaf & 31u);
+    if (__ldcg(a.touched + w) & bit) return;  // already recorded (the common case after the first pass)
+    if (atomicOr(a.touched + w, bit) & bit) return;
+    const uint32_t pos = atomicAdd(a.leaf_count, 1u);
+    if (pos < a.leaf_cap) a.leaf_list[pos] = leaf;
+}
+
 // kRetrace: recompute the hit leaf by traversal instead of reading hit_leaf.
-template <bool kTab, bool kRetrace>
+// kFused: dL/drgb = loss_scale (rgb - target) from the forward pass's rgb
+// instead of a d_rgb array, and the loss summed on the way.
+template <bool kTab, bool kRetrace, bool kFused>
 __global__ void k_diff_backward(DiffArgs a) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     RayStackFor<kTab> stk;
+    float loss = 0.0f;  // this lane's share of sum (rgb - target)^2
     unsigned long long base = 0, end = 0;
     while (true) {
         if (base >= end) {
@@ -183,12 +205,25 @@ __global__ void k_diff_backward(DiffArgs a) {
         }
         float gc0 = 0.f, gc1 = 0.f, gc2 = 0.f, gp0 = 0.f, gp1 = 0.f, gp2 = 0.f;
         bool contrib = leaf != 0xFFFFFFFFu;
+        float g0 = 0.f, g1 = 0.f, g2 = 0.f;
+        if (kFused && live) {
+            // every ray adds to the loss; a miss (rgb 0) contributes no gradient
+            const float *c3 = a.rgb + 3 * (uint64_t)idx, *t3 = a.target + 3 * (uint64_t)idx;
+            const float e0 = c3[0] - t3[0], e1 = c3[1] - t3[1], e2 = c3[2] - t3[2];
+            loss += e0 * e0 + e1 * e1 + e2 * e2;
+            g0 = a.loss_scale * e0;
+            g1 = a.loss_scale * e1;
+            g2 = a.loss_scale * e2;
+        }
         if (contrib) {
             float lx = a.lights[3 * view], ly = a.lights[3 * view + 1], lz = a.lights[3 * view + 2];
             Shading sh = shade_terms(a.p_n, leaf, dx, dy, dz, lx, ly, lz);
             const float *c = a.p_rgb + 3 * (uint64_t)leaf;
-            float g0 = a.d_rgb[3 * (uint64_t)idx], g1 = a.d_rgb[3 * (uint64_t)idx + 1],
-                  g2 = a.d_rgb[3 * (uint64_t)idx + 2];
+            if (!kFused) {
+                g0 = a.d_rgb[3 * (uint64_t)idx];
+                g1 = a.d_rgb[3 * (uint64_t)idx + 1];
+                g2 = a.d_rgb[3 * (uint64_t)idx + 2];
+            }
             gc0 = g0 * 0.9f * sh.a;
             gc1 = g1 * 0.9f * sh.a;
             gc2 = g2 * 0.9f * sh.a;
@@ -222,7 +257,14 @@ __global__ void k_diff_backward(DiffArgs a) {
             atomicAdd(gn, gp0);
             atomicAdd(gn + 1, gp1);
             atomicAdd(gn + 2, gp2);
+            if (a.touched) mark_touched(a, leaf);
         }
+    }
+    if (kFused && a.loss_sum) {
+        // one atomic per warp, at its end (a per-pass atomic on one address
+        // would serialise the warps)
+        for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(FULL, loss, o);
+        if (lane == 0) atomicAdd(a.loss_sum, (double)loss);
     }
 }
 
@@ -299,9 +341,42 @@ int svo_diff_backward(const svo_octree *oct, const float *rays, uint32_t width, 
     a.g_n = grad_normal;
     cudaStream_t st = (cudaStream_t)stream;
     a.tab = hit_leaf ? nullptr : octree_table(oct, st);  // the table only serves the retrace
-    if (a.tab) return launch_persistent(k_diff_backward<true, true>, a, st);
-    return hit_leaf ? launch_persistent(k_diff_backward<false, false>, a, st)
-                    : launch_persistent(k_diff_backward<false, true>, a, st);
+    if (a.tab) return launch_persistent(k_diff_backward<true, true, false>, a, st);
+    return hit_leaf ? launch_persistent(k_diff_backward<false, false, false>, a, st)
+                    : launch_persistent(k_diff_backward<false, true, false>, a, st);
+}
+
+int svo_diff_backward_l2(const svo_octree *oct, const float *rays, uint32_t width, uint32_t height,
+                         uint32_t n_views, const float *lights, const float *leaf_rgb, const float *leaf_normal,
+                         const uint32_t *hit_leaf, const float *rgb, const float *target, float loss_scale,
+                         float *grad_rgb, float *grad_normal, double *loss_sum, uint32_t *touched,
+                         uint32_t *leaf_list, uint32_t *leaf_count, uint64_t leaf_capacity, svo_stream stream) {
+    DiffArgs a;
+    int rc = prepare(oct, rays, width, height, n_views, lights, leaf_rgb, leaf_normal, a);
+    if (rc) return rc;
+    if (!rgb || !target || !grad_rgb || !grad_normal)
+        return set_error(SVO_ERR_INVALID, "rgb, target and gradient buffers required");
+    if ((touched != nullptr) != (leaf_list != nullptr) || (touched != nullptr) != (leaf_count != nullptr))
+        return set_error(SVO_ERR_INVALID, "touched, leaf_list and leaf_count go together");
+    if (touched && leaf_capacity < oct->n_words)
+        return set_error(SVO_ERR_INVALID, "leaf_list holds %llu entries; it needs one per octree word (%llu)",
+                         (unsigned long long)leaf_capacity, (unsigned long long)oct->n_words);
+    a.hit_leaf = const_cast<uint32_t *>(hit_leaf);
+    a.rgb = const_cast<float *>(rgb);
+    a.target = target;
+    a.loss_scale = loss_scale;
+    a.loss_sum = loss_sum;
+    a.g_rgb = grad_rgb;
+    a.g_n = grad_normal;
+    a.touched = touched;
+    a.leaf_list = leaf_list;
+    a.leaf_count = leaf_count;
+    a.leaf_cap = touched ? (uint32_t)oct->n_words : 0u;
+    cudaStream_t st = (cudaStream_t)stream;
+    a.tab = hit_leaf ? nullptr : octree_table(oct, st);
+    if (a.tab) return launch_persistent(k_diff_backward<true, true, true>, a, st);
+    return hit_leaf ? launch_persistent(k_diff_backward<false, false, true>, a, st)
+                    : launch_persistent(k_diff_backward<false, true, true>, a, st);
 }
 
 }  // extern "C"

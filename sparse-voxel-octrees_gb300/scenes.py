@@ -251,6 +251,18 @@ def camera(yaw, pitch, radius, center):
     return np.concatenate([Rt.reshape(9), pos]).astype(np.float32)
 
 
+def viewer_camera(yaw, pitch, radius, center):
+    """The orbit camera as the viewer's matrices give it: (rot (9,), trans
+    (3,), pos (3,)) float32, with [rot | trans] the inverse model-view matrix
+    and pos = (trans + center) + 1 formed in float32 as renderBatch forms its
+    eye position (Main.cpp:145)."""
+    cam = camera(yaw, pitch, radius, center)
+    rot = cam[:9].astype(np.float32)
+    trans = (rot.reshape(3, 3).astype(np.float64) @ np.array([0.0, 0.0, -radius])).astype(np.float32)
+    pos = ((trans + np.asarray(center, np.float32)).astype(np.float32) + np.float32(1.0)).astype(np.float32)
+    return rot, trans, pos
+
+
 def headlight(cam):
     """Main.cpp:163: normalize(R^T * (-1, 1, -1)), float32."""
     a = cam[:9].reshape(3, 3).astype(np.float32)

@@ -78,6 +78,7 @@ def golden():
         "codec": np.load(os.path.join(GOLDEN, "codec.npz")),
         "ply": np.load(os.path.join(GOLDEN, "ply.npz")),
         "volumes": np.load(os.path.join(GOLDEN, "volumes.npz")),
+        "frames": np.load(os.path.join(GOLDEN, "frames.npz")),
     }
 
 

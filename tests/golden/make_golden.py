@@ -20,8 +20,12 @@ Outputs (all produced by the reference's own code through oracle/_ref):
                for the same mesh, in one slab and in several, produced by the
                reference's own setupBlockProcessing / processBlock steps
                (oracle/ref_shim.cpp ref_ply_volume)
+  frames.npz   the viewer's 1280 x 720 frames of the dragon by the reference's
+               own renderBatch / renderTile (oracle/ref_render.cpp), full and
+               half size, with the cameras' matrices
 
   python tests/golden/make_golden.py volumes   writes volumes.npz only
+  python tests/golden/make_golden.py frames    writes frames.npz only
 """
 import hashlib
 import importlib.util
@@ -101,11 +105,35 @@ def make_volumes(R):
     print("volumes.npz", os.path.getsize(os.path.join(OUT, "volumes.npz")))
 
 
+# (yaw, pitch, radius, half size): viewer frames of the dragon
+FRAME_CASES = [(30.0, 20.0, 1.2, 0), (200.0, -35.0, 1.8, 0), (95.0, 60.0, 0.9, 1)]
+
+
+def make_frames(R):
+    g = np.load(os.path.join(OUT, "dragon.npz"))
+    tree = R.tree_from_words(g["words"], g["center"])
+    rots, transs, poss, halves, frames = [], [], [], [], []
+    for (yaw, pitch, radius, half) in FRAME_CASES:
+        rot, trans, pos = scenes.viewer_camera(yaw, pitch, radius, g["center"])
+        frames.append(R.render_frame(tree, rot, trans, bool(half)))
+        rots.append(rot)
+        transs.append(trans)
+        poss.append(pos)
+        halves.append(half)
+    R.free(tree)
+    np.savez_compressed(os.path.join(OUT, "frames.npz"), rot=np.array(rots), trans=np.array(transs),
+                        pos=np.array(poss), half=np.array(halves, np.int32), frames=np.array(frames))
+    print("frames.npz", os.path.getsize(os.path.join(OUT, "frames.npz")))
+
+
 def main():
     R = Reference()
     R.start_threads(4)
     if len(sys.argv) > 1 and sys.argv[1] == "volumes":
         make_volumes(R)
+        return
+    if len(sys.argv) > 1 and sys.argv[1] == "frames":
+        make_frames(R)
         return
     # ---- dragon
     path = os.path.join(REF_SRC, "models", "XYZRGB-Dragon.oct")
@@ -178,6 +206,7 @@ def main():
     for f in ("dragon.npz", "builds.npz", "codec.npz", "ply.npz"):
         print(f, os.path.getsize(os.path.join(OUT, f)))
     make_volumes(R)
+    make_frames(R)
 
 
 if __name__ == "__main__":

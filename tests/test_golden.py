@@ -57,3 +57,15 @@ def test_numpy_codec_matches_reference(scenes, golden):
     w = scenes.compress_material(n[:, 0], n[:, 1], n[:, 2], g["shade"])
     assert np.array_equal(w, g["packed"])
     assert np.array_equal(scenes.inv_sqrt(g["isqrt_x"]), g["isqrt_y"])
+
+
+def test_viewer_frames_match_reference_outputs(oracle, golden):
+    """render_oracle.c's frame against the reference's own renderBatch /
+    renderTile (Main.cpp:92-202) frames of the dragon, 1280 x 720 in the
+    viewer's 16 strips, full and half size."""
+    g, f = golden["dragon"], golden["frames"]
+    for rot, pos, half, ref in zip(f["rot"], f["pos"], f["half"], f["frames"]):
+        img = oracle.render_frame(g["words"], rot, pos, 1280, 720, 16, 3 if half else 1, threads=4)
+        assert np.array_equal(img, ref)
+        assert (ref != 0).mean() > 0.1
+    assert f["half"].any() and not f["half"].all()

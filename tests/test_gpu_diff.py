@@ -198,3 +198,81 @@ def test_leaf_adam_matches_torch_adam(cuda, svo):
         for r, m in zip(ref, mine):
             torch.testing.assert_close(m, r.detach(), rtol=2e-6, atol=2e-7)
             assert not m.grad.any()  # zeroed in the same pass
+
+
+def test_fused_l2_adjoint_matches_unfused(cuda, svo, problem):
+    """svo_diff_backward_l2 (the loss gradient formed in the kernel) against
+    svo_diff_backward fed with dL/drgb from torch; its loss sum, and its
+    record of touched leaves against the hit leaves."""
+    torch = cuda
+    pb = problem
+    rays, lights, p_rgb, p_n, target = _device(torch, pb)
+    R = rays.shape[0]
+    rgb = torch.empty((R, 3), dtype=torch.float32, device="cuda")
+    hit = torch.empty(R, dtype=torch.int32, device="cuda")
+    args = (rays, pb["W"], pb["H"], pb["V"], lights, p_rgb.detach(), p_n.detach())
+    pb["tree"].diff_forward(*args, rgb, hit_leaf=hit)
+    scale = 2.0 * pb["w"]
+    d_rgb = (rgb - target) * scale
+    g1 = [torch.zeros_like(p_rgb), torch.zeros_like(p_n)]
+    pb["tree"].diff_backward(*args, d_rgb, g1[0], g1[1], hit_leaf=hit)
+    g2 = [torch.zeros_like(p_rgb), torch.zeros_like(p_n)]
+    loss_sum = torch.zeros(1, dtype=torch.float64, device="cuda")
+    leaves = svo.LeafSet(pb["words"].size)
+    pb["tree"].diff_backward_l2(*args, rgb, target, scale, g2[0], g2[1], hit_leaf=hit, loss_sum=loss_sum,
+                                leaves=leaves)
+    # the re-traced form gives the same gradients and adds nothing new to the record
+    g3 = [torch.zeros_like(p_rgb), torch.zeros_like(p_n)]
+    pb["tree"].diff_backward_l2(*args, rgb, target, scale, g3[0], g3[1], leaves=leaves)
+    torch.cuda.synchronize()
+    for a, b, c in zip(g1, g2, g3):
+        torch.testing.assert_close(b, a, rtol=1e-5, atol=1e-12)
+        torch.testing.assert_close(c, a, rtol=1e-5, atol=1e-12)
+    ref_loss = float(((rgb.double() - target.double()) ** 2).sum().item())
+    assert abs(loss_sum.item() - ref_loss) <= 1e-5 * ref_loss
+    hit_leaves = np.unique(pb["leaf"][pb["leaf"] != 0xFFFFFFFF])
+    listed = leaves.list[:leaves.size()].cpu().numpy().view(np.uint32)
+    assert np.array_equal(np.sort(listed), hit_leaves)
+    bits = leaves.touched.cpu().numpy().view(np.uint32)
+    on = np.nonzero((bits[:, None] >> np.arange(32, dtype=np.uint32)) & 1)
+    assert np.array_equal(np.sort(on[0] * 32 + on[1]), hit_leaves)
+
+
+def test_sparse_adam_equals_dense_adam(cuda, svo, problem):
+    """Adam over the touched leaves only (svo_adam_step_leaves) gives the
+    dense svo_adam_step's parameters bit for bit, step after step: leaves
+    never touched keep zero moments, which the dense update leaves alone."""
+    torch = cuda
+    pb = problem
+    rays, lights, p0_rgb, p0_n, target = _device(torch, pb)
+    dense = [p0_rgb.detach().clone(), p0_n.detach().clone()]
+    sparse = [p0_rgb.detach().clone(), p0_n.detach().clone()]
+    leaves = svo.LeafSet(pb["words"].size)
+    opt_d = svo.LeafAdam(dense, lr=1e-2)
+    opt_s = svo.LeafAdam(sparse, lr=1e-2, leaves=leaves)
+    R = rays.shape[0]
+    rgb = torch.empty((R, 3), dtype=torch.float32, device="cuda")
+    hit = torch.empty(R, dtype=torch.int32, device="cuda")
+    # the views change every step, so the record grows over the steps
+    n_pix = pb["W"] * pb["H"]
+    for step in range(6):
+        v = step % pb["V"]
+        sl = slice(v * n_pix, (v + 1) * n_pix)
+        g = [torch.zeros_like(dense[0]), torch.zeros_like(dense[1])]
+        args = (rays[sl], pb["W"], pb["H"], 1, lights[v:v + 1], dense[0], dense[1])
+        pb["tree"].diff_forward(*args, rgb[sl], hit_leaf=hit[sl])
+        pb["tree"].diff_backward_l2(*args, rgb[sl], target[sl], 2.0 * pb["w"], g[0], g[1], hit_leaf=hit[sl],
+                                    leaves=leaves)
+        for p, gp in zip(dense, g):
+            p.grad = gp
+        for p, gp in zip(sparse, g):
+            p.grad = gp.clone()
+        opt_d.step()
+        opt_s.step()
+        torch.cuda.synchronize()
+        for a, b in zip(dense, sparse):
+            assert torch.equal(a.view(torch.int32), b.view(torch.int32)), step
+        for (m1, v1), (m2, v2) in zip(opt_d.state, opt_s.state):
+            assert torch.equal(m1, m2) and torch.equal(v1, v2), step
+        assert not sparse[0].grad.any() and not sparse[1].grad.any()
+    assert 0 < leaves.size() < pb["words"].size

@@ -1,6 +1,8 @@
-"""The viewer's frame (svo_render_frame) against the oracle's restatement of
-renderBatch + renderTile (oracle/render_oracle.c): bit-identical RGBA8
-frames across cameras, strip layouts, half-size mode and frame sizes."""
+"""The viewer's frame (svo_render_frame) against the reference's own
+renderBatch + renderTile frames of the dragon (tests/golden/frames.npz) and
+the oracle's restatement (oracle/render_oracle.c, pinned to those frames):
+bit-identical RGBA8 frames across cameras, strip layouts, half-size mode and
+frame sizes."""
 import numpy as np
 import pytest
 
@@ -45,3 +47,12 @@ def test_inside_the_tree_and_empty_view(cuda, svo, oracle, scenes):
     for cam in (inside, away):
         img = _frame(cuda, tree, cam, width=320, height=200, n_strips=4)
         assert np.array_equal(img, oracle.render_frame(words, cam[:9], cam[9:12], 320, 200, 4, 1, threads=4))
+
+
+def test_frames_match_reference_renderer(cuda, svo, golden):
+    g, f = golden["dragon"], golden["frames"]
+    tree = svo.VoxelOctree.from_words(g["words"], g["center"])
+    for rot, pos, half, ref in zip(f["rot"], f["pos"], f["half"], f["frames"]):
+        img = tree.render_frame(rot, pos, 1280, 720, 16, 3 if half else 1).cpu().numpy().view(np.uint32)
+        assert np.array_equal(img, ref)
+    assert tree.device_status() == 0

@@ -70,3 +70,23 @@ def test_reference_exits_are_rejected_by_oracle(oracle):
         oracle.build_dense(np.ones((40, 40, 40), np.uint32), mem=100)
     with pytest.raises(RuntimeError):
         oracle.build_dense(np.ones((1, 1, 1), np.uint32))
+
+
+@pytest.mark.parametrize("scene", ["dragon", "spheres"])
+def test_viewer_frames(oracle, reference, scenes, golden, scene):
+    """render_oracle.c against the reference's renderBatch / renderTile
+    (oracle/ref_render.cpp) over seeded orbit cameras, full and half size."""
+    if scene == "dragon":
+        words, center = golden["dragon"]["words"], golden["dragon"]["center"]
+    else:
+        words, center = oracle.build_dense(scenes.sphere_scene(128, 24, 9))
+    tree = reference.tree_from_words(words, center)
+    rng = np.random.default_rng(31)
+    for k in range(4):
+        rot, trans, pos = scenes.viewer_camera(rng.uniform(0, 360), rng.uniform(-80, 80), rng.uniform(0.6, 2.5),
+                                               center)
+        half = k % 2 == 1
+        ref = reference.render_frame(tree, rot, trans, half)
+        img = oracle.render_frame(words, rot, pos, 1280, 720, 16, 3 if half else 1, threads=4)
+        assert np.array_equal(img, ref), (scene, k)
+    reference.free(tree)
