@@ -199,18 +199,29 @@ __global__ void __launch_bounds__(kBrickThreads) k_brick_emit(GridGeom g, uint64
 }
 
 // ---- level grouping --------------------------------------------------------
+//
+// Every level kernel takes its element count twice: `n` from the host and
+// `dn`, a device copy or nullptr.  With dn the count stays on the device
+// (the small top levels are chained without host round trips); n is then an
+// upper bound that sizes the arrays and the grid.
 
-__global__ void k_heads(const uint64_t *__restrict__ key, uint64_t n, uint32_t *__restrict__ head) {
+__device__ __forceinline__ uint64_t level_count(uint64_t n, const uint32_t *dn) { return dn ? (uint64_t)*dn : n; }
+
+// head[i] = 1 where child i starts a new parent; zero for i in [count, n), so
+// a scan over all n entries totals the parents.
+__global__ void k_heads(const uint64_t *__restrict__ key, uint64_t n, const uint32_t *__restrict__ dn,
+                        uint32_t *__restrict__ head) {
     uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    head[i] = (i == 0 || (key[i] >> 3) != (key[i - 1] >> 3)) ? 1u : 0u;
+    const uint64_t c = level_count(n, dn);
+    head[i] = i < c && (i == 0 || (key[i] >> 3) != (key[i - 1] >> 3)) ? 1u : 0u;
 }
 
-__global__ void k_parents_from_heads(const uint64_t *__restrict__ ckey, uint64_t n, const uint32_t *__restrict__ head,
-                                     const uint32_t *__restrict__ pidx, uint64_t *__restrict__ pkey,
-                                     uint32_t *__restrict__ pstart) {
+__global__ void k_parents_from_heads(const uint64_t *__restrict__ ckey, uint64_t n, const uint32_t *__restrict__ dn,
+                                     const uint32_t *__restrict__ head, const uint32_t *__restrict__ pidx,
+                                     uint64_t *__restrict__ pkey, uint32_t *__restrict__ pstart) {
     uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || !head[i]) return;
+    if (i >= level_count(n, dn) || !head[i]) return;
     uint32_t p = pidx[i];
     pkey[p] = ckey[i] >> 3;
     pstart[p] = (uint32_t)i;
@@ -218,18 +229,19 @@ __global__ void k_parents_from_heads(const uint64_t *__restrict__ ckey, uint64_t
 
 // pidx holds the exclusive scan of head flags: right for a head, one too high
 // for the siblings after it.  Turn it into the parent index of every child.
-__global__ void k_child_pidx_from_heads(const uint32_t *__restrict__ head, uint64_t n, uint32_t *__restrict__ pidx) {
+__global__ void k_child_pidx_from_heads(const uint32_t *__restrict__ head, uint64_t n, const uint32_t *__restrict__ dn,
+                                        uint32_t *__restrict__ pidx) {
     uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= level_count(n, dn)) return;
     pidx[i] = pidx[i] + head[i] - 1u;
 }
 
 // Dense grouping at the cache-block level: blk_first[b] = first child of
 // block b (or 0xFFFFFFFF); present = has children or top flag.
-__global__ void k_block_first(const uint64_t *__restrict__ ckey, uint64_t n, const uint32_t *__restrict__ head,
-                              uint32_t *__restrict__ blk_first) {
+__global__ void k_block_first(const uint64_t *__restrict__ ckey, uint64_t n, const uint32_t *__restrict__ dn,
+                              const uint32_t *__restrict__ head, uint32_t *__restrict__ blk_first) {
     uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || !head[i]) return;
+    if (i >= level_count(n, dn) || !head[i]) return;
     blk_first[ckey[i] >> 3] = (uint32_t)i;
 }
 
@@ -242,41 +254,54 @@ __global__ void k_block_present(const uint32_t *__restrict__ blk_first, const ui
 
 __global__ void k_block_parents(const uint32_t *__restrict__ blk_first, const uint32_t *__restrict__ present,
                                 const uint32_t *__restrict__ bidx, uint64_t nb, uint64_t n_child,
-                                uint64_t *__restrict__ pkey, uint32_t *__restrict__ pstart) {
+                                const uint32_t *__restrict__ dn_child, uint64_t *__restrict__ pkey,
+                                uint32_t *__restrict__ pstart) {
     uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= nb || !present[b]) return;
     uint32_t p = bidx[b];
     pkey[p] = b;
-    pstart[p] = blk_first[b] != 0xFFFFFFFFu ? blk_first[b] : (uint32_t)n_child;
+    pstart[p] = blk_first[b] != 0xFFFFFFFFu ? blk_first[b] : (uint32_t)level_count(n_child, dn_child);
 }
 
-__global__ void k_child_pidx_from_blocks(const uint64_t *__restrict__ ckey, uint64_t n, const uint32_t *__restrict__ bidx,
-                                         uint32_t *__restrict__ pidx) {
+__global__ void k_child_pidx_from_blocks(const uint64_t *__restrict__ ckey, uint64_t n, const uint32_t *__restrict__ dn,
+                                         const uint32_t *__restrict__ bidx, uint32_t *__restrict__ pidx) {
     uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= level_count(n, dn)) return;
     pidx[i] = bidx[ckey[i] >> 3];
+}
+
+// The root exists even over an empty grid: a root level with no node gets
+// one, with no children (the device-count form of the host's fix-up).
+__global__ void k_root_node(uint32_t *__restrict__ dn, uint64_t *__restrict__ key, uint32_t *__restrict__ start) {
+    if (*dn == 0) {
+        *dn = 1;
+        key[0] = 0;
+        start[0] = 0;
+    }
 }
 
 // Per parent: valid mask and child count from its run of children.
 __global__ void k_parent_masks(const uint64_t *__restrict__ pkey, const uint32_t *__restrict__ pstart, uint64_t np,
-                               const uint64_t *__restrict__ ckey, uint64_t nc, uint8_t *__restrict__ mask,
+                               const uint32_t *__restrict__ dnp, const uint64_t *__restrict__ ckey, uint64_t nc,
+                               const uint32_t *__restrict__ dnc, uint8_t *__restrict__ mask,
                                uint8_t *__restrict__ count) {
     uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= np) return;
+    if (p >= level_count(np, dnp)) return;
+    const uint64_t c_n = level_count(nc, dnc);
     uint64_t k = pkey[p];
     uint32_t m = 0, c = 0;
-    for (uint64_t i = pstart[p]; i < nc && c < 8 && (ckey[i] >> 3) == k; ++i, ++c) m |= 1u << (ckey[i] & 7);
+    for (uint64_t i = pstart[p]; i < c_n && c < 8 && (ckey[i] >> 3) == k; ++i, ++c) m |= 1u << (ckey[i] & 7);
     mask[p] = (uint8_t)m;
     count[p] = (uint8_t)c;
 }
 
 // ---- subtree sizes and far-pointer decisions (bottom-up) -------------------
 
-__global__ void k_subtree(uint64_t np, const uint8_t *__restrict__ count, const uint32_t *__restrict__ pstart,
-                          const uint64_t *__restrict__ childS, int bottom, uint64_t *__restrict__ S,
-                          uint8_t *__restrict__ large) {
+__global__ void k_subtree(uint64_t np, const uint32_t *__restrict__ dnp, const uint8_t *__restrict__ count,
+                          const uint32_t *__restrict__ pstart, const uint64_t *__restrict__ childS, int bottom,
+                          uint64_t *__restrict__ S, uint8_t *__restrict__ large) {
     uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= np) return;
+    if (p >= level_count(np, dnp)) return;
     uint32_t k = count[p];
     if (bottom) {
         S[p] = k;
@@ -306,13 +331,14 @@ __global__ void k_root_word(const uint8_t *__restrict__ mask, const uint8_t *__r
 // children's descriptors; child_is_bottom selects leafMask = 0.
 // Every word write is checked against W; a violation (an internal
 // inconsistency) is skipped and reported through *err.
-__global__ void k_place(uint64_t np, const uint8_t *__restrict__ count, const uint32_t *__restrict__ pstart,
-                        const uint8_t *__restrict__ plarge, const uint64_t *__restrict__ pB,
-                        const uint64_t *__restrict__ cS, const uint8_t *__restrict__ cmask,
-                        const uint8_t *__restrict__ clarge, int child_is_bottom, uint64_t *__restrict__ cB,
-                        uint32_t *__restrict__ words, uint64_t W, uint32_t *__restrict__ err) {
+__global__ void k_place(uint64_t np, const uint32_t *__restrict__ dnp, const uint8_t *__restrict__ count,
+                        const uint32_t *__restrict__ pstart, const uint8_t *__restrict__ plarge,
+                        const uint64_t *__restrict__ pB, const uint64_t *__restrict__ cS,
+                        const uint8_t *__restrict__ cmask, const uint8_t *__restrict__ clarge, int child_is_bottom,
+                        uint64_t *__restrict__ cB, uint32_t *__restrict__ words, uint64_t W,
+                        uint32_t *__restrict__ err) {
     uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= np) return;
+    if (p >= level_count(np, dnp)) return;
     uint32_t k = count[p];
     bool far = plarge[p] != 0;
     uint64_t stride = far ? 2 : 1;
@@ -343,13 +369,13 @@ __global__ void k_place(uint64_t np, const uint8_t *__restrict__ count, const ui
 }
 
 __global__ void k_place_leaves(uint64_t n, const uint32_t *__restrict__ pidx, uint64_t np,
-                               const uint32_t *__restrict__ pstart, const uint64_t *__restrict__ pB,
-                               const uint32_t *__restrict__ payload, uint32_t *__restrict__ words, uint64_t W,
-                               uint32_t *__restrict__ err) {
+                               const uint32_t *__restrict__ dnp, const uint32_t *__restrict__ pstart,
+                               const uint64_t *__restrict__ pB, const uint32_t *__restrict__ payload,
+                               uint32_t *__restrict__ words, uint64_t W, uint32_t *__restrict__ err) {
     uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     uint32_t p = pidx[i];
-    if (p >= np || i < pstart[p] || i - pstart[p] >= 8) {
+    if (p >= level_count(np, dnp) || i < pstart[p] || i - pstart[p] >= 8) {
         atomicOr(err, 2u);
         return;
     }
@@ -439,7 +465,8 @@ struct DevBuf {
 };
 
 struct LevelArrays {
-    uint64_t n = 0;
+    uint64_t n = 0;                // node count, or its upper bound when dn != nullptr
+    const uint32_t *dn = nullptr;  // the node count on the device (levels chained without round trips)
     DevBuf<uint64_t> key;
     DevBuf<uint32_t> start;
     DevBuf<uint8_t> mask, count, large;
@@ -468,6 +495,18 @@ int scan_to(const uint32_t *in, TO *out, uint64_t n, TO *total_host, cudaStream_
     return SVO_OK;
 }
 
+// Exclusive scan with the total left on the device (no round trip).
+template <typename TO>
+int scan_on_device(const uint32_t *in, TO *out, uint64_t n, TO *d_total, cudaStream_t st, BuildArena &arena) {
+    DevBuf<TO> scratch;
+    SVO_TRY_ALLOC(scratch.alloc(scan_scratch_elems(n), arena));
+    SVO_CUDA_TRY((exclusive_scan<uint32_t, TO>(in, out, n, d_total, scratch.p, st)));
+    return SVO_OK;
+}
+
+// Levels whose children number at most this many are chained on the device.
+constexpr uint64_t kDeviceLevels = 1ull << 20;
+
 }  // namespace
 
 int build_from_sorted_device(const uint64_t *d_keys, const uint32_t *d_payload, uint64_t N, int log_side,
@@ -482,17 +521,28 @@ int build_from_sorted_device(const uint64_t *d_keys, const uint32_t *d_payload, 
     BuildArena arena(st);  // declared first: released after every array below
 
     // Phase 2: levels e = 1..D (node edge 2^e); level 0 is the leaves.
+    // While a level's children number more than kDeviceLevels, the parent
+    // count is read back (exact array sizes).  From the first level with
+    // fewer children on, the counts stay on the device (dcount[e]) and the
+    // arrays are sized by upper bounds: no host round trip per level.
     std::vector<LevelArrays> lv(D + 1);
-    DevBuf<uint32_t> leaf_pidx;
+    DevBuf<uint32_t> leaf_pidx, dcount;
+    SVO_TRY_ALLOC(dcount.alloc(D + 1, arena));
     const uint64_t *ckey = d_keys;
-    uint64_t nc = N;
+    uint64_t nc = N;              // children: exact count, or an upper bound when cdn != nullptr
+    const uint32_t *cdn = nullptr;  // device count of the children
+    bool on_device = false;
     for (int e = 1; e <= D; ++e) {
         LevelArrays &L = lv[e];
+        if (!on_device && nc <= kDeviceLevels) on_device = true;
+        uint32_t *dn = on_device ? dcount.p + e : nullptr;
+        // at most one node per cell of edge 2^e, and never more parents than children
+        const uint64_t cells = 3 * (D - e) >= 63 ? ~0ull : 1ull << (3 * (D - e));
         DevBuf<uint32_t> head, pidx;
         SVO_TRY_ALLOC(head.alloc(nc, arena));
         SVO_TRY_ALLOC(pidx.alloc(nc, arena));
         if (nc) {
-            k_heads<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, head.p);
+            k_heads<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, cdn, head.p);
             SVO_LAUNCH_CHECK("k_heads");
         }
         if (multi_block && e == log_block) {
@@ -503,43 +553,66 @@ int build_from_sorted_device(const uint64_t *d_keys, const uint32_t *d_payload, 
             SVO_TRY_ALLOC(present.alloc(n_blocks, arena));
             SVO_TRY_ALLOC(bidx.alloc(n_blocks, arena));
             SVO_CUDA_TRY(cudaMemsetAsync(first.p, 0xFF, n_blocks * sizeof(uint32_t), st));
-            if (nc) k_block_first<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, head.p, first.p);
+            if (nc) k_block_first<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, cdn, head.p, first.p);
             k_block_present<<<blocks_for(n_blocks), 256, 0, st>>>(first.p, d_topflag, n_blocks, present.p);
             SVO_LAUNCH_CHECK("k_block_present");
-            uint32_t np = 0;
-            rc = scan_to<uint32_t>(present.p, bidx.p, n_blocks, &np, st, &arena);
+            if (on_device) {
+                rc = scan_on_device<uint32_t>(present.p, bidx.p, n_blocks, dn, st, arena);
+                L.n = n_blocks;
+            } else {
+                uint32_t np = 0;
+                rc = scan_to<uint32_t>(present.p, bidx.p, n_blocks, &np, st, &arena);
+                L.n = np;
+            }
             if (rc) return rc;
-            L.n = np;
-            SVO_TRY_ALLOC(L.key.alloc(np, arena));
-            SVO_TRY_ALLOC(L.start.alloc(np, arena));
-            k_block_parents<<<blocks_for(n_blocks), 256, 0, st>>>(first.p, present.p, bidx.p, n_blocks, nc, L.key.p,
-                                                                  L.start.p);
-            if (nc) k_child_pidx_from_blocks<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, bidx.p, pidx.p);
+            SVO_TRY_ALLOC(L.key.alloc(L.n, arena));
+            SVO_TRY_ALLOC(L.start.alloc(L.n, arena));
+            k_block_parents<<<blocks_for(n_blocks), 256, 0, st>>>(first.p, present.p, bidx.p, n_blocks, nc, cdn,
+                                                                  L.key.p, L.start.p);
+            if (nc) k_child_pidx_from_blocks<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, cdn, bidx.p, pidx.p);
             SVO_LAUNCH_CHECK("k_child_pidx_from_blocks");
         } else {
-            uint32_t np = 0;
-            rc = scan_to<uint32_t>(head.p, pidx.p, nc, &np, st, &arena);
+            if (on_device) {
+                rc = scan_on_device<uint32_t>(head.p, pidx.p, nc, dn, st, arena);
+                L.n = std::min(nc, cells);
+            } else {
+                uint32_t np = 0;
+                rc = scan_to<uint32_t>(head.p, pidx.p, nc, &np, st, &arena);
+                L.n = np;
+            }
             if (rc) return rc;
-            L.n = np;
-            SVO_TRY_ALLOC(L.key.alloc(np, arena));
-            SVO_TRY_ALLOC(L.start.alloc(np, arena));
+            SVO_TRY_ALLOC(L.key.alloc(L.n, arena));
+            SVO_TRY_ALLOC(L.start.alloc(L.n, arena));
             if (nc) {
-                k_parents_from_heads<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, head.p, pidx.p, L.key.p, L.start.p);
-                k_child_pidx_from_heads<<<blocks_for(nc), 256, 0, st>>>(head.p, nc, pidx.p);
+                k_parents_from_heads<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, cdn, head.p, pidx.p, L.key.p,
+                                                                     L.start.p);
+                k_child_pidx_from_heads<<<blocks_for(nc), 256, 0, st>>>(head.p, nc, cdn, pidx.p);
                 SVO_LAUNCH_CHECK("k_child_pidx_from_heads");
             }
         }
         // The root always exists, even over an empty grid.
-        if (e == D && L.n == 0) {
-            L.n = 1;
-            SVO_TRY_ALLOC(L.key.alloc(1, arena));
-            SVO_TRY_ALLOC(L.start.alloc(1, arena));
-            SVO_CUDA_TRY(cudaMemsetAsync(L.key.p, 0, sizeof(uint64_t), st));
-            SVO_CUDA_TRY(cudaMemsetAsync(L.start.p, 0, sizeof(uint32_t), st));
+        if (e == D) {
+            if (on_device) {
+                if (L.n == 0) {  // bound 0: the arrays hold the one node the kernel may add
+                    L.n = 1;
+                    SVO_TRY_ALLOC(L.key.alloc(1, arena));
+                    SVO_TRY_ALLOC(L.start.alloc(1, arena));
+                }
+                k_root_node<<<1, 1, 0, st>>>(dn, L.key.p, L.start.p);
+                SVO_LAUNCH_CHECK("k_root_node");
+            } else if (L.n == 0) {
+                L.n = 1;
+                SVO_TRY_ALLOC(L.key.alloc(1, arena));
+                SVO_TRY_ALLOC(L.start.alloc(1, arena));
+                SVO_CUDA_TRY(cudaMemsetAsync(L.key.p, 0, sizeof(uint64_t), st));
+                SVO_CUDA_TRY(cudaMemsetAsync(L.start.p, 0, sizeof(uint32_t), st));
+            }
         }
+        L.dn = dn;
         SVO_TRY_ALLOC(L.mask.alloc(L.n, arena));
         SVO_TRY_ALLOC(L.count.alloc(L.n, arena));
-        k_parent_masks<<<blocks_for(L.n), 256, 0, st>>>(L.key.p, L.start.p, L.n, ckey, nc, L.mask.p, L.count.p);
+        k_parent_masks<<<blocks_for(L.n), 256, 0, st>>>(L.key.p, L.start.p, L.n, L.dn, ckey, nc, cdn, L.mask.p,
+                                                        L.count.p);
         SVO_LAUNCH_CHECK("k_parent_masks");
         if (e == 1) {
             leaf_pidx.p = pidx.p;
@@ -548,6 +621,7 @@ int build_from_sorted_device(const uint64_t *d_keys, const uint32_t *d_payload, 
         }
         ckey = L.key.p;
         nc = L.n;
+        cdn = L.dn;
     }
 
     // Subtree sizes, bottom-up.
@@ -555,7 +629,7 @@ int build_from_sorted_device(const uint64_t *d_keys, const uint32_t *d_payload, 
         LevelArrays &L = lv[e];
         SVO_TRY_ALLOC(L.S.alloc(L.n, arena));
         SVO_TRY_ALLOC(L.large.alloc(L.n, arena));
-        k_subtree<<<blocks_for(L.n), 256, 0, st>>>(L.n, L.count.p, L.start.p, e > 1 ? lv[e - 1].S.p : nullptr,
+        k_subtree<<<blocks_for(L.n), 256, 0, st>>>(L.n, L.dn, L.count.p, L.start.p, e > 1 ? lv[e - 1].S.p : nullptr,
                                                   e == 1, L.S.p, L.large.p);
         SVO_LAUNCH_CHECK("k_subtree");
     }
@@ -578,13 +652,13 @@ int build_from_sorted_device(const uint64_t *d_keys, const uint32_t *d_payload, 
         LevelArrays &P = lv[e];
         LevelArrays &C = lv[e - 1];
         SVO_TRY_ALLOC(C.B.alloc(C.n, arena));
-        k_place<<<blocks_for(P.n), 256, 0, st>>>(P.n, P.count.p, P.start.p, P.large.p, P.B.p, C.S.p, C.mask.p,
-                                                C.large.p, e - 1 == 1, C.B.p, words, W, err.p);
+        k_place<<<blocks_for(P.n), 256, 0, st>>>(P.n, P.dn, P.count.p, P.start.p, P.large.p, P.B.p, C.S.p,
+                                                C.mask.p, C.large.p, e - 1 == 1, C.B.p, words, W, err.p);
         SVO_LAUNCH_CHECK("k_place");
     }
     if (N) {
-        k_place_leaves<<<blocks_for(N), 256, 0, st>>>(N, leaf_pidx.p, lv[1].n, lv[1].start.p, lv[1].B.p, d_payload,
-                                                      words, W, err.p);
+        k_place_leaves<<<blocks_for(N), 256, 0, st>>>(N, leaf_pidx.p, lv[1].n, lv[1].dn, lv[1].start.p, lv[1].B.p,
+                                                      d_payload, words, W, err.p);
         SVO_LAUNCH_CHECK("k_place_leaves");
     }
     uint32_t err_h = 0;
@@ -786,7 +860,7 @@ int build_dense_noalloc(const uint32_t *d_grid, int w, int h, int d, int log_sid
         SVO_ARENA_TAKE(head, uint32_t, nc);
         SVO_ARENA_TAKE(pidx, uint32_t, nc);
         if (nc) {
-            k_heads<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, head);
+            k_heads<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, nullptr, head);
             SVO_LAUNCH_CHECK("k_heads");
         }
         uint32_t np = 0;
@@ -795,7 +869,7 @@ int build_dense_noalloc(const uint32_t *d_grid, int w, int h, int d, int log_sid
             SVO_ARENA_TAKE(present, uint32_t, n_blocks);
             SVO_ARENA_TAKE(bidx, uint32_t, n_blocks);
             SVO_CUDA_TRY(cudaMemsetAsync(first, 0xFF, n_blocks * sizeof(uint32_t), st));
-            if (nc) k_block_first<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, head, first);
+            if (nc) k_block_first<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, nullptr, head, first);
             k_block_present<<<blocks_for(n_blocks), 256, 0, st>>>(first, g.topflag, n_blocks, present);
             SVO_LAUNCH_CHECK("k_block_present");
             rc = arena_scan<uint32_t>(arena, present, bidx, n_blocks, &np, st);
@@ -805,8 +879,9 @@ int build_dense_noalloc(const uint32_t *d_grid, int w, int h, int d, int log_sid
             SVO_ARENA_TAKE(start, uint32_t, np);
             L.key = key;
             L.start = start;
-            k_block_parents<<<blocks_for(n_blocks), 256, 0, st>>>(first, present, bidx, n_blocks, nc, L.key, L.start);
-            if (nc) k_child_pidx_from_blocks<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, bidx, pidx);
+            k_block_parents<<<blocks_for(n_blocks), 256, 0, st>>>(first, present, bidx, n_blocks, nc, nullptr, L.key,
+                                                                  L.start);
+            if (nc) k_child_pidx_from_blocks<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, nullptr, bidx, pidx);
             SVO_LAUNCH_CHECK("k_child_pidx_from_blocks");
         } else {
             rc = arena_scan<uint32_t>(arena, head, pidx, nc, &np, st);
@@ -817,8 +892,8 @@ int build_dense_noalloc(const uint32_t *d_grid, int w, int h, int d, int log_sid
             L.key = key;
             L.start = start;
             if (nc) {
-                k_parents_from_heads<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, head, pidx, L.key, L.start);
-                k_child_pidx_from_heads<<<blocks_for(nc), 256, 0, st>>>(head, nc, pidx);
+                k_parents_from_heads<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, nullptr, head, pidx, L.key, L.start);
+                k_child_pidx_from_heads<<<blocks_for(nc), 256, 0, st>>>(head, nc, nullptr, pidx);
                 SVO_LAUNCH_CHECK("k_child_pidx_from_heads");
             }
         }
@@ -835,7 +910,8 @@ int build_dense_noalloc(const uint32_t *d_grid, int w, int h, int d, int log_sid
         SVO_ARENA_TAKE(count, uint8_t, L.n);
         L.mask = mask;
         L.count = count;
-        k_parent_masks<<<blocks_for(L.n), 256, 0, st>>>(L.key, L.start, L.n, ckey, nc, L.mask, L.count);
+        k_parent_masks<<<blocks_for(L.n), 256, 0, st>>>(L.key, L.start, L.n, nullptr, ckey, nc, nullptr, L.mask,
+                                                        L.count);
         SVO_LAUNCH_CHECK("k_parent_masks");
         if (e == 1) leaf_pidx = pidx;
         ckey = L.key;
@@ -847,7 +923,7 @@ int build_dense_noalloc(const uint32_t *d_grid, int w, int h, int d, int log_sid
         SVO_ARENA_TAKE(large, uint8_t, L.n);
         L.S = S;
         L.large = large;
-        k_subtree<<<blocks_for(L.n), 256, 0, st>>>(L.n, L.count, L.start, e > 1 ? lv[e - 1].S : nullptr, e == 1,
+        k_subtree<<<blocks_for(L.n), 256, 0, st>>>(L.n, nullptr, L.count, L.start, e > 1 ? lv[e - 1].S : nullptr, e == 1,
                                                   L.S, L.large);
         SVO_LAUNCH_CHECK("k_subtree");
     }
@@ -870,12 +946,12 @@ int build_dense_noalloc(const uint32_t *d_grid, int w, int h, int d, int log_sid
         ArenaLevel &C = lv[e - 1];
         SVO_ARENA_TAKE(cB, uint64_t, C.n);
         C.B = cB;
-        k_place<<<blocks_for(P.n), 256, 0, st>>>(P.n, P.count, P.start, P.large, P.B, C.S, C.mask, C.large,
+        k_place<<<blocks_for(P.n), 256, 0, st>>>(P.n, nullptr, P.count, P.start, P.large, P.B, C.S, C.mask, C.large,
                                                 e - 1 == 1, C.B, d_words, W, err);
         SVO_LAUNCH_CHECK("k_place");
     }
     if (N) {
-        k_place_leaves<<<blocks_for(N), 256, 0, st>>>(N, leaf_pidx, lv[1].n, lv[1].start, lv[1].B, lpay, d_words, W,
+        k_place_leaves<<<blocks_for(N), 256, 0, st>>>(N, leaf_pidx, lv[1].n, nullptr, lv[1].start, lv[1].B, lpay, d_words, W,
                                                       err);
         SVO_LAUNCH_CHECK("k_place_leaves");
     }
