@@ -918,9 +918,9 @@ MESH_SLAB_MEM = 1 << 28  # 270 of the volume's 1023 slices per slab: four slabs
 
 def profiled_launches_per_build():
     """Kernel launches of one mesh build, from the committed ncu launch list
-    (profiles/mesh_build_config2.md)."""
+    (profiles/mesh_build_icosphere1024.md)."""
     try:
-        for line in open(os.path.join(ROOT, "profiles", "mesh_build_config2.md")):
+        for line in open(os.path.join(ROOT, "profiles", "mesh_build_icosphere1024.md")):
             if line.startswith("launches per build:"):
                 return int(line.split(":")[1])
     except OSError:
@@ -1293,9 +1293,9 @@ def profiled_traffic(rays):
     """DRAM bytes per launch from the committed ncu summaries (per ray, times
     the launch's rays), and where the figure comes from: it is read from a
     committed capture, not measured in this run."""
-    for name, what in (("dram_config1_fullsize.txt", "one-pass ncu capture (dram__bytes_read.sum + "
+    for name, what in (("dram_trace_terrain2048.txt", "one-pass ncu capture (dram__bytes_read.sum + "
                                                       "dram__bytes_write.sum) of this kernel on this workload"),
-                       ("trace_image_config1.txt", "ncu capture of this kernel on the 1024^3 case")):
+                       ("trace_image_terrain1024.txt", "ncu capture of this kernel on the 1024^3 case")):
         try:
             for line in open(os.path.join(ROOT, "profiles", name)):
                 if line.startswith("dram_bytes_per_ray:"):
@@ -1311,7 +1311,7 @@ def profiled_issue():
     """Issue utilisation of the primary-ray kernel from the committed ncu
     summary: the bound this kernel actually meets (it is issue-bound on the
     ALU pipe, with DRAM at about 5% of peak)."""
-    path = os.path.join(ROOT, "profiles", "trace_image_config1.txt")
+    path = os.path.join(ROOT, "profiles", "trace_image_terrain1024.txt")
     import re
     out = {}
     first = lambda line: float(re.findall(r"(?<![\w.])(\d+\.\d+|\d+)(?![\w.])", line.split(")")[-1] if ")" in line
@@ -1326,7 +1326,7 @@ def profiled_issue():
                 out["simt_lanes_of_32"] = first(line)
     except (OSError, ValueError, IndexError):
         return None
-    out["source"] = "profiles/trace_image_config1.txt (ncu --set full, same kernel, smaller case)"
+    out["source"] = "profiles/trace_image_terrain1024.txt (ncu --set full, same kernel, smaller case)"
     return out or None
 
 

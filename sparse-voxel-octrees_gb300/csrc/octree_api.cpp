@@ -85,17 +85,19 @@ int make_handle(uint32_t *d_words, uint64_t n_words, const float center[3], svo_
     h->n_words = n_words;
     std::memcpy(h->center, center, sizeof(h->center));
     cudaGetDevice(&h->device);
-    // One 32-byte control block: the three work counters, then the error word.
+    // One control block: the work counters, then the error word.
+    const size_t ctrl_bytes = svo_octree::kQueues * sizeof(unsigned long long) + 8;
     void *ctrl = nullptr;
-    cudaError_t e = cudaMalloc(&ctrl, 32);
+    cudaError_t e = cudaMalloc(&ctrl, ctrl_bytes);
     if (e != cudaSuccess) {
         cudaFree(d_words);
         h->d_words = nullptr;
         return cuda_fail(e, "cudaMalloc(control block)");
     }
     h->d_queue = static_cast<unsigned long long *>(ctrl);
-    h->d_status = reinterpret_cast<uint32_t *>(static_cast<char *>(ctrl) + 3 * sizeof(unsigned long long));
-    e = cudaMemset(ctrl, 0, 32);
+    h->d_status = reinterpret_cast<uint32_t *>(static_cast<char *>(ctrl) +
+                                               svo_octree::kQueues * sizeof(unsigned long long));
+    e = cudaMemset(ctrl, 0, ctrl_bytes);
     if (e != cudaSuccess) {
         svo_octree_destroy(h.release());
         return cuda_fail(e, "cudaMemset(control block)");
@@ -151,38 +153,45 @@ static std::vector<uint64_t> plan_chunks(uint64_t total, uint64_t target, uint64
 }
 
 // The host-buffer pipeline of svo_trace_host and svo_trace_image_host.  Chunk
-// k's rays go in on a copy-in stream, are traced on trace stream k % 2 (the
-// two have separate work counters, so one chunk's persistent launch fills the
-// tail of the previous one) and come out on a copy-out stream.  Trace stream
-// h owns half h of the staging arena; the half's rays are overwritten only
-// after its previous trace, and its results only after their copy-out.
-// launch(d_rays, rays, outputs, stream, half) enqueues one chunk's trace.
+// k's rays go in on the copy-in stream into staging buffer k % B, are traced
+// on that buffer's trace stream (each with its own work counter, so one
+// chunk's persistent launch fills the tail of the previous one) and come out
+// on the copy-out stream.  A buffer's rays are overwritten only after its
+// previous trace, and its results only after their copy-out.  With two
+// buffers a buffer's whole cycle (copy in, trace, copy out) paced the copy-in
+// stream; with four, the copy-in stream runs back to back, which the host
+// link's transfer rate then bounds.
+// launch(d_rays, rays, outputs, stream, buffer) enqueues one chunk's trace.
 template <typename Launch>
-static int host_pipeline(svo_octree *oct, const float *rays, const std::vector<uint64_t> &plan, uint64_t max_chunk,
+static int host_pipeline(svo_octree *oct, const float *rays, const std::vector<uint64_t> &plan,
                          const svo_trace_out &out, Launch launch) {
-    const uint64_t C = max_chunk;
-    // Per half: rays 24 B, hit 1, t 4, leaf 4, word 4, rgb 12, rgba8 4 (256-byte aligned arrays).
+    uint64_t C = 0;
+    for (uint64_t m : plan) C = std::max(C, m);
+    const int B = (int)std::min<size_t>(svo_octree::kStageBuffers, plan.size());
+    // Per buffer: rays 24 B, hit 1, t 4, leaf 4, word 4, rgb 12, rgba8 4 (256-byte aligned arrays).
     auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
-    const size_t half = al(C * 24) + al(C) + al(C * 4) * 4 + al(C * 12);
-    int rc = ensure_staging(oct, 2 * half);
+    const size_t buf = al(C * 24) + al(C) + al(C * 4) * 4 + al(C * 12);
+    int rc = ensure_staging(oct, B * buf);
     if (rc) return rc;
-    if (!oct->img_streams[0]) {
-        for (auto &st : oct->img_streams) SVO_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-        for (int k = 0; k < 2; ++k) {
-            SVO_CUDA_TRY(cudaEventCreateWithFlags(&oct->img_in[k], cudaEventDisableTiming));
-            SVO_CUDA_TRY(cudaEventCreateWithFlags(&oct->img_traced[k], cudaEventDisableTiming));
-            SVO_CUDA_TRY(cudaEventCreateWithFlags(&oct->img_out[k], cudaEventDisableTiming));
+    if (!oct->copy_in) {
+        SVO_CUDA_TRY(cudaStreamCreateWithFlags(&oct->copy_in, cudaStreamNonBlocking));
+        SVO_CUDA_TRY(cudaStreamCreateWithFlags(&oct->copy_out, cudaStreamNonBlocking));
+        for (int k = 0; k < svo_octree::kStageBuffers; ++k) {
+            SVO_CUDA_TRY(cudaStreamCreateWithFlags(&oct->stage_trace[k], cudaStreamNonBlocking));
+            SVO_CUDA_TRY(cudaEventCreateWithFlags(&oct->stage_in[k], cudaEventDisableTiming));
+            SVO_CUDA_TRY(cudaEventCreateWithFlags(&oct->stage_traced[k], cudaEventDisableTiming));
+            SVO_CUDA_TRY(cudaEventCreateWithFlags(&oct->stage_out[k], cudaEventDisableTiming));
         }
     }
-    cudaStream_t si = oct->img_streams[0], so = oct->img_streams[3];
-    cudaStream_t skh[2] = {oct->img_streams[1], oct->img_streams[2]};
+    cudaStream_t si = oct->copy_in, so = oct->copy_out;
     auto enqueue = [&]() -> int {
         uint64_t c0 = 0;
         for (size_t j = 0; j < plan.size(); c0 += plan[j], ++j) {
-            const int h = (int)(j & 1);
+            const int h = (int)(j % (size_t)B);
+            const bool reused = j >= (size_t)B;
             const uint64_t m = plan[j];
-            cudaStream_t sk = skh[h];
-            uint8_t *base = (uint8_t *)oct->stage_dev + h * half;
+            cudaStream_t sk = oct->stage_trace[h];
+            uint8_t *base = (uint8_t *)oct->stage_dev + h * buf;
             float *d_rays = (float *)base;
             uint8_t *d_hit = base + al(C * 24);
             float *d_t = (float *)(d_hit + al(C));
@@ -190,11 +199,11 @@ static int host_pipeline(svo_octree *oct, const float *rays, const std::vector<u
             uint32_t *d_word = (uint32_t *)((uint8_t *)d_leaf + al(C * 4));
             float *d_rgb = (float *)((uint8_t *)d_word + al(C * 4));
             uint32_t *d_rgba8 = (uint32_t *)((uint8_t *)d_rgb + al(C * 12));
-            if (j >= 2) SVO_CUDA_TRY(cudaStreamWaitEvent(si, oct->img_traced[h], 0));
+            if (reused) SVO_CUDA_TRY(cudaStreamWaitEvent(si, oct->stage_traced[h], 0));
             SVO_CUDA_TRY(cudaMemcpyAsync(d_rays, rays + 6 * c0, m * 24, cudaMemcpyHostToDevice, si));
-            SVO_CUDA_TRY(cudaEventRecord(oct->img_in[h], si));
-            SVO_CUDA_TRY(cudaStreamWaitEvent(sk, oct->img_in[h], 0));
-            if (j >= 2) SVO_CUDA_TRY(cudaStreamWaitEvent(sk, oct->img_out[h], 0));
+            SVO_CUDA_TRY(cudaEventRecord(oct->stage_in[h], si));
+            SVO_CUDA_TRY(cudaStreamWaitEvent(sk, oct->stage_in[h], 0));
+            if (reused) SVO_CUDA_TRY(cudaStreamWaitEvent(sk, oct->stage_out[h], 0));
             svo_trace_out o;
             o.hit = out.hit ? d_hit : nullptr;
             o.t = out.t ? d_t : nullptr;
@@ -204,8 +213,8 @@ static int host_pipeline(svo_octree *oct, const float *rays, const std::vector<u
             o.rgba8 = out.rgba8 ? d_rgba8 : nullptr;
             rc = launch(d_rays, m, o, sk, h);
             if (rc) return rc;
-            SVO_CUDA_TRY(cudaEventRecord(oct->img_traced[h], sk));
-            SVO_CUDA_TRY(cudaStreamWaitEvent(so, oct->img_traced[h], 0));
+            SVO_CUDA_TRY(cudaEventRecord(oct->stage_traced[h], sk));
+            SVO_CUDA_TRY(cudaStreamWaitEvent(so, oct->stage_traced[h], 0));
             if (out.hit) SVO_CUDA_TRY(cudaMemcpyAsync(out.hit + c0, d_hit, m, cudaMemcpyDeviceToHost, so));
             if (out.t) SVO_CUDA_TRY(cudaMemcpyAsync(out.t + c0, d_t, m * 4, cudaMemcpyDeviceToHost, so));
             if (out.leaf) SVO_CUDA_TRY(cudaMemcpyAsync(out.leaf + c0, d_leaf, m * 4, cudaMemcpyDeviceToHost, so));
@@ -213,18 +222,21 @@ static int host_pipeline(svo_octree *oct, const float *rays, const std::vector<u
             if (out.rgb) SVO_CUDA_TRY(cudaMemcpyAsync(out.rgb + 3 * c0, d_rgb, m * 12, cudaMemcpyDeviceToHost, so));
             if (out.rgba8)
                 SVO_CUDA_TRY(cudaMemcpyAsync(out.rgba8 + c0, d_rgba8, m * 4, cudaMemcpyDeviceToHost, so));
-            SVO_CUDA_TRY(cudaEventRecord(oct->img_out[h], so));
+            SVO_CUDA_TRY(cudaEventRecord(oct->stage_out[h], so));
         }
         return SVO_OK;
     };
     rc = enqueue();
-    // All four streams are drained even when a chunk failed to enqueue: the
-    // staging halves must be idle before the next call reuses them.
+    // Every stream is drained even when a chunk failed to enqueue: the
+    // staging buffers must be idle before the next call reuses them.
     cudaError_t e = cudaSuccess;
-    for (cudaStream_t q : {si, skh[0], skh[1], so}) {
+    auto drain = [&](cudaStream_t q) {
         const cudaError_t eq = cudaStreamSynchronize(q);
         if (e == cudaSuccess) e = eq;
-    }
+    };
+    drain(si);
+    for (int k = 0; k < svo_octree::kStageBuffers; ++k) drain(oct->stage_trace[k]);
+    drain(so);
     if (rc) return rc;
     if (e != cudaSuccess) return cuda_fail(e, "host trace pipeline");
     return check_device_status(oct);
@@ -384,12 +396,13 @@ int svo_octree_destroy(svo_octree *oct) {
     if (oct->d_tab) cudaFree(oct->d_tab);
     if (oct->d_queue) cudaFree(oct->d_queue);  // the control block (d_status lies inside it)
     if (oct->stage_dev) cudaFree(oct->stage_dev);
-    for (auto &s : oct->img_streams)
-        if (s) cudaStreamDestroy(s);
-    for (int k = 0; k < 2; ++k) {
-        if (oct->img_in[k]) cudaEventDestroy(oct->img_in[k]);
-        if (oct->img_traced[k]) cudaEventDestroy(oct->img_traced[k]);
-        if (oct->img_out[k]) cudaEventDestroy(oct->img_out[k]);
+    if (oct->copy_in) cudaStreamDestroy(oct->copy_in);
+    if (oct->copy_out) cudaStreamDestroy(oct->copy_out);
+    for (int k = 0; k < svo_octree::kStageBuffers; ++k) {
+        if (oct->stage_trace[k]) cudaStreamDestroy(oct->stage_trace[k]);
+        if (oct->stage_in[k]) cudaEventDestroy(oct->stage_in[k]);
+        if (oct->stage_traced[k]) cudaEventDestroy(oct->stage_traced[k]);
+        if (oct->stage_out[k]) cudaEventDestroy(oct->stage_out[k]);
     }
     delete oct;
     return SVO_OK;
@@ -626,7 +639,7 @@ int svo_trace_host(svo_octree *oct, const float *rays, uint64_t n, float ray_sca
     std::lock_guard<std::mutex> lock(oct->staging_mtx);
     // warp-aligned chunks
     const std::vector<uint64_t> plan = plan_chunks(n, kStageRays, 32);
-    return host_pipeline(oct, rays, plan, kStageRays, *out,
+    return host_pipeline(oct, rays, plan, *out,
                          [&](const float *d_rays, uint64_t m, const svo_trace_out &o, cudaStream_t st, int) {
                              return launch_trace(oct, d_rays, m, ray_scale, light, o, st);
                          });
@@ -644,10 +657,10 @@ int svo_trace_image_host(svo_octree *oct, const float *rays, uint32_t width, uin
     const uint64_t rows = std::max<uint64_t>(4, (kStageRays / width) & ~uint64_t(3));
     std::vector<uint64_t> plan = plan_chunks(height, rows, 4);
     for (auto &c : plan) c *= width;
-    return host_pipeline(oct, rays, plan, rows * width, *out,
-                         [&](const float *d_rays, uint64_t m, const svo_trace_out &o, cudaStream_t st, int half) {
+    return host_pipeline(oct, rays, plan, *out,
+                         [&](const float *d_rays, uint64_t m, const svo_trace_out &o, cudaStream_t st, int buffer) {
                              return launch_trace_image(oct, d_rays, width, (uint32_t)(m / width), ray_scale, light,
-                                                       o, st, 1 + half);
+                                                       o, st, 1 + buffer);
                          });
 }
 

@@ -21,10 +21,10 @@ struct svo_octree {
     uint64_t n_words = 0;
     float center[3] = {0.0f, 0.0f, 0.0f};
     int device = 0;
-    // One 32-byte device control block: d_queue at its start, d_status at byte 24.
+    // One device control block: kQueues work counters, then d_status.
     uint32_t *d_status = nullptr;  // device error word: bit 0 = a ray ended with kFault
     unsigned long long *d_queue = nullptr;  // work counters: [0] svo_trace_image and the differentiable
-                                            // launches, [1] and [2] svo_trace_image_host's two trace streams
+                                            // launches, [1 + b] svo_trace_image_host's trace stream b
     int index_bits = 32;  // 64: svo_trace uses 64-bit word indices even when n_words fits 32 bits
 
     // Descriptor table of the table traversal (octree_table.cu), built by the
@@ -36,13 +36,17 @@ struct svo_octree {
     mutable std::mutex tab_mtx;
 
     // Host-buffer pipeline of svo_trace_host and svo_trace_image_host: one
-    // device staging arena split into two halves, copy-in, trace and copy-out
-    // streams, and per-half events (inputs landed, trace done, outputs copied).
+    // device staging arena split into kStageBuffers buffers, a copy-in and a
+    // copy-out stream, one trace stream per buffer, and per-buffer events
+    // (inputs landed, trace done, outputs copied).
+    static constexpr int kStageBuffers = 4;
+    static constexpr int kQueues = 1 + kStageBuffers;
     std::mutex staging_mtx;
     void *stage_dev = nullptr;
     size_t stage_dev_bytes = 0;
-    cudaStream_t img_streams[4] = {nullptr, nullptr, nullptr, nullptr};  // copy in, trace x2, copy out
-    cudaEvent_t img_in[2] = {nullptr, nullptr}, img_traced[2] = {nullptr, nullptr}, img_out[2] = {nullptr, nullptr};
+    cudaStream_t copy_in = nullptr, copy_out = nullptr;
+    cudaStream_t stage_trace[kStageBuffers] = {};
+    cudaEvent_t stage_in[kStageBuffers] = {}, stage_traced[kStageBuffers] = {}, stage_out[kStageBuffers] = {};
 };
 
 namespace svo {

@@ -435,6 +435,11 @@ struct FoldArgs {
     uint8_t *counts;
     uint32_t *next;  // work counter of this launch (zero at launch): bricks taken so far
     uint32_t brick_mask;  // the brick's Morton key within a pair key (slab mode keys carry the slab above it)
+    // Optional: per brick of the block (Morton index of the brick relative to
+    // org), nonzero where the buffer may hold a nonzero word before this
+    // fold.  A brick marked 0 starts from zeros and is not read.
+    const uint8_t *pre_dirty;
+    uint64_t n_pre;
 };
 
 // PlyLoader::writeTriangleCell on a register copy of one buffer cell.
@@ -549,12 +554,20 @@ __global__ void __launch_bounds__(kFoldWarps * 32, 8) k_fold_bricks(FoldArgs a) 
         const uint32_t key = a.bkey[j] & a.brick_mask;
         const int ox = (int)(compact3(key) << le), oy = (int)(compact3((uint64_t)key >> 1) << le),
                   oz = (int)(compact3((uint64_t)key >> 2) << le);
+        // a brick the buffer holds only zeros for is not read (the extraction
+        // cleared what earlier blocks left, except their dropped slices)
+        bool clean = false;
+        if (a.pre_dirty && ox >= a.org[0] && oy >= a.org[1] && oz >= a.org[2]) {
+            const uint64_t pm = morton3((uint32_t)((ox - a.org[0]) >> le), (uint32_t)((oy - a.org[1]) >> le),
+                                        (uint32_t)((oz - a.org[2]) >> le));
+            clean = pm < a.n_pre && a.pre_dirty[pm] == 0;
+        }
         __syncwarp();
         for (int i = lane; i < E3; i += 32) {
             int x = ox + (i & (E - 1)), y = oy + ((i >> le) & (E - 1)), z = oz + (i >> (2 * le));
             uint32_t wv = 0, cv = 0;
             // a slab's bricks may start below its first slice (z-slabs need not be brick-aligned)
-            if (x >= a.org[0] && y >= a.org[1] && z >= a.org[2] && x < end0 && y < end1 && z < end2) {
+            if (!clean && x >= a.org[0] && y >= a.org[1] && z >= a.org[2] && x < end0 && y < end1 && z < end2) {
                 uint64_t bi = (uint64_t)(x - a.org[0]) +
                               (uint64_t)a.buf[0] * ((uint64_t)(y - a.org[1]) + (uint64_t)a.buf[1] * (uint64_t)(z - a.org[2]));
                 wv = a.data[bi];
@@ -1112,7 +1125,8 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
     const uint32_t brick_mask = g.slab_mode ? (uint32_t)((1ull << g.brick_bits) - 1) : 0xFFFFFFFFu;
     // PlyLoader::processBlock (PlyLoader.cpp:439-458) of job ji, whose buffer
     // `data` starts at org with edges buf: its bricks' pairs folded into it
-    auto fold_block = [&](size_t ji, const int org[3], const int buf[3], uint32_t *data) -> int {
+    auto fold_block = [&](size_t ji, const int org[3], const int buf[3], uint32_t *data, const uint8_t *pre_dirty,
+                          uint64_t n_pre) -> int {
         const BlockJob &j = jobs[ji];
         if (j.last <= j.first) return SVO_OK;
         FoldArgs fa;
@@ -1138,6 +1152,8 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
         fa.counts = counts.p;
         fa.next = fold_next.p + ji;
         fa.brick_mask = brick_mask;
+        fa.pre_dirty = pre_dirty;
+        fa.n_pre = n_pre;
         unsigned grid = (unsigned)std::min<uint64_t>((j.last - j.first + kFoldWarps - 1) / kFoldWarps, fold_grid);
         k_fold_bricks<<<grid, kFoldWarps * 32, 0, st>>>(fa);
         SVO_LAUNCH_OK("k_fold_bricks");
@@ -1163,7 +1179,7 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
                                              cudaMemcpyDeviceToDevice, st));
             const int org[3] = {0, 0, s * slab}, buf[3] = {dims[0], dims[1], nz};
             if (ji < jobs.size() && jobs[ji].morton == (uint32_t)s) {
-                int rc = fold_block(ji, org, buf, region);
+                int rc = fold_block(ji, org, buf, region, nullptr, 0);
                 if (rc) return rc;
                 ++ji;
             }
@@ -1219,20 +1235,15 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
             if (fa.buf[k] <= 0) inside = false;
         }
         if (!inside) continue;  // VoxelData::prepareDataAccess returns early
-        int rc = fold_block((size_t)(&j - jobs.data()), fa.org, fa.buf, data_p);
-        if (rc) return rc;
-        // candidate bricks: folded here, or under an earlier block's dropped
-        // slice (all bricks, when those slices are large)
+        // Bricks under an earlier block's dropped slice may hold nonzero words
+        // before this fold; every other buffer cell is zero (the extraction
+        // cleared it).  When those slices are large, every brick counts.
         const uint64_t vol = (uint64_t)fa.buf[0] * fa.buf[1] * fa.buf[2];
-        if (ghost_len * 4 > vol) {
+        const bool all_dirty = ghost_len * 4 > vol;
+        if (all_dirty) {
             SVO_CUDA_TRY(cudaMemsetAsync(dirty.p, 1, n_e, st));
         } else {
             SVO_CUDA_TRY(cudaMemsetAsync(dirty.p, 0, n_e, st));
-            if (j.last > j.first) {
-                k_mark_folded<<<grid_for(j.last - j.first), 256, 0, st>>>(bkey.p, j.first, j.last, g.log_e, fa.org[0],
-                                                                         fa.org[1], fa.org[2], dirty.p, n_e);
-                SVO_LAUNCH_OK("k_mark_folded");
-            }
             for (const auto &r : ghosts) {
                 uint64_t s1 = std::min(r.second, vol);
                 if (r.first >= s1) continue;
@@ -1240,6 +1251,14 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
                                                                     g.log_e, dirty.p, n_e);
                 SVO_LAUNCH_OK("k_mark_range");
             }
+        }
+        int rc = fold_block((size_t)(&j - jobs.data()), fa.org, fa.buf, data_p, all_dirty ? nullptr : dirty.p, n_e);
+        if (rc) return rc;
+        // candidate bricks for the extraction: those, and the bricks folded here
+        if (!all_dirty && j.last > j.first) {
+            k_mark_folded<<<grid_for(j.last - j.first), 256, 0, st>>>(bkey.p, j.first, j.last, g.log_e, fa.org[0],
+                                                                     fa.org[1], fa.org[2], dirty.p, n_e);
+            SVO_LAUNCH_OK("k_mark_folded");
         }
         k_flag_to_u32<<<grid_for(n_e), 256, 0, st>>>(dirty.p, n_e, d32.p);
         SVO_LAUNCH_OK("k_flag_to_u32");
