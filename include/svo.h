@@ -320,6 +320,24 @@ int svo_trace_image(const svo_octree *oct, const float *rays, uint32_t width, ui
 int svo_trace_image_host(svo_octree *oct, const float *rays, uint32_t width, uint32_t height, float ray_scale,
                          const float light[3], const svo_trace_out *out);
 
+/* No counterpart in the reference (whose raymarch is one blocking call per
+ * ray).  svo_trace_host and svo_trace_image_host without the wait: the call
+ * queues its copies and traces on the handle's host pipeline and returns.
+ * Calls on one handle run in call order through that pipeline, so a second
+ * call's input copies overlap the first call's traces.  The rays must stay
+ * unchanged, and the outputs unread, until svo_octree_synchronize(oct)
+ * returns; with page-locked host memory the copies run asynchronously, with
+ * pageable memory the CUDA runtime stages them and the call returns later.
+ * Traversal faults (corrupt octrees) are reported by svo_octree_synchronize. */
+int svo_trace_host_async(svo_octree *oct, const float *rays, uint64_t n, float ray_scale, const float light[3],
+                         const svo_trace_out *out);
+int svo_trace_image_host_async(svo_octree *oct, const float *rays, uint32_t width, uint32_t height,
+                               float ray_scale, const float light[3], const svo_trace_out *out);
+
+/* Waits until every host trace queued on the handle (svo_trace_host_async,
+ * svo_trace_image_host_async) has its results on the host. */
+int svo_octree_synchronize(svo_octree *oct);
+
 /* Device-side load counter for the roofline: for each ray, the number of
  * octree words the reference's raymarch reads (descriptor fetches at
  * VoxelOctree.cpp:254, far words at :279, the leaf word at :282).  Slower

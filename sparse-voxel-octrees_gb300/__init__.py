@@ -124,6 +124,11 @@ def _load():
                                            ctypes.POINTER(TraceOut), _vp]),
         "svo_trace_image_host": (ctypes.c_int, [_vp, _vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float, _f32p,
                                                 ctypes.POINTER(TraceOut)]),
+        "svo_trace_host_async": (ctypes.c_int, [_vp, _vp, ctypes.c_uint64, ctypes.c_float, _f32p,
+                                                ctypes.POINTER(TraceOut)]),
+        "svo_trace_image_host_async": (ctypes.c_int, [_vp, _vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float,
+                                                      _f32p, ctypes.POINTER(TraceOut)]),
+        "svo_octree_synchronize": (ctypes.c_int, [_vp]),
         "svo_diff_forward": (ctypes.c_int, [_vp, _vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _vp, _vp, _vp,
                                             _vp, _vp, _vp]),
         "svo_diff_backward": (ctypes.c_int, [_vp, _vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _vp, _vp, _vp,
@@ -340,6 +345,7 @@ class VoxelOctree:
 
     def __init__(self, source=None, stream=None, _handle=None):
         self._h = _vp()
+        self._pending = []  # host arrays of asynchronous traces, kept alive until synchronize()
         if _handle is not None:
             self._h = _handle
         elif isinstance(source, (str, bytes, os.PathLike)):
@@ -379,8 +385,16 @@ class VoxelOctree:
 
     def close(self):
         if self._h:
-            lib.svo_octree_destroy(self._h)
+            lib.svo_octree_destroy(self._h)  # waits for queued host traces first
             self._h = _vp()
+        self._pending = []
+
+    def synchronize(self):
+        """Waits for the host traces queued with wait=False (svo_octree_synchronize)."""
+        try:
+            check(lib.svo_octree_synchronize(self._h))
+        finally:
+            self._pending = []
 
     def __del__(self):
         try:
@@ -470,9 +484,11 @@ class VoxelOctree:
                             ctypes.byref(o), _stream_ptr(stream)))
 
     def trace_host(self, rays, ray_scale=0.0, light=(0.0, 0.0, 1.0), outputs=("hit", "t", "leaf", "word", "rgb"),
-                   out=None):
+                   out=None, wait=True):
         """Host form: rays is a numpy (R, 6) float32 array (pinned or not);
-        returns a dict of numpy outputs (or fills `out`)."""
+        returns a dict of numpy outputs (or fills `out`).  wait=False queues
+        the work (svo_trace_host_async): the results are there after
+        synchronize()."""
         rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 6)
         R = rays.shape[0]
         shapes = {"hit": ((R,), np.uint8), "t": ((R,), np.float32), "leaf": ((R,), np.uint32),
@@ -483,8 +499,10 @@ class VoxelOctree:
             v = res.get(k)
             setattr(o, k, v.ctypes.data if v is not None else None)
         lt = np.ascontiguousarray(light, dtype=np.float32)
-        check(lib.svo_trace_host(self._h, _np_ptr(rays), R, float(ray_scale), lt.ctypes.data_as(_f32p),
-                                 ctypes.byref(o)))
+        fn = lib.svo_trace_host if wait else lib.svo_trace_host_async
+        check(fn(self._h, _np_ptr(rays), R, float(ray_scale), lt.ctypes.data_as(_f32p), ctypes.byref(o)))
+        if not wait:
+            self._pending.append((rays, res))
         return res
 
     def trace_image(self, rays, width, height, ray_scale=0.0, light=(0.0, 0.0, 1.0), out=None, stream=None):
@@ -498,7 +516,8 @@ class VoxelOctree:
                                   lt.ctypes.data_as(_f32p), ctypes.byref(o), _stream_ptr(stream)))
 
     def trace_image_host(self, rays, width, height, ray_scale=0.0, light=(0.0, 0.0, 1.0),
-                         outputs=("hit", "t", "leaf", "word", "rgb"), out=None):
+                         outputs=("hit", "t", "leaf", "word", "rgb"), out=None, wait=True):
+        """svo_trace_image_host (or, with wait=False, its asynchronous form)."""
         rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 6)
         R = rays.shape[0]
         if R != width * height:
@@ -511,8 +530,11 @@ class VoxelOctree:
             v = res.get(k)
             setattr(o, k, v.ctypes.data if v is not None else None)
         lt = np.ascontiguousarray(light, dtype=np.float32)
-        check(lib.svo_trace_image_host(self._h, _np_ptr(rays), int(width), int(height), float(ray_scale),
-                                       lt.ctypes.data_as(_f32p), ctypes.byref(o)))
+        fn = lib.svo_trace_image_host if wait else lib.svo_trace_image_host_async
+        check(fn(self._h, _np_ptr(rays), int(width), int(height), float(ray_scale), lt.ctypes.data_as(_f32p),
+                 ctypes.byref(o)))
+        if not wait:
+            self._pending.append((rays, res))
         return res
 
     def diff_forward(self, rays, width, height, n_views, lights, leaf_rgb, leaf_normal, rgb, hit_leaf=None,

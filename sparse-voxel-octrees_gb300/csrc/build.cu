@@ -295,6 +295,32 @@ __global__ void k_parent_masks(const uint64_t *__restrict__ pkey, const uint32_t
     count[p] = (uint8_t)c;
 }
 
+// The same per parent from its children, one thread per child: the lanes
+// holding one parent's children (a run, at most 8) find each other with a
+// match and OR their octant bits into the parent's valid mask with one warp
+// reduction.  The run's first lane writes mask and count; a run that started
+// in the previous warp is that warp's to write, and one that continues past
+// this warp is finished by reading its remaining children (at most 7).
+// Parents without children (cache blocks only the top table marks, an empty
+// root) are zeroed beforehand.
+__global__ void k_parent_masks_warp(const uint64_t *__restrict__ ckey, uint64_t nc, const uint32_t *__restrict__ dnc,
+                                    const uint32_t *__restrict__ pidx, uint8_t *__restrict__ mask,
+                                    uint8_t *__restrict__ count) {
+    const uint64_t n = level_count(nc, dnc);
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned lane = threadIdx.x & 31u;
+    const bool live = i < n;
+    const uint32_t p = live ? pidx[i] : 0xFFFFFFFFu;
+    const unsigned peers = __match_any_sync(0xffffffffu, p);
+    const unsigned m = __reduce_or_sync(peers, live ? 1u << (ckey[i] & 7) : 0u);
+    if (!live || lane != (unsigned)(__ffs(peers) - 1)) return;
+    if (lane == 0 && i > 0 && pidx[i - 1] == p) return;
+    unsigned mm = m, c = (unsigned)__popc(peers);
+    for (uint64_t k = i + c; k < n && c < 8 && pidx[k] == p; ++k, ++c) mm |= 1u << (ckey[k] & 7);
+    mask[p] = (uint8_t)mm;
+    count[p] = (uint8_t)c;
+}
+
 // ---- subtree sizes and far-pointer decisions (bottom-up) -------------------
 
 __global__ void k_subtree(uint64_t np, const uint32_t *__restrict__ dnp, const uint8_t *__restrict__ count,
@@ -611,9 +637,14 @@ int build_from_sorted_device(const uint64_t *d_keys, const uint32_t *d_payload, 
         L.dn = dn;
         SVO_TRY_ALLOC(L.mask.alloc(L.n, arena));
         SVO_TRY_ALLOC(L.count.alloc(L.n, arena));
-        k_parent_masks<<<blocks_for(L.n), 256, 0, st>>>(L.key.p, L.start.p, L.n, L.dn, ckey, nc, cdn, L.mask.p,
-                                                        L.count.p);
-        SVO_LAUNCH_CHECK("k_parent_masks");
+        if ((multi_block && e == log_block) || e == D) {  // levels that can hold parents without children
+            SVO_CUDA_TRY(cudaMemsetAsync(L.mask.p, 0, L.n, st));
+            SVO_CUDA_TRY(cudaMemsetAsync(L.count.p, 0, L.n, st));
+        }
+        if (nc) {
+            k_parent_masks_warp<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, cdn, pidx.p, L.mask.p, L.count.p);
+            SVO_LAUNCH_CHECK("k_parent_masks_warp");
+        }
         if (e == 1) {
             leaf_pidx.p = pidx.p;
             leaf_pidx.st = st;

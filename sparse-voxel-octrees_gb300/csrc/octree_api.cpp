@@ -152,31 +152,63 @@ static std::vector<uint64_t> plan_chunks(uint64_t total, uint64_t target, uint64
     return plan;
 }
 
-// The host-buffer pipeline of svo_trace_host and svo_trace_image_host.  Chunk
-// k's rays go in on the copy-in stream into staging buffer k % B, are traced
-// on that buffer's trace stream (each with its own work counter, so one
-// chunk's persistent launch fills the tail of the previous one) and come out
-// on the copy-out stream.  A buffer's rays are overwritten only after its
-// previous trace, and its results only after their copy-out.  With two
-// buffers a buffer's whole cycle (copy in, trace, copy out) paced the copy-in
-// stream; with four, the copy-in stream runs back to back, which the host
-// link's transfer rate then bounds.
-// launch(d_rays, rays, outputs, stream, buffer) enqueues one chunk's trace.
+// The host-buffer pipeline of svo_trace_host and svo_trace_image_host (and
+// their asynchronous forms).  Chunk k's rays go in on the copy-in stream into
+// staging buffer k % B, are traced on that buffer's trace stream (each with
+// its own work counter, so one chunk's persistent launch fills the tail of the
+// previous one) and come out on the copy-out stream.  A buffer's rays are
+// overwritten only after its previous trace, and its results only after their
+// copy-out.  With two buffers a buffer's whole cycle (copy in, trace, copy
+// out) paced the copy-in stream; with four, the copy-in stream runs back to
+// back, which the host link's transfer rate then bounds.  The chunk counter
+// carries over from call to call, so an asynchronous call's copies queue
+// behind the previous call's and overlap its traces.
+//
+// Waits for every enqueued chunk, then reports traversal faults.  Called with
+// staging_mtx held.
+static int host_drain(svo_octree *oct) {
+    if (!oct->stage_pending) return SVO_OK;
+    cudaError_t e = cudaSuccess;
+    auto drain = [&](cudaStream_t q) {
+        const cudaError_t eq = cudaStreamSynchronize(q);
+        if (e == cudaSuccess) e = eq;
+    };
+    drain(oct->copy_in);
+    for (int k = 0; k < svo_octree::kStageBuffers; ++k) drain(oct->stage_trace[k]);
+    drain(oct->copy_out);
+    oct->stage_pending = false;
+    if (e != cudaSuccess) return cuda_fail(e, "host trace pipeline");
+    return check_device_status(oct);
+}
+
+// Enqueues the chunks of `plan` (rays from `rays`, results to `out`, all host
+// memory); launch(d_rays, rays, outputs, stream, buffer) enqueues one chunk's
+// trace.  Called with staging_mtx held.  On an error, everything enqueued so
+// far is drained before returning.
 template <typename Launch>
-static int host_pipeline(svo_octree *oct, const float *rays, const std::vector<uint64_t> &plan,
-                         const svo_trace_out &out, Launch launch) {
-    uint64_t C = 0;
-    for (uint64_t m : plan) C = std::max(C, m);
-    const int B = (int)std::min<size_t>(svo_octree::kStageBuffers, plan.size());
+static int host_enqueue(svo_octree *oct, const float *rays, const std::vector<uint64_t> &plan,
+                        const svo_trace_out &out, Launch launch) {
+    constexpr int B = svo_octree::kStageBuffers;
+    uint64_t need = 0;
+    for (uint64_t m : plan) need = std::max(need, m);
     // Per buffer: rays 24 B, hit 1, t 4, leaf 4, word 4, rgb 12, rgba8 4 (256-byte aligned arrays).
     auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
-    const size_t buf = al(C * 24) + al(C) + al(C * 4) * 4 + al(C * 12);
-    int rc = ensure_staging(oct, B * buf);
-    if (rc) return rc;
+    auto buf_bytes = [&](uint64_t C) { return al(C * 24) + al(C) + al(C * 4) * 4 + al(C * 12); };
+    if (need > oct->stage_cap) {
+        // a larger arena: nothing may still be using the old one
+        int rc = host_drain(oct);
+        if (rc) return rc;
+        rc = ensure_staging(oct, B * buf_bytes(need));
+        if (rc) return rc;
+        oct->stage_cap = need;
+        for (bool &u : oct->stage_used) u = false;
+    }
+    const uint64_t C = oct->stage_cap;
+    const size_t buf = buf_bytes(C);
     if (!oct->copy_in) {
         SVO_CUDA_TRY(cudaStreamCreateWithFlags(&oct->copy_in, cudaStreamNonBlocking));
         SVO_CUDA_TRY(cudaStreamCreateWithFlags(&oct->copy_out, cudaStreamNonBlocking));
-        for (int k = 0; k < svo_octree::kStageBuffers; ++k) {
+        for (int k = 0; k < B; ++k) {
             SVO_CUDA_TRY(cudaStreamCreateWithFlags(&oct->stage_trace[k], cudaStreamNonBlocking));
             SVO_CUDA_TRY(cudaEventCreateWithFlags(&oct->stage_in[k], cudaEventDisableTiming));
             SVO_CUDA_TRY(cudaEventCreateWithFlags(&oct->stage_traced[k], cudaEventDisableTiming));
@@ -184,11 +216,13 @@ static int host_pipeline(svo_octree *oct, const float *rays, const std::vector<u
         }
     }
     cudaStream_t si = oct->copy_in, so = oct->copy_out;
+    oct->stage_pending = true;
     auto enqueue = [&]() -> int {
         uint64_t c0 = 0;
         for (size_t j = 0; j < plan.size(); c0 += plan[j], ++j) {
-            const int h = (int)(j % (size_t)B);
-            const bool reused = j >= (size_t)B;
+            const int h = (int)(oct->stage_seq++ % (uint64_t)B);
+            const bool reused = oct->stage_used[h];
+            oct->stage_used[h] = true;
             const uint64_t m = plan[j];
             cudaStream_t sk = oct->stage_trace[h];
             uint8_t *base = (uint8_t *)oct->stage_dev + h * buf;
@@ -211,7 +245,7 @@ static int host_pipeline(svo_octree *oct, const float *rays, const std::vector<u
             o.word = out.word ? d_word : nullptr;
             o.rgb = out.rgb ? d_rgb : nullptr;
             o.rgba8 = out.rgba8 ? d_rgba8 : nullptr;
-            rc = launch(d_rays, m, o, sk, h);
+            int rc = launch(d_rays, m, o, sk, h);
             if (rc) return rc;
             SVO_CUDA_TRY(cudaEventRecord(oct->stage_traced[h], sk));
             SVO_CUDA_TRY(cudaStreamWaitEvent(so, oct->stage_traced[h], 0));
@@ -226,20 +260,17 @@ static int host_pipeline(svo_octree *oct, const float *rays, const std::vector<u
         }
         return SVO_OK;
     };
-    rc = enqueue();
-    // Every stream is drained even when a chunk failed to enqueue: the
-    // staging buffers must be idle before the next call reuses them.
-    cudaError_t e = cudaSuccess;
-    auto drain = [&](cudaStream_t q) {
-        const cudaError_t eq = cudaStreamSynchronize(q);
-        if (e == cudaSuccess) e = eq;
-    };
-    drain(si);
-    for (int k = 0; k < svo_octree::kStageBuffers; ++k) drain(oct->stage_trace[k]);
-    drain(so);
-    if (rc) return rc;
-    if (e != cudaSuccess) return cuda_fail(e, "host trace pipeline");
-    return check_device_status(oct);
+    const int rc = enqueue();
+    if (rc) {
+        // Every stream is drained when a chunk failed to enqueue: the staging
+        // buffers must be idle before the next call reuses them.  The error
+        // recorded by the failed step is the one reported.
+        oct->stage_pending = true;
+        for (cudaStream_t q : {si, so}) cudaStreamSynchronize(q);
+        for (int k = 0; k < B; ++k) cudaStreamSynchronize(oct->stage_trace[k]);
+        oct->stage_pending = false;
+    }
+    return rc;
 }
 
 }  // namespace svo
@@ -392,6 +423,10 @@ int svo_octree_from_words(const uint32_t *words, uint64_t n_words, const float c
 
 int svo_octree_destroy(svo_octree *oct) {
     if (!oct) return SVO_OK;
+    if (oct->stage_pending) {  // asynchronous host traces still reading and writing the staging arena
+        std::lock_guard<std::mutex> lock(oct->staging_mtx);
+        host_drain(oct);
+    }
     if (oct->d_words) cudaFree(oct->d_words);
     if (oct->d_tab) cudaFree(oct->d_tab);
     if (oct->d_queue) cudaFree(oct->d_queue);  // the control block (d_status lies inside it)
@@ -631,37 +666,74 @@ int svo_trace_count_loads(const svo_octree *oct, const float *rays, uint64_t n, 
     return launch_count_loads(oct, rays, n, ray_scale, loads, (cudaStream_t)stream);
 }
 
-int svo_trace_host(svo_octree *oct, const float *rays, uint64_t n, float ray_scale, const float light[3],
-                   const svo_trace_out *out) {
+// svo_trace_host and svo_trace_host_async: the chunk plan and the per-chunk
+// launch; `wait` drains the pipeline before returning.
+static int trace_host(svo_octree *oct, const float *rays, uint64_t n, float ray_scale, const float light[3],
+                      const svo_trace_out *out, bool wait) {
     if (!oct || (!rays && n) || !out) return set_error(SVO_ERR_INVALID, "null argument");
     if (n > 0xFFFFFFFFull) return set_error(SVO_ERR_LIMIT, "more than 2^32-1 rays");
-    if (n == 0) return SVO_OK;
     std::lock_guard<std::mutex> lock(oct->staging_mtx);
-    // warp-aligned chunks
-    const std::vector<uint64_t> plan = plan_chunks(n, kStageRays, 32);
-    return host_pipeline(oct, rays, plan, *out,
-                         [&](const float *d_rays, uint64_t m, const svo_trace_out &o, cudaStream_t st, int) {
-                             return launch_trace(oct, d_rays, m, ray_scale, light, o, st);
-                         });
+    if (n) {
+        // warp-aligned chunks
+        const std::vector<uint64_t> plan = plan_chunks(n, kStageRays, 32);
+        const float lt[3] = {light ? light[0] : 0.0f, light ? light[1] : 0.0f, light ? light[2] : 0.0f};
+        int rc = host_enqueue(oct, rays, plan, *out,
+                              [&](const float *d_rays, uint64_t m, const svo_trace_out &o, cudaStream_t st, int) {
+                                  return launch_trace(oct, d_rays, m, ray_scale, lt, o, st);
+                              });
+        if (rc) return rc;
+    }
+    return wait ? host_drain(oct) : SVO_OK;
+}
+
+static int trace_image_host(svo_octree *oct, const float *rays, uint32_t width, uint32_t height, float ray_scale,
+                            const float light[3], const svo_trace_out *out, bool wait) {
+    if (!oct || (!rays && width && height) || !out) return set_error(SVO_ERR_INVALID, "null argument");
+    if ((uint64_t)width * height > 0xFFFFFFFFull) return set_error(SVO_ERR_LIMIT, "more than 2^32-1 pixels");
+    std::lock_guard<std::mutex> lock(oct->staging_mtx);
+    if (width && height) {
+        // Chunks of whole rows, a multiple of the 4-row tile height (all but
+        // the last), about kStageRays rays at full size; each chunk is traced
+        // as an image of its own.
+        const uint64_t rows = std::max<uint64_t>(4, (kStageRays / width) & ~uint64_t(3));
+        std::vector<uint64_t> plan = plan_chunks(height, rows, 4);
+        for (auto &c : plan) c *= width;
+        const float lt[3] = {light ? light[0] : 0.0f, light ? light[1] : 0.0f, light ? light[2] : 0.0f};
+        int rc = host_enqueue(oct, rays, plan, *out,
+                              [&](const float *d_rays, uint64_t m, const svo_trace_out &o, cudaStream_t st,
+                                  int buffer) {
+                                  return launch_trace_image(oct, d_rays, width, (uint32_t)(m / width), ray_scale,
+                                                            lt, o, st, 1 + buffer);
+                              });
+        if (rc) return rc;
+    }
+    return wait ? host_drain(oct) : SVO_OK;
+}
+
+int svo_trace_host(svo_octree *oct, const float *rays, uint64_t n, float ray_scale, const float light[3],
+                   const svo_trace_out *out) {
+    return trace_host(oct, rays, n, ray_scale, light, out, true);
+}
+
+int svo_trace_host_async(svo_octree *oct, const float *rays, uint64_t n, float ray_scale, const float light[3],
+                         const svo_trace_out *out) {
+    return trace_host(oct, rays, n, ray_scale, light, out, false);
 }
 
 int svo_trace_image_host(svo_octree *oct, const float *rays, uint32_t width, uint32_t height, float ray_scale,
                          const float light[3], const svo_trace_out *out) {
-    if (!oct || (!rays && width && height) || !out) return set_error(SVO_ERR_INVALID, "null argument");
-    if ((uint64_t)width * height > 0xFFFFFFFFull) return set_error(SVO_ERR_LIMIT, "more than 2^32-1 pixels");
-    if (width == 0 || height == 0) return SVO_OK;
+    return trace_image_host(oct, rays, width, height, ray_scale, light, out, true);
+}
+
+int svo_trace_image_host_async(svo_octree *oct, const float *rays, uint32_t width, uint32_t height,
+                               float ray_scale, const float light[3], const svo_trace_out *out) {
+    return trace_image_host(oct, rays, width, height, ray_scale, light, out, false);
+}
+
+int svo_octree_synchronize(svo_octree *oct) {
+    if (!oct) return set_error(SVO_ERR_INVALID, "null argument");
     std::lock_guard<std::mutex> lock(oct->staging_mtx);
-    // Chunks of whole rows, a multiple of the 4-row tile height (all but the
-    // last), about kStageRays rays at full size; each chunk is traced as an
-    // image of its own.
-    const uint64_t rows = std::max<uint64_t>(4, (kStageRays / width) & ~uint64_t(3));
-    std::vector<uint64_t> plan = plan_chunks(height, rows, 4);
-    for (auto &c : plan) c *= width;
-    return host_pipeline(oct, rays, plan, *out,
-                         [&](const float *d_rays, uint64_t m, const svo_trace_out &o, cudaStream_t st, int buffer) {
-                             return launch_trace_image(oct, d_rays, width, (uint32_t)(m / width), ray_scale, light,
-                                                       o, st, 1 + buffer);
-                         });
+    return host_drain(oct);
 }
 
 }  // extern "C"

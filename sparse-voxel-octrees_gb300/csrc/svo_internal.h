@@ -39,11 +39,15 @@ struct svo_octree {
     // device staging arena split into kStageBuffers buffers, a copy-in and a
     // copy-out stream, one trace stream per buffer, and per-buffer events
     // (inputs landed, trace done, outputs copied).
-    static constexpr int kStageBuffers = 4;
+    static constexpr int kStageBuffers = 4;  // stage_used has one flag per buffer
     static constexpr int kQueues = 1 + kStageBuffers;
     std::mutex staging_mtx;
     void *stage_dev = nullptr;
     size_t stage_dev_bytes = 0;
+    uint64_t stage_cap = 0;       // rays per staging buffer (the arena's layout)
+    uint64_t stage_seq = 0;       // chunks enqueued so far: chunk k uses buffer k % kStageBuffers
+    bool stage_used[4] = {};      // the buffer holds an earlier chunk (its events are waited on)
+    bool stage_pending = false;   // enqueued work not yet drained (svo_octree_synchronize)
     cudaStream_t copy_in = nullptr, copy_out = nullptr;
     cudaStream_t stage_trace[kStageBuffers] = {};
     cudaEvent_t stage_in[kStageBuffers] = {}, stage_traced[kStageBuffers] = {}, stage_out[kStageBuffers] = {};

@@ -219,6 +219,41 @@ def test_host_pipelines_long_calls(cuda, svo, oracle, scenes):
     assert tree.device_status() == 0
 
 
+def test_host_async_calls_match_sync_calls(cuda, svo, oracle, scenes):
+    """svo_trace_host_async / svo_trace_image_host_async queue on the host
+    pipeline and give, after svo_octree_synchronize, what the waiting calls
+    give: several calls in a row (their chunks share the staging buffers),
+    a small call followed by one that needs a larger staging arena (the
+    queued work is drained before it is replaced), and a pending call at
+    close."""
+    grid = scenes.sphere_scene(128, 24, 5)
+    words, center = oracle.build_dense(grid)
+    tree = svo.VoxelOctree.from_words(words, center)
+    cams = scenes.orbit_cameras(2, 13, center)
+    W, H = 1024, 4500  # 4.6 M rays: two image chunks, two linear chunks
+    img_rays = scenes.camera_rays(cams[0], W, H)
+    lin_rays = scenes.random_rays(300_000, 23)
+    small = scenes.camera_rays(cams[1], 40, 30)
+    light = (0.0, 1.0, 0.0)
+    outs = svo.TRACE_OUTPUTS
+    ref_img = tree.trace_image_host(img_rays, W, H, light=light, outputs=outs)
+    ref_lin = tree.trace_host(lin_rays, light=light, outputs=outs)
+    ref_small = tree.trace_host(small, light=light, outputs=outs)
+    tree.close()
+    tree = svo.VoxelOctree.from_words(words, center)  # fresh staging: the small call comes first
+    a = tree.trace_host(small, light=light, outputs=outs, wait=False)
+    b = tree.trace_image_host(img_rays, W, H, light=light, outputs=outs, wait=False)
+    c = tree.trace_host(lin_rays, light=light, outputs=outs, wait=False)
+    d = tree.trace_image_host(img_rays, W, H, light=light, outputs=outs, wait=False)
+    tree.synchronize()
+    for got, ref in ((a, ref_small), (b, ref_img), (c, ref_lin), (d, ref_img)):
+        for k in outs:
+            assert np.array_equal(np.asarray(got[k]).view(np.uint8), np.asarray(ref[k]).view(np.uint8)), k
+    tree.synchronize()  # nothing queued: returns at once
+    tree.trace_host(lin_rays, light=light, outputs=outs, wait=False)
+    tree.close()  # waits for the queued call before freeing the handle
+
+
 def test_sphere_union_256_views_match_oracle(cuda, svo, oracle, scenes):
     """The small plain-traversal workload in full: the 256^3 union of 48
     spheres (seed 0), built on the GPU, and 12 orbit views (radius 2, seeded
