@@ -292,6 +292,26 @@ def setup_scene(args, rank, torch, svo, scenes):
     return tree, prim, shadow, cam_slices, shadow_slices, info
 
 
+def host_link_rates(torch, host):
+    """This machine's host link: one pinned copy of `host` (a numpy array in
+    page-locked memory) to the device and back, GB/s each way.  It sets the
+    e2e figure, which moves the rays in and the results out; the rate differs
+    between boxes."""
+    src = torch.from_numpy(host.reshape(-1).view(np.uint8))
+    dev = torch.empty(src.numel(), dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    dev.copy_(src, non_blocking=True)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    src.copy_(dev, non_blocking=True)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    n = src.numel()
+    del dev
+    return {"h2d": round(n / (t1 - t0) / 1e9, 1), "d2h": round(n / (t2 - t1) / 1e9, 1), "bytes": int(n)}
+
+
 def workload_config(args, n_words, n_vox, Rp, Rs, world):
     """The plain-traversal workload's `config`, identical in both arms."""
     return {"workload": "plain traversal: %d^3 octree (terrain + %d spheres), %d cams %dx%d primary rays "
@@ -522,7 +542,8 @@ def run_ours(args):
                       "svo_octree_synchronize: pinned host rays in, t/word/rgba8 and shadow hit out",
                "exact": bool(exact_e2e), "step_ms": round(e2e_s / args.steps * 1e3, 3),
                "waiting_calls_ms": {"primary": round(t_calls[0] / n_sync * 1e3, 3),
-                                    "shadow": round(t_calls[1] / n_sync * 1e3, 3)}}
+                                    "shadow": round(t_calls[1] / n_sync * 1e3, 3)},
+               "link_gbs": host_link_rates(torch, hp_pin)}
         del hp_pin, hs_pin, op, os_
 
     peaks, peak_kind = load_peaks()
