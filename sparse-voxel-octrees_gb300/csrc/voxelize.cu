@@ -440,6 +440,12 @@ struct FoldArgs {
     // fold.  A brick marked 0 starts from zeros and is not read.
     const uint8_t *pre_dirty;
     uint64_t n_pre;
+    // Optional (the octree build's blocks): per brick of the block, set to 2
+    // (folded here) with the count of its nonzero words outside the dropped
+    // last slice (drop_z, or -1), the voxels the extraction will emit.
+    uint8_t *brick_flag;
+    uint32_t *brick_count;
+    int drop_z;
 };
 
 // PlyLoader::writeTriangleCell on a register copy of one buffer cell.
@@ -557,11 +563,11 @@ __global__ void __launch_bounds__(kFoldWarps * 32, 8) k_fold_bricks(FoldArgs a) 
         // a brick the buffer holds only zeros for is not read (the extraction
         // cleared what earlier blocks left, except their dropped slices)
         bool clean = false;
-        if (a.pre_dirty && ox >= a.org[0] && oy >= a.org[1] && oz >= a.org[2]) {
-            const uint64_t pm = morton3((uint32_t)((ox - a.org[0]) >> le), (uint32_t)((oy - a.org[1]) >> le),
-                                        (uint32_t)((oz - a.org[2]) >> le));
-            clean = pm < a.n_pre && a.pre_dirty[pm] == 0;
-        }
+        uint64_t pm = ~0ull;  // the brick's Morton index within the block
+        if (ox >= a.org[0] && oy >= a.org[1] && oz >= a.org[2])
+            pm = morton3((uint32_t)((ox - a.org[0]) >> le), (uint32_t)((oy - a.org[1]) >> le),
+                         (uint32_t)((oz - a.org[2]) >> le));
+        if (a.pre_dirty) clean = pm < a.n_pre && a.pre_dirty[pm] == 0;
         __syncwarp();
         for (int i = lane; i < E3; i += 32) {
             int x = ox + (i & (E - 1)), y = oy + ((i >> le) & (E - 1)), z = oz + (i >> (2 * le));
@@ -681,25 +687,28 @@ __global__ void __launch_bounds__(kFoldWarps * 32, 8) k_fold_bricks(FoldArgs a) 
             a.data[bi] = sm.w[i];
             a.counts[bi] = sm.cnt[i];
         }
+        if (a.brick_count && pm < a.n_pre) {
+            // the brick's whole buffer state is in shared memory: words read
+            // (or known zero) and folded
+            uint32_t n = 0;
+            for (int i = lane; i < E3; i += 32) {
+                int x = ox + (i & (E - 1)), y = oy + ((i >> le) & (E - 1)), z = oz + (i >> (2 * le));
+                if (x < end0 && y < end1 && z < end2 && z != a.drop_z && sm.w[i]) ++n;
+            }
+#pragma unroll
+            for (int o = 16; o; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
+            if (lane == 0) {
+                a.brick_count[pm] = n;
+                a.brick_flag[pm] = 2;
+            }
+        }
     }
 }
 
 // Bricks of the block (edge E, Morton-indexed within the block) that may
-// hold a nonzero buffer word: those this block folded ...
-__global__ void k_mark_folded(const uint32_t *__restrict__ bkey, uint32_t first, uint32_t last, int log_e, int ox,
-                              int oy, int oz, uint8_t *__restrict__ dirty, uint64_t n_dirty) {
-    uint32_t j = first + blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= last) return;
-    uint32_t key = bkey[j];
-    uint32_t x = ((compact3(key) << log_e) - ox) >> log_e;
-    uint32_t y = ((compact3((uint64_t)key >> 1) << log_e) - oy) >> log_e;
-    uint32_t z = ((compact3((uint64_t)key >> 2) << log_e) - oz) >> log_e;
-    uint64_t m = morton3(x, y, z);
-    if (m < n_dirty) dirty[m] = 1;
-}
-
-// ... and those holding a buffer index of an earlier block's dropped slice
-// ([s0, s1) flat), read in this block's w x h x d layout.
+// hold a nonzero buffer word before the fold: those holding a buffer index of
+// an earlier block's dropped slice ([s0, s1) flat), read in this block's
+// w x h x d layout.
 __global__ void k_mark_range(uint64_t s0, uint64_t s1, int w, int h, int d, int log_e, uint8_t *__restrict__ dirty,
                              uint64_t n_dirty) {
     uint64_t i = s0 + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -710,14 +719,9 @@ __global__ void k_mark_range(uint64_t s0, uint64_t s1, int w, int h, int d, int 
     if (m < n_dirty) dirty[m] = 1;
 }
 
-__global__ void k_compact_u8(const uint8_t *__restrict__ flag, uint64_t n, const uint32_t *__restrict__ idx,
-                             uint32_t *__restrict__ out) {
-    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n && flag[i]) out[idx[i]] = (uint32_t)i;
-}
-
 struct ExtractArgs {
-    const uint32_t *cand;  // candidate bricks (Morton index within the block), ascending
+    const uint8_t *flag;   // per brick of the block: 0 holds nothing, 1 earlier dropped-slice words only, 2 folded
+    uint64_t n_bricks;
     int log_e;
     int buf[3];
     int drop;              // the z == buf[2]-1 slice is never read (VoxelData.cpp:163-170)
@@ -725,8 +729,8 @@ struct ExtractArgs {
     uint32_t *data;
 };
 
-// Voxel m (local Morton index) of candidate brick c: buffer index, or
-// ~0 when the voxel lies outside the block or in a dropped slice.
+// Voxel m (local Morton index) of brick c: buffer index, or ~0 when the
+// voxel lies outside the block or in a dropped slice.
 __device__ __forceinline__ uint64_t cand_cell(const ExtractArgs &a, uint32_t c, uint32_t m) {
     const int le = a.log_e;
     int x = (int)((compact3(c) << le) + compact3(m)), y = (int)((compact3((uint64_t)c >> 1) << le) + compact3((uint64_t)m >> 1));
@@ -735,17 +739,17 @@ __device__ __forceinline__ uint64_t cand_cell(const ExtractArgs &a, uint32_t c, 
     return (uint64_t)x + (uint64_t)a.buf[0] * ((uint64_t)y + (uint64_t)a.buf[1] * (uint64_t)z);
 }
 
-// One warp per candidate brick (grid-stride over *n_cand): its occupied
-// voxels.
-__global__ void k_cand_count(ExtractArgs a, const uint32_t *__restrict__ n_cand, uint32_t *__restrict__ count) {
+// One warp per brick flagged 1 (dropped-slice words of earlier blocks, not
+// folded here, so the fold has not counted them): its occupied voxels.
+__global__ void k_ghost_count(ExtractArgs a, uint32_t *__restrict__ count) {
     const int lane = threadIdx.x & 31;
-    const uint32_t nc = *n_cand, E3 = 1u << (3 * a.log_e);
-    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < nc; c += nw) {
-        const uint32_t key = a.cand[c];
+    const uint32_t E3 = 1u << (3 * a.log_e);
+    const uint64_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint64_t c = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < a.n_bricks; c += nw) {
+        if (a.flag[c] != 1) continue;
         uint32_t n = 0;
         for (uint32_t m = lane; m < E3; m += 32) {
-            uint64_t bi = cand_cell(a, key, m);
+            uint64_t bi = cand_cell(a, (uint32_t)c, m);
             if (bi != ~0ull && a.data[bi]) ++n;
         }
 #pragma unroll
@@ -754,28 +758,28 @@ __global__ void k_cand_count(ExtractArgs a, const uint32_t *__restrict__ n_cand,
     }
 }
 
-// One warp per candidate brick: (key, word) of its occupied voxels in
-// Morton order at *base + off[c] (at most cap), and the emitted cells
-// cleared (the walk reads them with getVoxelDestructive).
-__global__ void k_cand_emit(ExtractArgs a, const uint32_t *__restrict__ n_cand, const uint64_t *__restrict__ off,
-                            const uint64_t *__restrict__ base_p, uint64_t cap, uint64_t *__restrict__ keys,
-                            uint32_t *__restrict__ payload, uint32_t *__restrict__ err) {
+// One warp per flagged brick: (key, word) of its occupied voxels in Morton
+// order at *base + off[c] (at most cap), and the emitted cells cleared (the
+// walk reads them with getVoxelDestructive).
+__global__ void k_cand_emit(ExtractArgs a, const uint64_t *__restrict__ off, const uint64_t *__restrict__ base_p,
+                            uint64_t cap, uint64_t *__restrict__ keys, uint32_t *__restrict__ payload,
+                            uint32_t *__restrict__ err) {
     const int lane = threadIdx.x & 31;
-    const uint32_t nc = *n_cand, E3 = 1u << (3 * a.log_e);
-    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t E3 = 1u << (3 * a.log_e);
+    const uint64_t nw = (gridDim.x * blockDim.x) >> 5;
     const uint32_t lt = (1u << lane) - 1u;
-    for (uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < nc; c += nw) {
-        const uint32_t key = a.cand[c];
+    for (uint64_t c = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < a.n_bricks; c += nw) {
+        if (a.flag[c] == 0) continue;
         uint64_t base = *base_p + off[c];
         for (uint32_t m0 = 0; m0 < E3; m0 += 32) {
             const uint32_t m = m0 + lane;
-            uint64_t bi = m < E3 ? cand_cell(a, key, m) : ~0ull;
+            uint64_t bi = m < E3 ? cand_cell(a, (uint32_t)c, m) : ~0ull;
             uint32_t v = bi != ~0ull ? a.data[bi] : 0u;
             uint32_t ball = __ballot_sync(0xffffffffu, v != 0);
             if (v) {
                 uint64_t o = base + __popc(ball & lt);
                 if (o < cap) {
-                    keys[o] = a.key_base + ((uint64_t)key << (3 * a.log_e)) + m;
+                    keys[o] = a.key_base + ((uint64_t)c << (3 * a.log_e)) + m;
                     payload[o] = v;
                     a.data[bi] = 0;
                 } else {
@@ -1126,7 +1130,7 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
     // PlyLoader::processBlock (PlyLoader.cpp:439-458) of job ji, whose buffer
     // `data` starts at org with edges buf: its bricks' pairs folded into it
     auto fold_block = [&](size_t ji, const int org[3], const int buf[3], uint32_t *data, const uint8_t *pre_dirty,
-                          uint64_t n_pre) -> int {
+                          uint64_t n_pre, uint8_t *brick_flag, uint32_t *brick_count, int drop_z) -> int {
         const BlockJob &j = jobs[ji];
         if (j.last <= j.first) return SVO_OK;
         FoldArgs fa;
@@ -1154,6 +1158,9 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
         fa.brick_mask = brick_mask;
         fa.pre_dirty = pre_dirty;
         fa.n_pre = n_pre;
+        fa.brick_flag = brick_flag;
+        fa.brick_count = brick_count;
+        fa.drop_z = drop_z;
         unsigned grid = (unsigned)std::min<uint64_t>((j.last - j.first + kFoldWarps - 1) / kFoldWarps, fold_grid);
         k_fold_bricks<<<grid, kFoldWarps * 32, 0, st>>>(fa);
         SVO_LAUNCH_OK("k_fold_bricks");
@@ -1179,7 +1186,7 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
                                              cudaMemcpyDeviceToDevice, st));
             const int org[3] = {0, 0, s * slab}, buf[3] = {dims[0], dims[1], nz};
             if (ji < jobs.size() && jobs[ji].morton == (uint32_t)s) {
-                int rc = fold_block(ji, org, buf, region, nullptr, 0);
+                int rc = fold_block(ji, org, buf, region, nullptr, 0, nullptr, nullptr, -1);
                 if (rc) return rc;
                 ++ji;
             }
@@ -1195,19 +1202,14 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
     // 4. blocks in order: fold, then extract (and clear) the block's voxels.
     // Counts stay on the device, so the loop queues its work without waiting.
     const uint64_t n_e = 1ull << (3 * (lb - g.log_e));  // bricks per block
-    Dev<uint8_t> dirty;
-    Dev<uint32_t> d32, didx, cand, ccount, ncand, sc32;
+    Dev<uint8_t> flag;    // per brick of the block: 0 nothing, 1 earlier dropped-slice words, 2 folded here
+    Dev<uint32_t> ccount;  // per brick: the voxels the extraction emits
     Dev<uint64_t> coff, bn, dN, sc64;
-    SVO_ALLOC(dirty, n_e);
-    SVO_ALLOC(d32, n_e);
-    SVO_ALLOC(didx, n_e);
-    SVO_ALLOC(cand, n_e);
+    SVO_ALLOC(flag, n_e);
     SVO_ALLOC(ccount, n_e);
     SVO_ALLOC(coff, n_e);
-    SVO_ALLOC(ncand, 1);
     SVO_ALLOC(bn, 1);
     SVO_ALLOC(dN, 1);
-    SVO_ALLOC(sc32, scan_scratch_elems(n_e));
     SVO_ALLOC(sc64, scan_scratch_elems(n_e));
     SVO_CUDA_TRY(cudaMemsetAsync(dN.p, 0, sizeof(uint64_t), st));
     // Every emitted voxel lies in a brick folded by its block or is a word an
@@ -1236,48 +1238,44 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
         }
         if (!inside) continue;  // VoxelData::prepareDataAccess returns early
         // Bricks under an earlier block's dropped slice may hold nonzero words
-        // before this fold; every other buffer cell is zero (the extraction
-        // cleared it).  When those slices are large, every brick counts.
+        // before this fold (flag 1); every other buffer cell is zero (the
+        // extraction cleared it).  When those slices are large, every brick
+        // is flagged.  The fold flags the bricks it folds 2 and counts their
+        // voxels.
         const uint64_t vol = (uint64_t)fa.buf[0] * fa.buf[1] * fa.buf[2];
         const bool all_dirty = ghost_len * 4 > vol;
         if (all_dirty) {
-            SVO_CUDA_TRY(cudaMemsetAsync(dirty.p, 1, n_e, st));
+            SVO_CUDA_TRY(cudaMemsetAsync(flag.p, 1, n_e, st));
         } else {
-            SVO_CUDA_TRY(cudaMemsetAsync(dirty.p, 0, n_e, st));
+            SVO_CUDA_TRY(cudaMemsetAsync(flag.p, 0, n_e, st));
             for (const auto &r : ghosts) {
                 uint64_t s1 = std::min(r.second, vol);
                 if (r.first >= s1) continue;
                 k_mark_range<<<grid_for(s1 - r.first), 256, 0, st>>>(r.first, s1, fa.buf[0], fa.buf[1], fa.buf[2],
-                                                                    g.log_e, dirty.p, n_e);
+                                                                    g.log_e, flag.p, n_e);
                 SVO_LAUNCH_OK("k_mark_range");
             }
         }
-        int rc = fold_block((size_t)(&j - jobs.data()), fa.org, fa.buf, data_p, all_dirty ? nullptr : dirty.p, n_e);
-        if (rc) return rc;
-        // candidate bricks for the extraction: those, and the bricks folded here
-        if (!all_dirty && j.last > j.first) {
-            k_mark_folded<<<grid_for(j.last - j.first), 256, 0, st>>>(bkey.p, j.first, j.last, g.log_e, fa.org[0],
-                                                                     fa.org[1], fa.org[2], dirty.p, n_e);
-            SVO_LAUNCH_OK("k_mark_folded");
-        }
-        k_flag_to_u32<<<grid_for(n_e), 256, 0, st>>>(dirty.p, n_e, d32.p);
-        SVO_LAUNCH_OK("k_flag_to_u32");
-        SVO_CUDA_TRY((exclusive_scan<uint32_t, uint32_t>(d32.p, didx.p, n_e, ncand.p, sc32.p, st)));
-        k_compact_u8<<<grid_for(n_e), 256, 0, st>>>(dirty.p, n_e, didx.p, cand.p);
-        SVO_LAUNCH_OK("k_compact_u8");
+        SVO_CUDA_TRY(cudaMemsetAsync(ccount.p, 0, n_e * sizeof(uint32_t), st));
         const int drop = ((fa.buf[2] & 1) && lb >= 2) ? 1 : 0;
+        const int drop_z = drop ? fa.org[2] + fa.buf[2] - 1 : -1;
+        int rc = fold_block((size_t)(&j - jobs.data()), fa.org, fa.buf, data_p, all_dirty ? nullptr : flag.p, n_e,
+                            flag.p, ccount.p, drop_z);
+        if (rc) return rc;
         ExtractArgs ea;
-        ea.cand = cand.p;
+        ea.flag = flag.p;
+        ea.n_bricks = n_e;
         ea.log_e = g.log_e;
         for (int k = 0; k < 3; ++k) ea.buf[k] = fa.buf[k];
         ea.drop = drop;
         ea.key_base = (uint64_t)j.morton << (3 * lb);
         ea.data = data.p;
-        SVO_CUDA_TRY(cudaMemsetAsync(ccount.p, 0, n_e * sizeof(uint32_t), st));
-        k_cand_count<<<warp_grid, 256, 0, st>>>(ea, ncand.p, ccount.p);
-        SVO_LAUNCH_OK("k_cand_count");
+        if (all_dirty || !ghosts.empty()) {
+            k_ghost_count<<<warp_grid, 256, 0, st>>>(ea, ccount.p);
+            SVO_LAUNCH_OK("k_ghost_count");
+        }
         SVO_CUDA_TRY((exclusive_scan<uint32_t, uint64_t>(ccount.p, coff.p, n_e, bn.p, sc64.p, st)));
-        k_cand_emit<<<warp_grid, 256, 0, st>>>(ea, ncand.p, coff.p, dN.p, cap, keys.p, pay.p, err.p);
+        k_cand_emit<<<warp_grid, 256, 0, st>>>(ea, coff.p, dN.p, cap, keys.p, pay.p, err.p);
         SVO_LAUNCH_OK("k_cand_emit");
         k_add_u64<<<1, 1, 0, st>>>(dN.p, bn.p);
         if (drop) {  // the walk never reads this slice; it stays in the buffer
