@@ -301,8 +301,10 @@ int svo_trace(const svo_octree *oct, const float *rays, uint64_t n, float ray_sc
               const svo_trace_out *out, svo_stream stream);
 
 /* Same as svo_trace with host arrays: rays are copied in and results out
- * through the handle's staging buffers in chunks, copies overlapped with
- * tracing on two internal streams.  Returns when results are on the host. */
+ * through the handle's four staging buffers in chunks of about 4 M rays, on
+ * internal copy-in, copy-out and per-buffer trace streams, so copies overlap
+ * tracing.  Returns when results are on the host (after any work queued
+ * earlier by the asynchronous forms below). */
 int svo_trace_host(svo_octree *oct, const float *rays, uint64_t n, float ray_scale, const float light[3],
                    const svo_trace_out *out);
 
