@@ -739,14 +739,25 @@ __device__ __forceinline__ uint64_t cand_cell(const ExtractArgs &a, uint32_t c, 
     return (uint64_t)x + (uint64_t)a.buf[0] * ((uint64_t)y + (uint64_t)a.buf[1] * (uint64_t)z);
 }
 
+// Each warp takes 32 bricks at a time: every lane reads one brick's flag,
+// and the whole warp then runs body(c) for each brick c whose flag passes,
+// one after another.
+template <typename Pred, typename Body>
+__device__ __forceinline__ void for_flagged_bricks(const ExtractArgs &a, Pred pred, Body body) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t step = (uint64_t)((gridDim.x * blockDim.x) >> 5) * 32;
+    for (uint64_t c0 = (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; c0 < a.n_bricks; c0 += step) {
+        unsigned ball = __ballot_sync(0xffffffffu, c0 + lane < a.n_bricks && pred(a.flag[c0 + lane]));
+        for (; ball; ball &= ball - 1) body(c0 + (unsigned)(__ffs(ball) - 1));
+    }
+}
+
 // One warp per brick flagged 1 (dropped-slice words of earlier blocks, not
 // folded here, so the fold has not counted them): its occupied voxels.
 __global__ void k_ghost_count(ExtractArgs a, uint32_t *__restrict__ count) {
     const int lane = threadIdx.x & 31;
     const uint32_t E3 = 1u << (3 * a.log_e);
-    const uint64_t nw = (gridDim.x * blockDim.x) >> 5;
-    for (uint64_t c = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < a.n_bricks; c += nw) {
-        if (a.flag[c] != 1) continue;
+    for_flagged_bricks(a, [](uint8_t f) { return f == 1; }, [&](uint64_t c) {
         uint32_t n = 0;
         for (uint32_t m = lane; m < E3; m += 32) {
             uint64_t bi = cand_cell(a, (uint32_t)c, m);
@@ -755,7 +766,7 @@ __global__ void k_ghost_count(ExtractArgs a, uint32_t *__restrict__ count) {
 #pragma unroll
         for (int o = 16; o; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
         if (lane == 0) count[c] = n;
-    }
+    });
 }
 
 // One warp per flagged brick: (key, word) of its occupied voxels in Morton
@@ -766,10 +777,8 @@ __global__ void k_cand_emit(ExtractArgs a, const uint64_t *__restrict__ off, con
                             uint32_t *__restrict__ err) {
     const int lane = threadIdx.x & 31;
     const uint32_t E3 = 1u << (3 * a.log_e);
-    const uint64_t nw = (gridDim.x * blockDim.x) >> 5;
     const uint32_t lt = (1u << lane) - 1u;
-    for (uint64_t c = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < a.n_bricks; c += nw) {
-        if (a.flag[c] == 0) continue;
+    for_flagged_bricks(a, [](uint8_t f) { return f != 0; }, [&](uint64_t c) {
         uint64_t base = *base_p + off[c];
         for (uint32_t m0 = 0; m0 < E3; m0 += 32) {
             const uint32_t m = m0 + lane;
@@ -788,7 +797,7 @@ __global__ void k_cand_emit(ExtractArgs a, const uint64_t *__restrict__ off, con
             }
             base += __popc(ball);
         }
-    }
+    });
 }
 
 __global__ void k_add_u64(uint64_t *__restrict__ acc, const uint64_t *__restrict__ add) { *acc += *add; }
