@@ -739,16 +739,19 @@ __device__ __forceinline__ uint64_t cand_cell(const ExtractArgs &a, uint32_t c, 
     return (uint64_t)x + (uint64_t)a.buf[0] * ((uint64_t)y + (uint64_t)a.buf[1] * (uint64_t)z);
 }
 
-// Each warp takes 32 bricks at a time: every lane reads one brick's flag,
-// and the whole warp then runs body(c) for each brick c whose flag passes,
-// one after another.
+// Warp w of nw handles bricks w, w + nw, w + 2 nw, ...: every lane reads one
+// of those bricks' flags, and the whole warp then runs body(c) for each
+// brick c whose flag passes, one after another.  The interleaving spreads
+// the flagged bricks, which cluster along the surface, over all warps.
 template <typename Pred, typename Body>
 __device__ __forceinline__ void for_flagged_bricks(const ExtractArgs &a, Pred pred, Body body) {
     const int lane = threadIdx.x & 31;
-    const uint64_t step = (uint64_t)((gridDim.x * blockDim.x) >> 5) * 32;
-    for (uint64_t c0 = (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; c0 < a.n_bricks; c0 += step) {
-        unsigned ball = __ballot_sync(0xffffffffu, c0 + lane < a.n_bricks && pred(a.flag[c0 + lane]));
-        for (; ball; ball &= ball - 1) body(c0 + (unsigned)(__ffs(ball) - 1));
+    const uint64_t nw = (gridDim.x * blockDim.x) >> 5;
+    const uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    for (uint64_t j0 = 0; w + j0 * nw < a.n_bricks; j0 += 32) {
+        const uint64_t mine = w + (j0 + lane) * nw;
+        unsigned ball = __ballot_sync(0xffffffffu, mine < a.n_bricks && pred(a.flag[mine]));
+        for (; ball; ball &= ball - 1) body(w + (j0 + (unsigned)(__ffs(ball) - 1)) * nw);
     }
 }
 
