@@ -445,6 +445,7 @@ struct FoldArgs {
     // last slice (drop_z, or -1), the voxels the extraction will emit.
     uint8_t *brick_flag;
     uint32_t *brick_count;
+    uint32_t *brick_bits;  // and, 16 words per brick, which of its 512 cells those are
     int drop_z;
 };
 
@@ -691,12 +692,17 @@ __global__ void __launch_bounds__(kFoldWarps * 32, 8) k_fold_bricks(FoldArgs a) 
             // the brick's whole buffer state is in shared memory: words read
             // (or known zero) and folded
             uint32_t n = 0;
-            for (int i = lane; i < E3; i += 32) {
-                int x = ox + (i & (E - 1)), y = oy + ((i >> le) & (E - 1)), z = oz + (i >> (2 * le));
-                if (x < end0 && y < end1 && z < end2 && z != a.drop_z && sm.w[i]) ++n;
+            for (int i0 = 0; i0 < E3; i0 += 32) {
+                const int i = i0 + lane;
+                bool on = false;
+                if (i < E3) {
+                    int x = ox + (i & (E - 1)), y = oy + ((i >> le) & (E - 1)), z = oz + (i >> (2 * le));
+                    on = x < end0 && y < end1 && z < end2 && z != a.drop_z && sm.w[i] != 0;
+                }
+                const uint32_t bits = __ballot_sync(0xffffffffu, on);
+                if (lane == 0) a.brick_bits[pm * 16 + (uint64_t)(i0 >> 5)] = bits;
+                n += (uint32_t)__popc(bits);
             }
-#pragma unroll
-            for (int o = 16; o; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
             if (lane == 0) {
                 a.brick_count[pm] = n;
                 a.brick_flag[pm] = 2;
@@ -775,17 +781,26 @@ __global__ void k_ghost_count(ExtractArgs a, uint32_t *__restrict__ count) {
 // One warp per flagged brick: (key, word) of its occupied voxels in Morton
 // order at *base + off[c] (at most cap), and the emitted cells cleared (the
 // walk reads them with getVoxelDestructive).
-__global__ void k_cand_emit(ExtractArgs a, const uint64_t *__restrict__ off, const uint64_t *__restrict__ base_p,
-                            uint64_t cap, uint64_t *__restrict__ keys, uint32_t *__restrict__ payload,
-                            uint32_t *__restrict__ err) {
+__global__ void k_cand_emit(ExtractArgs a, const uint32_t *__restrict__ bits, const uint64_t *__restrict__ off,
+                            const uint64_t *__restrict__ base_p, uint64_t cap, uint64_t *__restrict__ keys,
+                            uint32_t *__restrict__ payload, uint32_t *__restrict__ err) {
     const int lane = threadIdx.x & 31;
     const uint32_t E3 = 1u << (3 * a.log_e);
     const uint32_t lt = (1u << lane) - 1u;
     for_flagged_bricks(a, [](uint8_t f) { return f != 0; }, [&](uint64_t c) {
         uint64_t base = *base_p + off[c];
+        // a brick the fold counted comes with the positions of its voxels:
+        // only those cells are read
+        const bool folded = a.flag[c] == 2;
         for (uint32_t m0 = 0; m0 < E3; m0 += 32) {
             const uint32_t m = m0 + lane;
-            uint64_t bi = m < E3 ? cand_cell(a, (uint32_t)c, m) : ~0ull;
+            uint32_t on = 1u;
+            if (folded) {
+                const uint32_t word = bits[c * 16 + (m0 >> 5)];
+                if (word == 0) continue;
+                on = (word >> lane) & 1u;
+            }
+            uint64_t bi = m < E3 && on ? cand_cell(a, (uint32_t)c, m) : ~0ull;
             uint32_t v = bi != ~0ull ? a.data[bi] : 0u;
             uint32_t ball = __ballot_sync(0xffffffffu, v != 0);
             if (v) {
@@ -1142,7 +1157,8 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
     // PlyLoader::processBlock (PlyLoader.cpp:439-458) of job ji, whose buffer
     // `data` starts at org with edges buf: its bricks' pairs folded into it
     auto fold_block = [&](size_t ji, const int org[3], const int buf[3], uint32_t *data, const uint8_t *pre_dirty,
-                          uint64_t n_pre, uint8_t *brick_flag, uint32_t *brick_count, int drop_z) -> int {
+                          uint64_t n_pre, uint8_t *brick_flag, uint32_t *brick_count, uint32_t *brick_bits,
+                          int drop_z) -> int {
         const BlockJob &j = jobs[ji];
         if (j.last <= j.first) return SVO_OK;
         FoldArgs fa;
@@ -1172,6 +1188,7 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
         fa.n_pre = n_pre;
         fa.brick_flag = brick_flag;
         fa.brick_count = brick_count;
+        fa.brick_bits = brick_bits;
         fa.drop_z = drop_z;
         unsigned grid = (unsigned)std::min<uint64_t>((j.last - j.first + kFoldWarps - 1) / kFoldWarps, fold_grid);
         k_fold_bricks<<<grid, kFoldWarps * 32, 0, st>>>(fa);
@@ -1198,7 +1215,7 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
                                              cudaMemcpyDeviceToDevice, st));
             const int org[3] = {0, 0, s * slab}, buf[3] = {dims[0], dims[1], nz};
             if (ji < jobs.size() && jobs[ji].morton == (uint32_t)s) {
-                int rc = fold_block(ji, org, buf, region, nullptr, 0, nullptr, nullptr, -1);
+                int rc = fold_block(ji, org, buf, region, nullptr, 0, nullptr, nullptr, nullptr, -1);
                 if (rc) return rc;
                 ++ji;
             }
@@ -1216,9 +1233,11 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
     const uint64_t n_e = 1ull << (3 * (lb - g.log_e));  // bricks per block
     Dev<uint8_t> flag;    // per brick of the block: 0 nothing, 1 earlier dropped-slice words, 2 folded here
     Dev<uint32_t> ccount;  // per brick: the voxels the extraction emits
+    Dev<uint32_t> cbits;   // per folded brick: which cells those are (16 words)
     Dev<uint64_t> coff, bn, dN, sc64;
     SVO_ALLOC(flag, n_e);
     SVO_ALLOC(ccount, n_e);
+    SVO_ALLOC(cbits, n_e * 16);
     SVO_ALLOC(coff, n_e);
     SVO_ALLOC(bn, 1);
     SVO_ALLOC(dN, 1);
@@ -1272,7 +1291,7 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
         const int drop = ((fa.buf[2] & 1) && lb >= 2) ? 1 : 0;
         const int drop_z = drop ? fa.org[2] + fa.buf[2] - 1 : -1;
         int rc = fold_block((size_t)(&j - jobs.data()), fa.org, fa.buf, data_p, all_dirty ? nullptr : flag.p, n_e,
-                            flag.p, ccount.p, drop_z);
+                            flag.p, ccount.p, cbits.p, drop_z);
         if (rc) return rc;
         ExtractArgs ea;
         ea.flag = flag.p;
@@ -1287,7 +1306,7 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
             SVO_LAUNCH_OK("k_ghost_count");
         }
         SVO_CUDA_TRY((exclusive_scan<uint32_t, uint64_t>(ccount.p, coff.p, n_e, bn.p, sc64.p, st)));
-        k_cand_emit<<<warp_grid, 256, 0, st>>>(ea, coff.p, dN.p, cap, keys.p, pay.p, err.p);
+        k_cand_emit<<<warp_grid, 256, 0, st>>>(ea, cbits.p, coff.p, dN.p, cap, keys.p, pay.p, err.p);
         SVO_LAUNCH_OK("k_cand_emit");
         k_add_u64<<<1, 1, 0, st>>>(dN.p, bn.p);
         if (drop) {  // the walk never reads this slice; it stays in the buffer
