@@ -237,7 +237,12 @@ void svo_mesh_destroy(svo_mesh *mesh);
  * `threads` sub-blocks with their own culled triangle lists
  * (PlyLoader.cpp:381-437), and on `mem`, which sets the cache block; both
  * are parameters here and the words match the reference's for the same
- * pair.  side in [5, 2^20]. */
+ * pair.  side in [5, 2^20].  Cache blocks are folded one after another
+ * through one block buffer, as the reference does, only when a block's
+ * dropped last slice lands in a later block's buffer volume; otherwise all
+ * blocks are folded at once with no buffer.  Setting the environment
+ * variable SVO_MESH_BLOCK_BUFFER=1 keeps the block-by-block path everywhere
+ * (the words are the same; the tests run both). */
 int svo_octree_build_mesh(const svo_mesh *mesh, int side, int threads, uint64_t mem, svo_stream stream,
                           svo_octree **out);
 

@@ -447,6 +447,13 @@ struct FoldArgs {
     uint32_t *brick_count;
     uint32_t *brick_bits;  // and, 16 words per brick, which of its 512 cells those are
     int drop_z;
+    // The direct fold (every brick starts from zeros): each brick's block
+    // comes from its key (blocks of edge 2^log_block clamped to dims), and
+    // brick j's voxels go to slot[j * E^3 ...] in Morton order, with their
+    // count and cell bits at brick_count[j] and brick_bits[j * 16].
+    int dims[3];
+    int log_block;
+    uint32_t *slot;
 };
 
 // PlyLoader::writeTriangleCell on a register copy of one buffer cell.
@@ -541,13 +548,15 @@ __device__ __forceinline__ void divmod_small(int v, int n, int rcp, int &q, int 
 //      hits in pair order with writeTriangleCell (PlyLoader.cpp:296-336).
 // A voxel lies in exactly one sub-block, so only pairs of its own cell reach
 // it, in ascending triangle order as that cell's list holds them.
+template <bool kDirect>
 __global__ void __launch_bounds__(kFoldWarps * 32, 8) k_fold_bricks(FoldArgs a) {
     __shared__ FoldSmem smem[kFoldWarps];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     FoldSmem &sm = smem[wid];
     const int le = a.log_e, E = 1 << le, E3 = 1 << (3 * le);
     const float hv[3] = {a.half, a.half, a.half};
-    const int end0 = a.org[0] + a.buf[0], end1 = a.org[1] + a.buf[1], end2 = a.org[2] + a.buf[2];
+    int end0 = a.org[0] + a.buf[0], end1 = a.org[1] + a.buf[1], end2 = a.org[2] + a.buf[2];
+    int drop_z = a.drop_z;
     const uint32_t lt = (1u << lane) - 1u;
     // Warps take bricks from a counter: a brick's cost grows with its
     // triangles, and a fixed stride left most warps idle behind the few that
@@ -563,12 +572,24 @@ __global__ void __launch_bounds__(kFoldWarps * 32, 8) k_fold_bricks(FoldArgs a) 
                   oz = (int)(compact3((uint64_t)key >> 2) << le);
         // a brick the buffer holds only zeros for is not read (the extraction
         // cleared what earlier blocks left, except their dropped slices)
-        bool clean = false;
+        bool clean = kDirect;
         uint64_t pm = ~0ull;  // the brick's Morton index within the block
-        if (ox >= a.org[0] && oy >= a.org[1] && oz >= a.org[2])
-            pm = morton3((uint32_t)((ox - a.org[0]) >> le), (uint32_t)((oy - a.org[1]) >> le),
-                         (uint32_t)((oz - a.org[2]) >> le));
-        if (a.pre_dirty) clean = pm < a.n_pre && a.pre_dirty[pm] == 0;
+        if (kDirect) {
+            // the brick's block: its bounds and dropped slice (VoxelData.cpp:163-170)
+            const int lb = a.log_block, B = 1 << lb;
+            const uint64_t blk = (uint64_t)key >> (3 * (lb - le));
+            const int bx = (int)(compact3(blk) << lb), by = (int)(compact3(blk >> 1) << lb),
+                      bz = (int)(compact3(blk >> 2) << lb);
+            end0 = min(bx + B, a.dims[0]);
+            end1 = min(by + B, a.dims[1]);
+            end2 = min(bz + B, a.dims[2]);
+            drop_z = (((end2 - bz) & 1) && end2 > bz && lb >= 2) ? end2 - 1 : -1;
+        } else {
+            if (ox >= a.org[0] && oy >= a.org[1] && oz >= a.org[2])
+                pm = morton3((uint32_t)((ox - a.org[0]) >> le), (uint32_t)((oy - a.org[1]) >> le),
+                             (uint32_t)((oz - a.org[2]) >> le));
+            if (a.pre_dirty) clean = pm < a.n_pre && a.pre_dirty[pm] == 0;
+        }
         __syncwarp();
         for (int i = lane; i < E3; i += 32) {
             int x = ox + (i & (E - 1)), y = oy + ((i >> le) & (E - 1)), z = oz + (i >> (2 * le));
@@ -679,33 +700,58 @@ __global__ void __launch_bounds__(kFoldWarps * 32, 8) k_fold_bricks(FoldArgs a) 
             }
         }
         __syncwarp();
-        for (int i = lane; i < E3; i += 32) {
-            if (!((sm.touched[i >> 5] >> (i & 31)) & 1u)) continue;
-            int x = ox + (i & (E - 1)), y = oy + ((i >> le) & (E - 1)), z = oz + (i >> (2 * le));
-            if (x < a.org[0] || y < a.org[1] || z < a.org[2] || x >= end0 || y >= end1 || z >= end2) continue;
-            uint64_t bi = (uint64_t)(x - a.org[0]) +
-                          (uint64_t)a.buf[0] * ((uint64_t)(y - a.org[1]) + (uint64_t)a.buf[1] * (uint64_t)(z - a.org[2]));
-            a.data[bi] = sm.w[i];
-            a.counts[bi] = sm.cnt[i];
-        }
-        if (a.brick_count && pm < a.n_pre) {
-            // the brick's whole buffer state is in shared memory: words read
-            // (or known zero) and folded
+        if constexpr (kDirect) {
+            // the brick's voxels outside the dropped slice, in Morton order
+            // (shared memory is x-fastest), compacted into its slot
             uint32_t n = 0;
-            for (int i0 = 0; i0 < E3; i0 += 32) {
-                const int i = i0 + lane;
-                bool on = false;
-                if (i < E3) {
-                    int x = ox + (i & (E - 1)), y = oy + ((i >> le) & (E - 1)), z = oz + (i >> (2 * le));
-                    on = x < end0 && y < end1 && z < end2 && z != a.drop_z && sm.w[i] != 0;
+            uint32_t *dst = a.slot + (uint64_t)j * (uint32_t)E3;
+            for (int m0 = 0; m0 < E3; m0 += 32) {
+                const int m = m0 + lane;
+                uint32_t wv = 0;
+                if (m < E3) {
+                    const int lx = (int)compact3((uint64_t)m), ly = (int)compact3((uint64_t)m >> 1),
+                              lz = (int)compact3((uint64_t)m >> 2);
+                    const int x = ox + lx, y = oy + ly, z = oz + lz;
+                    if (x < end0 && y < end1 && z < end2 && z != drop_z) wv = sm.w[lx + (ly << le) + (lz << (2 * le))];
                 }
-                const uint32_t bits = __ballot_sync(0xffffffffu, on);
-                if (lane == 0) a.brick_bits[pm * 16 + (uint64_t)(i0 >> 5)] = bits;
+                const uint32_t bits = __ballot_sync(0xffffffffu, wv != 0);
+                if (wv) dst[n + __popc(bits & lt)] = wv;
+                if (lane == 0) a.brick_bits[(uint64_t)j * 16 + (uint64_t)(m0 >> 5)] = bits;
                 n += (uint32_t)__popc(bits);
             }
-            if (lane == 0) {
-                a.brick_count[pm] = n;
-                a.brick_flag[pm] = 2;
+            if (lane == 0) a.brick_count[j] = n;
+        } else {
+            for (int i = lane; i < E3; i += 32) {
+                if (!((sm.touched[i >> 5] >> (i & 31)) & 1u)) continue;
+                int x = ox + (i & (E - 1)), y = oy + ((i >> le) & (E - 1)), z = oz + (i >> (2 * le));
+                if (x < a.org[0] || y < a.org[1] || z < a.org[2] || x >= end0 || y >= end1 || z >= end2) continue;
+                uint64_t bi = (uint64_t)(x - a.org[0]) +
+                              (uint64_t)a.buf[0] * ((uint64_t)(y - a.org[1]) + (uint64_t)a.buf[1] * (uint64_t)(z - a.org[2]));
+                a.data[bi] = sm.w[i];
+                a.counts[bi] = sm.cnt[i];
+            }
+            if (a.brick_count && pm < a.n_pre) {
+                // the brick's whole buffer state is in shared memory: words read
+                // (or known zero) and folded.  The bits follow the extraction's
+                // order, the brick-local Morton index m (shared memory is x-fastest).
+                uint32_t n = 0;
+                for (int m0 = 0; m0 < E3; m0 += 32) {
+                    const int m = m0 + lane;
+                    bool on = false;
+                    if (m < E3) {
+                        const int lx = (int)compact3((uint64_t)m), ly = (int)compact3((uint64_t)m >> 1),
+                                  lz = (int)compact3((uint64_t)m >> 2);
+                        const int x = ox + lx, y = oy + ly, z = oz + lz;
+                        on = x < end0 && y < end1 && z < end2 && z != drop_z && sm.w[lx + (ly << le) + (lz << (2 * le))] != 0;
+                    }
+                    const uint32_t bits = __ballot_sync(0xffffffffu, on);
+                    if (lane == 0) a.brick_bits[pm * 16 + (uint64_t)(m0 >> 5)] = bits;
+                    n += (uint32_t)__popc(bits);
+                }
+                if (lane == 0) {
+                    a.brick_count[pm] = n;
+                    a.brick_flag[pm] = 2;
+                }
             }
         }
     }
@@ -781,9 +827,9 @@ __global__ void k_ghost_count(ExtractArgs a, uint32_t *__restrict__ count) {
 // One warp per flagged brick: (key, word) of its occupied voxels in Morton
 // order at *base + off[c] (at most cap), and the emitted cells cleared (the
 // walk reads them with getVoxelDestructive).
-__global__ void k_cand_emit(ExtractArgs a, const uint32_t *__restrict__ bits, const uint64_t *__restrict__ off,
-                            const uint64_t *__restrict__ base_p, uint64_t cap, uint64_t *__restrict__ keys,
-                            uint32_t *__restrict__ payload, uint32_t *__restrict__ err) {
+__global__ void k_cand_emit(ExtractArgs a, const uint32_t *__restrict__ bits, const uint32_t *__restrict__ count,
+                            const uint64_t *__restrict__ off, const uint64_t *__restrict__ base_p, uint64_t cap,
+                            uint64_t *__restrict__ keys, uint32_t *__restrict__ payload, uint32_t *__restrict__ err) {
     const int lane = threadIdx.x & 31;
     const uint32_t E3 = 1u << (3 * a.log_e);
     const uint32_t lt = (1u << lane) - 1u;
@@ -815,7 +861,43 @@ __global__ void k_cand_emit(ExtractArgs a, const uint32_t *__restrict__ bits, co
             }
             base += __popc(ball);
         }
+        // the counted voxels are exactly those emitted, or the key array has a
+        // gap the level build must not read: report it instead
+        if (lane == 0 && base != *base_p + off[c] + count[c]) atomicOr(err, 16u);
     });
+}
+
+// One warp per brick j of the direct fold: its voxels' (key, word) pairs
+// at off[j], keys in Morton order from the brick's cell bits, words from its
+// slot (at most cap).
+__global__ void k_direct_emit(uint64_t nb, int log_e, const uint32_t *__restrict__ bkey,
+                              const uint32_t *__restrict__ bits, const uint32_t *__restrict__ slot,
+                              const uint64_t *__restrict__ off, uint64_t cap, uint64_t *__restrict__ keys,
+                              uint32_t *__restrict__ payload, uint32_t *__restrict__ err) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t lt = (1u << lane) - 1u;
+    const uint32_t E3 = 1u << (3 * log_e);
+    const int chunks = (int)((E3 + 31) >> 5);
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t j = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; j < nb; j += nw) {
+        const uint32_t mine = lane < chunks ? bits[j * 16 + (uint64_t)lane] : 0u;
+        const uint64_t key0 = (uint64_t)bkey[j] << (3 * log_e), base = off[j];
+        const uint32_t *src = slot + j * E3;
+        uint32_t rank = 0;
+        for (int c = 0; c < chunks; ++c) {
+            const uint32_t b = __shfl_sync(0xffffffffu, mine, c);
+            if ((b >> lane) & 1u) {
+                const uint32_t r = rank + (uint32_t)__popc(b & lt);
+                if (base + r < cap) {
+                    keys[base + r] = key0 + (uint64_t)(c * 32 + lane);
+                    payload[base + r] = src[r];
+                } else {
+                    atomicOr(err, 8u);
+                }
+            }
+            rank += (uint32_t)__popc(b);
+        }
+    }
 }
 
 __global__ void k_add_u64(uint64_t *__restrict__ acc, const uint64_t *__restrict__ add) { *acc += *add; }
@@ -1120,6 +1202,46 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
     rfirst.release();
     rlast.release();
 
+    // The direct fold.  The extraction leaves the block buffer zero except
+    // for each block's dropped last slice (VoxelData.cpp:163-170).  When no
+    // such slice lies inside the volume of a block visited after it, every
+    // brick is folded from zeros and the blocks need no shared buffer: one
+    // fold over all bricks writes each brick's voxels to a slot of its own,
+    // and one scan places them.  Bricks are sorted by key and blocks are
+    // visited in Morton order, so the bricks of consecutive blocks follow
+    // one another and the result is in Morton order.
+    bool direct = !volume && nb > 0;
+    if (direct) {
+        uint32_t next = 0;
+        std::vector<std::pair<uint64_t, uint64_t>> gs;  // flat ranges of the dropped slices so far
+        for (const BlockJob &j : jobs) {
+            if (j.last > j.first) {
+                if (j.first != next) direct = false;
+                next = j.last;
+            }
+            int o[3] = {(int)(compact3(j.morton) << lb), (int)(compact3((uint64_t)j.morton >> 1) << lb),
+                        (int)(compact3((uint64_t)j.morton >> 2) << lb)};
+            int bb[3];
+            bool inside = true;
+            for (int k = 0; k < 3; ++k) {
+                bb[k] = std::min(B, dims[k] - o[k]);
+                if (bb[k] <= 0) inside = false;
+            }
+            if (!inside) continue;
+            const uint64_t vol = (uint64_t)bb[0] * bb[1] * bb[2];
+            for (const auto &r : gs)
+                if (std::min(r.second, vol) > r.first) direct = false;
+            if ((bb[2] & 1) && lb >= 2) {
+                const uint64_t plane = (uint64_t)bb[0] * bb[1];
+                gs.emplace_back(plane * (uint64_t)(bb[2] - 1), plane * (uint64_t)bb[2]);
+            }
+        }
+        if (next != nb) direct = false;
+        // SVO_MESH_BLOCK_BUFFER=1 keeps the per-block buffer path (same words)
+        const char *env = std::getenv("SVO_MESH_BLOCK_BUFFER");
+        if (env && *env && *env != '0') direct = false;
+    }
+
     // the persistent block buffer (VoxelData::_bufferedData, zeroed) and the
     // loader's per-cell counts, sized for the largest block volume (a whole
     // w x h x S slab in the conversion)
@@ -1136,12 +1258,14 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
     Dev<uint8_t> counts;
     Dev<float> acc;
     // the conversion folds every slab in place in its output (region 0 zeroed here)
-    if (!volume) SVO_ALLOC(data, buf_cells);
+    if (!volume && !direct) SVO_ALLOC(data, buf_cells);
     uint32_t *const data_p = volume ? d_volume : data.p;
-    SVO_ALLOC(counts, buf_cells);
+    if (!direct) {
+        SVO_ALLOC(counts, buf_cells);
+        SVO_CUDA_TRY(cudaMemsetAsync(data_p, 0, buf_cells * sizeof(uint32_t), st));
+        SVO_CUDA_TRY(cudaMemsetAsync(counts.p, 0, buf_cells, st));
+    }
     SVO_ALLOC(acc, (uint64_t)n_l * K);
-    SVO_CUDA_TRY(cudaMemsetAsync(data_p, 0, buf_cells * sizeof(uint32_t), st));
-    SVO_CUDA_TRY(cudaMemsetAsync(counts.p, 0, buf_cells, st));
     const float hx = 1.0f / (float)(side - 4);
     k_center_table<<<grid_for(n_l), 256, 0, st>>>(n_l, K, hx, acc.p);
     SVO_LAUNCH_OK("k_center_table");
@@ -1150,23 +1274,18 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
     SVO_CUDA_TRY(cudaGetDevice(&dev));
     SVO_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     const unsigned fold_grid = (unsigned)sms * 8, warp_grid = (unsigned)sms * 16;
-    Dev<uint32_t> fold_next;  // one work counter per block's fold launch
-    SVO_ALLOC(fold_next, jobs.size());
-    SVO_CUDA_TRY(cudaMemsetAsync(fold_next.p, 0, jobs.size() * sizeof(uint32_t), st));
+    Dev<uint32_t> fold_next;  // one work counter per fold launch
+    const size_t n_next = std::max<size_t>(jobs.size(), 1);
+    SVO_ALLOC(fold_next, n_next);
+    SVO_CUDA_TRY(cudaMemsetAsync(fold_next.p, 0, n_next * sizeof(uint32_t), st));
     const uint32_t brick_mask = g.slab_mode ? (uint32_t)((1ull << g.brick_bits) - 1) : 0xFFFFFFFFu;
-    // PlyLoader::processBlock (PlyLoader.cpp:439-458) of job ji, whose buffer
-    // `data` starts at org with edges buf: its bricks' pairs folded into it
-    auto fold_block = [&](size_t ji, const int org[3], const int buf[3], uint32_t *data, const uint8_t *pre_dirty,
-                          uint64_t n_pre, uint8_t *brick_flag, uint32_t *brick_count, uint32_t *brick_bits,
-                          int drop_z) -> int {
-        const BlockJob &j = jobs[ji];
-        if (j.last <= j.first) return SVO_OK;
-        FoldArgs fa;
+    // what every fold launch shares
+    auto fold_args = [&]() -> FoldArgs {
+        FoldArgs fa{};
         for (int k = 0; k < 3; ++k) {
-            fa.org[k] = org[k];
-            fa.buf[k] = buf[k];
             fa.sub[k] = sub[k];
             fa.grid[k] = g.grid[k];
+            fa.dims[k] = dims[k];
         }
         fa.tris = m->d_tris;
         fa.box = box.p;
@@ -1174,16 +1293,74 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
         fa.pair_cell = scell;
         fa.bkey = bkey.p;
         fa.bstart = bstart.p;
-        fa.b_first = j.first;
-        fa.b_last = j.last;
         fa.log_e = g.log_e;
+        fa.log_block = lb;
         fa.acc = acc.p;
         fa.K = K;
         fa.half = 0.5f * hx;
+        fa.brick_mask = brick_mask;
+        fa.drop_z = -1;
+        return fa;
+    };
+
+    if (direct) {
+        // PlyLoader::processBlock (PlyLoader.cpp:439-458) of every block at
+        // once, then the walk's voxels (VoxelOctree.cpp:66-103) from the slots
+        const uint32_t E3 = 1u << (3 * g.log_e);
+        const uint64_t cap = (uint64_t)nb * E3;
+        Dev<uint32_t> slot, ccount, cbits, pay;
+        Dev<uint64_t> coff, dN, sc64, keys;
+        SVO_ALLOC(slot, cap);
+        SVO_ALLOC(ccount, nb);
+        SVO_ALLOC(cbits, (uint64_t)nb * 16);
+        SVO_ALLOC(coff, nb);
+        SVO_ALLOC(dN, 1);
+        SVO_ALLOC(sc64, scan_scratch_elems(nb));
+        SVO_ALLOC(keys, cap);
+        SVO_ALLOC(pay, cap);
+        FoldArgs fa = fold_args();
+        fa.b_first = 0;
+        fa.b_last = nb;
+        fa.next = fold_next.p;
+        fa.slot = slot.p;
+        fa.brick_count = ccount.p;
+        fa.brick_bits = cbits.p;
+        const unsigned grid = (unsigned)std::min<uint64_t>((nb + kFoldWarps - 1) / kFoldWarps, fold_grid);
+        k_fold_bricks<true><<<grid, kFoldWarps * 32, 0, st>>>(fa);
+        SVO_LAUNCH_OK("k_fold_bricks<direct>");
+        SVO_CUDA_TRY((exclusive_scan<uint32_t, uint64_t>(ccount.p, coff.p, nb, dN.p, sc64.p, st)));
+        k_direct_emit<<<warp_grid, 256, 0, st>>>(nb, g.log_e, bkey.p, cbits.p, slot.p, coff.p, cap, keys.p, pay.p,
+                                                err.p);
+        SVO_LAUNCH_OK("k_direct_emit");
+        uint64_t N = 0;
+        uint32_t e_h = 0;
+        SVO_CUDA_TRY(cudaMemcpyAsync(&N, dN.p, sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+        SVO_CUDA_TRY(cudaMemcpyAsync(&e_h, err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        SVO_CUDA_TRY(cudaStreamSynchronize(st));
+        if (e_h) return set_error(SVO_ERR_DEVICE, "mesh build: voxel extraction check failed (flags %u)", e_h);
+        slot.release();
+        acc.release();
+        if (N >= 0xFFFFFFFFull) return set_error(SVO_ERR_LIMIT, "%llu voxels exceed 2^32-1", (unsigned long long)N);
+        return build_from_sorted_device(keys.p, pay.p, N, D, lb, lb < D ? bflag.p : nullptr, st, d_words, n_words);
+    }
+
+    // PlyLoader::processBlock (PlyLoader.cpp:439-458) of job ji, whose buffer
+    // `data` starts at org with edges buf: its bricks' pairs folded into it
+    auto fold_block = [&](size_t ji, const int org[3], const int buf[3], uint32_t *data, const uint8_t *pre_dirty,
+                          uint64_t n_pre, uint8_t *brick_flag, uint32_t *brick_count, uint32_t *brick_bits,
+                          int drop_z) -> int {
+        const BlockJob &j = jobs[ji];
+        if (j.last <= j.first) return SVO_OK;
+        FoldArgs fa = fold_args();
+        for (int k = 0; k < 3; ++k) {
+            fa.org[k] = org[k];
+            fa.buf[k] = buf[k];
+        }
+        fa.b_first = j.first;
+        fa.b_last = j.last;
         fa.data = data;
         fa.counts = counts.p;
         fa.next = fold_next.p + ji;
-        fa.brick_mask = brick_mask;
         fa.pre_dirty = pre_dirty;
         fa.n_pre = n_pre;
         fa.brick_flag = brick_flag;
@@ -1191,7 +1368,7 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
         fa.brick_bits = brick_bits;
         fa.drop_z = drop_z;
         unsigned grid = (unsigned)std::min<uint64_t>((j.last - j.first + kFoldWarps - 1) / kFoldWarps, fold_grid);
-        k_fold_bricks<<<grid, kFoldWarps * 32, 0, st>>>(fa);
+        k_fold_bricks<false><<<grid, kFoldWarps * 32, 0, st>>>(fa);
         SVO_LAUNCH_OK("k_fold_bricks");
         return SVO_OK;
     };
@@ -1306,7 +1483,7 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
             SVO_LAUNCH_OK("k_ghost_count");
         }
         SVO_CUDA_TRY((exclusive_scan<uint32_t, uint64_t>(ccount.p, coff.p, n_e, bn.p, sc64.p, st)));
-        k_cand_emit<<<warp_grid, 256, 0, st>>>(ea, cbits.p, coff.p, dN.p, cap, keys.p, pay.p, err.p);
+        k_cand_emit<<<warp_grid, 256, 0, st>>>(ea, cbits.p, ccount.p, coff.p, dN.p, cap, keys.p, pay.p, err.p);
         SVO_LAUNCH_OK("k_cand_emit");
         k_add_u64<<<1, 1, 0, st>>>(dN.p, bn.p);
         if (drop) {  // the walk never reads this slice; it stays in the buffer

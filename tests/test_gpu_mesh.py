@@ -9,6 +9,8 @@ from conftest import golden_ply, golden_volumes
 
 pytestmark = pytest.mark.gpu
 
+_ORACLE_CACHE = {}
+
 
 def _swap_floats(v):
     return np.asarray(v, np.float32).astype(">f4").view("<f4").astype(np.float32)
@@ -21,12 +23,24 @@ def _be_floats(v):
     return g.view(">f4").astype(np.float32)
 
 
+@pytest.fixture(params=["direct", "block_buffer"])
+def fold_path(request, monkeypatch):
+    """Both mesh fold paths: all cache blocks folded at once where no dropped
+    slice reaches a later block (the default), and block after block through
+    one buffer as the reference does (SVO_MESH_BLOCK_BUFFER=1)."""
+    if request.param == "block_buffer":
+        monkeypatch.setenv("SVO_MESH_BLOCK_BUFFER", "1")
+    else:
+        monkeypatch.delenv("SVO_MESH_BLOCK_BUFFER", raising=False)
+    return request.param
+
+
 def _gpu_build(svo, path, side, threads, mem):
     tree = svo.VoxelOctree(svo.VoxelData(svo.PlyLoader(path), side, mem, threads))
     return tree.words(), tree.center(), tree
 
 
-def test_golden_ply_builds(cuda, svo, scenes, golden, tmp_path):
+def test_golden_ply_builds(cuda, svo, scenes, golden, tmp_path, fold_path):
     n = 0
     for mesh, side, threads, mem, words, center in golden_ply(golden):
         path = str(tmp_path / "g.ply")
@@ -44,7 +58,7 @@ def test_golden_ply_builds(cuda, svo, scenes, golden, tmp_path):
     (4, 200, 6, 3 << 20), (3, 45, 8, 5 * 8 ** 3 + 2000), (5, 256, 16, 1 << 30), (5, 256, 8, 1 << 20),
     (2, 16, 2, 1 << 30), (3, 9, 3, 1 << 30),
 ])
-def test_build_matches_oracle(cuda, svo, oracle, scenes, tmp_path, level, side, threads, mem):
+def test_build_matches_oracle(cuda, svo, oracle, scenes, tmp_path, level, side, threads, mem, fold_path):
     pos, faces, col = scenes.edge_case_mesh(level, side + threads)
     path = str(tmp_path / "m.ply")
     scenes.write_ply(path, pos, faces, colors=col)
@@ -56,7 +70,7 @@ def test_build_matches_oracle(cuda, svo, oracle, scenes, tmp_path, level, side, 
     assert nl > 0
 
 
-def test_formats_and_normals(cuda, svo, oracle, scenes, tmp_path):
+def test_formats_and_normals(cuda, svo, oracle, scenes, tmp_path, fold_path):
     pos, faces, col = scenes.edge_case_mesh(3, 21)
     nrm = np.random.default_rng(4).normal(size=pos.shape).astype(np.float32)
     ow, oc = oracle.build_mesh(pos, faces, 96, 8, 1 << 30, colors=col.astype(np.float32), normals=nrm)
@@ -90,14 +104,16 @@ def test_from_arrays_matches_file(cuda, svo, scenes, tmp_path):
     assert np.array_equal(tree.words(), w) and np.array_equal(tree.center(), c)
 
 
-def test_workload_mesh_matches_oracle(cuda, svo, oracle, scenes, tmp_path):
+def test_workload_mesh_matches_oracle(cuda, svo, oracle, scenes, tmp_path, fold_path):
     """The bench's mesh (level-7 displaced icosphere, 327,680 triangles) at
     1024^3 with 16 sub-blocks per 512^3 cache block (1 GiB budget)."""
     pos, f, col = scenes.displaced_icosphere(7, 3)
     path = str(tmp_path / "ico7.ply")
     scenes.write_ply(path, pos, f, colors=col)
     w, c, tree = _gpu_build(svo, path, 1024, 16, 1 << 30)
-    ow, oc = oracle.build_mesh(pos, f, 1024, 16, 1 << 30, colors=col.astype(np.float32))
+    if "ico7" not in _ORACLE_CACHE:  # both fold paths check against one oracle build
+        _ORACLE_CACHE["ico7"] = oracle.build_mesh(pos, f, 1024, 16, 1 << 30, colors=col.astype(np.float32))
+    ow, oc = _ORACLE_CACHE["ico7"]
     assert np.array_equal(w, ow) and np.array_equal(c, oc)
     assert w.size > 1_000_000
 
