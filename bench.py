@@ -510,10 +510,12 @@ def run_ours(args):
               "rgba8": torch.empty(Rp, dtype=torch.int32).pin_memory().numpy()}
         os_ = {"hit": torch.empty(Rs, dtype=torch.uint8).pin_memory().numpy()}
         def host_step():
-            # both calls queued on the handle's host pipeline: the shadow rays'
-            # copies overlap the primary rays' traces
-            tree.trace_image_host(hp_pin, W, H, light=LIGHT, out=op, wait=False)
+            # both calls queued on the handle's host pipeline.  The shadow call
+            # (trace-bound) goes first, so its traces run while the primary
+            # call's rays (copy-bound) cross the link: 12.2 ms per step against
+            # 12.6-13.3 ms in the other order, alternated in one run
             tree.trace_host(hs_pin, out=os_, wait=False)
+            tree.trace_image_host(hp_pin, W, H, light=LIGHT, out=op, wait=False)
             tree.synchronize()
 
         for _ in range(max(1, args.warmup)):
@@ -538,7 +540,7 @@ def run_ours(args):
             t_calls[1] += time.perf_counter() - tb
         e2e = {"value": round(total_rays / e2e_s / 1e6, 2), "unit": "Mrays/s",
                "h2d_bytes_per_step": (Rp + Rs) * 24, "d2h_bytes_per_step": Rp * 12 + Rs * 1,
-               "api": "svo_trace_image_host_async (primary) + svo_trace_host_async (shadow) + "
+               "api": "svo_trace_host_async (shadow) + svo_trace_image_host_async (primary) + "
                       "svo_octree_synchronize: pinned host rays in, t/word/rgba8 and shadow hit out",
                "exact": bool(exact_e2e), "step_ms": round(e2e_s / args.steps * 1e3, 3),
                "waiting_calls_ms": {"primary": round(t_calls[0] / n_sync * 1e3, 3),
