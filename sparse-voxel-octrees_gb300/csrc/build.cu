@@ -236,6 +236,133 @@ __global__ void k_child_pidx_from_heads(const uint32_t *__restrict__ head, uint6
     pidx[i] = pidx[i] + head[i] - 1u;
 }
 
+// Fused grouping of one level's children (sorted Morton keys) into parents,
+// in tiles of kLvlTile children.  k_level_count counts each tile's heads
+// (children whose key >> 3 differs from the previous child's); an exclusive
+// scan of those counts gives each tile's first parent; k_level_emit stages
+// the tile's keys in shared memory and writes every parent's key, first
+// child, valid mask and child count.  The keys are read twice and only the
+// parents are written, where head flags, a scan over every child and
+// separate passes for the parents, the children's parent indices and the
+// masks read and wrote about three times as many bytes per child.
+constexpr int kLvlThreads = 256, kLvlItems = 8, kLvlTile = kLvlThreads * kLvlItems;
+
+__global__ void __launch_bounds__(kLvlThreads) k_level_count(const uint64_t *__restrict__ ckey, uint64_t n,
+                                                             const uint32_t *__restrict__ dn,
+                                                             uint32_t *__restrict__ tile_heads) {
+    __shared__ uint32_t wsum[kLvlThreads / 32];
+    const uint64_t c = level_count(n, dn);
+    const uint64_t base = (uint64_t)blockIdx.x * kLvlTile;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    uint64_t k[kLvlItems], k0[kLvlItems];
+    // every load issued before any is used; lane 0 also reads the child
+    // before its own (the previous lane's in every other lane)
+#pragma unroll
+    for (int j = 0; j < kLvlItems; ++j) {
+        const uint64_t i = base + (uint64_t)(j * kLvlThreads + threadIdx.x);
+        k[j] = i < c ? __ldg(ckey + i) : 0ull;
+        k0[j] = (lane == 0 && i > 0 && i < c) ? __ldg(ckey + i - 1) : 0ull;
+    }
+    uint32_t cnt = 0;
+#pragma unroll
+    for (int j = 0; j < kLvlItems; ++j) {
+        const uint64_t i = base + (uint64_t)(j * kLvlThreads + threadIdx.x);
+        uint64_t prev = __shfl_up_sync(0xffffffffu, k[j], 1);
+        if (lane == 0) prev = k0[j];
+        const bool head = i < c && (i == 0 || (k[j] >> 3) != (prev >> 3));
+        cnt += (uint32_t)__popc(__ballot_sync(0xffffffffu, head));
+    }
+    if (lane == 0) wsum[wid] = cnt;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+#pragma unroll
+        for (int w = 0; w < kLvlThreads / 32; ++w) t += wsum[w];
+        tile_heads[blockIdx.x] = t;
+    }
+}
+
+// Children go through the tile in rounds of kLvlThreads, so each warp holds
+// 32 consecutive children per round.  A child's parent index is the number
+// of heads up to it, minus one.  The lanes of one parent's run (at most 8
+// children) find each other with a match and OR their octant bits into the
+// valid mask with one reduction; the run's head writes the parent, and
+// finishes a run that continues past its warp's 32 children from shared
+// memory (the tile's keys plus the 7 after it).
+__global__ void __launch_bounds__(kLvlThreads) k_level_emit(const uint64_t *__restrict__ ckey, uint64_t n,
+                                                            const uint32_t *__restrict__ dn,
+                                                            const uint32_t *__restrict__ tile_first,
+                                                            uint64_t *__restrict__ pkey, uint32_t *__restrict__ pstart,
+                                                            uint8_t *__restrict__ pmask, uint8_t *__restrict__ pcount) {
+    // sk[0]: the child before the tile; sk[1 + q]: child base + q, for q below
+    // kLvlTile + 7
+    __shared__ uint64_t sk[kLvlTile + 8];
+    __shared__ uint32_t wpre[kLvlItems * (kLvlThreads / 32)];  // heads per (round, warp), then their exclusive prefix
+    const uint64_t c = level_count(n, dn);
+    const uint64_t base = (uint64_t)blockIdx.x * kLvlTile;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    constexpr int kWarps = kLvlThreads / 32;
+#pragma unroll
+    for (int j = 0; j < kLvlItems; ++j) {
+        const int q = j * kLvlThreads + threadIdx.x;
+        sk[1 + q] = base + q < c ? __ldg(ckey + base + q) : 0ull;
+    }
+    if (threadIdx.x < 8) {
+        if (threadIdx.x == 0)
+            sk[0] = (base > 0 && base - 1 < c) ? __ldg(ckey + base - 1) : 0ull;
+        else {
+            const uint64_t i = base + kLvlTile + threadIdx.x - 1;
+            sk[kLvlTile + threadIdx.x] = i < c ? __ldg(ckey + i) : 0ull;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < kLvlItems; ++j) {
+        const int q = j * kLvlThreads + threadIdx.x;
+        const bool head = base + q < c && (base + q == 0 || (sk[1 + q] >> 3) != (sk[q] >> 3));
+        const unsigned b = __ballot_sync(0xffffffffu, head);
+        if (lane == 0) wpre[j * kWarps + wid] = (uint32_t)__popc(b);
+    }
+    __syncthreads();
+    static_assert(kLvlItems * kWarps == 64, "one warp scans two entries per lane");
+    if (wid == 0) {
+        const uint32_t a0 = wpre[2 * lane], a1 = wpre[2 * lane + 1];
+        uint32_t incl = a0 + a1;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        const uint32_t ex = incl - a0 - a1;
+        wpre[2 * lane] = ex;
+        wpre[2 * lane + 1] = ex + a0;
+    }
+    __syncthreads();
+    const uint32_t first = tile_first[blockIdx.x];
+    const unsigned upto = 0xffffffffu >> (31 - lane);  // lanes 0..lane
+#pragma unroll 1
+    for (int j = 0; j < kLvlItems; ++j) {
+        const int q = j * kLvlThreads + threadIdx.x;
+        const uint64_t i = base + q;
+        const bool live = i < c;
+        const uint64_t k = sk[1 + q];
+        const bool head = live && (i == 0 || (k >> 3) != (sk[q] >> 3));
+        const unsigned b = __ballot_sync(0xffffffffu, head);
+        const uint32_t p = first + wpre[j * kWarps + wid] + (uint32_t)__popc(b & upto) - 1u;
+        const unsigned peers = __match_any_sync(0xffffffffu, live ? p : 0xFFFFFFFFu);
+        const unsigned m = __reduce_or_sync(peers, live ? 1u << (k & 7) : 0u);
+        if (head) {
+            unsigned mm = m, cnt = (unsigned)__popc(peers);
+            for (int t = q + (int)cnt; cnt < 8 && base + t < c && (sk[1 + t] >> 3) == (k >> 3); ++t, ++cnt)
+                mm |= 1u << (sk[1 + t] & 7);
+            pkey[p] = k >> 3;
+            pstart[p] = (uint32_t)i;
+            pmask[p] = (uint8_t)mm;
+            pcount[p] = (uint8_t)cnt;
+        }
+    }
+}
+
 // Dense grouping at the cache-block level: blk_first[b] = first child of
 // block b (or 0xFFFFFFFF); present = has children or top flag.
 __global__ void k_block_first(const uint64_t *__restrict__ ckey, uint64_t n, const uint32_t *__restrict__ dn,
@@ -413,6 +540,25 @@ __global__ void k_place_leaves(uint64_t n, const uint32_t *__restrict__ pidx, ui
     words[dst] = payload[i];
 }
 
+// The leaves: every bottom-level parent copies its run of leaf words into
+// its child block, in key order (the slots k_place_leaves fills one leaf at
+// a time).  A run reaching past the word count or the leaves is reported
+// through *err.
+__global__ void k_place_leaf_runs(uint64_t np, const uint32_t *__restrict__ dnp, const uint8_t *__restrict__ count,
+                                  const uint32_t *__restrict__ pstart, const uint64_t *__restrict__ pB,
+                                  const uint32_t *__restrict__ payload, uint64_t n_leaves,
+                                  uint32_t *__restrict__ words, uint64_t W, uint32_t *__restrict__ err) {
+    const uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= level_count(np, dnp)) return;
+    const uint32_t k = count[p];
+    const uint64_t s0 = pstart[p], B = pB[p];
+    if (B + k > W || s0 + k > n_leaves) {
+        atomicOr(err, 4u);
+        return;
+    }
+    for (uint32_t j = 0; j < k; ++j) words[B + j] = payload[s0 + j];
+}
+
 __global__ void k_set_u64(uint64_t *p, uint64_t v) { *p = v; }
 
 inline unsigned blocks_for(uint64_t n, int t = 256) {
@@ -552,7 +698,7 @@ int build_from_sorted_device(const uint64_t *d_keys, const uint32_t *d_payload, 
     // fewer children on, the counts stay on the device (dcount[e]) and the
     // arrays are sized by upper bounds: no host round trip per level.
     std::vector<LevelArrays> lv(D + 1);
-    DevBuf<uint32_t> leaf_pidx, dcount;
+    DevBuf<uint32_t> dcount;
     SVO_TRY_ALLOC(dcount.alloc(D + 1, arena));
     const uint64_t *ckey = d_keys;
     uint64_t nc = N;              // children: exact count, or an upper bound when cdn != nullptr
@@ -564,20 +710,19 @@ int build_from_sorted_device(const uint64_t *d_keys, const uint32_t *d_payload, 
         uint32_t *dn = on_device ? dcount.p + e : nullptr;
         // at most one node per cell of edge 2^e, and never more parents than children
         const uint64_t cells = 3 * (D - e) >= 63 ? ~0ull : 1ull << (3 * (D - e));
-        DevBuf<uint32_t> head, pidx;
-        SVO_TRY_ALLOC(head.alloc(nc, arena));
-        SVO_TRY_ALLOC(pidx.alloc(nc, arena));
-        if (nc) {
-            k_heads<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, cdn, head.p);
-            SVO_LAUNCH_CHECK("k_heads");
-        }
         if (multi_block && e == log_block) {
             // Dense grouping over cache blocks, adding blocks that only the top
             // lookup table marks (descriptors without children).
-            DevBuf<uint32_t> first, present, bidx;
+            DevBuf<uint32_t> head, pidx, first, present, bidx;
+            SVO_TRY_ALLOC(head.alloc(nc, arena));
+            SVO_TRY_ALLOC(pidx.alloc(nc, arena));
             SVO_TRY_ALLOC(first.alloc(n_blocks, arena));
             SVO_TRY_ALLOC(present.alloc(n_blocks, arena));
             SVO_TRY_ALLOC(bidx.alloc(n_blocks, arena));
+            if (nc) {
+                k_heads<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, cdn, head.p);
+                SVO_LAUNCH_CHECK("k_heads");
+            }
             SVO_CUDA_TRY(cudaMemsetAsync(first.p, 0xFF, n_blocks * sizeof(uint32_t), st));
             if (nc) k_block_first<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, cdn, head.p, first.p);
             k_block_present<<<blocks_for(n_blocks), 256, 0, st>>>(first.p, d_topflag, n_blocks, present.p);
@@ -591,65 +736,66 @@ int build_from_sorted_device(const uint64_t *d_keys, const uint32_t *d_payload, 
                 L.n = np;
             }
             if (rc) return rc;
+            if (e == D && L.n == 0) L.n = 1;  // the root (fixed up below)
             SVO_TRY_ALLOC(L.key.alloc(L.n, arena));
             SVO_TRY_ALLOC(L.start.alloc(L.n, arena));
+            SVO_TRY_ALLOC(L.mask.alloc(L.n, arena));
+            SVO_TRY_ALLOC(L.count.alloc(L.n, arena));
+            // blocks only the top table marks keep mask and count 0
+            SVO_CUDA_TRY(cudaMemsetAsync(L.mask.p, 0, L.n, st));
+            SVO_CUDA_TRY(cudaMemsetAsync(L.count.p, 0, L.n, st));
             k_block_parents<<<blocks_for(n_blocks), 256, 0, st>>>(first.p, present.p, bidx.p, n_blocks, nc, cdn,
                                                                   L.key.p, L.start.p);
-            if (nc) k_child_pidx_from_blocks<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, cdn, bidx.p, pidx.p);
-            SVO_LAUNCH_CHECK("k_child_pidx_from_blocks");
+            if (nc) {
+                k_child_pidx_from_blocks<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, cdn, bidx.p, pidx.p);
+                k_parent_masks_warp<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, cdn, pidx.p, L.mask.p, L.count.p);
+                SVO_LAUNCH_CHECK("k_parent_masks_warp");
+            }
         } else {
+            // Fused grouping: tile head counts, their scan, then the parents.
+            const uint64_t tiles = (nc + kLvlTile - 1) / kLvlTile;
+            DevBuf<uint32_t> th, tf;
+            SVO_TRY_ALLOC(th.alloc(tiles, arena));
+            SVO_TRY_ALLOC(tf.alloc(tiles, arena));
+            if (nc) {
+                k_level_count<<<(unsigned)tiles, kLvlThreads, 0, st>>>(ckey, nc, cdn, th.p);
+                SVO_LAUNCH_CHECK("k_level_count");
+            }
             if (on_device) {
-                rc = scan_on_device<uint32_t>(head.p, pidx.p, nc, dn, st, arena);
+                if (tiles)
+                    rc = scan_on_device<uint32_t>(th.p, tf.p, tiles, dn, st, arena);
+                else
+                    SVO_CUDA_TRY(cudaMemsetAsync(dn, 0, sizeof(uint32_t), st));
                 L.n = std::min(nc, cells);
             } else {
                 uint32_t np = 0;
-                rc = scan_to<uint32_t>(head.p, pidx.p, nc, &np, st, &arena);
+                if (tiles) rc = scan_to<uint32_t>(th.p, tf.p, tiles, &np, st, &arena);
                 L.n = np;
             }
             if (rc) return rc;
+            if (e == D && L.n == 0) L.n = 1;  // the root (fixed up below)
             SVO_TRY_ALLOC(L.key.alloc(L.n, arena));
             SVO_TRY_ALLOC(L.start.alloc(L.n, arena));
+            SVO_TRY_ALLOC(L.mask.alloc(L.n, arena));
+            SVO_TRY_ALLOC(L.count.alloc(L.n, arena));
+            if (e == D) {  // a root added over an empty grid has no children
+                SVO_CUDA_TRY(cudaMemsetAsync(L.key.p, 0, sizeof(uint64_t), st));
+                SVO_CUDA_TRY(cudaMemsetAsync(L.start.p, 0, sizeof(uint32_t), st));
+                SVO_CUDA_TRY(cudaMemsetAsync(L.mask.p, 0, 1, st));
+                SVO_CUDA_TRY(cudaMemsetAsync(L.count.p, 0, 1, st));
+            }
             if (nc) {
-                k_parents_from_heads<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, cdn, head.p, pidx.p, L.key.p,
-                                                                     L.start.p);
-                k_child_pidx_from_heads<<<blocks_for(nc), 256, 0, st>>>(head.p, nc, cdn, pidx.p);
-                SVO_LAUNCH_CHECK("k_child_pidx_from_heads");
+                k_level_emit<<<(unsigned)tiles, kLvlThreads, 0, st>>>(ckey, nc, cdn, tf.p, L.key.p, L.start.p,
+                                                                    L.mask.p, L.count.p);
+                SVO_LAUNCH_CHECK("k_level_emit");
             }
         }
         // The root always exists, even over an empty grid.
-        if (e == D) {
-            if (on_device) {
-                if (L.n == 0) {  // bound 0: the arrays hold the one node the kernel may add
-                    L.n = 1;
-                    SVO_TRY_ALLOC(L.key.alloc(1, arena));
-                    SVO_TRY_ALLOC(L.start.alloc(1, arena));
-                }
-                k_root_node<<<1, 1, 0, st>>>(dn, L.key.p, L.start.p);
-                SVO_LAUNCH_CHECK("k_root_node");
-            } else if (L.n == 0) {
-                L.n = 1;
-                SVO_TRY_ALLOC(L.key.alloc(1, arena));
-                SVO_TRY_ALLOC(L.start.alloc(1, arena));
-                SVO_CUDA_TRY(cudaMemsetAsync(L.key.p, 0, sizeof(uint64_t), st));
-                SVO_CUDA_TRY(cudaMemsetAsync(L.start.p, 0, sizeof(uint32_t), st));
-            }
+        if (e == D && on_device) {
+            k_root_node<<<1, 1, 0, st>>>(dn, L.key.p, L.start.p);
+            SVO_LAUNCH_CHECK("k_root_node");
         }
         L.dn = dn;
-        SVO_TRY_ALLOC(L.mask.alloc(L.n, arena));
-        SVO_TRY_ALLOC(L.count.alloc(L.n, arena));
-        if ((multi_block && e == log_block) || e == D) {  // levels that can hold parents without children
-            SVO_CUDA_TRY(cudaMemsetAsync(L.mask.p, 0, L.n, st));
-            SVO_CUDA_TRY(cudaMemsetAsync(L.count.p, 0, L.n, st));
-        }
-        if (nc) {
-            k_parent_masks_warp<<<blocks_for(nc), 256, 0, st>>>(ckey, nc, cdn, pidx.p, L.mask.p, L.count.p);
-            SVO_LAUNCH_CHECK("k_parent_masks_warp");
-        }
-        if (e == 1) {
-            leaf_pidx.p = pidx.p;
-            leaf_pidx.st = st;
-            pidx.p = nullptr;
-        }
         ckey = L.key.p;
         nc = L.n;
         cdn = L.dn;
@@ -688,9 +834,9 @@ int build_from_sorted_device(const uint64_t *d_keys, const uint32_t *d_payload, 
         SVO_LAUNCH_CHECK("k_place");
     }
     if (N) {
-        k_place_leaves<<<blocks_for(N), 256, 0, st>>>(N, leaf_pidx.p, lv[1].n, lv[1].dn, lv[1].start.p, lv[1].B.p,
-                                                      d_payload, words, W, err.p);
-        SVO_LAUNCH_CHECK("k_place_leaves");
+        k_place_leaf_runs<<<blocks_for(lv[1].n), 256, 0, st>>>(lv[1].n, lv[1].dn, lv[1].count.p, lv[1].start.p,
+                                                               lv[1].B.p, d_payload, N, words, W, err.p);
+        SVO_LAUNCH_CHECK("k_place_leaf_runs");
     }
     uint32_t err_h = 0;
     cudaError_t e = cudaMemcpyAsync(&err_h, err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
