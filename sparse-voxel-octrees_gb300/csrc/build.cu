@@ -129,24 +129,30 @@ __global__ void __launch_bounds__(kBrickThreads) k_brick_count(GridGeom g, uint6
     }
 }
 
-// Phase 1b: emit (key, payload) for V' in Morton order.  The brick is staged
-// in shared memory with coalesced row reads; each thread counts a run of
-// consecutive local Morton codes, a block scan places the runs, the occupied
-// codes are compacted into shared memory in Morton order, and the CTA writes
-// the brick's keys and payloads with consecutive threads on consecutive
-// elements.
+// Phase 1b: emit (key, payload) for V' in Morton order.  The brick goes into
+// shared memory in local Morton order as it is read (a thread's uint4 holds
+// cells x .. x+3 of a row, whose codes are m, m+1, m+8 and m+9 with m the
+// code of x), so nothing is decoded afterwards.  Warp w then owns codes
+// [w * span, (w + 1) * span): one pass counts its occupied cells with
+// ballots, and after the warps' totals are known, a second pass writes their
+// keys and payloads at consecutive positions.
 __global__ void __launch_bounds__(kBrickThreads) k_brick_emit(GridGeom g, uint64_t n_bricks, const uint32_t *__restrict__ counts,
                                                             const uint64_t *__restrict__ offsets,
                                                             uint64_t *__restrict__ keys, uint32_t *__restrict__ payload) {
-    __shared__ __align__(16) uint32_t tile[16 * 16 * 16];
-    __shared__ uint16_t order[16 * 16 * 16];  // the brick's occupied local Morton codes, ascending
-    const int E = 1 << g.log_brick;
+    constexpr int kWarps = kBrickThreads / 32;
+    __shared__ __align__(16) uint32_t tile[16 * 16 * 16];  // the brick's words by local Morton code
+    __shared__ uint32_t wtot[kWarps];
+    const int lb = g.log_brick;
+    const int E = 1 << lb;
     const int cells = E * E * E;
-    const int per = (cells + kBrickThreads - 1) / kBrickThreads;
+    const int span = (cells + kWarps - 1) / kWarps;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const uint32_t lt = (1u << lane) - 1u;
+    const int m_lo = wid * span, m_hi = min(cells, m_lo + span);
     for (uint64_t b = blockIdx.x; b < n_bricks; b += gridDim.x) {
         if (counts[b] == 0) continue;  // uniform across the CTA
         uint32_t bx = compact3(b), by = compact3(b >> 1), bz = compact3(b >> 2);
-        int gx0 = (int)(bx << g.log_brick), gy0 = (int)(by << g.log_brick), gz0 = (int)(bz << g.log_brick);
+        int gx0 = (int)(bx << lb), gy0 = (int)(by << lb), gz0 = (int)(bz << lb);
         if (brick_vec4(g, gx0, gy0, gz0)) {
             uint4 v[4];
             brick_load4(g, gx0, gy0, gz0, v);
@@ -154,47 +160,46 @@ __global__ void __launch_bounds__(kBrickThreads) k_brick_emit(GridGeom g, uint64
             for (int k = 0; k < 4; ++k) {
                 const int q = threadIdx.x + k * 256;
                 if (g.drop_last_z && gz0 + (q >> 6) == g.d - 1) v[k] = make_uint4(0u, 0u, 0u, 0u);
-                reinterpret_cast<uint4 *>(tile)[q] = v[k];  // cells 4q .. 4q+3
+                const uint32_t m = (uint32_t)morton3((uint32_t)((q & 3) << 2), (uint32_t)((q >> 2) & 15),
+                                                     (uint32_t)(q >> 6));
+                tile[m] = v[k].x;
+                tile[m + 1] = v[k].y;
+                tile[m + 8] = v[k].z;
+                tile[m + 9] = v[k].w;
             }
         } else {
             for (int c = threadIdx.x; c < cells; c += kBrickThreads) {
-                int gx = gx0 + (c & (E - 1)), gy = gy0 + ((c >> g.log_brick) & (E - 1)),
-                    gz = gz0 + (c >> (2 * g.log_brick));
+                int lx = c & (E - 1), ly = (c >> lb) & (E - 1), lz = c >> (2 * lb);
+                int gx = gx0 + lx, gy = gy0 + ly, gz = gz0 + lz;
                 uint32_t v = 0;
                 if (gx < g.w && gy < g.h && gz < g.d && !(g.drop_last_z && gz == g.d - 1))
                     v = __ldg(g.grid + (uint64_t)gx + (uint64_t)g.w * ((uint64_t)gy + (uint64_t)g.h * gz));
-                tile[c] = v;
+                tile[morton3((uint32_t)lx, (uint32_t)ly, (uint32_t)lz)] = v;
             }
         }
         __syncthreads();
-        uint32_t cnt = 0;
-        int m0 = threadIdx.x * per;
-        for (int k = 0; k < per; ++k) {
-            int m = m0 + k;
-            if (m < cells) {
-                uint32_t lx = compact3((uint64_t)m), ly = compact3((uint64_t)m >> 1), lz = compact3((uint64_t)m >> 2);
-                cnt += tile[lx + E * (ly + E * lz)] != 0;
-            }
+        uint32_t run = 0;
+        for (int m0 = m_lo; m0 < m_hi; m0 += 32) {
+            const int m = m0 + lane;
+            run += (uint32_t)__popc(__ballot_sync(0xffffffffu, m < m_hi && tile[m] != 0u));
         }
-        uint32_t total;
-        uint32_t o = block_excl_scan<uint32_t>(cnt, &total);
-        for (int k = 0; k < per; ++k) {
-            int m = m0 + k;
-            if (m < cells) {
-                uint32_t lx = compact3((uint64_t)m), ly = compact3((uint64_t)m >> 1), lz = compact3((uint64_t)m >> 2);
-                if (tile[lx + E * (ly + E * lz)]) order[o++] = (uint16_t)m;
-            }
-        }
+        if (lane == 0) wtot[wid] = run;
         __syncthreads();
-        const uint64_t out0 = offsets[b];
-        const uint64_t kbase = b << (3 * g.log_brick);
-        for (uint32_t i = threadIdx.x; i < total; i += kBrickThreads) {
-            const uint32_t m = order[i];
-            const uint32_t lx = compact3((uint64_t)m), ly = compact3((uint64_t)m >> 1), lz = compact3((uint64_t)m >> 2);
-            keys[out0 + i] = kbase | (uint64_t)m;
-            payload[out0 + i] = tile[lx + E * (ly + E * lz)];
+        uint64_t out = offsets[b];
+        for (int w = 0; w < wid; ++w) out += wtot[w];
+        const uint64_t kbase = b << (3 * lb);
+        for (int m0 = m_lo; m0 < m_hi; m0 += 32) {
+            const int m = m0 + lane;
+            const uint32_t v = m < m_hi ? tile[m] : 0u;
+            const uint32_t ball = __ballot_sync(0xffffffffu, v != 0u);
+            if (v) {
+                const uint64_t o = out + (uint64_t)__popc(ball & lt);
+                keys[o] = kbase | (uint64_t)m;
+                payload[o] = v;
+            }
+            out += (uint64_t)__popc(ball);
         }
-        __syncthreads();
+        __syncthreads();  // the next brick overwrites tile and wtot
     }
 }
 
