@@ -76,7 +76,7 @@ __device__ __forceinline__ void brick_load4(const GridGeom &g, int gx0, int gy0,
 // Phase 1a: per brick, count voxels that survive (V') and flag M-blocks that
 // hold any voxel (V).  One CTA per brick; consecutive threads read
 // consecutive x so each warp load covers whole 32-byte sectors of a row.
-__global__ void __launch_bounds__(kBrickThreads) k_brick_count(GridGeom g, uint64_t n_bricks, uint32_t *__restrict__ counts) {
+__global__ void __launch_bounds__(kBrickThreads, 8) k_brick_count(GridGeom g, uint64_t n_bricks, uint32_t *__restrict__ counts) {
     const int lb = g.log_brick;
     const int E = 1 << lb;
     const int cells = E * E * E;
@@ -545,23 +545,61 @@ __global__ void k_place_leaves(uint64_t n, const uint32_t *__restrict__ pidx, ui
     words[dst] = payload[i];
 }
 
-// The leaves: every bottom-level parent copies its run of leaf words into
-// its child block, in key order (the slots k_place_leaves fills one leaf at
-// a time).  A run reaching past the word count or the leaves is reported
-// through *err.
-__global__ void k_place_leaf_runs(uint64_t np, const uint32_t *__restrict__ dnp, const uint8_t *__restrict__ count,
-                                  const uint32_t *__restrict__ pstart, const uint64_t *__restrict__ pB,
-                                  const uint32_t *__restrict__ payload, uint64_t n_leaves,
-                                  uint32_t *__restrict__ words, uint64_t W, uint32_t *__restrict__ err) {
-    const uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= level_count(np, dnp)) return;
-    const uint32_t k = count[p];
-    const uint64_t s0 = pstart[p], B = pB[p];
-    if (B + k > W || s0 + k > n_leaves) {
-        atomicOr(err, 4u);
+// The leaves: every bottom-level parent's run of leaf words goes into its
+// child block, in key order (the slots k_place_leaves fills one leaf at a
+// time).  A warp takes 32 consecutive parents, whose runs are consecutive
+// (each starts where the previous one ends), so their at most 256 leaves are
+// one range: each lane marks its run's slots in a per-warp owner table, then
+// the warp copies the range with consecutive lanes on consecutive leaves.
+// A run reaching past the word count or the leaves is reported through *err.
+__global__ void __launch_bounds__(256) k_place_leaf_runs(uint64_t np, const uint32_t *__restrict__ dnp,
+                                                         const uint8_t *__restrict__ count,
+                                                         const uint32_t *__restrict__ pstart,
+                                                         const uint64_t *__restrict__ pB,
+                                                         const uint32_t *__restrict__ payload, uint64_t n_leaves,
+                                                         uint32_t *__restrict__ words, uint64_t W,
+                                                         uint32_t *__restrict__ err) {
+    __shared__ uint8_t owner[8][256];  // per warp: the lane whose parent holds leaf slot s0 + i
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const uint64_t n = level_count(np, dnp);
+    const uint64_t p0 = ((uint64_t)blockIdx.x * blockDim.x) + (uint64_t)wid * 32;
+    if (p0 >= n) return;  // uniform per warp
+    const uint64_t p = p0 + lane;
+    const bool live = p < n;
+    const uint32_t k = live ? count[p] : 0u;
+    const uint64_t s = live ? pstart[p] : 0ull, B = live ? pB[p] : 0ull;
+    // parents without children (cache blocks only the top table marks) have
+    // no run; the others' runs follow one another from the first one's start
+    const unsigned runs = __ballot_sync(0xffffffffu, k != 0);
+    if (!runs) return;
+    const uint64_t s0 = __shfl_sync(0xffffffffu, s, __ffs(runs) - 1);
+    // the runs must tile the range in lane order: each starts where the
+    // earlier lanes' runs end
+    uint32_t before = k;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, before, o);
+        if (lane >= o) before += t;
+    }
+    before -= k;
+    const bool bad = k != 0 && (B + k > W || s + k > n_leaves || s != s0 + before);
+    if (__any_sync(0xffffffffu, bad)) {
+        if (bad) atomicOr(err, 4u);
         return;
     }
-    for (uint32_t j = 0; j < k; ++j) words[B + j] = payload[s0 + j];
+    const uint32_t rel = k ? (uint32_t)(s - s0) : 0u;
+    for (uint32_t j = 0; j < k; ++j) owner[wid][rel + j] = (uint8_t)lane;
+    const uint32_t total = __reduce_max_sync(0xffffffffu, k ? rel + k : 0u);
+    __syncwarp();
+    // every lane takes the same number of rounds: the shuffles read lanes
+    // that may own no leaf of the round
+    for (uint32_t i0 = 0; i0 < total; i0 += 32) {
+        const uint32_t i = i0 + lane;
+        const int l = i < total ? owner[wid][i] : 0;
+        const uint64_t Bl = __shfl_sync(0xffffffffu, B, l);
+        const uint64_t sl = __shfl_sync(0xffffffffu, s, l);
+        if (i < total) words[Bl + (s0 + i - sl)] = payload[s0 + i];
+    }
 }
 
 __global__ void k_set_u64(uint64_t *p, uint64_t v) { *p = v; }
