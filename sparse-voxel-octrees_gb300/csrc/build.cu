@@ -87,19 +87,34 @@ __global__ void __launch_bounds__(kBrickThreads, 8) k_brick_count(GridGeom g, ui
         if (brick_vec4(g, gx0, gy0, gz0)) {
             uint4 v[4];
             brick_load4(g, gx0, gy0, gz0, v);
+            if (!(g.topflag && g.log_block < lb)) {
+                // no cell-level flags: count the row's nonzero words and OR
+                // them for the brick's flag (a scan of the grid is otherwise
+                // bound by these instructions, not by its loads)
+                uint32_t bits = 0;
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const int q = threadIdx.x + k * 256;
-                const int gx = gx0 + ((q & 3) << 2), gy = gy0 + ((q >> 2) & 15), gz = gz0 + (q >> 6);
-                const uint32_t e[4] = {v[k].x, v[k].y, v[k].z, v[k].w};
+                for (int k = 0; k < 4; ++k) {
+                    const int gz = gz0 + ((threadIdx.x + k * 256) >> 6);
+                    bits |= v[k].x | v[k].y | v[k].z | v[k].w;
+                    const uint32_t nz = (uint32_t)(v[k].x != 0u) + (uint32_t)(v[k].y != 0u) +
+                                        (uint32_t)(v[k].z != 0u) + (uint32_t)(v[k].w != 0u);
+                    if (!(g.drop_last_z && gz == g.d - 1)) cnt += nz;
+                }
+                any = bits != 0u;
+            } else {
 #pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    if (e[j]) {
-                        any = 1;
-                        if (!(g.drop_last_z && gz == g.d - 1)) ++cnt;
-                        if (g.topflag && g.log_block < lb)
+                for (int k = 0; k < 4; ++k) {
+                    const int q = threadIdx.x + k * 256;
+                    const int gx = gx0 + ((q & 3) << 2), gy = gy0 + ((q >> 2) & 15), gz = gz0 + (q >> 6);
+                    const uint32_t e[4] = {v[k].x, v[k].y, v[k].z, v[k].w};
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        if (e[j]) {
+                            any = 1;
+                            if (!(g.drop_last_z && gz == g.d - 1)) ++cnt;
                             g.topflag[morton3((uint32_t)(gx + j) >> g.log_block, (uint32_t)gy >> g.log_block,
                                               (uint32_t)gz >> g.log_block)] = 1;
+                        }
                     }
                 }
             }
@@ -289,10 +304,10 @@ __global__ void __launch_bounds__(kLvlThreads) k_level_count(const uint64_t *__r
 
 // Children go through the tile in rounds of kLvlThreads, so each warp holds
 // 32 consecutive children per round.  A child's parent index is the number
-// of heads up to it, minus one.  The lanes of one parent's run (at most 8
-// children) find each other with a match and OR their octant bits into the
-// valid mask with one reduction; the run's head writes the parent, and
-// finishes a run that continues past its warp's 32 children from shared
+// of heads up to it, minus one.  A parent's run (at most 8 children) is the
+// lanes from its head to the next head; three shuffle steps OR the run's
+// octant bits into the head's valid mask, and the head writes the parent,
+// finishing a run that continues past its warp's 32 children from shared
 // memory (the tile's keys plus the 7 after it).
 __global__ void __launch_bounds__(kLvlThreads) k_level_emit(const uint64_t *__restrict__ ckey, uint64_t n,
                                                             const uint32_t *__restrict__ dn,
@@ -353,11 +368,21 @@ __global__ void __launch_bounds__(kLvlThreads) k_level_emit(const uint64_t *__re
         const uint64_t k = sk[1 + q];
         const bool head = live && (i == 0 || (k >> 3) != (sk[q] >> 3));
         const unsigned b = __ballot_sync(0xffffffffu, head);
-        const uint32_t p = first + wpre[j * kWarps + wid] + (uint32_t)__popc(b & upto) - 1u;
-        const unsigned peers = __match_any_sync(0xffffffffu, live ? p : 0xFFFFFFFFu);
-        const unsigned m = __reduce_or_sync(peers, live ? 1u << (k & 7) : 0u);
+        // a run ends at the next head or at the first lane past the last child
+        const unsigned after = (b | ~__ballot_sync(0xffffffffu, live)) & ~upto;
+        const int hi = after ? __ffs(after) - 1 : 32;
+        // octant bits of this lane and the run-mates after it (at most 7),
+        // by doubling: runs are contiguous, so lane + d in the run means the
+        // lanes between are too
+        unsigned m = live ? 1u << (k & 7) : 0u;
+#pragma unroll
+        for (int d = 1; d < 8; d <<= 1) {
+            const unsigned o = __shfl_down_sync(0xffffffffu, m, d);
+            if (lane + d < hi) m |= o;
+        }
         if (head) {
-            unsigned mm = m, cnt = (unsigned)__popc(peers);
+            const uint32_t p = first + wpre[j * kWarps + wid] + (uint32_t)__popc(b & upto) - 1u;
+            unsigned mm = m, cnt = (unsigned)(hi - lane);
             for (int t = q + (int)cnt; cnt < 8 && base + t < c && (sk[1 + t] >> 3) == (k >> 3); ++t, ++cnt)
                 mm |= 1u << (sk[1 + t] & 7);
             pkey[p] = k >> 3;
