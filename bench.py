@@ -674,7 +674,9 @@ def summary_of(line):
          "fwd_bwd_fd_own_truncation_max_rel": g(line, "fwd_bwd", "check", "fp64_analytic_vs_fd_max_rel"),
          "fwd_bwd_richardson_fd_max_rel": g(line, "fwd_bwd", "check", "richardson_fd_max_rel"),
          "mesh_build_ms": g(line, "mesh_build", "build_ms"),
-         "mesh_build_exact": g(line, "mesh_build", "exact_vs_oracle")}
+         "mesh_build_exact": g(line, "mesh_build", "exact_vs_oracle"),
+         "octree_build_warm_ms": None if g(line, "build", "build_warm_s") is None
+         else round(g(line, "build", "build_warm_s") * 1e3, 2)}
     return s
 
 
