@@ -336,12 +336,15 @@ __global__ void __launch_bounds__(kLvlThreads) k_level_emit(const uint64_t *__re
         }
     }
     __syncthreads();
+    // heads (parent keys differ: the keys differ above their low 3 bits),
+    // kept as this warp's ballot per round
+    unsigned hb[kLvlItems];
 #pragma unroll
     for (int j = 0; j < kLvlItems; ++j) {
         const int q = j * kLvlThreads + threadIdx.x;
-        const bool head = base + q < c && (base + q == 0 || (sk[1 + q] >> 3) != (sk[q] >> 3));
-        const unsigned b = __ballot_sync(0xffffffffu, head);
-        if (lane == 0) wpre[j * kWarps + wid] = (uint32_t)__popc(b);
+        const bool head = base + q < c && (base + q == 0 || ((sk[1 + q] ^ sk[q]) & ~7ull) != 0ull);
+        hb[j] = __ballot_sync(0xffffffffu, head);
+        if (lane == 0) wpre[j * kWarps + wid] = (uint32_t)__popc(hb[j]);
     }
     __syncthreads();
     static_assert(kLvlItems * kWarps == 64, "one warp scans two entries per lane");
@@ -360,16 +363,19 @@ __global__ void __launch_bounds__(kLvlThreads) k_level_emit(const uint64_t *__re
     __syncthreads();
     const uint32_t first = tile_first[blockIdx.x];
     const unsigned upto = 0xffffffffu >> (31 - lane);  // lanes 0..lane
-#pragma unroll 1
+#pragma unroll
     for (int j = 0; j < kLvlItems; ++j) {
         const int q = j * kLvlThreads + threadIdx.x;
         const uint64_t i = base + q;
         const bool live = i < c;
         const uint64_t k = sk[1 + q];
-        const bool head = live && (i == 0 || (k >> 3) != (sk[q] >> 3));
-        const unsigned b = __ballot_sync(0xffffffffu, head);
-        // a run ends at the next head or at the first lane past the last child
-        const unsigned after = (b | ~__ballot_sync(0xffffffffu, live)) & ~upto;
+        const unsigned b = hb[j];
+        const bool head = (b >> lane) & 1u;
+        // a run ends at the next head or at the first lane past the last
+        // child (the live lanes are a prefix of the warp's 32)
+        const uint64_t w0 = base + (uint64_t)(q - lane);
+        const unsigned livem = w0 >= c ? 0u : (c - w0 >= 32 ? 0xffffffffu : (1u << (uint32_t)(c - w0)) - 1u);
+        const unsigned after = (b | ~livem) & ~upto;
         const int hi = after ? __ffs(after) - 1 : 32;
         // octant bits of this lane and the run-mates after it (at most 7),
         // by doubling: runs are contiguous, so lane + d in the run means the
@@ -383,7 +389,7 @@ __global__ void __launch_bounds__(kLvlThreads) k_level_emit(const uint64_t *__re
         if (head) {
             const uint32_t p = first + wpre[j * kWarps + wid] + (uint32_t)__popc(b & upto) - 1u;
             unsigned mm = m, cnt = (unsigned)(hi - lane);
-            for (int t = q + (int)cnt; cnt < 8 && base + t < c && (sk[1 + t] >> 3) == (k >> 3); ++t, ++cnt)
+            for (int t = q + (int)cnt; cnt < 8 && base + t < c && ((sk[1 + t] ^ k) & ~7ull) == 0ull; ++t, ++cnt)
                 mm |= 1u << (sk[1 + t] & 7);
             pkey[p] = k >> 3;
             pstart[p] = (uint32_t)i;
@@ -568,6 +574,105 @@ __global__ void k_place_leaves(uint64_t n, const uint32_t *__restrict__ pidx, ui
         return;
     }
     words[dst] = payload[i];
+}
+
+// The same placement with a lane per child: a warp takes 32 consecutive
+// parents, whose children follow one another (at most 256), marks which lane
+// owns each child in a per-warp table, and places the children 32 at a time.
+// A child's block offset is the sum of the subtree sizes of its earlier
+// siblings: a segmented scan over the round's lanes (runs are at most 8
+// long, so three shuffle steps), plus what a run that began in the previous
+// round carried over.  The descriptors and far words are those of k_place.
+__global__ void __launch_bounds__(256) k_place_warp(uint64_t np, const uint32_t *__restrict__ dnp,
+                                                    const uint8_t *__restrict__ count,
+                                                    const uint32_t *__restrict__ pstart,
+                                                    const uint8_t *__restrict__ plarge,
+                                                    const uint64_t *__restrict__ pB, const uint64_t *__restrict__ cS,
+                                                    const uint8_t *__restrict__ cmask,
+                                                    const uint8_t *__restrict__ clarge, int child_is_bottom,
+                                                    uint64_t nc, const uint32_t *__restrict__ dnc,
+                                                    uint64_t *__restrict__ cB, uint32_t *__restrict__ words,
+                                                    uint64_t W, uint32_t *__restrict__ err) {
+    __shared__ uint8_t owner[8][256];  // per warp: the lane whose parent holds child s0 + i
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const unsigned upto = 0xffffffffu >> (31 - lane);
+    const uint64_t n = level_count(np, dnp);
+    const uint64_t p0 = ((uint64_t)blockIdx.x * blockDim.x) + (uint64_t)wid * 32;
+    if (p0 >= n) return;  // uniform per warp
+    const uint64_t p = p0 + lane;
+    const bool live = p < n;
+    const uint32_t k = live ? count[p] : 0u;
+    const uint32_t stride = (live && plarge[p]) ? 2u : 1u;
+    const uint64_t s = live ? pstart[p] : 0ull, B = live ? pB[p] : 0ull;
+    // parents without children (cache blocks only the top table marks) have
+    // none to place; the others' children follow one another
+    const unsigned runs = __ballot_sync(0xffffffffu, k != 0);
+    if (!runs) return;
+    const uint64_t s0 = __shfl_sync(0xffffffffu, s, __ffs(runs) - 1);
+    uint32_t before = k;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, before, o);
+        if (lane >= o) before += t;
+    }
+    before -= k;
+    const bool bad = k != 0 && (s != s0 + before || s + k > level_count(nc, dnc));
+    if (__any_sync(0xffffffffu, bad)) {
+        if (bad) atomicOr(err, 2u);
+        return;
+    }
+    for (uint32_t j = 0; j < k; ++j) owner[wid][before + j] = (uint8_t)lane;
+    const uint32_t total = __reduce_max_sync(0xffffffffu, k ? before + k : 0u);
+    __syncwarp();
+    uint64_t carry = 0;  // subtree sizes of the earlier siblings of the round's first child, from earlier rounds
+    for (uint32_t i0 = 0; i0 < total; i0 += 32) {
+        const uint32_t i = i0 + lane;
+        const bool in = i < total;
+        const int l = in ? owner[wid][i] : 0;
+        const uint64_t c = s0 + i;
+        const uint64_t S = in ? cS[c] : 0ull;
+        // the lanes of one parent in this round form a segment
+        const bool start = !in || lane == 0 || owner[wid][i - 1] != (uint8_t)l;
+        const unsigned starts = __ballot_sync(0xffffffffu, start);
+        const int lo = 31 - __clz((int)(starts & upto));
+        uint64_t incl = S;
+#pragma unroll
+        for (int d = 1; d < 8; d <<= 1) {
+            const uint64_t t = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane - d >= lo) incl += t;
+        }
+        const uint64_t Bl = __shfl_sync(0xffffffffu, B, l);
+        const uint64_t sl = __shfl_sync(0xffffffffu, s, l);
+        const uint32_t kl = __shfl_sync(0xffffffffu, k, l);
+        const uint32_t stl = __shfl_sync(0xffffffffu, stride, l);
+        // the first segment continues a run from the previous round when its
+        // first child is not its parent's first
+        const uint64_t add = (lo == 0 && i0 > 0 && s0 + i0 != sl) ? carry : 0ull;
+        const uint64_t run = add + incl - S;
+        // what the last lane's run carries into the next round
+        const uint64_t last_total = __shfl_sync(0xffffffffu, add + incl, 31);
+        carry = last_total;
+        if (in) {
+            const uint64_t jj = c - sl;
+            const uint64_t pos = Bl + jj * stl;
+            const uint64_t blk = Bl + (uint64_t)kl * stl + run;
+            cB[c] = blk;
+            const uint64_t off = blk - pos;
+            const uint32_t m = cmask[c];
+            uint32_t w = (m << 8) | (child_is_bottom ? 0u : m) | (clarge[c] ? 0x10000u : 0u);
+            if (pos + (stl == 2u ? 1u : 0u) >= W) {
+                atomicOr(err, 1u);
+            } else {
+                if (stl == 2u) {
+                    w |= 0x20000u | (uint32_t)((off >> 32) << 18);
+                    words[pos + 1] = (uint32_t)off;
+                } else {
+                    w |= (uint32_t)(off << 18);
+                }
+                words[pos] = w;
+            }
+        }
+    }
 }
 
 // The leaves: every bottom-level parent's run of leaf words goes into its
@@ -897,9 +1002,10 @@ int build_from_sorted_device(const uint64_t *d_keys, const uint32_t *d_payload, 
         LevelArrays &P = lv[e];
         LevelArrays &C = lv[e - 1];
         SVO_TRY_ALLOC(C.B.alloc(C.n, arena));
-        k_place<<<blocks_for(P.n), 256, 0, st>>>(P.n, P.dn, P.count.p, P.start.p, P.large.p, P.B.p, C.S.p,
-                                                C.mask.p, C.large.p, e - 1 == 1, C.B.p, words, W, err.p);
-        SVO_LAUNCH_CHECK("k_place");
+        k_place_warp<<<blocks_for(P.n), 256, 0, st>>>(P.n, P.dn, P.count.p, P.start.p, P.large.p, P.B.p, C.S.p,
+                                                     C.mask.p, C.large.p, e - 1 == 1, C.n, C.dn, C.B.p, words, W,
+                                                     err.p);
+        SVO_LAUNCH_CHECK("k_place_warp");
     }
     if (N) {
         k_place_leaf_runs<<<blocks_for(lv[1].n), 256, 0, st>>>(lv[1].n, lv[1].dn, lv[1].count.p, lv[1].start.p,
