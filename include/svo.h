@@ -239,8 +239,10 @@ void svo_mesh_destroy(svo_mesh *mesh);
  * are parameters here and the words match the reference's for the same
  * pair.  side in [5, 2^20].  Cache blocks are folded one after another
  * through one block buffer, as the reference does, only when a block's
- * dropped last slice lands in a later block's buffer volume; otherwise all
- * blocks are folded at once with no buffer.  Setting the environment
+ * dropped last slice lands in a later block's buffer volume, or when the
+ * all-at-once form's scratch (16 bytes per cell of every brick a triangle
+ * touches) would exceed half the free device memory; otherwise all blocks
+ * are folded at once with no buffer.  Setting the environment
  * variable SVO_MESH_BLOCK_BUFFER=1 keeps the block-by-block path everywhere
  * (the words are the same; the tests run both). */
 int svo_octree_build_mesh(const svo_mesh *mesh, int side, int threads, uint64_t mem, svo_stream stream,

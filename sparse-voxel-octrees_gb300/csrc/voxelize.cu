@@ -1237,6 +1237,12 @@ int build_mesh_device(const svo_mesh *m, int side, int threads, uint64_t mem, cu
             }
         }
         if (next != nb) direct = false;
+        // the direct fold's scratch (a slot of E^3 words per brick, besides
+        // the keys and words both paths hold) must fit comfortably
+        size_t free_b = 0, total_b = 0;
+        if (direct && cudaMemGetInfo(&free_b, &total_b) == cudaSuccess &&
+            (uint64_t)nb * (1ull << (3 * g.log_e)) * 16ull > (uint64_t)free_b / 2)
+            direct = false;
         // SVO_MESH_BLOCK_BUFFER=1 keeps the per-block buffer path (same words)
         const char *env = std::getenv("SVO_MESH_BLOCK_BUFFER");
         if (env && *env && *env != '0') direct = false;
