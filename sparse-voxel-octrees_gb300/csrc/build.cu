@@ -306,9 +306,11 @@ __global__ void __launch_bounds__(kLvlThreads) k_level_count(const uint64_t *__r
 // 32 consecutive children per round.  A child's parent index is the number
 // of heads up to it, minus one.  A parent's run (at most 8 children) is the
 // lanes from its head to the next head; three shuffle steps OR the run's
-// octant bits into the head's valid mask, and the head writes the parent,
-// finishing a run that continues past its warp's 32 children from shared
-// memory (the tile's keys plus the 7 after it).
+// octant bits into the head's valid mask, and the head writes the parent.
+// A run that continues past its warp's 32 children ends in the next 32
+// children's leading run, which that round's lane 0 has already ORed and
+// counted (one table entry per round); past the tile's last round it ends
+// in the keys that follow the tile, staged in shared memory.
 __global__ void __launch_bounds__(kLvlThreads) k_level_emit(const uint64_t *__restrict__ ckey, uint64_t n,
                                                             const uint32_t *__restrict__ dn,
                                                             const uint32_t *__restrict__ tile_first,
@@ -318,6 +320,8 @@ __global__ void __launch_bounds__(kLvlThreads) k_level_emit(const uint64_t *__re
     // kLvlTile + 7
     __shared__ uint64_t sk[kLvlTile + 8];
     __shared__ uint32_t wpre[kLvlItems * (kLvlThreads / 32)];  // heads per (round, warp), then their exclusive prefix
+    __shared__ uint16_t mh[kLvlItems][kLvlThreads];  // per child: run mask (low 8 bits) and run end lane
+    __shared__ uint32_t lead[kLvlItems * (kLvlThreads / 32)];  // per round: its leading run's mask and length
     const uint64_t c = level_count(n, dn);
     const uint64_t base = (uint64_t)blockIdx.x * kLvlTile;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -363,6 +367,9 @@ __global__ void __launch_bounds__(kLvlThreads) k_level_emit(const uint64_t *__re
     __syncthreads();
     const uint32_t first = tile_first[blockIdx.x];
     const unsigned upto = 0xffffffffu >> (31 - lane);  // lanes 0..lane
+    // Pass 2a: each lane's octant bits with its run-mates' after it, and its
+    // run's end; each round's leading run (the lanes before its first head,
+    // the tail of the previous round's last parent) as one table entry.
 #pragma unroll
     for (int j = 0; j < kLvlItems; ++j) {
         const int q = j * kLvlThreads + threadIdx.x;
@@ -370,7 +377,6 @@ __global__ void __launch_bounds__(kLvlThreads) k_level_emit(const uint64_t *__re
         const bool live = i < c;
         const uint64_t k = sk[1 + q];
         const unsigned b = hb[j];
-        const bool head = (b >> lane) & 1u;
         // a run ends at the next head or at the first lane past the last
         // child (the live lanes are a prefix of the warp's 32)
         const uint64_t w0 = base + (uint64_t)(q - lane);
@@ -386,16 +392,39 @@ __global__ void __launch_bounds__(kLvlThreads) k_level_emit(const uint64_t *__re
             const unsigned o = __shfl_down_sync(0xffffffffu, m, d);
             if (lane + d < hi) m |= o;
         }
-        if (head) {
-            const uint32_t p = first + wpre[j * kWarps + wid] + (uint32_t)__popc(b & upto) - 1u;
-            unsigned mm = m, cnt = (unsigned)(hi - lane);
-            for (int t = q + (int)cnt; cnt < 8 && base + t < c && ((sk[1 + t] ^ k) & ~7ull) == 0ull; ++t, ++cnt)
-                mm |= 1u << (sk[1 + t] & 7);
-            pkey[p] = k >> 3;
-            pstart[p] = (uint32_t)i;
-            pmask[p] = (uint8_t)mm;
-            pcount[p] = (uint8_t)cnt;
+        mh[j][threadIdx.x] = (uint16_t)(m | ((unsigned)hi << 8));
+        if (lane == 0) lead[j * kWarps + wid] = (b & 1u) || !live ? 0u : (m | ((unsigned)hi << 8));
+    }
+    __syncthreads();
+    // Pass 2b: the heads write their parents; a run reaching its round's last
+    // lane continues in the next round's leading run (runs are at most 8
+    // long), and past the tile's last round in the keys that follow it.
+#pragma unroll
+    for (int j = 0; j < kLvlItems; ++j) {
+        const unsigned b = hb[j];
+        if (!((b >> lane) & 1u)) continue;
+        const int q = j * kLvlThreads + threadIdx.x;
+        const uint64_t i = base + q;
+        const uint64_t k = sk[1 + q];
+        const unsigned v = mh[j][threadIdx.x];
+        const int hi = (int)(v >> 8);
+        unsigned mm = v & 0xFFu, cnt = (unsigned)(hi - lane);
+        if (hi == 32) {
+            const int nxt = j * kWarps + wid + 1;  // the next round of 32 children
+            if (nxt < kLvlItems * kWarps) {
+                const unsigned l = lead[nxt];
+                mm |= l & 0xFFu;
+                cnt += l >> 8;
+            } else {
+                for (int t = q + (int)cnt; cnt < 8 && base + t < c && ((sk[1 + t] ^ k) & ~7ull) == 0ull; ++t, ++cnt)
+                    mm |= 1u << (sk[1 + t] & 7);
+            }
         }
+        const uint32_t p = first + wpre[j * kWarps + wid] + (uint32_t)__popc(b & upto) - 1u;
+        pkey[p] = k >> 3;
+        pstart[p] = (uint32_t)i;
+        pmask[p] = (uint8_t)mm;
+        pcount[p] = (uint8_t)cnt;
     }
 }
 
