@@ -57,6 +57,47 @@ def test_edge_grids(svo, oracle):
     assert np.array_equal(_build(svo, np.zeros((2, 2, 2), np.uint32))[0], np.array([1 << 18], np.uint32))
 
 
+def _morton_grid(side, keep):
+    """A side^3 grid holding a voxel at each Morton code m < side^3 with
+    keep(m) true (value m + 1), laid out z, y, x."""
+    m = np.arange(side ** 3, dtype=np.int64)
+    x = np.zeros_like(m)
+    y = np.zeros_like(m)
+    z = np.zeros_like(m)
+    for b in range(int(np.log2(side))):
+        x |= ((m >> (3 * b)) & 1) << b
+        y |= ((m >> (3 * b + 1)) & 1) << b
+        z |= ((m >> (3 * b + 2)) & 1) << b
+    g = np.zeros((side, side, side), np.uint32)
+    sel = keep(m)
+    g[z[sel], y[sel], x[sel]] = (m[sel] + 1).astype(np.uint32)
+    return g
+
+
+def test_level_grouping_runs_and_tiles(svo, oracle):
+    """Runs of siblings that cross 32-child rounds and 2048-child tiles (the
+    level grouping finishes them from the next round's leading run, or past a
+    tile from the keys after it), ragged last tiles, and dense rounds."""
+    side = 64
+    cases = [
+        _morton_grid(side, lambda k: np.ones_like(k, bool)),  # every code: full runs of 8
+        _morton_grid(side, lambda k: (k % 8) >= 3),  # runs of 5 starting at octant 3
+        _morton_grid(side, lambda k: (k // 8) % 3 != 1),  # full runs with gaps between parents
+        _morton_grid(side, lambda k: (k % 8 == 7) | (k % 16 == 8)),  # runs of 1 and 2
+        _morton_grid(side, lambda k: k < 2048 * 5 + 37),  # a ragged last tile at level 1
+        _morton_grid(side, lambda k: (k >= 2048 - 5) & (k < 2048 + 3)),  # one run across a tile
+    ]
+    rng = np.random.default_rng(77)
+    for _ in range(3):  # random run lengths: each parent keeps a random prefix of its octants
+        lens = rng.integers(0, 9, side ** 3 // 8)
+        cases.append(_morton_grid(side, lambda k, lens=lens: (k % 8) < lens[k // 8]))
+    for g in cases:
+        ow, oc = oracle.build_dense(g)
+        gw, gc, _ = _build(svo, g)
+        assert np.array_equal(gw, ow), int((g != 0).sum())
+        assert np.array_equal(gc, oc)
+
+
 def test_odd_slice_empty_descriptor(svo, oracle):
     # Cache blocks of 8^3 (mem 3000 at side 64) and odd depth 41: a block whose
     # only voxels lie in the last z slice becomes a descriptor with no children.
