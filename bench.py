@@ -1226,14 +1226,30 @@ def run_leaf_shading(args, torch, svo, scenes, n_steps=200):
 
     def train(steps, fused):
         """`steps` optimisation steps from the initial parameters.  fused:
-        svo_diff_backward_l2 (loss gradient and loss sum in the adjoint,
-        touched leaves recorded) + svo_adam_step_leaves; else the loss
-        gradient in torch + svo_diff_backward + dense svo_adam_step."""
-        p_rgb, p_n = p0_rgb.clone(), p0_n.clone()
-        g_rgb, g_n = torch.zeros_like(p_rgb), torch.zeros_like(p_n)
-        p_rgb.grad, p_n.grad = g_rgb, g_n
-        leaves = svo.LeafSet(nw) if fused else None
-        opt = svo.LeafAdam([p_rgb, p_n], lr=1e-2, leaves=leaves)  # zeroes the gradients it reads
+        the parameters as 8-float leaf records, svo_diff_backward_l2 (loss
+        gradient and loss sum in the adjoint, touched leaves recorded) +
+        svo_adam_step_leaves; else 3-float arrays, the loss gradient in torch
+        + svo_diff_backward + dense svo_adam_step."""
+        if fused:
+            # one 32-byte record per leaf (rgb, normal, 2 unused floats):
+            # each gather and each leaf's gradient atomics touch one sector,
+            # and one Adam launch updates whole records
+            rec = torch.zeros((nw, 8), dtype=torch.float32, device="cuda")
+            rec[:, 0:3] = p0_rgb
+            rec[:, 3:6] = p0_n
+            grec = torch.zeros_like(rec)
+            rec.grad = grec
+            p_rgb, p_n, g_rgb, g_n = rec[:, 0:3], rec[:, 3:6], grec[:, 0:3], grec[:, 3:6]
+            stride = 8
+            leaves = svo.LeafSet(nw)
+            opt = svo.LeafAdam([rec], lr=1e-2, leaves=leaves, width=8)  # zeroes the gradients it reads
+        else:
+            p_rgb, p_n = p0_rgb.clone(), p0_n.clone()
+            g_rgb, g_n = torch.zeros_like(p_rgb), torch.zeros_like(p_n)
+            p_rgb.grad, p_n.grad = g_rgb, g_n
+            stride = 3
+            leaves = None
+            opt = svo.LeafAdam([p_rgb, p_n], lr=1e-2)
         loss_sum = torch.zeros(steps, dtype=torch.float64, device="cuda")
         ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(steps)]
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -1241,12 +1257,14 @@ def run_leaf_shading(args, torch, svo, scenes, n_steps=200):
         e0.record(stream)
         for k in range(steps):
             ev[k][0].record(stream)
-            tree.diff_forward(rays, W, H, V, lights, p_rgb, p_n, rgb, hit_leaf=leaf, stream=stream)
+            tree.diff_forward(rays, W, H, V, lights, p_rgb, p_n, rgb, hit_leaf=leaf, stream=stream,
+                              param_stride=stride)
             ev[k][1].record(stream)
             if fused:
                 ev[k][2].record(stream)
                 tree.diff_backward_l2(rays, W, H, V, lights, p_rgb, p_n, rgb, target, scale, g_rgb, g_n,
-                                      hit_leaf=leaf, loss_sum=loss_sum[k:k + 1], leaves=leaves, stream=stream)
+                                      hit_leaf=leaf, loss_sum=loss_sum[k:k + 1], leaves=leaves, stream=stream,
+                                      param_stride=stride)
             else:
                 torch.sub(rgb, target, out=d_rgb)
                 loss_sum[k:k + 1] = d_rgb.double().square().sum()
@@ -1274,9 +1292,10 @@ def run_leaf_shading(args, torch, svo, scenes, n_steps=200):
                         "rgb+normal params; L2 loss vs 3-octave noise colour field; Adam lr 1e-2" % nw,
             "rays_per_step": R, "steps": n_steps, "fwd_ms": round(main["fwd_ms"], 3),
             "bwd_ms": round(main["bwd_ms"], 3), "fwd_bwd_mrays_s": round(R / fb / 1e3, 1),
-            "fwd_bwd_note": "svo_diff_forward + svo_diff_backward_l2 kernel time (CUDA events); the adjoint forms the "
-                            "L2 loss gradient and the loss itself; step_ms_with_adam adds svo_adam_step_leaves over "
-                            "the leaves the adjoint has touched (identical to the dense Adam pass)",
+            "fwd_bwd_note": "svo_diff_forward + svo_diff_backward_l2 kernel time (CUDA events), parameters as 8-float "
+                            "leaf records; the adjoint forms the L2 loss gradient and the loss itself; "
+                            "step_ms_with_adam adds svo_adam_step_leaves over the leaves the adjoint has touched "
+                            "(identical to the dense Adam pass)",
             "step_ms_with_adam": round(main["step_ms"], 3), "touched_leaves": main["touched_leaves"],
             "loss_first_last": [[0, round(float(main["loss"][0]), 6)],
                                 [n_steps - 1, round(float(main["loss"][-1]), 6)]],

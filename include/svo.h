@@ -420,6 +420,30 @@ int svo_diff_backward_l2(const svo_octree *oct, const float *rays, uint32_t widt
                          float *grad_rgb, float *grad_normal, double *loss_sum, uint32_t *touched,
                          uint32_t *leaf_list, uint32_t *leaf_count, uint64_t leaf_capacity, svo_stream stream);
 
+/* The same three calls with the leaves' parameters and gradients at
+ * param_stride floats apart (>= 3) instead of 3: leaf i's colour is
+ * leaf_rgb[param_stride*i ..], its normal leaf_normal[param_stride*i ..],
+ * and the gradients are laid out the same way.  With param_stride = 8 and
+ * leaf_normal = leaf_rgb + 3 (and grad_normal = grad_rgb + 3), a leaf's
+ * colour and normal share one 32-byte record, so each gather and each
+ * leaf's set of gradient atomics touches one memory sector instead of two;
+ * svo_adam_step_leaves with width 8 then updates whole records (the two
+ * unused floats get no gradient and stay as they are).  The results are
+ * those of the 3-float layout. */
+int svo_diff_forward_stride(const svo_octree *oct, const float *rays, uint32_t width, uint32_t height,
+                            uint32_t n_views, const float *lights, const float *leaf_rgb, const float *leaf_normal,
+                            uint32_t param_stride, uint32_t *hit_leaf, float *rgb, svo_stream stream);
+int svo_diff_backward_stride(const svo_octree *oct, const float *rays, uint32_t width, uint32_t height,
+                             uint32_t n_views, const float *lights, const float *leaf_rgb, const float *leaf_normal,
+                             uint32_t param_stride, const uint32_t *hit_leaf, const float *d_rgb, float *grad_rgb,
+                             float *grad_normal, svo_stream stream);
+int svo_diff_backward_l2_stride(const svo_octree *oct, const float *rays, uint32_t width, uint32_t height,
+                                uint32_t n_views, const float *lights, const float *leaf_rgb,
+                                const float *leaf_normal, uint32_t param_stride, const uint32_t *hit_leaf,
+                                const float *rgb, const float *target, float loss_scale, float *grad_rgb,
+                                float *grad_normal, double *loss_sum, uint32_t *touched, uint32_t *leaf_list,
+                                uint32_t *leaf_count, uint64_t leaf_capacity, svo_stream stream);
+
 /* No counterpart in the reference.  One Adam step (no weight decay, no
  * amsgrad) over n parameters in one pass: exp_avg = beta1 exp_avg + (1 -
  * beta1) g, exp_avg_sq = beta2 exp_avg_sq + (1 - beta2) g^2, params -=

@@ -136,6 +136,13 @@ def _load():
         "svo_diff_backward_l2": (ctypes.c_int, [_vp, _vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _vp, _vp,
                                                 _vp, _vp, _vp, _vp, ctypes.c_float, _vp, _vp, _vp, _vp, _vp, _vp,
                                                 ctypes.c_uint64, _vp]),
+        "svo_diff_forward_stride": (ctypes.c_int, [_vp, _vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _vp,
+                                                   _vp, _vp, ctypes.c_uint32, _vp, _vp, _vp]),
+        "svo_diff_backward_stride": (ctypes.c_int, [_vp, _vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _vp,
+                                                    _vp, _vp, ctypes.c_uint32, _vp, _vp, _vp, _vp, _vp]),
+        "svo_diff_backward_l2_stride": (ctypes.c_int, [_vp, _vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                                       _vp, _vp, _vp, ctypes.c_uint32, _vp, _vp, _vp, ctypes.c_float,
+                                                       _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_uint64, _vp]),
         "svo_adam_step_leaves": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_uint64, ctypes.c_uint32, _vp, _vp,
                                                 ctypes.c_uint64, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                                 ctypes.c_float, ctypes.c_int, ctypes.c_int, _vp]),
@@ -538,21 +545,25 @@ class VoxelOctree:
         return res
 
     def diff_forward(self, rays, width, height, n_views, lights, leaf_rgb, leaf_normal, rgb, hit_leaf=None,
-                     stream=None):
-        """Differentiable shading forward (all CUDA tensors); see svo_diff_forward."""
-        check(lib.svo_diff_forward(self._h, _dev_ptr(rays), int(width), int(height), int(n_views), _dev_ptr(lights),
-                                   _dev_ptr(leaf_rgb), _dev_ptr(leaf_normal), _dev_ptr(hit_leaf), _dev_ptr(rgb),
-                                   _stream_ptr(stream)))
+                     stream=None, param_stride=3):
+        """Differentiable shading forward (all CUDA tensors); see svo_diff_forward.
+        param_stride: floats from one leaf's parameters to the next (8 with
+        leaf_normal = the record's floats 3..5: svo_diff_forward_stride)."""
+        check(lib.svo_diff_forward_stride(self._h, _dev_ptr(rays), int(width), int(height), int(n_views),
+                                          _dev_ptr(lights), _dev_ptr(leaf_rgb), _dev_ptr(leaf_normal),
+                                          int(param_stride), _dev_ptr(hit_leaf), _dev_ptr(rgb), _stream_ptr(stream)))
 
     def diff_backward(self, rays, width, height, n_views, lights, leaf_rgb, leaf_normal, d_rgb, grad_rgb,
-                      grad_normal, hit_leaf=None, stream=None):
+                      grad_normal, hit_leaf=None, stream=None, param_stride=3):
         """Adjoint: accumulates parameter gradients; hit_leaf=None re-traces."""
-        check(lib.svo_diff_backward(self._h, _dev_ptr(rays), int(width), int(height), int(n_views), _dev_ptr(lights),
-                                    _dev_ptr(leaf_rgb), _dev_ptr(leaf_normal), _dev_ptr(hit_leaf), _dev_ptr(d_rgb),
-                                    _dev_ptr(grad_rgb), _dev_ptr(grad_normal), _stream_ptr(stream)))
+        check(lib.svo_diff_backward_stride(self._h, _dev_ptr(rays), int(width), int(height), int(n_views),
+                                           _dev_ptr(lights), _dev_ptr(leaf_rgb), _dev_ptr(leaf_normal),
+                                           int(param_stride), _dev_ptr(hit_leaf), _dev_ptr(d_rgb), _dev_ptr(grad_rgb),
+                                           _dev_ptr(grad_normal), _stream_ptr(stream)))
 
     def diff_backward_l2(self, rays, width, height, n_views, lights, leaf_rgb, leaf_normal, rgb, target, loss_scale,
-                         grad_rgb, grad_normal, hit_leaf=None, loss_sum=None, leaves=None, stream=None):
+                         grad_rgb, grad_normal, hit_leaf=None, loss_sum=None, leaves=None, stream=None,
+                         param_stride=3):
         """Adjoint of the L2 loss loss_scale/2 * sum (rgb - target)^2 with the
         loss gradient formed in the kernel (svo_diff_backward_l2); loss_sum
         (a float64 CUDA tensor) accumulates sum (rgb - target)^2, and
@@ -561,11 +572,12 @@ class VoxelOctree:
         cap = 0
         if leaves is not None:
             tb, ll, lc, cap = leaves.touched, leaves.list, leaves.count, leaves.list.numel()
-        check(lib.svo_diff_backward_l2(self._h, _dev_ptr(rays), int(width), int(height), int(n_views),
-                                       _dev_ptr(lights), _dev_ptr(leaf_rgb), _dev_ptr(leaf_normal), _dev_ptr(hit_leaf),
-                                       _dev_ptr(rgb), _dev_ptr(target), float(loss_scale), _dev_ptr(grad_rgb),
-                                       _dev_ptr(grad_normal), _dev_ptr(loss_sum), _dev_ptr(tb), _dev_ptr(ll),
-                                       _dev_ptr(lc), int(cap), _stream_ptr(stream)))
+        check(lib.svo_diff_backward_l2_stride(self._h, _dev_ptr(rays), int(width), int(height), int(n_views),
+                                              _dev_ptr(lights), _dev_ptr(leaf_rgb), _dev_ptr(leaf_normal),
+                                              int(param_stride), _dev_ptr(hit_leaf), _dev_ptr(rgb), _dev_ptr(target),
+                                              float(loss_scale), _dev_ptr(grad_rgb), _dev_ptr(grad_normal),
+                                              _dev_ptr(loss_sum), _dev_ptr(tb), _dev_ptr(ll), _dev_ptr(lc), int(cap),
+                                              _stream_ptr(stream)))
 
     def render_frame(self, rot, pos, width=1280, height=720, n_strips=16, pixel_stride=1, out=None, stream=None):
         """The viewer's frame (svo_render_frame) into `out`, an int32 CUDA

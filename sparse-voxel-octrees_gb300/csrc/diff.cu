@@ -36,6 +36,7 @@ struct DiffArgs {
     uint64_t total;
     const float *lights;  // 3 per view (device)
     const float *p_rgb, *p_n;
+    uint32_t stride;  // floats from one leaf's parameters (and gradients) to the next
     uint32_t *hit_leaf;
     float *rgb;
     const float *d_rgb;
@@ -69,10 +70,11 @@ struct Shading {
     float nx, ny, nz, inv_len, ln, a, nd, s;
 };
 
-__device__ __forceinline__ Shading shade_terms(const float *p_n, uint32_t leaf, float dx, float dy, float dz, float lx,
-                                               float ly, float lz) {
+__device__ __forceinline__ Shading shade_terms(const float *p_n, uint32_t stride, uint32_t leaf, float dx, float dy,
+                                               float dz, float lx, float ly, float lz) {
     Shading sh;
-    float px = p_n[3 * (uint64_t)leaf], py = p_n[3 * (uint64_t)leaf + 1], pz = p_n[3 * (uint64_t)leaf + 2];
+    const float *pn = p_n + (uint64_t)stride * leaf;
+    float px = pn[0], py = pn[1], pz = pn[2];
     float len2 = px * px + py * py + pz * pz;
     sh.inv_len = len2 > 0.0f ? 1.0f / sqrtf(len2) : 0.0f;
     sh.nx = px * sh.inv_len;
@@ -122,9 +124,9 @@ __global__ void k_diff_forward(DiffArgs a) {
         float c0 = 0.0f, c1 = 0.0f, c2 = 0.0f;
         if (hit) {
             float lx = a.lights[3 * view], ly = a.lights[3 * view + 1], lz = a.lights[3 * view + 2];
-            Shading sh = shade_terms(a.p_n, res.leaf, p1.y, p2.x, p2.y, lx, ly, lz);
+            Shading sh = shade_terms(a.p_n, a.stride, res.leaf, p1.y, p2.x, p2.y, lx, ly, lz);
             float spec = sh.s * sh.s * 0.2f;
-            const float *c = a.p_rgb + 3 * (uint64_t)res.leaf;
+            const float *c = a.p_rgb + (uint64_t)a.stride * res.leaf;
             c0 = c[0] * 0.9f * sh.a + spec;
             c1 = c[1] * 0.9f * sh.a + spec;
             c2 = c[2] * 0.9f * sh.a + spec;
@@ -217,8 +219,8 @@ __global__ void k_diff_backward(DiffArgs a) {
         }
         if (contrib) {
             float lx = a.lights[3 * view], ly = a.lights[3 * view + 1], lz = a.lights[3 * view + 2];
-            Shading sh = shade_terms(a.p_n, leaf, dx, dy, dz, lx, ly, lz);
-            const float *c = a.p_rgb + 3 * (uint64_t)leaf;
+            Shading sh = shade_terms(a.p_n, a.stride, leaf, dx, dy, dz, lx, ly, lz);
+            const float *c = a.p_rgb + (uint64_t)a.stride * leaf;
             if (!kFused) {
                 g0 = a.d_rgb[3 * (uint64_t)idx];
                 g1 = a.d_rgb[3 * (uint64_t)idx + 1];
@@ -249,8 +251,8 @@ __global__ void k_diff_backward(DiffArgs a) {
         gp1 = group_sum(peers, rank, size, gp1);
         gp2 = group_sum(peers, rank, size, gp2);
         if (contrib && rank == 0) {
-            float *gr = a.g_rgb + 3 * (uint64_t)leaf;
-            float *gn = a.g_n + 3 * (uint64_t)leaf;
+            float *gr = a.g_rgb + (uint64_t)a.stride * leaf;
+            float *gn = a.g_n + (uint64_t)a.stride * leaf;
             atomicAdd(gr, gc0);
             atomicAdd(gr + 1, gc1);
             atomicAdd(gr + 2, gc2);
@@ -269,9 +271,10 @@ __global__ void k_diff_backward(DiffArgs a) {
 }
 
 int prepare(const svo_octree *oct, const float *rays, uint32_t width, uint32_t height, uint32_t n_views,
-            const float *lights, const float *p_rgb, const float *p_n, DiffArgs &a) {
+            const float *lights, const float *p_rgb, const float *p_n, uint32_t stride, DiffArgs &a) {
     if (!oct || !rays || !lights || !p_rgb || !p_n || width == 0 || height == 0 || n_views == 0)
         return set_error(SVO_ERR_INVALID, "bad arguments");
+    if (stride < 3) return set_error(SVO_ERR_INVALID, "parameter stride %u below 3", stride);
     if ((uint64_t)width * height * n_views > 0xFFFFFFFFull) return set_error(SVO_ERR_LIMIT, "more than 2^32-1 rays");
     if (wide_octree(oct)) return set_error(SVO_ERR_LIMIT, "leaf shading takes octrees of up to 2^32-1 words");
     std::memset(&a, 0, sizeof(a));
@@ -286,6 +289,7 @@ int prepare(const svo_octree *oct, const float *rays, uint32_t width, uint32_t h
     a.lights = lights;
     a.p_rgb = p_rgb;
     a.p_n = p_n;
+    a.stride = stride;
     a.queue = oct->d_queue;
     a.status = oct->d_status;
     return SVO_OK;
@@ -310,11 +314,11 @@ using namespace svo;
 
 extern "C" {
 
-int svo_diff_forward(const svo_octree *oct, const float *rays, uint32_t width, uint32_t height, uint32_t n_views,
-                     const float *lights, const float *leaf_rgb, const float *leaf_normal, uint32_t *hit_leaf,
-                     float *rgb, svo_stream stream) {
+int svo_diff_forward_stride(const svo_octree *oct, const float *rays, uint32_t width, uint32_t height,
+                            uint32_t n_views, const float *lights, const float *leaf_rgb, const float *leaf_normal,
+                            uint32_t param_stride, uint32_t *hit_leaf, float *rgb, svo_stream stream) {
     DiffArgs a;
-    int rc = prepare(oct, rays, width, height, n_views, lights, leaf_rgb, leaf_normal, a);
+    int rc = prepare(oct, rays, width, height, n_views, lights, leaf_rgb, leaf_normal, param_stride, a);
     if (rc) return rc;
     if (!rgb) return set_error(SVO_ERR_INVALID, "rgb output required");
     a.hit_leaf = hit_leaf;
@@ -328,11 +332,12 @@ int svo_diff_forward(const svo_octree *oct, const float *rays, uint32_t width, u
                     : launch_persistent(k_diff_forward<false, false>, a, st);
 }
 
-int svo_diff_backward(const svo_octree *oct, const float *rays, uint32_t width, uint32_t height, uint32_t n_views,
-                      const float *lights, const float *leaf_rgb, const float *leaf_normal, const uint32_t *hit_leaf,
-                      const float *d_rgb, float *grad_rgb, float *grad_normal, svo_stream stream) {
+int svo_diff_backward_stride(const svo_octree *oct, const float *rays, uint32_t width, uint32_t height,
+                             uint32_t n_views, const float *lights, const float *leaf_rgb, const float *leaf_normal,
+                             uint32_t param_stride, const uint32_t *hit_leaf, const float *d_rgb, float *grad_rgb,
+                             float *grad_normal, svo_stream stream) {
     DiffArgs a;
-    int rc = prepare(oct, rays, width, height, n_views, lights, leaf_rgb, leaf_normal, a);
+    int rc = prepare(oct, rays, width, height, n_views, lights, leaf_rgb, leaf_normal, param_stride, a);
     if (rc) return rc;
     if (!d_rgb || !grad_rgb || !grad_normal) return set_error(SVO_ERR_INVALID, "gradient buffers required");
     a.hit_leaf = const_cast<uint32_t *>(hit_leaf);
@@ -346,13 +351,14 @@ int svo_diff_backward(const svo_octree *oct, const float *rays, uint32_t width, 
                     : launch_persistent(k_diff_backward<false, true, false>, a, st);
 }
 
-int svo_diff_backward_l2(const svo_octree *oct, const float *rays, uint32_t width, uint32_t height,
-                         uint32_t n_views, const float *lights, const float *leaf_rgb, const float *leaf_normal,
-                         const uint32_t *hit_leaf, const float *rgb, const float *target, float loss_scale,
-                         float *grad_rgb, float *grad_normal, double *loss_sum, uint32_t *touched,
-                         uint32_t *leaf_list, uint32_t *leaf_count, uint64_t leaf_capacity, svo_stream stream) {
+int svo_diff_backward_l2_stride(const svo_octree *oct, const float *rays, uint32_t width, uint32_t height,
+                                uint32_t n_views, const float *lights, const float *leaf_rgb,
+                                const float *leaf_normal, uint32_t param_stride, const uint32_t *hit_leaf,
+                                const float *rgb, const float *target, float loss_scale, float *grad_rgb,
+                                float *grad_normal, double *loss_sum, uint32_t *touched, uint32_t *leaf_list,
+                                uint32_t *leaf_count, uint64_t leaf_capacity, svo_stream stream) {
     DiffArgs a;
-    int rc = prepare(oct, rays, width, height, n_views, lights, leaf_rgb, leaf_normal, a);
+    int rc = prepare(oct, rays, width, height, n_views, lights, leaf_rgb, leaf_normal, param_stride, a);
     if (rc) return rc;
     if (!rgb || !target || !grad_rgb || !grad_normal)
         return set_error(SVO_ERR_INVALID, "rgb, target and gradient buffers required");
@@ -377,6 +383,31 @@ int svo_diff_backward_l2(const svo_octree *oct, const float *rays, uint32_t widt
     if (a.tab) return launch_persistent(k_diff_backward<true, true, true>, a, st);
     return hit_leaf ? launch_persistent(k_diff_backward<false, false, true>, a, st)
                     : launch_persistent(k_diff_backward<false, true, true>, a, st);
+}
+
+// The separate-array forms: 3 floats per leaf in each array.
+int svo_diff_forward(const svo_octree *oct, const float *rays, uint32_t width, uint32_t height, uint32_t n_views,
+                     const float *lights, const float *leaf_rgb, const float *leaf_normal, uint32_t *hit_leaf,
+                     float *rgb, svo_stream stream) {
+    return svo_diff_forward_stride(oct, rays, width, height, n_views, lights, leaf_rgb, leaf_normal, 3, hit_leaf,
+                                   rgb, stream);
+}
+
+int svo_diff_backward(const svo_octree *oct, const float *rays, uint32_t width, uint32_t height, uint32_t n_views,
+                      const float *lights, const float *leaf_rgb, const float *leaf_normal, const uint32_t *hit_leaf,
+                      const float *d_rgb, float *grad_rgb, float *grad_normal, svo_stream stream) {
+    return svo_diff_backward_stride(oct, rays, width, height, n_views, lights, leaf_rgb, leaf_normal, 3, hit_leaf,
+                                    d_rgb, grad_rgb, grad_normal, stream);
+}
+
+int svo_diff_backward_l2(const svo_octree *oct, const float *rays, uint32_t width, uint32_t height,
+                         uint32_t n_views, const float *lights, const float *leaf_rgb, const float *leaf_normal,
+                         const uint32_t *hit_leaf, const float *rgb, const float *target, float loss_scale,
+                         float *grad_rgb, float *grad_normal, double *loss_sum, uint32_t *touched,
+                         uint32_t *leaf_list, uint32_t *leaf_count, uint64_t leaf_capacity, svo_stream stream) {
+    return svo_diff_backward_l2_stride(oct, rays, width, height, n_views, lights, leaf_rgb, leaf_normal, 3, hit_leaf,
+                                       rgb, target, loss_scale, grad_rgb, grad_normal, loss_sum, touched, leaf_list,
+                                       leaf_count, leaf_capacity, stream);
 }
 
 }  // extern "C"

@@ -276,3 +276,56 @@ def test_sparse_adam_equals_dense_adam(cuda, svo, problem):
             assert torch.equal(m1, m2) and torch.equal(v1, v2), step
         assert not sparse[0].grad.any() and not sparse[1].grad.any()
     assert 0 < leaves.size() < pb["words"].size
+
+
+def test_leaf_records_match_separate_arrays(cuda, svo, problem):
+    """The 8-float leaf record layout (rgb at 0..2, normal at 3..5, through
+    the *_stride entry points) against the two 3-float arrays: the same
+    colours and hit leaves bit for bit, the same gradients up to the order of
+    the atomic sums, and Adam over whole records (width 8) gives the same
+    parameters while the two unused floats stay as they are."""
+    torch = cuda
+    pb = problem
+    rays, lights, p_rgb, p_n, target = _device(torch, pb)
+    p_rgb, p_n = p_rgb.detach(), p_n.detach()
+    nw = p_rgb.shape[0]
+    rec = torch.full((nw, 8), 7.0, dtype=torch.float32, device="cuda")
+    rec[:, 0:3] = p_rgb
+    rec[:, 3:6] = p_n
+    R = rays.shape[0]
+    geo = (rays, pb["W"], pb["H"], pb["V"], lights)
+    rgb3, rgb8 = (torch.empty((R, 3), dtype=torch.float32, device="cuda") for _ in range(2))
+    hit3, hit8 = (torch.empty(R, dtype=torch.int32, device="cuda") for _ in range(2))
+    pb["tree"].diff_forward(*geo, p_rgb, p_n, rgb3, hit_leaf=hit3)
+    pb["tree"].diff_forward(*geo, rec[:, 0:3], rec[:, 3:6], rgb8, hit_leaf=hit8, param_stride=8)
+    torch.cuda.synchronize()
+    assert torch.equal(rgb3.view(torch.int32), rgb8.view(torch.int32)) and torch.equal(hit3, hit8)
+    scale = 2.0 * pb["w"]
+    g3 = [torch.zeros_like(p_rgb), torch.zeros_like(p_n)]
+    grec = torch.zeros_like(rec)
+    leaves3, leaves8 = svo.LeafSet(nw), svo.LeafSet(nw)
+    pb["tree"].diff_backward_l2(*geo, p_rgb, p_n, rgb3, target, scale, g3[0], g3[1], hit_leaf=hit3, leaves=leaves3)
+    pb["tree"].diff_backward_l2(*geo, rec[:, 0:3], rec[:, 3:6], rgb8, target, scale, grec[:, 0:3], grec[:, 3:6],
+                                hit_leaf=hit8, leaves=leaves8, param_stride=8)
+    # the plain adjoint with dL/drgb from torch, in records too
+    grec2 = torch.zeros_like(rec)
+    pb["tree"].diff_backward(*geo, rec[:, 0:3], rec[:, 3:6], (rgb8 - target) * scale, grec2[:, 0:3],
+                             grec2[:, 3:6], hit_leaf=hit8, param_stride=8)
+    torch.cuda.synchronize()
+    torch.testing.assert_close(grec[:, 0:3], g3[0], rtol=1e-5, atol=1e-12)
+    torch.testing.assert_close(grec[:, 3:6], g3[1], rtol=1e-5, atol=1e-12)
+    torch.testing.assert_close(grec2[:, 0:6], grec[:, 0:6], rtol=1e-5, atol=1e-12)
+    assert not grec[:, 6:].any()
+    assert leaves8.size() == leaves3.size()
+    # one sparse Adam step each, from the same gradients
+    sep = [p_rgb.clone(), p_n.clone()]
+    sep[0].grad, sep[1].grad = grec[:, 0:3].contiguous(), grec[:, 3:6].contiguous()
+    rec.grad = grec
+    svo.LeafAdam(sep, lr=1e-2, leaves=leaves3).step()
+    svo.LeafAdam([rec], lr=1e-2, leaves=leaves8, width=8).step()
+    torch.cuda.synchronize()
+    assert torch.equal(rec[:, 0:3].contiguous().view(torch.int32), sep[0].view(torch.int32))
+    assert torch.equal(rec[:, 3:6].contiguous().view(torch.int32), sep[1].view(torch.int32))
+    assert bool((rec[:, 6:] == 7.0).all())
+    with pytest.raises(Exception):
+        pb["tree"].diff_forward(*geo, p_rgb, p_n, rgb3, param_stride=2)
